@@ -1,0 +1,278 @@
+"""crispy_gb300 -- GB300 (sm_103a) engine for CRiSPy's kmerDist and genDist.
+
+The engine is the C-ABI library ``lib/libcrispy_gb300.so`` (declared in
+``include/crispy_gb300.h``); this module binds it with ctypes, the same way
+a Python caller of the reference's stages would.  There is no CPU fallback:
+if the library is missing or cannot reach an sm_103a GPU, every call raises.
+
+Stage mirror of the reference (src/kmerDist, src/genDist):
+    compute_kmer_dist(fasta, k, thr, dists)   -> writes <fasta>.kpair [.kdist]
+    compute_gen_dist(fasta, band, thr)        -> writes <fasta>.npair_N / .ndist_N
+and the lower-level ``Engine`` for device-resident work.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libcrispy_gb300.so")
+BIN_DIR = os.path.join(_PKG, "bin")
+
+OK, E_INPUT, E_OOM, E_DEVICE, E_TIMEOUT, E_STATE, E_IO, E_UNSUPPORTED = range(8)
+MODE_PLAIN, MODE_BATCHED = 0, 1
+GEN_WINDOW = 589824
+MAX_READ_LEN = 2048
+MAX_NUM_READS = 1024 * 1024
+
+_STATUS = {0: "OK", 1: "E_INPUT", 2: "E_OOM", 3: "E_DEVICE", 4: "E_TIMEOUT", 5: "E_STATE",
+           6: "E_IO", 7: "E_UNSUPPORTED"}
+
+
+class CrispyError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+SINK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_float), C.c_int64)
+
+
+class Stats(C.Structure):
+    _fields_ = [("kmer_kernel_ms", C.c_double), ("kmer_launches", C.c_int64),
+                ("gen_kernel_ms", C.c_double), ("gen_launches", C.c_int64),
+                ("total_ms", C.c_double), ("kmer_pairs", C.c_int64),
+                ("kmer_survivors", C.c_int64), ("gen_pairs", C.c_int64),
+                ("gen_cells", C.c_int64), ("gen_survivors", C.c_int64),
+                ("kernels_launched", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_P = C.c_void_p
+_i64p = C.POINTER(C.c_int64)
+
+# name -> (restype, argtypes); exactly the declarations of include/crispy_gb300.h
+PROTOTYPES = {
+    "crispy_version": (C.c_char_p, []),
+    "crispy_last_error": (C.c_char_p, [_P]),
+    "crispy_ctx_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
+    "crispy_ctx_destroy": (C.c_int, [_P]),
+    "crispy_ctx_set_stream": (C.c_int, [_P, _P]),
+    "crispy_reads_load_fasta": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+    "crispy_reads_view": (C.c_int, [_P, C.POINTER(C.c_char_p), C.POINTER(_i64p),
+                                    C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32)]),
+    "crispy_reads_free": (None, [_P]),
+    "crispy_default_threshold": (C.c_float, [C.c_int, C.c_float, C.c_int]),
+    "crispy_array_dim": (C.c_int, [C.c_int]),
+    "crispy_kmer_prepare": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int]),
+    "crispy_kmer_run": (C.c_int, [_P, C.c_float, C.c_int, C.c_int, _i64p]),
+    "crispy_kmer_fetch": (C.c_int, [_P, _P, _P, C.c_int64, _i64p]),
+    "crispy_kmer_stream": (C.c_int, [_P, SINK, _P]),
+    "crispy_gen_prepare": (C.c_int, [_P, _P, _P, _P, C.c_int]),
+    "crispy_gen_run": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
+    "crispy_gen_run_from_kmer": (C.c_int, [_P, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
+    "crispy_gen_align": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P]),
+    "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "crispy_set_timing": (C.c_int, [_P, C.c_int]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load the engine; raise (never fall back) when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CrispyError(E_DEVICE, f"{path} is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def default_threshold(n: int, user_thr: float = -1.0, stage: int = 0) -> float:
+    return float(load_library().crispy_default_threshold(n, user_thr, stage))
+
+
+def array_dim(n: int) -> int:
+    return int(load_library().crispy_array_dim(n))
+
+
+def read_fasta(path: str, flavour: int = 0):
+    """Parse like the reference's readFile: (bytes buffer, offsets, lengths)."""
+    lib = load_library()
+    h = _P()
+    rc = lib.crispy_reads_load_fasta(path.encode(), flavour, C.byref(h))
+    if rc != OK:
+        raise CrispyError(rc, lib.crispy_last_error(None).decode())
+    try:
+        buf = C.c_char_p()
+        off = _i64p()
+        ln = C.POINTER(C.c_int32)()
+        n = C.c_int32()
+        mx = C.c_int32()
+        lib.crispy_reads_view(h, C.byref(buf), C.byref(off), C.byref(ln), C.byref(n), C.byref(mx))
+        cnt = n.value
+        offs = np.ctypeslib.as_array(off, shape=(cnt,)).copy() if cnt else np.zeros(0, np.int64)
+        lens = np.ctypeslib.as_array(ln, shape=(cnt,)).copy() if cnt else np.zeros(0, np.int32)
+        total = int(offs[-1] + lens[-1]) if cnt else 0
+        data = np.frombuffer(C.string_at(buf, total), dtype=np.uint8).copy()
+    finally:
+        lib.crispy_reads_free(h)
+    return data, offs, lens
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+class Engine:
+    """One context on one GPU (the C ABI's crispy_ctx)."""
+
+    def __init__(self, device: int = 0, timing: bool = False):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.crispy_ctx_create(device, C.byref(h))
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(None).decode())
+        self.h = h
+        if timing:
+            self.lib.crispy_set_timing(self.h, 1)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.crispy_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(self.h).decode())
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.lib.crispy_ctx_set_stream(self.h, stream_handle))
+
+    def set_timing(self, on: bool):
+        self._check(self.lib.crispy_set_timing(self.h, 1 if on else 0))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.crispy_get_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    # ---- kmerDist ----
+    def kmer_prepare(self, buf: np.ndarray, offs: np.ndarray, lens: np.ndarray, k: int = 6):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        lens = np.ascontiguousarray(lens, dtype=np.int32)
+        self._check(self.lib.crispy_kmer_prepare(self.h, _ptr(buf), _ptr(offs), _ptr(lens),
+                                                 len(lens), k))
+
+    def kmer_run(self, thr: float, mode: int = MODE_BATCHED, dists: bool = True) -> int:
+        n = C.c_int64()
+        self._check(self.lib.crispy_kmer_run(self.h, thr, mode, 1 if dists else 0, C.byref(n)))
+        return n.value
+
+    def kmer_fetch(self, count: int, dists: bool = True):
+        pairs = np.empty((max(count, 1), 2), dtype=np.int32)
+        d = np.empty(max(count, 1), dtype=np.float32) if dists else None
+        got = C.c_int64()
+        self._check(self.lib.crispy_kmer_fetch(self.h, _ptr(pairs), _ptr(d), count, C.byref(got)))
+        return pairs[:got.value], (d[:got.value] if dists else None)
+
+    # ---- genDist ----
+    def gen_prepare(self, buf: np.ndarray, offs: np.ndarray, lens: np.ndarray):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        offs = np.ascontiguousarray(offs, dtype=np.int64)
+        lens = np.ascontiguousarray(lens, dtype=np.int32)
+        self._check(self.lib.crispy_gen_prepare(self.h, _ptr(buf), _ptr(offs), _ptr(lens), len(lens)))
+
+    def gen_align(self, pairs: np.ndarray, band: int, mode: int = MODE_BATCHED):
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        n = len(pairs)
+        dist = np.empty(max(n, 1), np.float32)
+        score = np.empty(max(n, 1), np.int32)
+        ml = np.empty(max(n, 1), np.int32)
+        al = np.empty(max(n, 1), np.int32)
+        self._check(self.lib.crispy_gen_align(self.h, _ptr(pairs), n, band, mode, _ptr(dist),
+                                              _ptr(score), _ptr(ml), _ptr(al)))
+        return dist[:n], score[:n], ml[:n], al[:n]
+
+    def _collect(self):
+        chunks = []
+
+        def cb(user, chunk_id, pairs, dists, count):
+            p = np.ctypeslib.as_array(C.cast(pairs, C.POINTER(C.c_uint32)), shape=(count, 2)).copy() if count else np.zeros((0, 2), np.uint32)
+            d = np.ctypeslib.as_array(dists, shape=(count,)).copy() if count else np.zeros(0, np.float32)
+            chunks.append((chunk_id, p, d))
+            return 0
+
+        return chunks, SINK(cb)
+
+    def gen_run(self, pairs: np.ndarray, band: int, thr: float, mode: int = MODE_BATCHED):
+        """Returns the list of chunks [(chunk_id, uint32 pairs[N,2], float32 dists[N])]."""
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        chunks, cb = self._collect()
+        ns = C.c_int64()
+        self._check(self.lib.crispy_gen_run(self.h, _ptr(pairs), len(pairs), band, thr, mode, cb,
+                                            None, C.byref(ns)))
+        return chunks
+
+    def gen_run_from_kmer(self, band: int, thr: float, mode: int = MODE_BATCHED):
+        chunks, cb = self._collect()
+        ns = C.c_int64()
+        self._check(self.lib.crispy_gen_run_from_kmer(self.h, band, thr, mode, cb, None, C.byref(ns)))
+        return chunks
+
+
+def compute_kmer_dist(fasta: str, k: int = 6, thr: float = -1.0, dists: bool = False,
+                      mode: int = MODE_BATCHED, engine: Engine | None = None) -> int:
+    """kmerDist -i fasta -k k [-t thr] [-d]: writes <fasta>.kpair (and .kdist)."""
+    buf, offs, lens = read_fasta(fasta, 0)
+    t = default_threshold(len(lens), thr, 0)
+    eng = engine or Engine()
+    eng.kmer_prepare(buf, offs, lens, k)
+    n = eng.kmer_run(t, mode, dists)
+    pairs, d = eng.kmer_fetch(n, dists)
+    pairs.astype(np.int32).tofile(fasta + ".kpair")
+    if dists:
+        d.astype(np.float32).tofile(fasta + ".kdist")
+    return n
+
+
+def compute_gen_dist(fasta: str, band: int = 2, thr: float = -1.0, mode: int = MODE_BATCHED,
+                     engine: Engine | None = None) -> int:
+    """genDist -i fasta -b band [-t thr]: writes <fasta>.npair_N / .ndist_N."""
+    buf, offs, lens = read_fasta(fasta, 1)
+    t = default_threshold(len(lens), thr, 1)
+    raw = np.fromfile(fasta + ".kpair", dtype=np.int32)
+    pairs = raw[: (len(raw) // 2) * 2].reshape(-1, 2)
+    eng = engine or Engine()
+    eng.gen_prepare(buf, offs, lens)
+    total = 0
+    for cid, p, d in eng.gen_run(pairs, band if band > 0 else 2, t, mode):
+        p.astype(np.uint32).tofile(f"{fasta}.npair_{cid}")
+        d.astype(np.float32).tofile(f"{fasta}.ndist_{cid}")
+        total += len(d)
+    return total

@@ -1,0 +1,212 @@
+// ctx.cu -- context lifetime, error reporting, memory and timing helpers.
+//
+// Replaces the reference's process-global CUDA setup and its
+// checkCudaErrors -> exit(-1) error model (kmerKernel.h:17-26,
+// genKernel.h:17-26): every failure becomes a status code plus a message.
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+
+#include "internal.h"
+
+namespace {
+std::mutex g_err_mu;
+std::string g_err;  // errors raised before a context exists
+
+__global__ void probe_kernel(int* p) {
+    if (p) *p = 1;
+}
+}  // namespace
+
+namespace crispy {
+
+int fail(crispy_ctx* ctx, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) {
+        ctx->err = buf;
+    } else {
+        std::lock_guard<std::mutex> g(g_err_mu);
+        g_err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(crispy_ctx* ctx, cudaError_t e, const char* what, const char* file, int line) {
+    int code = (e == cudaErrorMemoryAllocation) ? CRISPY_E_OOM : CRISPY_E_DEVICE;
+    return fail(ctx, code, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.ptr) return CRISPY_OK;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.ptr, want);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return fail(ctx, CRISPY_E_OOM, "device allocation of %zu bytes failed: %s", want,
+                    cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return CRISPY_OK;
+}
+
+int ensure_host(crispy_ctx* ctx, HostBuf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.ptr) return CRISPY_OK;
+    if (b.ptr) cudaFreeHost(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMallocHost(&b.ptr, want);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        return fail(ctx, CRISPY_E_OOM, "pinned host allocation of %zu bytes failed: %s", want,
+                    cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return CRISPY_OK;
+}
+
+void release(DevBuf& b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+void release_host(HostBuf& b) {
+    if (b.ptr) cudaFreeHost(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+cudaEvent_t ev_begin(crispy_ctx* ctx, StreamEvents& ev, cudaStream_t s) {
+    if (!ctx->timing) return nullptr;
+    if (ev.used == ev.start.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        ev.start.push_back(a);
+        ev.stop.push_back(b);
+    }
+    cudaEventRecord(ev.start[ev.used], s);
+    return ev.start[ev.used];
+}
+
+void ev_end(crispy_ctx* ctx, StreamEvents& ev, cudaStream_t s) {
+    if (!ctx->timing) return;
+    cudaEventRecord(ev.stop[ev.used], s);
+    ++ev.used;
+}
+
+double ev_sum_ms(StreamEvents& ev) {
+    double total = 0;
+    for (size_t i = 0; i < ev.used; ++i) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ev.start[i], ev.stop[i]) == cudaSuccess) total += ms;
+    }
+    return total;
+}
+
+void count_launch(crispy_ctx* ctx, int n) { ctx->stats.kernels_launched += n; }
+
+}  // namespace crispy
+
+using namespace crispy;
+
+extern "C" {
+
+const char* crispy_version(void) { return "crispy_gb300 1.0 (sm_103a)"; }
+
+int crispy_ctx_create(int device, crispy_ctx** out) {
+    if (!out) return fail(nullptr, CRISPY_E_INPUT, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, CRISPY_E_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return fail(nullptr, CRISPY_E_INPUT, "device %d out of range (%d devices)", device, ndev);
+    if ((e = cudaSetDevice(device)) != cudaSuccess)
+        return fail(nullptr, CRISPY_E_DEVICE, "cudaSetDevice: %s", cudaGetErrorString(e));
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, probe_kernel)) != cudaSuccess)
+        return fail(nullptr, CRISPY_E_DEVICE,
+                    "this library holds sm_103a code only and cannot run here: %s",
+                    cudaGetErrorString(e));
+    crispy_ctx* ctx = new crispy_ctx();
+    ctx->device = device;
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, device);
+    ctx->sm_count = p.multiProcessorCount;
+    ctx->smem_optin = p.sharedMemPerBlockOptin;
+    if ((e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete ctx;
+        return fail(nullptr, CRISPY_E_DEVICE, "stream: %s", cudaGetErrorString(e));
+    }
+    for (auto& s : ctx->side) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    ctx->stream = ctx->own_stream;
+    cudaEventCreate(&ctx->t_begin);
+    cudaEventCreate(&ctx->t_end);
+    *out = ctx;
+    return CRISPY_OK;
+}
+
+int crispy_ctx_destroy(crispy_ctx* ctx) {
+    if (!ctx) return CRISPY_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    KmerJob& k = ctx->kmer;
+    for (DevBuf* b : {&k.seq, &k.off, &k.len, &k.t, &k.gstart, &k.gent, &k.ent, &k.cntmax,
+                      &k.hinfo, &k.keys, &k.keys_alt, &k.vals, &k.vals_alt, &k.pairs, &k.dists,
+                      &k.counter, &k.mmin, &k.smin, &k.work, &k.sort_tmp})
+        release(*b);
+    GenJob& g = ctx->gen;
+    for (DevBuf* b : {&g.seq, &g.off, &g.len, &g.woff, &g.packed, &g.pairs, &g.dist, &g.score,
+                      &g.ml, &g.al, &g.flags, &g.scan, &g.blocksum, &g.surv_idx, &g.keys,
+                      &g.keys_alt, &g.vals, &g.vals_alt, &g.out_pairs, &g.out_dists, &g.order,
+                      &g.buckets, &g.queue, &g.err})
+        release(*b);
+    release_host(g.h_pairs);
+    release_host(g.h_dists);
+    for (auto* ev : {&ctx->ev_kmer, &ctx->ev_gen}) {
+        for (auto e : ev->start) cudaEventDestroy(e);
+        for (auto e : ev->stop) cudaEventDestroy(e);
+    }
+    cudaEventDestroy(ctx->t_begin);
+    cudaEventDestroy(ctx->t_end);
+    for (auto& s : ctx->side) cudaStreamDestroy(s);
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return CRISPY_OK;
+}
+
+int crispy_ctx_set_stream(crispy_ctx* ctx, void* cuda_stream) {
+    if (!ctx) return CRISPY_E_INPUT;
+    ctx->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : ctx->own_stream;
+    return CRISPY_OK;
+}
+
+const char* crispy_last_error(const crispy_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    std::lock_guard<std::mutex> g(g_err_mu);
+    return g_err.c_str();
+}
+
+int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out) {
+    if (!ctx || !out) return CRISPY_E_INPUT;
+    *out = ctx->stats;
+    return CRISPY_OK;
+}
+
+int crispy_set_timing(crispy_ctx* ctx, int enable) {
+    if (!ctx) return CRISPY_E_INPUT;
+    ctx->timing = enable != 0;
+    return CRISPY_OK;
+}
+
+}  // extern "C"

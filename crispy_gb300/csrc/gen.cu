@@ -1,0 +1,819 @@
+// gen.cu -- genDist on GB300: banded Needleman-Wunsch genetic distance.
+//
+// Reference semantics (genCPU.cpp:290-466 restated by genKernel.cu:372-780):
+// rows i = 1..L2 run over read2 = pair[1], columns j = 1..L1 over read1 =
+// pair[0]; cell (i, j) is in band iff |i - j| <= kBand, kBand =
+// (L1 + L2) / (2 * band); row 0 / column 0 cells within the band hold
+// M = 0, ML = 0, AL = index.  With up = (i, j-1), left = (i-1, j),
+//   up   = M[up]   + GO*[up was diag]   + GE*[up was up]      (out of band: -1e6)
+//   left = M[left] + GO*[left was diag] + GE*[left was left]  (out of band: -1e6)
+//   diag = M[i-1][j-1] + (symbols equal ? 5 : -4)
+//   M = max(diag, up, left), ties resolved diag > up > left;
+//   ML = diag ? ML_d - match + 1 : ML_pred + 1;  AL = AL_pred + 1.
+// The distance takes the last maximum (>=) of the last row and of the last
+// column, prefers the column-of-last-row value only when strictly larger,
+// and is (float)ML / (float)AL.  Symbols compare as 2-bit codes.
+//
+// GB300 design: one warp per pair sweeps anti-diagonals s = i + j.  The
+// band's cells on one anti-diagonal sit at d = i - j with d = s (mod 2);
+// slot q = (d + kBand) / 2 hosts them, so kBand + 1 slots cover the band and
+// a slot alternates between diagonals 2q - kBand and 2q - kBand + 1.  Lane l
+// owns C consecutive slots in registers.  Per step every slot needs its own
+// previous cell (up or left), the neighbouring slot's previous cell (the
+// other one) and its own cell two steps back (diag): one shuffle of the
+// edge slot per step.  Each cell exports M plus the two gap-penalised copies
+// M + pen_up and M + pen_left, so the receiver adds nothing.  Sequences sit
+// 2 bits per symbol in shared memory and reach the slots through 16-symbol
+// register windows refilled every 30 steps.  Steps away from the matrix
+// border run a check-free body.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace crispy {
+namespace {
+
+constexpr int kNeg = -1048576;          // below any reachable score (|M| < 45,056)
+constexpr int kRefNegInf = -1000000;    // genCPU.cpp:350 initial last-row/column maximum
+constexpr int kGO = -10, kGE = -1, kMatch = 5, kMismatch = -4;  // genMain.h:32-35
+constexpr int kGenThreads = 256;
+constexpr int kGenWarps = kGenThreads / 32;
+constexpr int kSmWords = 132;           // 128 words of 16 symbols + refill padding
+
+struct GenArgs {
+    const uint32_t* packed;
+    const int64_t* woff;
+    const int32_t* len;
+    const int2* pairs;
+    const uint32_t* order;   // optional permutation (length buckets)
+    int64_t count;
+    int band;
+    float* dist;
+    int32_t* score;
+    int32_t* ml;
+    int32_t* al;
+    unsigned int* queue;     // optional work counter (persistent launch)
+};
+
+__device__ __forceinline__ int kband_of(int l1, int l2, int band) {
+    return band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
+}
+
+// 16 symbols starting at position pos (may be negative: zeros shift in).
+__device__ __forceinline__ uint32_t window_at(const uint32_t* sm, int pos) {
+    if (pos >= 16 * (kSmWords - 2)) return 0u;   // past any read: symbols unused
+    if (pos >= 0) {
+        const int k = pos >> 4, sh = (pos & 15) * 2;
+        return sh ? (sm[k] << sh) | (sm[k + 1] >> (32 - sh)) : sm[k];
+    }
+    if (pos > -16) return sm[0] >> (-pos * 2);
+    return 0u;
+}
+
+struct Best {
+    int m;
+    uint32_t l;
+    int at;
+};
+
+__device__ __forceinline__ void track(Best& b, int m, uint32_t l, int at) {
+    if (m >= b.m) { b.m = m; b.l = l; b.at = at; }
+}
+
+// Largest m over the warp, ties to the largest index `at`; returns the
+// winner's packed ML|AL.
+__device__ __forceinline__ Best warp_best(Best b) {
+    const long long mine = (long long)b.m * 4294967296LL + (long long)(unsigned)(b.at + 1);
+    long long key = mine;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long other = __shfl_xor_sync(0xffffffffu, key, o);
+        key = other > key ? other : key;
+    }
+    const unsigned who = __ballot_sync(0xffffffffu, mine == key);
+    const int src = __ffs(who) - 1;
+    Best r;
+    r.m = (int)(key >> 32);
+    r.at = (int)(unsigned)(key & 0xffffffffu) - 1;
+    r.l = __shfl_sync(0xffffffffu, b.l, src);
+    return r;
+}
+
+template <int C>
+struct Lane {
+    int cM[C], cU[C], cF[C];
+    uint32_t cL[C];
+    int pM[C];
+    uint32_t pL[C];
+    uint32_t w1[C], w2[C];
+};
+
+// One anti-diagonal step at parity P for all C slots of this lane.
+// kChecked adds the matrix-border logic (boundary cells, cells before the
+// matrix, last-row / last-column tracking).
+template <int C, int P, bool kChecked>
+__device__ __forceinline__ void step(Lane<C>& st, int lane, int s, int kb, int l1, int l2,
+                                     uint32_t band_ok, Best& col, Best& row) {
+    int nbM;
+    uint32_t nbL;
+    if (P == 0) {
+        // left = slot q-1 (its gap-left copy), from the previous lane for c = 0
+        nbM = __shfl_up_sync(0xffffffffu, st.cF[C - 1], 1);
+        nbL = __shfl_up_sync(0xffffffffu, st.cL[C - 1], 1);
+        if (lane == 0) nbM = kNeg;
+    } else {
+        // up = slot q+1 (its gap-up copy), from the next lane for c = C-1
+        nbM = __shfl_down_sync(0xffffffffu, st.cU[0], 1);
+        nbL = __shfl_down_sync(0xffffffffu, st.cL[0], 1);
+        if (lane == 31) nbM = kNeg;
+    }
+    int nM[C], nU[C], nF[C];
+    uint32_t nL[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        int upM, lfM;
+        uint32_t upL, lfL;
+        if (P == 0) {
+            upM = st.cU[c]; upL = st.cL[c];
+            lfM = c > 0 ? st.cF[c - 1] : nbM;
+            lfL = c > 0 ? st.cL[c - 1] : nbL;
+        } else {
+            upM = c < C - 1 ? st.cU[c + 1] : nbM;
+            upL = c < C - 1 ? st.cL[c + 1] : nbL;
+            lfM = st.cF[c]; lfL = st.cL[c];
+        }
+        const bool match = (st.w1[c] ^ st.w2[c]) < 0x40000000u;
+        const int md = st.pM[c] + (match ? kMatch : kMismatch);
+        const int mx = max(md, max(upM, lfM));
+        const bool isD = mx == md;
+        const bool isU = upM >= lfM;
+        const uint32_t lpred = isU ? upL : lfL;
+        uint32_t l = isD ? st.pL[c] + (match ? 0x1u : 0x10001u) : lpred + 0x10001u;
+        int pu = isD ? kGO : (isU ? kGE : 0);
+        int pf = isD ? kGO : (isU ? 0 : kGE);
+        int m = mx;
+        const int q = lane * C + c;
+        const int d = 2 * q - kb + P;
+        if (kChecked) {
+            const int i = (s + d) >> 1, j = (s - d) >> 1;
+            if (!((band_ok >> (2 * c + P)) & 1u) || i < 0 || j < 0) {
+                m = kNeg; pu = 0; pf = 0; l = 0;
+            } else if (i == 0 || j == 0) {
+                m = 0; pu = 0; pf = 0; l = (uint32_t)(i + j);
+            } else {
+                if (i == l2 && j <= l1) track(col, m, l, j);
+                if (j == l1 && i <= l2) track(row, m, l, i);
+            }
+        } else {
+            if (!((band_ok >> (2 * c + P)) & 1u)) { m = kNeg; pu = 0; pf = 0; l = 0; }
+        }
+        nM[c] = m; nU[c] = m + pu; nF[c] = m + pf; nL[c] = l;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        st.pM[c] = st.cM[c]; st.pL[c] = st.cL[c];
+        st.cM[c] = nM[c]; st.cU[c] = nU[c]; st.cF[c] = nF[c]; st.cL[c] = nL[c];
+        if (P == 0) st.w2[c] <<= 2; else st.w1[c] <<= 2;
+    }
+}
+
+// A block of kBlockSteps steps: each 16-symbol window advances at most 15
+// times inside it (it advances on every other step), so the 16 symbols
+// loaded at the block start cover every position the block touches.
+constexpr int kBlockSteps = 30;
+
+template <int C, int P0, bool kChecked>
+__device__ __forceinline__ void block_steps(Lane<C>& st, int lane, int s0, int kb, int l1, int l2,
+                                            uint32_t band_ok, Best& col, Best& row) {
+#pragma unroll 3
+    for (int t = 0; t < kBlockSteps; t += 2) {
+        step<C, P0, kChecked>(st, lane, s0 + t, kb, l1, l2, band_ok, col, row);
+        step<C, P0 ^ 1, kChecked>(st, lane, s0 + t + 1, kb, l1, l2, band_ok, col, row);
+    }
+}
+
+template <int C, int P0>
+__device__ void align_sweep(Lane<C>& st, const uint32_t* sm1, const uint32_t* sm2, int lane,
+                            int kb, int l1, int l2, Best& col, Best& row) {
+    uint32_t band_ok = 0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const int q = lane * C + c;
+        if (2 * q - kb <= kb) band_ok |= 1u << (2 * c);          // parity 0 diagonal in band
+        if (2 * q - kb + 1 <= kb) band_ok |= 1u << (2 * c + 1);  // parity 1 diagonal in band
+    }
+    const int s_end = l1 + l2;
+    const int clean_hi = 2 * min(l1, l2) - kb - 1;
+    for (int s0 = 0; s0 <= s_end; s0 += kBlockSteps) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int d = 2 * (lane * C + c) - kb + P0;
+            const int i = (s0 + d) >> 1, j = (s0 - d) >> 1;
+            st.w2[c] = window_at(sm2, i - 1);
+            st.w1[c] = window_at(sm1, j - 1);
+        }
+        if (s0 >= kb + 2 && s0 + kBlockSteps - 1 < clean_hi)
+            block_steps<C, P0, false>(st, lane, s0, kb, l1, l2, band_ok, col, row);
+        else
+            block_steps<C, P0, true>(st, lane, s0, kb, l1, l2, band_ok, col, row);
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
+    __shared__ uint32_t smem[kGenWarps][2][kSmWords];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* sm1 = smem[warp][0];
+    uint32_t* sm2 = smem[warp][1];
+    int64_t item = a.queue ? -1 : (int64_t)blockIdx.x * kGenWarps + warp;
+    const int64_t stride = (int64_t)gridDim.x * kGenWarps;
+    for (;;) {
+        if (a.queue) {
+            unsigned w = 0;
+            if (lane == 0) w = atomicAdd(a.queue, 1u);
+            item = __shfl_sync(0xffffffffu, w, 0);
+        }
+        if (item >= a.count) break;
+        const int64_t p = a.order ? (int64_t)a.order[item] : item;
+        const int2 pr = a.pairs[p];
+        const int l1 = a.len[pr.x], l2 = a.len[pr.y];
+        const int kb = kband_of(l1, l2, a.band);
+        const int nw1 = (l1 + 15) >> 4, nw2 = (l2 + 15) >> 4;
+        const uint32_t* g1 = a.packed + a.woff[pr.x];
+        const uint32_t* g2 = a.packed + a.woff[pr.y];
+        for (int k = lane; k < kSmWords; k += 32) {
+            sm1[k] = k < nw1 ? g1[k] : 0u;
+            sm2[k] = k < nw2 ? g2[k] : 0u;
+        }
+        __syncwarp();
+        Lane<C> st;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            st.cM[c] = kNeg; st.cU[c] = kNeg; st.cF[c] = kNeg; st.cL[c] = 0;
+            st.pM[c] = kNeg; st.pL[c] = 0;
+        }
+        Best col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
+        if (kb & 1) align_sweep<C, 1>(st, sm1, sm2, lane, kb, l1, l2, col, row);
+        else align_sweep<C, 0>(st, sm1, sm2, lane, kb, l1, l2, col, row);
+        col = warp_best(col);
+        row = warp_best(row);
+        if (lane == 0) {
+            const bool use_col = col.m > row.m;   // genKernel.cu:765-768
+            const uint32_t l = use_col ? col.l : row.l;
+            const int mlv = (int)(l >> 16), alv = (int)(l & 0xffffu);
+            a.dist[p] = __fdiv_rn((float)mlv, (float)alv);
+            if (a.score) a.score[p] = use_col ? col.m : row.m;
+            if (a.ml) a.ml[p] = mlv;
+            if (a.al) a.al[p] = alv;
+        }
+        __syncwarp();
+        if (!a.queue) item += stride;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wide-band path (kBand + 1 > 32 * 8 slots, e.g. -b 1, or -b 2 on long
+// reads): one thread per pair, two band rows in global scratch, row by row
+// over band cells only.  Same recurrence and tie-breaks.  Band coordinates:
+// cell (i, j) sits at x = j - i + kBand + 1 in its row, so diag = (row-1, x),
+// left = (row-1, x+1), up = (row, x-1); x = 0 and x = 2*kBand + 2 are guard
+// slots that stay at the out-of-band sentinel.
+// ---------------------------------------------------------------------------
+struct WideArgs {
+    GenArgs g;
+    int* scratch;        // per thread: 2 rows x {M, code, ML|AL} x row_stride ints
+    int row_stride;      // 2 * kbmax + 3
+};
+
+__device__ __forceinline__ uint32_t sym_at(const uint32_t* s, int p) {
+    return (s[p >> 4] >> (30 - 2 * (p & 15))) & 3u;
+}
+
+__global__ void __launch_bounds__(128) gen_wide_kernel(WideArgs w) {
+    const GenArgs& a = w.g;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    const int rs = w.row_stride;
+    int* base = w.scratch + tid * (int64_t)rs * 6;
+    for (int64_t item = tid; item < a.count; item += nthreads) {
+        const int64_t p = a.order ? (int64_t)a.order[item] : item;
+        const int2 pr = a.pairs[p];
+        const int l1 = a.len[pr.x], l2 = a.len[pr.y];
+        const int kb = kband_of(l1, l2, a.band);
+        const int width = 2 * kb + 3;
+        const uint32_t* s1 = a.packed + a.woff[pr.x];
+        const uint32_t* s2 = a.packed + a.woff[pr.y];
+        int* rowM[2] = {base, base + 3 * rs};
+        int* rowC[2] = {base + rs, base + 4 * rs};     // 0 boundary, 1 diag, 2 left, 4 up
+        int* rowL[2] = {base + 2 * rs, base + 5 * rs};
+        for (int x = 0; x < width; ++x) { rowM[0][x] = kNeg; rowC[0][x] = 0; rowL[0][x] = 0; }
+        for (int j = 0; j <= min(kb, l1); ++j) {     // row 0 (genCPU.cpp:367-379)
+            rowM[0][j + kb + 1] = 0; rowL[0][j + kb + 1] = j;
+        }
+        Best col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
+        int cur = 0;
+        for (int i = 1; i <= l2; ++i) {
+            const int pre = cur;
+            cur ^= 1;
+            int* Mc = rowM[cur]; int* Cc = rowC[cur]; int* Lc = rowL[cur];
+            const int* Mp = rowM[pre]; const int* Cp = rowC[pre]; const int* Lp = rowL[pre];
+            for (int x = 0; x < width; ++x) { Mc[x] = kNeg; Cc[x] = 0; Lc[x] = 0; }
+            if (i <= kb) { Mc[kb - i + 1] = 0; Lc[kb - i + 1] = i; }   // column 0
+            const uint32_t c2 = sym_at(s2, i - 1);
+            const int jlo = max(1, i - kb), jhi = min(l1, i + kb);
+            for (int j = jlo; j <= jhi; ++j) {
+                const int x = j - i + kb + 1;
+                const bool match = sym_at(s1, j - 1) == c2;
+                const int md = Mp[x] + (match ? kMatch : kMismatch);
+                const int cu = Cc[x - 1], cl = Cp[x + 1];
+                const int upM = Mc[x - 1] + (cu == 1 ? kGO : (cu == 4 ? kGE : 0));
+                const int lfM = Mp[x + 1] + (cl == 1 ? kGO : (cl == 2 ? kGE : 0));
+                const int mx = max(md, max(upM, lfM));
+                uint32_t l;
+                int code;
+                if (mx == md) { code = 1; l = (uint32_t)Lp[x] + (match ? 0x1u : 0x10001u); }
+                else if (mx == upM) { code = 4; l = (uint32_t)Lc[x - 1] + 0x10001u; }
+                else { code = 2; l = (uint32_t)Lp[x + 1] + 0x10001u; }
+                Mc[x] = mx; Cc[x] = code; Lc[x] = (int)l;
+                if (i == l2) track(col, mx, l, j);
+                if (j == l1) track(row, mx, l, i);
+            }
+        }
+        const bool use_col = col.m > row.m;
+        const uint32_t l = use_col ? col.l : row.l;
+        const int mlv = (int)(l >> 16), alv = (int)(l & 0xffffu);
+        a.dist[p] = __fdiv_rn((float)mlv, (float)alv);
+        if (a.score) a.score[p] = use_col ? col.m : row.m;
+        if (a.ml) a.ml[p] = mlv;
+        if (a.al) a.al[p] = alv;
+    }
+}
+
+// 2-bit packing, 16 symbols per word, first symbol in the top bits
+// (the reference packs 4 per ushort the same way, genMain.cpp:280-321).
+__global__ void gen_pack_kernel(const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
+                                const int32_t* __restrict__ len, const int64_t* __restrict__ woff,
+                                int n, uint32_t* __restrict__ packed) {
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const int L = len[r];
+        const int nw = (L + 15) >> 4;
+        const uint8_t* s = seq + off[r];
+        for (int k = threadIdx.x; k < nw; k += blockDim.x) {
+            uint32_t w = 0;
+            for (int q = 0; q < 16; ++q) {
+                const int p = k * 16 + q;
+                uint32_t c = 0;
+                if (p < L) {
+                    const uint8_t ch = s[p];
+                    c = ch == 'G' ? 1u : ch == 'T' ? 2u : ch == 'C' ? 3u : 0u;
+                }
+                w |= c << (30 - 2 * q);
+            }
+            packed[woff[r] + k] = w;
+        }
+    }
+}
+
+// genCUDA.cu:219: keep iff dist < thr or |dist - thr| < 1e-5 (float
+// subtraction, double comparison).
+__global__ void gen_flag_kernel(const float* __restrict__ dist, int64_t n, float thr,
+                                uint8_t* __restrict__ flags) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = dist[i];
+    flags[i] = (d < thr || (double)fabsf(__fsub_rn(d, thr)) < 0.00001) ? 1 : 0;
+}
+
+__global__ void gen_keys_kernel(const float* __restrict__ dist, const uint32_t* __restrict__ surv,
+                                int64_t base, int64_t count, uint32_t* __restrict__ keys,
+                                uint32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t p = surv[base + i];
+    keys[i] = __float_as_uint(dist[p]);
+    vals[i] = p;
+}
+
+__global__ void gen_gather_kernel(const int2* __restrict__ pairs, const uint32_t* __restrict__ keys,
+                                  const uint32_t* __restrict__ vals, int64_t count,
+                                  uint2* __restrict__ out_pairs, float* __restrict__ out_dists) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int2 pr = pairs[vals[i]];
+    out_pairs[i] = make_uint2((uint32_t)pr.x, (uint32_t)pr.y);
+    out_dists[i] = __uint_as_float(keys[i]);
+}
+
+int slots_per_lane(int kb) { return (kb + 1 + 31) / 32; }
+
+// register-resident widths compiled; wider bands use gen_wide_kernel
+int bucket_c(int c) {
+    if (c <= 1) return 1;
+    if (c <= 2) return 2;
+    if (c <= 3) return 3;
+    if (c <= 4) return 4;
+    if (c <= 6) return 6;
+    if (c <= 8) return 8;
+    return 0;
+}
+
+using WarpFn = void (*)(GenArgs);
+WarpFn warp_fn(int c) {
+    switch (c) {
+        case 1: return gen_warp_kernel<1>;
+        case 2: return gen_warp_kernel<2>;
+        case 3: return gen_warp_kernel<3>;
+        case 4: return gen_warp_kernel<4>;
+        case 6: return gen_warp_kernel<6>;
+        default: return gen_warp_kernel<8>;
+    }
+}
+
+int64_t band_cells(int l1, int l2, int band) {
+    const int kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
+    // rows i = 1..l2, columns max(1, i-kb)..min(l1, i+kb)
+    int64_t cells = 0;
+    for (int i = 1; i <= l2; ++i) {
+        const int lo = std::max(1, i - kb), hi = std::min(l1, i + kb);
+        if (hi >= lo) cells += hi - lo + 1;
+    }
+    return cells;
+}
+
+}  // namespace
+
+}  // namespace crispy
+
+namespace crispy {
+
+// Plain: per 589,824-pair load window, one launch of the width the window's
+// widest pair needs (the reference launches per window and stream,
+// genCUDA.cu:156-209).  Batched: pairs bucketed by register width (the
+// length buckets), longest first, one persistent launch per bucket on a
+// device work counter.
+int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t count,
+                      int band, int mode, float* d_dist, int32_t* d_score, int32_t* d_ml,
+                      int32_t* d_al, const int32_t* h_pairs) {
+    GenJob& g = ctx->gen;
+    if (count <= 0) return CRISPY_OK;
+    std::vector<uint8_t> cls(count);
+    int kbmax = 0;
+    int64_t cells = 0;
+    for (int64_t p = 0; p < count; ++p) {
+        const int l1 = g.h_len[h_pairs[2 * p]], l2 = g.h_len[h_pairs[2 * p + 1]];
+        const int kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
+        cls[p] = (uint8_t)bucket_c(slots_per_lane(kb));
+        if (cls[p] == 0) kbmax = std::max(kbmax, kb);
+        cells += band_cells(l1, l2, band);
+    }
+    ctx->stats.gen_cells += cells;
+    ctx->stats.gen_pairs += count;
+    GenArgs base{};
+    base.packed = g.packed.as<uint32_t>();
+    base.woff = g.woff.as<int64_t>();
+    base.len = g.len.as<int32_t>();
+    base.pairs = d_pairs;
+    base.band = band;
+    base.dist = d_dist; base.score = d_score; base.ml = d_ml; base.al = d_al;
+    const int wpb = kGenWarps;
+    auto launch_wide = [&](const GenArgs& ga, const uint32_t* order, int64_t n_items) -> int {
+        const int rs = 2 * kbmax + 3;
+        const int threads = 128;
+        const int64_t want_threads = std::min<int64_t>(n_items, (int64_t)ctx->sm_count * 4 * threads);
+        const int blocks = (int)((want_threads + threads - 1) / threads);
+        CRISPY_TRY(ensure(ctx, g.buckets, (size_t)blocks * threads * rs * 6 * sizeof(int)));
+        WideArgs w{};
+        w.g = ga; w.g.order = order; w.g.count = n_items;
+        w.scratch = g.buckets.as<int>(); w.row_stride = rs;
+        ev_begin(ctx, ctx->ev_gen, s);
+        gen_wide_kernel<<<blocks, threads, 0, s>>>(w);
+        ev_end(ctx, ctx->ev_gen, s);
+        count_launch(ctx);
+        ctx->stats.gen_launches++;
+        return CRISPY_OK;
+    };
+    if (mode == CRISPY_MODE_PLAIN) {
+        // wide pairs are rare; plain mode sends every window with one to the wide kernel
+        for (int64_t w0 = 0; w0 < count; w0 += CRISPY_GEN_WINDOW) {
+            const int64_t n_items = std::min<int64_t>(CRISPY_GEN_WINDOW, count - w0);
+            int cmax = 1;
+            bool wide = false;
+            for (int64_t p = w0; p < w0 + n_items; ++p) {
+                if (cls[p] == 0) wide = true;
+                cmax = std::max<int>(cmax, cls[p]);
+            }
+            GenArgs a = base;
+            a.pairs = d_pairs + w0;
+            a.count = n_items;
+            a.dist = d_dist + w0;
+            a.score = d_score ? d_score + w0 : nullptr;
+            a.ml = d_ml ? d_ml + w0 : nullptr;
+            a.al = d_al ? d_al + w0 : nullptr;
+            if (wide) {
+                CRISPY_TRY(launch_wide(a, nullptr, n_items));
+                continue;
+            }
+            const int blocks = (int)std::min<int64_t>((n_items + wpb - 1) / wpb, (int64_t)ctx->sm_count * 8);
+            ev_begin(ctx, ctx->ev_gen, s);
+            warp_fn(cmax)<<<blocks, kGenThreads, 0, s>>>(a);
+            ev_end(ctx, ctx->ev_gen, s);
+            count_launch(ctx);
+            ctx->stats.gen_launches++;
+        }
+        CRISPY_CK(ctx, cudaGetLastError());
+        return CRISPY_OK;
+    }
+    // batched: bucket order (counting sort by class, longest pairs first inside
+    // a class so the persistent queue drains evenly)
+    const int classes[7] = {1, 2, 3, 4, 6, 8, 0};
+    std::vector<uint32_t> order(count);
+    std::vector<int64_t> start(8, 0);
+    {
+        std::vector<int64_t> cnt(9, 0);
+        for (int64_t p = 0; p < count; ++p) cnt[cls[p]]++;
+        int64_t at = 0;
+        for (int ci = 0; ci < 7; ++ci) {
+            start[ci] = at;
+            at += cnt[classes[ci]];
+        }
+        start[7] = at;
+        std::vector<int64_t> fill(start.begin(), start.end());
+        std::vector<int> slot(9, -1);
+        for (int ci = 0; ci < 7; ++ci) slot[classes[ci]] = ci;
+        for (int64_t p = 0; p < count; ++p) order[fill[slot[cls[p]]]++] = (uint32_t)p;
+    }
+    CRISPY_TRY(ensure(ctx, g.order, (size_t)count * 4));
+    CRISPY_TRY(ensure(ctx, g.queue, 64));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.order.ptr, order.data(), (size_t)count * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemsetAsync(g.queue.ptr, 0, 64, s));
+    for (int ci = 0; ci < 7; ++ci) {
+        const int64_t n_items = start[ci + 1] - start[ci];
+        if (n_items == 0) continue;
+        const uint32_t* ord = g.order.as<uint32_t>() + start[ci];
+        if (classes[ci] == 0) {
+            CRISPY_TRY(launch_wide(base, ord, n_items));
+            continue;
+        }
+        GenArgs a = base;
+        a.order = ord;
+        a.count = n_items;
+        a.queue = g.queue.as<unsigned int>() + ci;
+        int per_sm = 1;
+        WarpFn fn = warp_fn(classes[ci]);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGenThreads, 0);
+        const int blocks = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
+                                                  (n_items + wpb - 1) / wpb);
+        ev_begin(ctx, ctx->ev_gen, s);
+        fn<<<blocks, kGenThreads, 0, s>>>(a);
+        ev_end(ctx, ctx->ev_gen, s);
+        count_launch(ctx);
+        ctx->stats.gen_launches++;
+    }
+    CRISPY_CK(ctx, cudaGetLastError());
+    return CRISPY_OK;
+}
+
+}  // namespace crispy
+
+using namespace crispy;
+
+namespace {
+
+int gen_check_pairs(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs) {
+    const int n = ctx->gen.n;
+    for (int64_t p = 0; p < 2 * npairs; ++p)
+        if (pairs[p] < 0 || pairs[p] >= n)
+            return fail(ctx, CRISPY_E_INPUT, "pair %lld holds read index %d outside [0, %d)",
+                        (long long)(p / 2), pairs[p], n);
+    return CRISPY_OK;
+}
+
+// Threshold, windows, chunking, stable sort; delivers chunks to the sink.
+int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npairs, float thr,
+               crispy_sink sink, void* user, int64_t* nsurv) {
+    GenJob& g = ctx->gen;
+    *nsurv = 0;
+    if (npairs == 0) return CRISPY_OK;
+    CRISPY_TRY(ensure(ctx, g.flags, (size_t)npairs));
+    CRISPY_TRY(ensure(ctx, g.surv_idx, (size_t)npairs * 4));
+    const int64_t ntiles = (npairs + kScanTile - 1) / kScanTile;
+    CRISPY_TRY(ensure(ctx, g.blocksum, (size_t)ntiles * 4));
+    gen_flag_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, s>>>(g.dist.as<float>(), npairs, thr,
+                                                                   g.flags.as<uint8_t>());
+    count_launch(ctx);
+    int64_t total = 0;
+    CRISPY_TRY(compact_flags(ctx, s, g.flags.as<uint8_t>(), npairs, g.surv_idx.as<uint32_t>(),
+                             g.blocksum.as<uint32_t>(), g.scan, &total));
+    std::vector<uint32_t> tile_counts(ntiles);
+    CRISPY_CK(ctx, cudaMemcpyAsync(tile_counts.data(), g.blocksum.ptr, (size_t)ntiles * 4,
+                                   cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    // chunk boundaries: genCUDA.cu:156-254 -- after each load window, flush
+    // when the accumulated survivors reach the window size
+    const int64_t tiles_per_window = CRISPY_GEN_WINDOW / kScanTile;
+    std::vector<std::pair<int64_t, int64_t>> chunks;
+    int64_t at = 0, pending = 0;
+    for (int64_t t0 = 0; t0 < ntiles; t0 += tiles_per_window) {
+        for (int64_t t = t0; t < std::min(ntiles, t0 + tiles_per_window); ++t) pending += tile_counts[t];
+        if (pending >= CRISPY_GEN_WINDOW) {
+            chunks.push_back({at, pending});
+            at += pending;
+            pending = 0;
+        }
+    }
+    if (pending > 0) chunks.push_back({at, pending});
+    int64_t maxc = 0;
+    for (auto& c : chunks) maxc = std::max(maxc, c.second);
+    CRISPY_TRY(ensure(ctx, g.keys, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    CRISPY_TRY(ensure(ctx, g.keys_alt, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    CRISPY_TRY(ensure(ctx, g.vals, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    CRISPY_TRY(ensure(ctx, g.vals_alt, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    CRISPY_TRY(ensure(ctx, g.out_pairs, (size_t)std::max<int64_t>(maxc, 1) * 8));
+    CRISPY_TRY(ensure(ctx, g.out_dists, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    CRISPY_TRY(ensure_host(ctx, g.h_pairs, (size_t)std::max<int64_t>(maxc, 1) * 8));
+    CRISPY_TRY(ensure_host(ctx, g.h_dists, (size_t)std::max<int64_t>(maxc, 1) * 4));
+    for (size_t ci = 0; ci < chunks.size(); ++ci) {
+        const int64_t b = chunks[ci].first, c = chunks[ci].second;
+        const unsigned blocks = (unsigned)((c + 255) / 256);
+        gen_keys_kernel<<<blocks, 256, 0, s>>>(g.dist.as<float>(), g.surv_idx.as<uint32_t>(), b, c,
+                                              g.keys.as<uint32_t>(), g.vals.as<uint32_t>());
+        count_launch(ctx);
+        uint32_t *sk = nullptr, *sv = nullptr;
+        // distances lie in [0, 1]: 30 significant bits
+        CRISPY_TRY(sort_u32_payload(ctx, s, g.keys.as<uint32_t>(), g.keys_alt.as<uint32_t>(),
+                                    g.vals.as<uint32_t>(), g.vals_alt.as<uint32_t>(), c, 32, &sk,
+                                    &sv, g.scan));
+        gen_gather_kernel<<<blocks, 256, 0, s>>>(d_pairs, sk, sv, c, g.out_pairs.as<uint2>(),
+                                                g.out_dists.as<float>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+        if (sink) {
+            CRISPY_CK(ctx, cudaMemcpyAsync(g.h_pairs.ptr, g.out_pairs.ptr, (size_t)c * 8, cudaMemcpyDeviceToHost, s));
+            CRISPY_CK(ctx, cudaMemcpyAsync(g.h_dists.ptr, g.out_dists.ptr, (size_t)c * 4, cudaMemcpyDeviceToHost, s));
+            CRISPY_CK(ctx, cudaStreamSynchronize(s));
+            if (sink(user, (int)ci, g.h_pairs.ptr, g.h_dists.as<float>(), c) != 0)
+                return fail(ctx, CRISPY_E_IO, "sink aborted at chunk %zu", ci);
+        }
+    }
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    *nsurv = total;
+    return CRISPY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int crispy_gen_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offsets,
+                       const int32_t* lengths, int n) {
+    if (!ctx) return CRISPY_E_INPUT;
+    if (!seqbuf || !offsets || !lengths || n <= 0)
+        return fail(ctx, CRISPY_E_INPUT, "gen_prepare: empty or NULL read set");
+    if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
+    cudaSetDevice(ctx->device);
+    GenJob& g = ctx->gen;
+    g.ready = false;
+    g.n = n;
+    g.h_len.assign(lengths, lengths + n);
+    g.h_woff.resize(n + 1);
+    int64_t end = 0, words = 0;
+    g.max_len = 0;
+    for (int r = 0; r < n; ++r) {
+        if (lengths[r] > CRISPY_MAX_READ_LEN)
+            return fail(ctx, CRISPY_E_UNSUPPORTED, "read %d length %d > %d", r, lengths[r], CRISPY_MAX_READ_LEN);
+        if (lengths[r] <= 0 || offsets[r] < 0) return fail(ctx, CRISPY_E_INPUT, "read %d is empty", r);
+        g.h_woff[r] = words;
+        words += (lengths[r] + 15) / 16;
+        end = std::max(end, offsets[r] + lengths[r]);
+        g.max_len = std::max(g.max_len, (int)lengths[r]);
+    }
+    g.h_woff[n] = words;
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, g.seq, (size_t)end + 16));
+    CRISPY_TRY(ensure(ctx, g.off, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, g.len, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, g.woff, (size_t)(n + 1) * 8));
+    CRISPY_TRY(ensure(ctx, g.packed, (size_t)(words + 4) * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.len.ptr, lengths, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.woff.ptr, g.h_woff.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    gen_pack_kernel<<<std::min(n, ctx->sm_count * 16), 128, 0, s>>>(
+        g.seq.as<uint8_t>(), g.off.as<int64_t>(), g.len.as<int32_t>(), g.woff.as<int64_t>(), n,
+        g.packed.as<uint32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    g.ready = true;
+    return CRISPY_OK;
+}
+
+int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int band, int mode,
+                     float* dist, int32_t* score, int32_t* ml, int32_t* al) {
+    if (!ctx) return CRISPY_E_INPUT;
+    GenJob& g = ctx->gen;
+    if (!g.ready) return fail(ctx, CRISPY_E_STATE, "gen_align before gen_prepare");
+    if (npairs < 0 || (npairs > 0 && !pairs)) return fail(ctx, CRISPY_E_INPUT, "bad pair list");
+    if (band <= 0) band = 2;
+    CRISPY_TRY(gen_check_pairs(ctx, pairs, npairs));
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    ctx->stats = crispy_stats{};
+    ctx->ev_gen.used = 0;
+    if (npairs == 0) return CRISPY_OK;
+    CRISPY_TRY(ensure(ctx, g.pairs, (size_t)npairs * 8));
+    CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
+    CRISPY_TRY(ensure(ctx, g.score, (size_t)npairs * 4));
+    CRISPY_TRY(ensure(ctx, g.ml, (size_t)npairs * 4));
+    CRISPY_TRY(ensure(ctx, g.al, (size_t)npairs * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, pairs, (size_t)npairs * 8, cudaMemcpyHostToDevice, s));
+    CRISPY_TRY(gen_dispatch_impl(ctx, s, g.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
+                                 g.score.as<int32_t>(), g.ml.as<int32_t>(), g.al.as<int32_t>(), pairs));
+    if (dist) CRISPY_CK(ctx, cudaMemcpyAsync(dist, g.dist.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
+    if (score) CRISPY_CK(ctx, cudaMemcpyAsync(score, g.score.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
+    if (ml) CRISPY_CK(ctx, cudaMemcpyAsync(ml, g.ml.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
+    if (al) CRISPY_CK(ctx, cudaMemcpyAsync(al, g.al.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    ctx->stats.gen_kernel_ms = ev_sum_ms(ctx->ev_gen);
+    return CRISPY_OK;
+}
+
+int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int band, float thr,
+                   int mode, crispy_sink sink, void* user, int64_t* nsurvivors) {
+    if (!ctx) return CRISPY_E_INPUT;
+    GenJob& g = ctx->gen;
+    if (!g.ready) return fail(ctx, CRISPY_E_STATE, "gen_run before gen_prepare");
+    if (npairs < 0 || (npairs > 0 && !pairs)) return fail(ctx, CRISPY_E_INPUT, "bad pair list");
+    if (band <= 0) band = 2;   // genMain.cpp:356-364
+    CRISPY_TRY(gen_check_pairs(ctx, pairs, npairs));
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    ctx->stats = crispy_stats{};
+    ctx->ev_gen.used = 0;
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
+    int64_t ns = 0;
+    if (npairs > 0) {
+        CRISPY_TRY(ensure(ctx, g.pairs, (size_t)npairs * 8));
+        CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
+        CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, pairs, (size_t)npairs * 8, cudaMemcpyHostToDevice, s));
+        CRISPY_TRY(gen_dispatch_impl(ctx, s, g.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
+                                     nullptr, nullptr, nullptr, pairs));
+        CRISPY_TRY(gen_finish(ctx, s, g.pairs.as<int2>(), npairs, thr, sink, user, &ns));
+    }
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->t_begin, ctx->t_end);
+    ctx->stats.total_ms = tot;
+    ctx->stats.gen_kernel_ms = ev_sum_ms(ctx->ev_gen);
+    ctx->stats.gen_survivors = ns;
+    if (nsurvivors) *nsurvivors = ns;
+    return CRISPY_OK;
+}
+
+int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, crispy_sink sink,
+                             void* user, int64_t* nsurvivors) {
+    if (!ctx) return CRISPY_E_INPUT;
+    GenJob& g = ctx->gen;
+    KmerJob& k = ctx->kmer;
+    if (!g.ready || !k.ready) return fail(ctx, CRISPY_E_STATE, "gen_run_from_kmer needs kmer_run and gen_prepare");
+    if (g.n != k.n) return fail(ctx, CRISPY_E_STATE, "kmer and gen read sets differ (%d vs %d reads)", k.n, g.n);
+    if (band <= 0) band = 2;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const int64_t npairs = k.nsurv;
+    // the bucketing needs read lengths per pair on the host
+    std::vector<int32_t> hp((size_t)npairs * 2);
+    if (npairs > 0)
+        CRISPY_CK(ctx, cudaMemcpyAsync(hp.data(), k.pairs.ptr, (size_t)npairs * 8, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    const crispy_stats kst = ctx->stats;
+    ctx->stats = crispy_stats{};
+    ctx->ev_gen.used = 0;
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
+    int64_t ns = 0;
+    if (npairs > 0) {
+        CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
+        CRISPY_TRY(gen_dispatch_impl(ctx, s, k.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
+                                     nullptr, nullptr, nullptr, hp.data()));
+        CRISPY_TRY(gen_finish(ctx, s, k.pairs.as<int2>(), npairs, thr, sink, user, &ns));
+    }
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->t_begin, ctx->t_end);
+    ctx->stats.total_ms = tot;
+    ctx->stats.gen_kernel_ms = ev_sum_ms(ctx->ev_gen);
+    ctx->stats.gen_survivors = ns;
+    ctx->stats.kmer_kernel_ms = kst.kmer_kernel_ms;
+    ctx->stats.kmer_pairs = kst.kmer_pairs;
+    ctx->stats.kmer_survivors = kst.kmer_survivors;
+    if (nsurvivors) *nsurvivors = ns;
+    return CRISPY_OK;
+}
+
+}  // extern "C"

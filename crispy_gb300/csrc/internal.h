@@ -1,0 +1,129 @@
+// internal.h -- host-side state shared by the translation units of
+// libcrispy_gb300.so.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/crispy_gb300.h"
+
+namespace crispy {
+
+// Grow-only device allocation owned by a context.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Grow-only pinned host allocation owned by a context.
+struct HostBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Device-resident k-mer job: the reads of one kmerDist invocation.
+struct KmerJob {
+    bool ready = false;
+    int n = 0, k = 0, max_len = 0, max_t = 0;
+    int ngroups = 0;            // 32-read groups
+    int64_t nent = 0;           // entries in the interleaved level-entry array
+    std::vector<int32_t> h_t;   // tuples per read (L - K + 1)
+    std::vector<int32_t> h_cntmax;   // largest k-mer multiplicity per read
+    std::vector<int64_t> h_gstart;   // first entry of each group
+    std::vector<int32_t> h_gent;     // entries per lane in each group (multiple of 16)
+    DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo;
+    // last run's survivors, in stage order
+    int64_t nsurv = 0;
+    bool have_dists = false;
+    DevBuf keys, keys_alt, vals, vals_alt, pairs, dists, counter, mmin, smin, work;
+    DevBuf sort_tmp;
+};
+
+// Device-resident genDist job: 2-bit packed reads.
+struct GenJob {
+    bool ready = false;
+    int n = 0, max_len = 0;
+    std::vector<int32_t> h_len;
+    std::vector<int64_t> h_woff;     // first packed word of each read
+    DevBuf seq, off, len, woff, packed;
+    DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
+        vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err;
+    HostBuf h_pairs, h_dists;
+};
+
+struct StreamEvents {
+    std::vector<cudaEvent_t> start, stop;
+    size_t used = 0;
+};
+
+}  // namespace crispy
+
+struct crispy_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t side[8] = {};
+    bool timing = false;
+    std::string err;
+    crispy_stats stats{};
+    crispy::KmerJob kmer;
+    crispy::GenJob gen;
+    crispy::StreamEvents ev_kmer, ev_gen;
+    cudaEvent_t t_begin = nullptr, t_end = nullptr;
+    // autotuned parameters, keyed by workload shape (see tune.cu)
+    int kmer_chunk_groups = 0;   // column groups per batched work item (0 = auto)
+    int gen_warps_per_block = 0;
+};
+
+namespace crispy {
+
+int fail(crispy_ctx* ctx, int code, const char* fmt, ...);
+int cuda_fail(crispy_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
+int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes);
+int ensure_host(crispy_ctx* ctx, HostBuf& b, size_t bytes);
+void release(DevBuf& b);
+void release_host(HostBuf& b);
+
+// Event pair around a launch, when timing is enabled.
+cudaEvent_t ev_begin(crispy_ctx* ctx, StreamEvents& ev, cudaStream_t s);
+void ev_end(crispy_ctx* ctx, StreamEvents& ev, cudaStream_t s);
+double ev_sum_ms(StreamEvents& ev);
+
+// kernel counter (every launch of this library increments it)
+void count_launch(crispy_ctx* ctx, int n = 1);
+
+// radix sort / scan helpers (sort.cu)
+int sort_u64_payload(crispy_ctx* ctx, cudaStream_t s, uint64_t* keys, uint64_t* keys_alt,
+                     uint32_t* vals, uint32_t* vals_alt, int64_t n, int key_bits,
+                     bool with_vals, uint64_t** sorted_keys, uint32_t** sorted_vals,
+                     DevBuf& tmp);
+int sort_u32_payload(crispy_ctx* ctx, cudaStream_t s, uint32_t* keys, uint32_t* keys_alt,
+                     uint32_t* vals, uint32_t* vals_alt, int64_t n, int key_bits,
+                     uint32_t** sorted_keys, uint32_t** sorted_vals, DevBuf& tmp);
+// Stable compaction of indices with flag != 0; per-tile counts returned on
+// the device in tile_counts (tile = kScanTile items).
+constexpr int kScanTile = 4608;   // divides the 589,824-pair window (128 tiles)
+int compact_flags(crispy_ctx* ctx, cudaStream_t s, const uint8_t* flags, int64_t n,
+                  uint32_t* out_idx, uint32_t* tile_counts, DevBuf& tmp, int64_t* total);
+
+}  // namespace crispy
+
+#define CRISPY_CK(ctx, call)                                                        \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) return crispy::cuda_fail(ctx, e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define CRISPY_TRY(call)                 \
+    do {                                 \
+        int rc_ = (call);                \
+        if (rc_ != CRISPY_OK) return rc_; \
+    } while (0)

@@ -1,0 +1,818 @@
+// kmer.cu -- kmerDist on GB300: all-pairs k-mer distance with the cut
+// threshold and sparse-pair compaction fused into the tile kernel.
+//
+// Reference semantics (kmerMain.cpp:117-216, kmerKernel.cu:19-51,
+// kmerCUDA.cu:14-126): each read's K-mers are 2-bit codes (A0 G1 T2 C3,
+// others 0) over T = L-K+1 windows; the count of shared K-mers between two
+// reads is the sorted-merge count, which for K <= 7 equals the multiset
+// min-sum  m = sum_k min(cnt_a[k], cnt_b[k]);  dist = 1 - m / min(Ta, Tb) in
+// single precision; a pair survives iff dist < thr or |dist - thr| < 1e-5.
+//
+// GB300 design (no tensor cores: a min-sum is not a dense contraction):
+//   * min(a, b) = sum_{t>=1} [a >= t][b >= t].  Every read becomes a list of
+//     T "level entries" (t-1)*4^K + kmer, one per occurrence, where t is the
+//     occurrence rank of that K-mer in the read.  Then
+//         m(a, b) = #{ entries e of b : P_a[e] }   with P_a = entry set of a.
+//   * A block owns 32 row reads and keeps their entry sets in shared memory
+//     as bit planes: word P[e] has bit r set iff row read r holds entry e.
+//     One 32-bit shared load answers one column entry for 32 row reads.
+//   * A warp owns 32 column reads (one per lane) and streams their entries
+//     from an interleaved layout (entry e of the 32 reads of a group is one
+//     128-byte line), gathers P[e], and adds the word into 32 bit-sliced
+//     counters with a Harley-Seal carry-save tree (LOP3 work only).
+//   * The threshold is an integer test m >= mmin[min(Ta, Tb)], with mmin
+//     tabulated on the host from the reference's float expression (the pass
+//     predicate is monotone in m), first as a bit-sliced compare against a
+//     per-lane lower bound, then exactly for the few candidates.  Survivors
+//     leave through warp-aggregated atomics as (stage, row, col) sort keys;
+//     one stable radix sort restores the reference's stage order.
+//   * Rows whose K-mer multiplicity exceeds the shared-memory level budget,
+//     and K = 8 (whose reference count is not the min-sum, see
+//     kmer_dense_kernel), run through an exact dense-table kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace crispy {
+namespace {
+
+constexpr uint32_t kSentinel = 0xFFFFFFFFu;
+constexpr int kTileThreads = 256;
+constexpr int kTileWarps = kTileThreads / 32;
+constexpr int kSmemBudget = 200 * 1024;
+
+__device__ __forceinline__ uint32_t sym2(uint8_t c) {
+    // A=0 G=1 T=2 C=3, everything else 0 (kmerMain.cpp:137-152)
+    return c == 'G' ? 1u : c == 'T' ? 2u : c == 'C' ? 3u : 0u;
+}
+
+__device__ __forceinline__ uint32_t kmer_at(const uint8_t* s, int p, int K) {
+    uint32_t v = 0;
+    for (int q = 0; q < K; ++q) v = (v << 2) | sym2(s[p + q]);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Preparation: one block per read.  Occurrence ranks come from a shared
+// histogram with two 16-bit counters per word (counts <= 2048), so K = 8
+// (65,536 bins) fits in 128 KB.  Writes the read's level entries into its
+// lane of the group's interleaved block, its largest multiplicity, and for
+// K = 8 the (largest K-mer >= 0x8000, its count) key used by the quirk.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) kmer_prep_kernel(
+    const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
+    const int32_t* __restrict__ tcount, int n, int K, const int64_t* __restrict__ gstart,
+    const int32_t* __restrict__ gent, uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax,
+    uint32_t* __restrict__ hinfo) {
+    extern __shared__ uint32_t hist[];
+    __shared__ int s_max;
+    __shared__ uint32_t s_hmax;
+    const uint32_t K4 = 1u << (2 * K);
+    const int hwords = (int)((K4 + 1) / 2);
+    for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; }
+        __syncthreads();
+        const int T = tcount[r];
+        const uint8_t* s = seq + off[r];
+        uint32_t* dst = ent + gstart[r >> 5] + (r & 31);
+        const int E = gent[r >> 5];
+        for (int p = threadIdx.x; p < T; p += blockDim.x) {
+            const uint32_t v = kmer_at(s, p, K);
+            const uint32_t sh = (v & 1u) * 16u;
+            const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
+            const uint32_t t = (old >> sh) & 0xFFFFu;
+            dst[(int64_t)p * 32] = t * K4 + v;
+        }
+        for (int p = T + threadIdx.x; p < E; p += blockDim.x) dst[(int64_t)p * 32] = kSentinel;
+        __syncthreads();
+        int mx = 0;
+        uint32_t hm = 0;
+        for (int p = threadIdx.x; p < T; p += blockDim.x) {
+            const uint32_t v = kmer_at(s, p, K);
+            const int c = (int)((hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu);
+            mx = max(mx, c);
+            if (v >= 0x8000u) hm = max(hm, v);
+        }
+        atomicMax(&s_max, mx);
+        atomicMax(&s_hmax, hm);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cntmax[r] = s_max;
+            uint32_t info = 0;
+            if (K == 8 && s_hmax >= 0x8000u) {
+                const uint32_t c = (hist[s_hmax >> 1] >> ((s_hmax & 1u) * 16u)) & 0xFFFFu;
+                info = (s_hmax << 16) | c;
+            }
+            hinfo[r] = info;
+        }
+        __syncthreads();
+        for (int p = threadIdx.x; p < T; p += blockDim.x) hist[kmer_at(s, p, K) >> 1] = 0;
+        __syncthreads();
+    }
+}
+
+struct TileArgs {
+    const uint32_t* ent;
+    const int64_t* gstart;
+    const int32_t* gent;
+    const int32_t* tcount;
+    const int32_t* cntmax;
+    const uint16_t* mmin;
+    const uint16_t* smin;
+    int n;
+    uint32_t K4;
+    int levels_cap;   // level planes that fit the dynamic shared memory
+    int A, stage_dim;
+    unsigned long long* counter;
+    uint64_t* keys;
+    uint32_t* vals;
+    int64_t cap;
+    // plain: one rectangle of rows x cols (one reference stage)
+    int r_lo, r_hi, c_lo, c_hi;
+    // batched: work queue of (row group, first col group, end col group)
+    const int4* items;
+    int nitems;
+    unsigned int* queue_head;
+};
+
+__device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
+    const uint32_t u = l ^ a;
+    h = (l & a) | (u & b);
+    l = u ^ b;
+}
+
+__device__ __forceinline__ uint64_t stage_key(int r, int c, int n, int A, int sd) {
+    // kmerCUDA.cu:79-111 + Trag_reverse_eq (kmerMain.cpp:205-216): stages
+    // enumerate the upper triangle of the stageDim grid row-major; inside a
+    // stage the host scan is row-major (kmerMain.cpp:175-195).
+    const int64_t sx = r / A, sy = c / A;
+    const int64_t s = sx * sd - sx * (sx - 1) / 2 + (sy - sx);
+    return ((uint64_t)s * (uint64_t)n + (uint64_t)r) * (uint64_t)n + (uint64_t)c;
+}
+
+// Survivor emission with one atomic per warp.  All 32 lanes call it.
+__device__ __forceinline__ void emit(const TileArgs& a, bool pass, int r, int c, int m, int mn) {
+    const unsigned pm = __ballot_sync(0xffffffffu, pass);
+    if (!pm) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    const int leader = __ffs(pm) - 1;
+    if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(pm));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pass) {
+        const unsigned long long idx = base + __popc(pm & ((1u << lane) - 1u));
+        if (idx < (unsigned long long)a.cap) {
+            a.keys[idx] = stage_key(r, c, a.n, a.A, a.stage_dim);
+            // kmerKernel.cu:47: 1.0f - (float)matches / min(T1, T2), IEEE
+            const float d = __fsub_rn(1.0f, __fdiv_rn((float)m, (float)mn));
+            a.vals[idx] = __float_as_uint(d);
+        }
+    }
+}
+
+template <int B>
+__device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P, uint32_t limit,
+                             int rg, uint32_t rows_ok, int t_min, const int* s_rowT, int cg0,
+                             int cg1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = rg * 32;
+    for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
+        const int c = cg * 32 + lane;
+        const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
+        uint32_t vmask = 0;
+        if (col_ok) {
+            const int span = c - r0;  // rows r0+b < c  <=>  b < span
+            vmask = span >= 32 ? 0xffffffffu : (span <= 0 ? 0u : ((1u << span) - 1u));
+            vmask &= rows_ok;
+        }
+        if (!__any_sync(0xffffffffu, vmask)) continue;
+        const int E = a.gent[cg];
+        const uint32_t* __restrict__ ep = a.ent + a.gstart[cg] + lane;
+        uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
+        uint32_t S[B - 4];
+#pragma unroll
+        for (int k = 0; k < B - 4; ++k) S[k] = 0;
+        for (int e = 0; e < E; e += 16) {
+            uint32_t w[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const uint32_t idx = __ldg(ep + (int64_t)(e + q) * 32);
+                w[q] = idx < limit ? P[idx] : 0u;
+            }
+            uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+            csa(twosA, ones, w[0], w[1]);
+            csa(twosB, ones, w[2], w[3]);
+            csa(foursA, twos, twosA, twosB);
+            csa(twosA, ones, w[4], w[5]);
+            csa(twosB, ones, w[6], w[7]);
+            csa(foursB, twos, twosA, twosB);
+            csa(eightsA, fours, foursA, foursB);
+            csa(twosA, ones, w[8], w[9]);
+            csa(twosB, ones, w[10], w[11]);
+            csa(foursA, twos, twosA, twosB);
+            csa(twosA, ones, w[12], w[13]);
+            csa(twosB, ones, w[14], w[15]);
+            csa(foursB, twos, twosA, twosB);
+            csa(eightsB, fours, foursA, foursB);
+            csa(sixteens, eights, eightsA, eightsB);
+            uint32_t carry = sixteens;
+#pragma unroll
+            for (int k = 0; k < B - 4; ++k) {
+                const uint32_t t = S[k] & carry;
+                S[k] ^= carry;
+                carry = t;
+            }
+        }
+        // bit planes X[k] of the 32 per-row counts
+        uint32_t X[B];
+        X[0] = X[1] = X[2] = X[3] = 0;
+#pragma unroll
+        for (int k = 4; k < B; ++k) X[k] = S[k - 4];
+        auto add_at = [&](uint32_t v, int p) {
+            uint32_t carry = v;
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                if (k >= p) {
+                    const uint32_t t = X[k] & carry;
+                    X[k] ^= carry;
+                    carry = t;
+                }
+            }
+        };
+        add_at(eights, 3);
+        add_at(fours, 2);
+        add_at(twos, 1);
+        add_at(ones, 0);
+        // candidates: count >= a lower bound of mmin over the lane's pairs
+        const int tc = col_ok ? a.tcount[c] : 0;
+        const uint32_t lo = a.smin[min(t_min, tc)];
+        uint32_t cand = 0;
+        if (vmask && lo < (1u << B)) {
+            uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+            for (int k = B - 1; k >= 0; --k) {
+                const uint32_t bit = 0u - ((lo >> k) & 1u);
+                gt |= eq & X[k] & ~bit;
+                eq &= ~(X[k] ^ bit);
+            }
+            cand = (gt | eq) & vmask;
+        }
+        while (__any_sync(0xffffffffu, cand)) {
+            bool pass = false;
+            int r = 0, m = 0, mn = 1;
+            if (cand) {
+                const int b = __ffs(cand) - 1;
+                cand &= cand - 1;
+#pragma unroll
+                for (int k = 0; k < B; ++k) m |= (int)((X[k] >> b) & 1u) << k;
+                r = r0 + b;
+                mn = min(s_rowT[b], tc);
+                pass = m >= (int)a.mmin[mn];
+            }
+            emit(a, pass, r, c, m, mn);
+        }
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(kTileThreads) kmer_tile_kernel(TileArgs a) {
+    extern __shared__ __align__(16) uint32_t P[];
+    __shared__ int s_rowT[32];
+    __shared__ int s_cm[32];
+    __shared__ int s_item[4];
+    __shared__ int s_L, s_tmin;
+    __shared__ uint32_t s_rows_ok;
+    const bool queued = a.items != nullptr;
+    int cur_rg = -1, cur_L = 0;
+    for (int it = queued ? -1 : 0;; ) {
+        // ---- fetch work ----
+        if (threadIdx.x == 0) {
+            if (queued) {
+                const unsigned w = atomicAdd(a.queue_head, 1u);
+                if ((int)w < a.nitems) {
+                    const int4 q = a.items[w];
+                    s_item[0] = q.x; s_item[1] = q.y; s_item[2] = q.z; s_item[3] = 1;
+                } else {
+                    s_item[3] = 0;
+                }
+            } else {
+                s_item[0] = a.r_lo / 32 + blockIdx.x;
+                s_item[1] = a.c_lo / 32;
+                s_item[2] = (a.c_hi + 31) / 32;
+                s_item[3] = it == 0 ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        if (!s_item[3]) break;
+        const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
+        ++it;
+        const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
+        if (rg != cur_rg) {
+            // ---- row group set-up: multiplicities, lengths, planes ----
+            if (threadIdx.x < 32) {
+                const int r = rg * 32 + threadIdx.x;
+                const bool ok = r >= rlo && r < rhi;
+                const int tr = ok ? a.tcount[r] : INT_MAX;
+                const int cm = ok ? a.cntmax[r] : 0;
+                s_rowT[threadIdx.x] = tr;
+                s_cm[threadIdx.x] = cm;
+                const unsigned okm = __ballot_sync(0xffffffffu, ok);
+                const int L = __reduce_max_sync(0xffffffffu, (unsigned)cm);
+                const int tm = __reduce_min_sync(0xffffffffu, (unsigned)tr);
+                if (threadIdx.x == 0) { s_L = L; s_tmin = tm; s_rows_ok = okm; }
+            }
+            __syncthreads();
+            cur_rg = rg;
+            cur_L = s_L;
+            if (cur_L > a.levels_cap) {   // handled by kmer_dense_kernel
+                __syncthreads();
+                continue;
+            }
+            const int words = cur_L * (int)a.K4;
+            uint4* P4 = reinterpret_cast<uint4*>(P);
+            for (int i = threadIdx.x; i < (words + 3) / 4; i += kTileThreads)
+                P4[i] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            for (int b = warp; b < 32; b += kTileWarps) {
+                if (!((s_rows_ok >> b) & 1u)) continue;
+                const int r = rg * 32 + b;
+                const uint32_t* src = a.ent + a.gstart[rg] + b;
+                const int T = s_rowT[b];
+                for (int e = lane; e < T; e += 32) atomicOr(&P[src[(int64_t)e * 32]], 1u << b);
+                (void)r;
+            }
+            __syncthreads();
+        }
+        if (cur_L <= a.levels_cap) {
+            tile_columns<B>(a, P, (uint32_t)cur_L * a.K4, rg, s_rows_ok, s_tmin, s_rowT,
+                            max(cg0, rg), cg1);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exact dense-table kernel: one row read per block with its full count
+// table (two 16-bit counts per word) in shared memory; one column per
+// thread walks its level entries (t, kmer) and counts [cnt_row[kmer] > t].
+// Covers any K <= 8 and any multiplicity.  For K = 8 the reference's merge
+// compares unsigned values over lists sorted as signed shorts
+// (kmerMain.cpp:275-278 vs kmerKernel.cu:37-45), which yields
+//     m = minsum(H) + [same] * minsum(L)
+// with H = K-mers >= 0x8000, L = the rest, and [same] true iff both reads
+// have no H K-mer or both have the same largest H K-mer with the same
+// multiplicity.  The kernel keeps the two partial sums apart for that.
+// ---------------------------------------------------------------------------
+struct DenseArgs {
+    const uint8_t* seq;
+    const int64_t* off;
+    const uint32_t* ent;
+    const int64_t* gstart;
+    const int32_t* tcount;
+    const int32_t* cntmax;
+    const uint32_t* hinfo;
+    const uint16_t* mmin;
+    int n, K;
+    int levels_cap;   // rows of groups whose level need is <= this are skipped
+    int r_lo, r_hi, c_lo, c_hi;
+    int A, stage_dim;
+    const uint8_t* heavy_group;   // nullptr: every row
+    unsigned long long* counter;
+    uint64_t* keys;
+    uint32_t* vals;
+    int64_t cap;
+};
+
+__global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
+    extern __shared__ uint32_t hist[];
+    const uint32_t K4 = 1u << (2 * a.K);
+    const int hwords = (int)((K4 + 1) / 2);
+    for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    TileArgs ta{};
+    ta.n = a.n; ta.A = a.A; ta.stage_dim = a.stage_dim; ta.counter = a.counter;
+    ta.keys = a.keys; ta.vals = a.vals; ta.cap = a.cap;
+    for (int r = a.r_lo + blockIdx.x; r < a.r_hi && r < a.n; r += gridDim.x) {
+        if (a.heavy_group && !a.heavy_group[r >> 5]) continue;   // uniform per block
+        const int Tr = a.tcount[r];
+        const uint8_t* s = a.seq + a.off[r];
+        for (int p = threadIdx.x; p < Tr; p += blockDim.x) {
+            const uint32_t v = kmer_at(s, p, a.K);
+            atomicAdd(&hist[v >> 1], 1u << ((v & 1u) * 16u));
+        }
+        __syncthreads();
+        const uint32_t hr = a.hinfo[r];
+        const int cstart = max(a.c_lo, r + 1);
+        const int cend = min(a.c_hi, a.n);
+        // whole warps iterate together so that emit() sees 32 lanes
+        const int span = cend - cstart;
+        const int rounds = span > 0 ? (span + blockDim.x - 1) / blockDim.x : 0;
+        for (int q = 0; q < rounds; ++q) {
+            const int c = cstart + q * blockDim.x + threadIdx.x;
+            const bool ok = c < cend;
+            int m = 0, mn = 1;
+            bool pass = false;
+            if (ok) {
+                const int Tc = a.tcount[c];
+                const uint32_t* ep = a.ent + a.gstart[c >> 5] + (c & 31);
+                int sum_lo = 0, sum_hi = 0;
+                for (int e = 0; e < Tc; ++e) {
+                    const uint32_t idx = __ldg(ep + (int64_t)e * 32);
+                    const uint32_t t = idx / K4, v = idx - t * K4;
+                    const uint32_t cnt = (hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu;
+                    const int hit = cnt > t;
+                    if (v >= 0x8000u) sum_hi += hit; else sum_lo += hit;
+                }
+                if (a.K == 8) {
+                    const uint32_t hc = a.hinfo[c];
+                    const bool same = (hr == 0 && hc == 0) || (hr != 0 && hr == hc);
+                    m = sum_hi + (same ? sum_lo : 0);
+                } else {
+                    m = sum_hi + sum_lo;
+                }
+                mn = min(Tr, Tc);
+                pass = m >= (int)a.mmin[mn];
+            }
+            emit(ta, pass, r, c, m, mn);
+        }
+        __syncthreads();
+        for (int p = threadIdx.x; p < Tr; p += blockDim.x) hist[kmer_at(s, p, a.K) >> 1] = 0;
+        __syncthreads();
+    }
+}
+
+__global__ void kmer_decode_kernel(const uint64_t* __restrict__ keys,
+                                   const uint32_t* __restrict__ vals, int64_t count, int n,
+                                   int2* __restrict__ pairs, float* __restrict__ dists) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint64_t k = keys[i];
+    const uint64_t rc = k % ((uint64_t)n * (uint64_t)n);
+    pairs[i] = make_int2((int)(rc / (uint64_t)n), (int)(rc % (uint64_t)n));
+    if (dists) dists[i] = __uint_as_float(vals[i]);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+// Pass predicate of kmerMain.cpp:180, evaluated in the reference's types.
+inline bool keep_host(float d, float thr) {
+    return d < thr || (double)std::fabs(d - thr) < 0.00001;
+}
+
+// mmin[t] = smallest m in [0, t] whose distance 1 - m/t passes, 0xFFFF if
+// none.  The predicate is monotone in m (IEEE division and subtraction are
+// monotone), so "m >= mmin[t]" is exactly the reference's test.
+void build_mmin(float thr, int max_t, std::vector<uint16_t>& mmin, std::vector<uint16_t>& smin) {
+    mmin.assign(max_t + 1, 0xFFFF);
+    for (int t = 0; t <= max_t; ++t) {
+        for (int m = 0; m <= t; ++m) {
+            volatile float q = (float)m / (float)t;
+            volatile float d = 1.0f - q;
+            if (keep_host(d, thr)) { mmin[t] = (uint16_t)m; break; }
+        }
+    }
+    smin.assign(max_t + 1, 0xFFFF);
+    uint16_t run = 0xFFFF;
+    for (int t = max_t; t >= 0; --t) {
+        run = std::min(run, mmin[t]);
+        smin[t] = run;
+    }
+}
+
+int bits_for(uint64_t v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) ++b;
+    return b;
+}
+
+int levels_cap_for(int K) {
+    const int per_level = (1 << (2 * K)) * 4;
+    if (K >= 8) return 0;
+    return std::min(16, kSmemBudget / per_level);
+}
+
+using TileFn = void (*)(TileArgs);
+TileFn tile_fn_for(int B) {
+    switch (B) {
+        case 5: return kmer_tile_kernel<5>;
+        case 6: return kmer_tile_kernel<6>;
+        case 7: return kmer_tile_kernel<7>;
+        case 8: return kmer_tile_kernel<8>;
+        case 9: return kmer_tile_kernel<9>;
+        case 10: return kmer_tile_kernel<10>;
+        case 11: return kmer_tile_kernel<11>;
+        default: return kmer_tile_kernel<12>;
+    }
+}
+
+}  // namespace
+}  // namespace crispy
+
+using namespace crispy;
+
+extern "C" {
+
+int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offsets,
+                        const int32_t* lengths, int n, int k) {
+    if (!ctx) return CRISPY_E_INPUT;
+    if (!seqbuf || !offsets || !lengths || n <= 0)
+        return fail(ctx, CRISPY_E_INPUT, "kmer_prepare: empty or NULL read set");
+    if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
+    if (k < 1 || k > 8) return fail(ctx, CRISPY_E_UNSUPPORTED, "K = %d outside 1..8", k);
+    cudaSetDevice(ctx->device);
+    KmerJob& j = ctx->kmer;
+    j.ready = false;
+    j.n = n;
+    j.k = k;
+    j.h_t.resize(n);
+    int64_t end = 0;
+    j.max_len = 0;
+    j.max_t = 0;
+    for (int r = 0; r < n; ++r) {
+        if (lengths[r] > CRISPY_MAX_READ_LEN)
+            return fail(ctx, CRISPY_E_UNSUPPORTED, "read %d length %d > %d", r, lengths[r], CRISPY_MAX_READ_LEN);
+        if (lengths[r] < k - 1 || offsets[r] < 0)
+            return fail(ctx, CRISPY_E_INPUT, "read %d length %d shorter than K-1", r, lengths[r]);
+        j.h_t[r] = lengths[r] - k + 1;
+        j.max_len = std::max(j.max_len, (int)lengths[r]);
+        j.max_t = std::max(j.max_t, j.h_t[r]);
+        end = std::max(end, offsets[r] + lengths[r]);
+    }
+    j.ngroups = (n + 31) / 32;
+    j.h_gent.assign(j.ngroups, 0);
+    j.h_gstart.assign(j.ngroups + 1, 0);
+    for (int r = 0; r < n; ++r) j.h_gent[r >> 5] = std::max(j.h_gent[r >> 5], j.h_t[r]);
+    for (int g = 0; g < j.ngroups; ++g) {
+        j.h_gent[g] = (j.h_gent[g] + 15) / 16 * 16;
+        j.h_gstart[g + 1] = j.h_gstart[g] + 32LL * j.h_gent[g];
+    }
+    j.nent = j.h_gstart[j.ngroups];
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, j.seq, (size_t)end + 16));
+    CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.gstart, (size_t)(j.ngroups + 1) * 8));
+    CRISPY_TRY(ensure(ctx, j.gent, (size_t)j.ngroups * 4));
+    CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 1) * 4));
+    CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.hinfo, (size_t)n * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.gstart.ptr, j.h_gstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.gent.ptr, j.h_gent.data(), (size_t)j.ngroups * 4,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 1) * 4, s));
+    const size_t hsmem = (size_t)(((1u << (2 * k)) + 1) / 2) * 4;
+    CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)hsmem));
+    const int grid = std::min(n, ctx->sm_count * (k >= 8 ? 1 : 8));
+    kmer_prep_kernel<<<grid, 256, hsmem, s>>>(j.seq.as<uint8_t>(), j.off.as<int64_t>(),
+                                              j.t.as<int32_t>(), n, k, j.gstart.as<int64_t>(),
+                                              j.gent.as<int32_t>(), j.ent.as<uint32_t>(),
+                                              j.cntmax.as<int32_t>(), j.hinfo.as<uint32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    j.h_cntmax.resize(n);
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.h_cntmax.data(), j.cntmax.ptr, (size_t)n * 4,
+                                   cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    j.ready = true;
+    j.nsurv = 0;
+    return CRISPY_OK;
+}
+
+int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* npairs) {
+    if (!ctx) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_run before kmer_prepare");
+    const int n = j.n, K = j.k;
+    const int A = crispy_array_dim(n);
+    if (A <= 0) return fail(ctx, CRISPY_E_UNSUPPORTED, "fewer than 10 reads: the reference has no tile size (arrayDim = 0)");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    ctx->stats = crispy_stats{};
+    ctx->ev_kmer.used = 0;
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
+    const int sd = (n + A - 1) / A;
+    const int64_t nstages = (int64_t)sd * (sd + 1) / 2;
+
+    std::vector<uint16_t> mmin, smin;
+    build_mmin(thr, j.max_t, mmin, smin);
+    CRISPY_TRY(ensure(ctx, j.mmin, mmin.size() * 2));
+    CRISPY_TRY(ensure(ctx, j.smin, smin.size() * 2));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.mmin.ptr, mmin.data(), mmin.size() * 2, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.smin.ptr, smin.data(), smin.size() * 2, cudaMemcpyHostToDevice, s));
+
+    // level need per 32-read group and the groups the dense kernel must take
+    const int cap_levels = levels_cap_for(K);
+    std::vector<uint8_t> heavy(j.ngroups, 0);
+    int lmax_fast = 1;
+    bool any_heavy = false;
+    for (int g = 0; g < j.ngroups; ++g) {
+        int L = 0;
+        for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) L = std::max(L, j.h_cntmax[r]);
+        if (L > cap_levels) { heavy[g] = 1; any_heavy = true; }
+        else lmax_fast = std::max(lmax_fast, L);
+    }
+    CRISPY_TRY(ensure(ctx, j.work, (size_t)j.ngroups));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.work.ptr, heavy.data(), j.ngroups, cudaMemcpyHostToDevice, s));
+
+    const uint32_t K4 = 1u << (2 * K);
+    const int B = std::max(5, bits_for((uint64_t)j.max_t));
+    TileFn tile = tile_fn_for(B);
+    const size_t tsmem = cap_levels > 0 ? (size_t)lmax_fast * K4 * 4 : 0;
+    const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
+    if (cap_levels > 0)
+        CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+
+    int64_t cap = std::max<int64_t>(j.keys.bytes / 8, std::max<int64_t>(1 << 20, 16LL * n));
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        CRISPY_TRY(ensure(ctx, j.keys, (size_t)cap * 8));
+        CRISPY_TRY(ensure(ctx, j.keys_alt, (size_t)cap * 8));
+        CRISPY_TRY(ensure(ctx, j.vals, (size_t)cap * 4));
+        CRISPY_TRY(ensure(ctx, j.vals_alt, (size_t)cap * 4));
+        CRISPY_TRY(ensure(ctx, j.counter, 64));
+        CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
+
+        TileArgs ta{};
+        ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
+        ta.tcount = j.t.as<int32_t>(); ta.cntmax = j.cntmax.as<int32_t>();
+        ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
+        ta.n = n; ta.K4 = K4; ta.levels_cap = cap_levels; ta.A = A; ta.stage_dim = sd;
+        ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
+        ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
+        DenseArgs da{};
+        da.seq = j.seq.as<uint8_t>(); da.off = j.off.as<int64_t>(); da.ent = ta.ent; da.gstart = ta.gstart;
+        da.tcount = ta.tcount; da.cntmax = ta.cntmax; da.hinfo = j.hinfo.as<uint32_t>(); da.mmin = ta.mmin;
+        da.n = n; da.K = K; da.levels_cap = cap_levels; da.A = A; da.stage_dim = sd;
+        da.heavy_group = (cap_levels > 0) ? j.work.as<uint8_t>() : nullptr;
+        da.counter = ta.counter; da.keys = ta.keys; da.vals = ta.vals; da.cap = cap;
+        const bool fast = cap_levels > 0;
+
+        if (mode == CRISPY_MODE_PLAIN) {
+            // One launch per reference stage, round-robin over 8 streams like
+            // the reference's stage loop (kmerCUDA.cu:79-111).
+            cudaEvent_t fork;
+            CRISPY_CK(ctx, cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+            CRISPY_CK(ctx, cudaEventRecord(fork, s));
+            for (auto& ss : ctx->side) CRISPY_CK(ctx, cudaStreamWaitEvent(ss, fork, 0));
+            ev_begin(ctx, ctx->ev_kmer, s);
+            int64_t st = 0;
+            for (int sx = 0; sx < sd; ++sx) {
+                for (int sy = sx; sy < sd; ++sy, ++st) {
+                    cudaStream_t ss = ctx->side[st % 8];
+                    TileArgs t2 = ta;
+                    t2.r_lo = sx * A; t2.r_hi = std::min(n, sx * A + A);
+                    t2.c_lo = sy * A; t2.c_hi = std::min(n, sy * A + A);
+                    if (fast) {
+                        const int rg0 = t2.r_lo / 32, rg1 = (t2.r_hi - 1) / 32;
+                        tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
+                        count_launch(ctx);
+                    }
+                    if (!fast || any_heavy) {
+                        DenseArgs d2 = da;
+                        d2.r_lo = t2.r_lo; d2.r_hi = t2.r_hi; d2.c_lo = t2.c_lo; d2.c_hi = t2.c_hi;
+                        kmer_dense_kernel<<<std::min(t2.r_hi - t2.r_lo, 4 * ctx->sm_count), 256, dsmem, ss>>>(d2);
+                        count_launch(ctx);
+                    }
+                }
+            }
+            for (auto& ss : ctx->side) {
+                cudaEvent_t join;
+                CRISPY_CK(ctx, cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+                CRISPY_CK(ctx, cudaEventRecord(join, ss));
+                CRISPY_CK(ctx, cudaStreamWaitEvent(s, join, 0));
+                cudaEventDestroy(join);
+            }
+            ev_end(ctx, ctx->ev_kmer, s);
+            cudaEventDestroy(fork);
+            ctx->stats.kmer_launches += nstages;
+        } else {
+            // Batched: one persistent launch over a work queue of (row group,
+            // column-group range) items covering the whole upper triangle.
+            const int cw = ctx->kmer_chunk_groups > 0 ? ctx->kmer_chunk_groups : 64;
+            std::vector<int4> items;
+            if (fast) {
+                for (int rg = 0; rg < j.ngroups; ++rg) {
+                    if (heavy[rg]) continue;
+                    for (int c0 = rg; c0 < j.ngroups; c0 += cw)
+                        items.push_back(make_int4(rg, c0, std::min(j.ngroups, c0 + cw), 0));
+                }
+            }
+            if (!items.empty()) {
+                CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int4) + 64));
+                unsigned int* head = reinterpret_cast<unsigned int*>(j.sort_tmp.as<char>() + items.size() * sizeof(int4));
+                CRISPY_CK(ctx, cudaMemcpyAsync(j.sort_tmp.ptr, items.data(), items.size() * sizeof(int4),
+                                               cudaMemcpyHostToDevice, s));
+                CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 4, s));
+                TileArgs t2 = ta;
+                t2.r_lo = 0; t2.r_hi = n; t2.c_lo = 0; t2.c_hi = n;
+                t2.items = j.sort_tmp.as<int4>(); t2.nitems = (int)items.size(); t2.queue_head = head;
+                int per_sm = 1;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile, kTileThreads, tsmem);
+                per_sm = std::max(1, per_sm);
+                const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)items.size());
+                ev_begin(ctx, ctx->ev_kmer, s);
+                tile<<<grid, kTileThreads, tsmem, s>>>(t2);
+                ev_end(ctx, ctx->ev_kmer, s);
+                count_launch(ctx);
+                ctx->stats.kmer_launches += 1;
+            }
+            if (!fast || any_heavy) {
+                DenseArgs d2 = da;
+                d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
+                kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
+                count_launch(ctx);
+            }
+        }
+        CRISPY_CK(ctx, cudaGetLastError());
+        unsigned long long total = 0;
+        CRISPY_CK(ctx, cudaMemcpyAsync(&total, j.counter.ptr, 8, cudaMemcpyDeviceToHost, s));
+        CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        if ((int64_t)total <= cap) {
+            j.nsurv = (int64_t)total;
+            break;
+        }
+        cap = (int64_t)total + total / 8 + 1024;
+        if (attempt == 2) return fail(ctx, CRISPY_E_STATE, "survivor buffer did not converge");
+    }
+    // stable order: (stage, row, col)
+    const int key_bits = bits_for((uint64_t)nstages * (uint64_t)n * (uint64_t)n);
+    uint64_t* sk = nullptr;
+    uint32_t* sv = nullptr;
+    CRISPY_TRY(sort_u64_payload(ctx, s, j.keys.as<uint64_t>(), j.keys_alt.as<uint64_t>(),
+                                j.vals.as<uint32_t>(), j.vals_alt.as<uint32_t>(), j.nsurv, key_bits,
+                                dists != 0, &sk, &sv, j.sort_tmp));
+    CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));
+    CRISPY_TRY(ensure(ctx, j.dists, (size_t)std::max<int64_t>(j.nsurv, 1) * 4));
+    if (j.nsurv > 0) {
+        kmer_decode_kernel<<<(unsigned)((j.nsurv + 255) / 256), 256, 0, s>>>(
+            sk, sv, j.nsurv, n, j.pairs.as<int2>(), dists ? j.dists.as<float>() : nullptr);
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+    }
+    j.have_dists = dists != 0;
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->t_begin, ctx->t_end);
+    ctx->stats.total_ms = tot;
+    ctx->stats.kmer_kernel_ms = ev_sum_ms(ctx->ev_kmer);
+    ctx->stats.kmer_pairs = (int64_t)n * (n - 1) / 2;
+    ctx->stats.kmer_survivors = j.nsurv;
+    if (npairs) *npairs = j.nsurv;
+    return CRISPY_OK;
+}
+
+int crispy_kmer_fetch(crispy_ctx* ctx, int32_t* pairs, float* dists, int64_t cap, int64_t* count) {
+    if (!ctx) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_fetch before kmer_run");
+    if (dists && !j.have_dists) return fail(ctx, CRISPY_E_STATE, "distances were not kept by kmer_run");
+    const int64_t c = std::min(cap, j.nsurv);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (c > 0 && pairs)
+        CRISPY_CK(ctx, cudaMemcpyAsync(pairs, j.pairs.ptr, (size_t)c * 8, cudaMemcpyDeviceToHost, s));
+    if (c > 0 && dists)
+        CRISPY_CK(ctx, cudaMemcpyAsync(dists, j.dists.ptr, (size_t)c * 4, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    if (count) *count = c;
+    return CRISPY_OK;
+}
+
+int crispy_kmer_stream(crispy_ctx* ctx, crispy_sink sink, void* user) {
+    if (!ctx || !sink) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_stream before kmer_run");
+    const int64_t batch = 1 << 20;
+    std::vector<int32_t> p((size_t)std::min(batch, std::max<int64_t>(j.nsurv, 1)) * 2);
+    std::vector<float> d(j.have_dists ? p.size() / 2 : 0);
+    cudaStream_t s = ctx->stream;
+    for (int64_t at = 0; at < j.nsurv; at += batch) {
+        const int64_t c = std::min(batch, j.nsurv - at);
+        CRISPY_CK(ctx, cudaMemcpyAsync(p.data(), j.pairs.as<char>() + at * 8, (size_t)c * 8,
+                                       cudaMemcpyDeviceToHost, s));
+        if (j.have_dists)
+            CRISPY_CK(ctx, cudaMemcpyAsync(d.data(), j.dists.as<char>() + at * 4, (size_t)c * 4,
+                                           cudaMemcpyDeviceToHost, s));
+        CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        if (sink(user, 0, p.data(), j.have_dists ? d.data() : nullptr, c) != 0)
+            return fail(ctx, CRISPY_E_IO, "sink aborted");
+    }
+    return CRISPY_OK;
+}
+
+}  // extern "C"

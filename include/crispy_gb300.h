@@ -1,0 +1,173 @@
+/*
+ * crispy_gb300.h -- C ABI of libcrispy_gb300.so, the GB300 (sm_103a) engine
+ * behind CRiSPy's two pairwise-distance stages.
+ *
+ * The reference has no library API: its boundary is the bin/kmerDist and
+ * bin/genDist command lines plus their binary files, and internally the C++
+ * seams computeKmerDist_CUDA (src/kmerDist/kmerMain.h:73) and
+ * computeGenDist_CUDA (src/genDist/genMain.h:77).  Each entry point below
+ * replaces one part of those seams; the citation on each says which.  The
+ * drop-in executables built from crispy_gb300/csrc/cli_*.cpp call only this
+ * header.
+ *
+ * Conventions
+ *   - Every function returns an int status: CRISPY_OK (0) or a CRISPY_E_*
+ *     code.  Nothing calls exit(); crispy_last_error() describes the last
+ *     failure on a context (or globally when ctx is NULL).
+ *   - Plain pointers and sizes only.  Host buffers belong to the caller and
+ *     are never retained past the call.  Device memory belongs to the
+ *     context and is released by crispy_ctx_destroy().
+ *   - One context per host thread.  A context drives one GPU (device index
+ *     given at creation) on one CUDA stream.
+ *   - Results are bit-exact to the reference: integer k-mer counts, DP
+ *     scores, mismatch/alignment-length counts, FP32 distances evaluated in
+ *     the reference's own expression order, and the reference's output
+ *     order (stage order for .kpair, stable distance order per chunk for
+ *     .npair_N/.ndist_N).
+ */
+#ifndef CRISPY_GB300_H
+#define CRISPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference exits with -1 on every one of these,
+ *      kmerKernel.h:17-26, genMain.cpp:117-126) ---- */
+#define CRISPY_OK          0
+#define CRISPY_E_INPUT     1   /* bad argument, malformed file, read index out of range */
+#define CRISPY_E_OOM       2   /* device or pinned-host allocation failed */
+#define CRISPY_E_DEVICE    3   /* CUDA error, no device, or missing sm_103a image */
+#define CRISPY_E_TIMEOUT   4   /* a bounded device-side wait ran out */
+#define CRISPY_E_STATE     5   /* call out of order (e.g. run before prepare) */
+#define CRISPY_E_IO        6   /* file could not be opened, read or written */
+#define CRISPY_E_UNSUPPORTED 7 /* limits of the reference: n > 1,048,576, length > 2048, K outside 1..8 */
+
+/* ---- limits shared with the reference (kmerMain.h:28-30, genMain.h:29-30) ---- */
+#define CRISPY_MAX_READ_LEN   2048
+#define CRISPY_MAX_NUM_READS  (1024 * 1024)
+#define CRISPY_GEN_WINDOW     589824   /* genMain.h:24-27: pairs per load window and chunk flush size */
+
+/* ---- run modes ---- */
+#define CRISPY_MODE_PLAIN    0  /* one launch per reference stage (kmer) / per load window (gen) */
+#define CRISPY_MODE_BATCHED  1  /* length-bucketed persistent kernels on a device work queue, CUDA-graph launched */
+
+typedef struct crispy_ctx crispy_ctx;
+
+/* Receives output in the reference's order, in consecutive batches.
+ * For kmer: pairs = int32[2*count] (row, col), dists = float[count].
+ * For gen:  called once per chunk file (chunk_id = the _<f> suffix) with
+ *           pairs = uint32[2*count], dists = float[count].
+ * Return 0 to continue, non-zero to abort the run (status CRISPY_E_IO). */
+typedef int (*crispy_sink)(void* user, int chunk_id, const void* pairs,
+                           const float* dists, int64_t count);
+
+/* Context lifetime.  Replaces the implicit device-0 setup and the
+ * checkCudaErrors/exit(-1) error model of kmerKernel.h:17-26. */
+int crispy_ctx_create(int device, crispy_ctx** out);
+int crispy_ctx_destroy(crispy_ctx* ctx);
+/* Run on a caller-owned cudaStream_t (pass NULL for the context's own). */
+int crispy_ctx_set_stream(crispy_ctx* ctx, void* cuda_stream);
+const char* crispy_last_error(const crispy_ctx* ctx);
+const char* crispy_version(void);
+
+/* ---- host helpers (no device work) ---- */
+
+/* FASTA parse of readFile (kmerMain.cpp:298-397 when flavour = 0,
+ * genMain.cpp:184-277 when flavour = 1): reads concatenated into one buffer.
+ * The handle owns the memory; crispy_reads_free releases it. */
+typedef struct crispy_reads crispy_reads;
+int crispy_reads_load_fasta(const char* path, int flavour, crispy_reads** out);
+int crispy_reads_view(const crispy_reads* r, const char** seqbuf,
+                      const int64_t** offsets, const int32_t** lengths,
+                      int32_t* n, int32_t* max_len);
+void crispy_reads_free(crispy_reads* r);
+
+/* Default cut threshold: kmerMain.cpp:43-48 (stage = 0, 2/log n) and
+ * genMain.cpp:42-47 (stage = 1, 1/log n); user_thr in [0,1] wins. */
+float crispy_default_threshold(int n, float user_thr, int stage);
+/* Stage tile size arrayDim of kmerMain.cpp:50-53 (0 for n < 10). */
+int crispy_array_dim(int n);
+
+/* ---- kmerDist (replaces computeKmerDist_CUDA, kmerCUDA.cu:14-126) ---- */
+
+/* Upload reads and build the per-read k-mer structures on the device
+ * (replaces formTuples/sortTuples, kmerMain.cpp:117-159, and the texture
+ * upload of kmerCUDA.cu:37-71).  seqbuf holds the reads back to back. */
+int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf,
+                        const int64_t* offsets, const int32_t* lengths,
+                        int n, int k);
+
+/* All-pairs k-mer distance with the cut threshold and sparse compaction
+ * fused into the kernel (kmerKernel.cu:19-51 + writeToFile,
+ * kmerMain.cpp:161-203).  Survivors stay on the device, already in the
+ * reference's stage order; *npairs gets their count.  dists selects whether
+ * distances are kept (the -d flag). */
+int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists,
+                    int64_t* npairs);
+
+/* Copy the survivors of the last crispy_kmer_run to host memory (pairs:
+ * int32[2*cap], dists: float[cap] or NULL), or stream them to a sink in
+ * batches.  *count receives the number copied. */
+int crispy_kmer_fetch(crispy_ctx* ctx, int32_t* pairs, float* dists,
+                      int64_t cap, int64_t* count);
+int crispy_kmer_stream(crispy_ctx* ctx, crispy_sink sink, void* user);
+
+/* ---- genDist (replaces computeGenDist_CUDA, genCUDA.cu:83-270) ---- */
+
+/* Upload reads (genDist flavour: the same buffer layout) and 2-bit pack them
+ * on the device (replaces convertToBinary, genMain.cpp:280-321, and the
+ * texture upload of genCUDA.cu:130-142). */
+int crispy_gen_prepare(crispy_ctx* ctx, const char* seqbuf,
+                       const int64_t* offsets, const int32_t* lengths, int n);
+
+/* Banded NW distance for every pair, threshold filter, 589,824-pair load
+ * windows, chunk flush and stable per-chunk sort by distance
+ * (genKernel.cu:707-780, genCUDA.cu:150-254, :17-81).  pairs is
+ * int32[2*npairs] in .kpair order on the host; band <= 0 means 2
+ * (genMain.cpp:356-364) and band == 1 is the unbanded alignment.  Each
+ * chunk goes to the sink in file order; *nsurvivors gets the total. */
+int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs,
+                   int band, float thr, int mode, crispy_sink sink,
+                   void* user, int64_t* nsurvivors);
+
+/* The same, consuming the survivors of the last crispy_kmer_run directly
+ * from device memory (no .kpair round trip).  Requires crispy_gen_prepare
+ * on the same reads. */
+int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode,
+                             crispy_sink sink, void* user,
+                             int64_t* nsurvivors);
+
+/* Per-pair alignment results without threshold or chunking (for parity
+ * checks): dist[i], and when non-NULL score[i] (selected last-row/column
+ * maximum), ml[i] (mismatches + gap columns) and al[i] (alignment length),
+ * exactly the quantities of genKernel.cu:765-768. */
+int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs,
+                     int band, int mode, float* dist, int32_t* score,
+                     int32_t* ml, int32_t* al);
+
+/* ---- timing of the last run (CUDA events on the context's stream) ---- */
+typedef struct crispy_stats {
+    double kmer_kernel_ms;     /* summed duration of the k-mer tile kernel launches */
+    int64_t kmer_launches;
+    double gen_kernel_ms;      /* summed duration of the DP kernel launches */
+    int64_t gen_launches;
+    double total_ms;           /* whole call, device side */
+    int64_t kmer_pairs;        /* all-pairs count n(n-1)/2 of the last kmer run */
+    int64_t kmer_survivors;
+    int64_t gen_pairs;         /* pairs aligned by the last gen run */
+    int64_t gen_cells;         /* band cells of those pairs */
+    int64_t gen_survivors;
+    int64_t kernels_launched;  /* every kernel this library launched in the last run */
+} crispy_stats;
+int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
+/* Enable per-launch event timing (adds events around the hot kernels). */
+int crispy_set_timing(crispy_ctx* ctx, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRISPY_GB300_H */

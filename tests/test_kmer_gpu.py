@@ -1,0 +1,102 @@
+"""kmerDist on the GPU vs the oracle: survivors, order and distances bit-exact.
+
+Cases follow what the reference handles: default and user thresholds, every
+K in 1..8 (K = 8 carries the signed-sort merge quirk), read counts that give
+each stage tile size (arrayDim 4, 32, 256, 1536), reads with K-mer
+multiplicities beyond the shared-memory level budget, reads of length K-1
+(no tuples), plain and batched modes.
+"""
+import numpy as np
+import pytest
+
+import crispy_gb300 as cg
+import oracle
+from crispy_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _reads(n, seed, root=260, cents=20, dist="normal", a=250, b=15, k=6):
+    return synth.make_read_set(synth.ReadSetSpec(n, cents, root, dist, a, b, k, seed))
+
+
+def _check(engine, reads, k, thr, mode):
+    buf, offs, lens = synth.pack_reads(reads)
+    engine.kmer_prepare(buf, offs, lens, k)
+    cnt = engine.kmer_run(thr, mode, True)
+    pairs, d = engine.kmer_fetch(cnt, True)
+    op, od = oracle.kmer_all(buf, offs, lens, k, thr)
+    assert cnt == len(op)
+    assert np.array_equal(pairs, op)
+    assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
+    return cnt
+
+
+@pytest.mark.parametrize("mode", [cg.MODE_PLAIN, cg.MODE_BATCHED])
+@pytest.mark.parametrize("k", [4, 5, 6, 7, 8])
+def test_kmer_k_modes(engine, k, mode):
+    reads = _reads(400, 100 + k, k=k)
+    thr = 0.45 if k < 8 else 0.6
+    assert _check(engine, reads, k, thr, mode) > 0
+
+
+@pytest.mark.parametrize("n", [10, 37, 99, 150, 1200])
+def test_kmer_tile_sizes_default_threshold(engine, n):
+    reads = _reads(n + n // 10 + 5, 7 + n)[:n]
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    _check(engine, reads, 6, t, cg.MODE_BATCHED)
+    _check(engine, reads, 6, t, cg.MODE_PLAIN)
+
+
+def test_kmer_k1_k3(engine):
+    reads = _reads(120, 5)
+    for k in (1, 2, 3):
+        _check(engine, reads, k, 0.2, cg.MODE_BATCHED)
+
+
+def test_kmer_heavy_multiplicity(engine):
+    # homopolymer runs push one 6-mer's count far past the level budget (12)
+    rng = np.random.default_rng(3)
+    reads = _reads(200, 9)
+    heavy = []
+    for i in range(40):
+        s = bytearray(reads[i])
+        run = 20 + (i % 30)
+        s[10:10 + run] = b"A" * run
+        heavy.append(bytes(s))
+    reads = synth.preprocess_order(reads[40:] + heavy)
+    _check(engine, reads, 6, 0.5, cg.MODE_BATCHED)
+    _check(engine, reads, 6, 0.5, cg.MODE_PLAIN)
+    # long degenerate reads: counts above 255
+    long = [b"A" * (400 + i) for i in range(5)] + [b"AC" * (150 + i) for i in range(5)]
+    _check(engine, synth.preprocess_order(long + reads[:30]), 6, 0.9, cg.MODE_BATCHED)
+
+
+def test_kmer_short_reads_no_tuples(engine):
+    reads = synth.preprocess_order([b"ACGTA", b"ACGTC", b"GGGGGG", b"ACGTACGTAA"] + _reads(40, 11))
+    _check(engine, reads, 6, 1.0, cg.MODE_BATCHED)
+
+
+def test_kmer_long_reads(engine):
+    reads = _reads(150, 21, root=2100, dist="uniform", a=1500, b=2048, cents=6)
+    _check(engine, reads, 6, 0.5, cg.MODE_BATCHED)
+    _check(engine, reads, 8, 0.7, cg.MODE_BATCHED)
+
+
+def test_kmer_uneven_lengths(engine):
+    reads = _reads(3000, 31, root=520, dist="uniform", a=300, b=500, cents=60)
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    a = _check(engine, reads, 6, t, cg.MODE_BATCHED)
+    b = _check(engine, reads, 6, t, cg.MODE_PLAIN)
+    assert a == b
+
+
+def test_kmer_nonacgt(engine):
+    reads = _reads(100, 41)
+    mixed = []
+    for i, s in enumerate(reads):
+        s = bytearray(s)
+        s[5 + i % 50] = ord("N")
+        s[80 + i % 20] = ord("a")
+        mixed.append(bytes(s))
+    _check(engine, synth.preprocess_order(mixed), 6, 0.4, cg.MODE_BATCHED)
