@@ -1,0 +1,428 @@
+#!/usr/bin/env python
+"""Throughput of the kmerDist -> genDist hot path on GB300.
+
+One step = one pass of both stages over one synthetic read set:
+  kmerDist  all-pairs k-mer distance + fused threshold/compaction, survivors
+            ordered as the reference orders .kpair;
+  genDist   banded NW over those survivors, threshold, 589,824-pair windows,
+            chunk flush, stable per-chunk sort, chunks delivered to host memory.
+
+value  = all-pairs count n(n-1)/2 / step time, batched form, reads resident in
+         HBM (the device rebuilds the k-mer structures inside the step).
+e2e    = the same through the public C ABI with host buffers (reads uploaded
+         twice, .kpair pairs fetched to the host and sent back, chunks read
+         back), as the drop-in executables do minus disk I/O.
+plain  = the same pipeline with the plain kernels (one launch per reference
+         stage / per load window) for the batched-vs-plain ratio.
+
+--impl reference times the reference's CPU algorithm (the oracle port,
+OpenMP on every host core) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from crispy_gb300 import synth  # noqa: E402
+
+METRIC = "banded-NW GCUPS & k-mer pairs/s, batched vs plain; serve p50/p99, bit-exact"
+UNIT = "k-mer pairs/s"
+KMER_OPS_NOTE = "kmer: (Ta+Tb) int ops per pair; genDist: 10 int ops per band cell"
+
+WORKLOADS = {
+    # name: (synth workload, k, band)
+    "uneven_100k": ("uneven_100k", 6, 10),
+    "plain_20k": ("plain_20k", 6, 10),
+    "small_1k": ("small_1k", 6, 10),
+}
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend="gloo")
+        return dist, ws, rank, local
+    return None, 1, 0, local
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _read_set(name: str, rank: int):
+    spec = synth.WORKLOADS[WORKLOADS[name][0]]
+    if rank:
+        spec = synth.ReadSetSpec(**{**spec.__dict__, "seed": spec.seed + 1000 * rank})
+    return synth.make_read_set(spec)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle port of the reference's CPU path)
+# ---------------------------------------------------------------------------
+
+def _cpu_sample(reads, k, band, m, workdir):
+    """Run the oracle CLI on a deterministic subset of m reads; returns
+    (kmer pairs/s, band-GCUPS, cores, description)."""
+    import oracle
+
+    if not os.path.exists(oracle.CLI_PATH):
+        oracle.build()
+    rng = np.random.default_rng(1234)
+    idx = np.sort(rng.choice(len(reads), size=min(m, len(reads)), replace=False))
+    sub = [reads[i] for i in idx]
+    fa = os.path.join(workdir, "cpu_sample_Clean")
+    synth.write_fasta(fa, sub)
+    cores = os.cpu_count() or 1
+    n = len(sub)
+    # the full workload's thresholds (the subset keeps its read lengths)
+    from crispy_gb300 import default_threshold
+
+    tk = default_threshold(len(reads), -1.0, 0)
+    tg = default_threshold(len(reads), -1.0, 1)
+    t0 = time.perf_counter()
+    subprocess.run([oracle.CLI_PATH, "kmer", "-i", fa, "-k", str(k), "-t", repr(tk), "-n", str(cores)],
+                   check=True, stdout=subprocess.DEVNULL)
+    tkmer = time.perf_counter() - t0
+    pairs = np.fromfile(fa + ".kpair", np.int32).reshape(-1, 2)
+    lens = np.array([len(s) for s in sub])
+    t0 = time.perf_counter()
+    subprocess.run([oracle.CLI_PATH, "gen", "-i", fa, "-b", str(band), "-t", repr(tg), "-n", str(cores)],
+                   check=True, stdout=subprocess.DEVNULL)
+    tgen = time.perf_counter() - t0
+    cells = sum(oracle.band_cells(int(lens[a]), int(lens[b]), band) for a, b in pairs) if len(pairs) else 0
+    kpps = n * (n - 1) / 2 / tkmer
+    gcups = cells / tgen / 1e9 if cells else None
+    desc = (f"{n} of {len(reads)} reads (seeded subset), all {n*(n-1)//2} k-mer pairs "
+            f"({tkmer:.2f} s) + genDist on its {len(pairs)} survivors ({cells} cells, {tgen:.2f} s)")
+    return kpps, gcups, cores, desc, tkmer + tgen
+
+
+def _cpu_pipeline_rate(kpps, gcups, n_pairs_full, cells_full):
+    t = n_pairs_full / kpps + (cells_full / (gcups * 1e9) if gcups and cells_full else 0.0)
+    return n_pairs_full / t
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, dist, ws, rank, local):
+    import torch
+
+    import crispy_gb300 as cg
+
+    torch.cuda.set_device(local)
+    reads = _read_set(args.workload, rank)
+    _, k, band = WORKLOADS[args.workload]
+    buf, offs, lens = synth.pack_reads(reads)
+    n = len(lens)
+    n_pairs = n * (n - 1) // 2
+    thr_k = cg.default_threshold(n, -1.0, 0)
+    thr_g = cg.default_threshold(n, -1.0, 1)
+
+    eng = cg.Engine(local, timing=True)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.kmer_prepare(buf, offs, lens, k)
+    eng.gen_prepare(buf, offs, lens)
+    int_peak_gops = eng.probe_int32_gops()
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def pipeline(mode):
+        eng.kmer_rebuild()
+        kp = eng.kmer_run(thr_k, mode, False)
+        st_k = eng.stats()
+        chunks = eng.gen_run_from_kmer(band, thr_g, mode)
+        st_g = eng.stats()
+        return kp, chunks, st_k, st_g
+
+    def timed(mode, steps, warm):
+        for _ in range(warm):
+            pipeline(mode)
+        torch.cuda.synchronize()
+        _barrier(dist)
+        torch.cuda.synchronize()
+        ms, kms, gms, launches, last = [], [], [], 0, None
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()          # L2 flush between timed iterations
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+            last = pipeline(mode)
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            kms.append(last[2]["kmer_kernel_ms"])
+            gms.append(last[3]["gen_kernel_ms"])
+            launches += last[2]["kernels_launched"] + last[3]["kernels_launched"]
+        torch.cuda.synchronize()
+        _barrier(dist)
+        return ms, kms, gms, launches, last
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_b, kms_b, gms_b, launches_b, last_b = timed(cg.MODE_BATCHED, args.steps, args.warmup)
+    clk = clocks.stop()
+    plain_steps = max(1, min(args.steps, 3))
+    ms_p, kms_p, gms_p, _, last_p = timed(cg.MODE_PLAIN, plain_steps, 1)
+
+    kp, chunks, st_k, st_g = last_b
+    survivors = sum(len(c[2]) for c in chunks)
+    assert kp == last_p[0] and survivors == sum(len(c[2]) for c in last_p[1]), "plain/batched disagree"
+    cells = st_g["gen_cells"]
+    mean_t = float(np.mean(np.maximum(np.array(lens) - k + 1, 0)))
+
+    step_s = _max_over_ranks(dist, float(np.mean(ms_b)) / 1e3)
+    value = ws * n_pairs / step_s
+    kmer_s = float(np.mean(kms_b)) / 1e3
+    gen_s = float(np.mean(gms_b)) / 1e3
+    plain_s = float(np.mean(ms_p)) / 1e3
+
+    # e2e through the public API with host buffers
+    def e2e_step():
+        eng.kmer_prepare(buf, offs, lens, k)
+        c = eng.kmer_run(thr_k, cg.MODE_BATCHED, False)
+        pairs, _ = eng.kmer_fetch(c, False)
+        eng.gen_prepare(buf, offs, lens)
+        out = eng.gen_run(pairs, band, thr_g, cg.MODE_BATCHED)
+        return c, out
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c, out = e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_s = _max_over_ranks(dist, float(np.mean(e2e_ms)) / 1e3)
+    h2d = 2 * (buf.nbytes + offs.nbytes + lens.nbytes) + c * 8
+    d2h = c * 8 + sum(len(o[2]) for o in out) * 12 + n * 4
+
+    kmer_ops = n_pairs * 2 * mean_t            # frozen: (Ta + Tb) per pair
+    gen_ops = cells * 10                        # frozen: 10 per band cell
+    roof_k = {"kernel": "kmer_tile_kernel", "bound": "int32", "unit": "Gop/s",
+              "achieved": kmer_ops / kmer_s / 1e9, "peak": int_peak_gops,
+              "frac": kmer_ops / kmer_s / 1e9 / int_peak_gops,
+              "work_per_unit": f"{2*mean_t:.1f} ops per k-mer pair", "traffic": None,
+              "peak_source": "measured: crispy_probe_int32 (IADD3/LOP3 chains), this run"}
+    roof_g = {"kernel": "gen_warp_kernel", "bound": "int32", "unit": "Gop/s",
+              "achieved": gen_ops / gen_s / 1e9, "peak": int_peak_gops,
+              "frac": gen_ops / gen_s / 1e9 / int_peak_gops,
+              "work_per_unit": "10 ops per band cell", "traffic": None,
+              "peak_source": "measured: crispy_probe_int32 (IADD3/LOP3 chains), this run"}
+    dominant = roof_g if gen_s >= kmer_s else roof_k
+    _attach_traffic(roof_k, roof_g, n_pairs, cells)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded 16S-like generator, preprocess order)",
+        "config": {"workload": args.workload, "n_reads": n, "k": k, "band": band,
+                   "kmer_threshold": thr_k, "gen_threshold": thr_g, "mode": "batched",
+                   "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{ws}"},
+        "kmer_pairs_per_s": n_pairs / kmer_s, "kmer_survivors": kp,
+        "gen_gcups": cells / gen_s / 1e9, "gen_cells": cells, "gen_survivors": survivors,
+        "kmer_kernel_ms": kmer_s * 1e3, "gen_kernel_ms": gen_s * 1e3,
+        "plain": {"ms_per_step": plain_s * 1e3, "value": n_pairs / plain_s,
+                  "kmer_kernel_ms": float(np.mean(kms_p)), "gen_kernel_ms": float(np.mean(gms_p))},
+        "batched_over_plain": plain_s / step_s,
+        "e2e": {"value": ws * n_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": int(launches_b),
+        "roofline": dominant, "roofline_kmer": roof_k, "roofline_gen": roof_g,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        with tempfile.TemporaryDirectory() as td:
+            kpps, gcups, cores, desc, _ = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
+        line["cpu_baseline"] = {"value": _cpu_pipeline_rate(kpps, gcups, n_pairs, cells), "unit": UNIT,
+                                "cores": cores, "kind": "port", "sample": desc,
+                                "kmer_pairs_per_s": kpps, "gen_gcups": gcups,
+                                "note": "extrapolated to the full workload from the sample rates"}
+    eng.close()
+    return line
+
+
+def _attach_traffic(roof_k, roof_g, n_pairs, cells):
+    """DRAM bytes per launch from a committed ncu summary, scaled by units."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(p):
+        return
+    try:
+        t = json.load(open(p))
+    except (OSError, ValueError):
+        return
+    if "kmer_bytes_per_pair" in t:
+        roof_k["traffic"] = t["kmer_bytes_per_pair"] * n_pairs
+        roof_k["traffic_source"] = t.get("source")
+    if "gen_bytes_per_cell" in t:
+        roof_g["traffic"] = t["gen_bytes_per_cell"] * cells
+        roof_g["traffic_source"] = t.get("source")
+
+
+def run_reference(args, dist, ws, rank):
+    if rank != 0:
+        return None
+    reads = _read_set(args.workload, 0)
+    _, k, band = WORKLOADS[args.workload]
+    n = len(reads)
+    n_pairs = n * (n - 1) // 2
+    lens = np.array([len(s) for s in reads])
+    rates = []
+    with tempfile.TemporaryDirectory() as td:
+        for i in range(args.warmup + args.steps):
+            kpps, gcups, cores, desc, secs = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
+            if i >= args.warmup:
+                rates.append((kpps, gcups, secs))
+    kpps = float(np.mean([r[0] for r in rates]))
+    gcups_list = [r[1] for r in rates if r[1]]
+    gcups = float(np.mean(gcups_list)) if gcups_list else None
+    # band cells of the full workload: same per-pair mean as the sample survivors
+    # is not known without running genDist on the full set; use the GPU arm's
+    # definition when available, else the sample's cells-per-pair estimate
+    cells_full = None
+    p = os.path.join(ROOT, "profiles", "workload_cells.json")
+    if os.path.exists(p):
+        try:
+            cells_full = json.load(open(p)).get(args.workload)
+        except ValueError:
+            cells_full = None
+    value = _cpu_pipeline_rate(kpps, gcups, n_pairs, cells_full) if cells_full else kpps
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r[2] for r in rates])) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded 16S-like generator, preprocess order)",
+            "config": {"workload": args.workload, "n_reads": n, "k": k, "band": band,
+                       "mode": "reference CPU algorithm"},
+            "kmer_pairs_per_s": kpps, "gen_gcups": gcups,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("CRISPY_BENCH_WORKLOAD", "uneven_100k"),
+                    choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sample-reads", type=int, default=_env_int("CRISPY_CPU_SAMPLE", 6000))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist, ws, rank, local = _dist()
+    if args.impl == "reference":
+        line = run_reference(args, dist, ws, rank)
+    else:
+        line = run_ours(args, dist, ws, rank, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

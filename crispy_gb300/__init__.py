@@ -70,6 +70,7 @@ PROTOTYPES = {
     "crispy_default_threshold": (C.c_float, [C.c_int, C.c_float, C.c_int]),
     "crispy_array_dim": (C.c_int, [C.c_int]),
     "crispy_kmer_prepare": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int]),
+    "crispy_kmer_rebuild": (C.c_int, [_P]),
     "crispy_kmer_run": (C.c_int, [_P, C.c_float, C.c_int, C.c_int, _i64p]),
     "crispy_kmer_fetch": (C.c_int, [_P, _P, _P, C.c_int64, _i64p]),
     "crispy_kmer_stream": (C.c_int, [_P, SINK, _P]),
@@ -79,6 +80,7 @@ PROTOTYPES = {
     "crispy_gen_align": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P]),
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
+    "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -188,6 +190,14 @@ class Engine:
         lens = np.ascontiguousarray(lens, dtype=np.int32)
         self._check(self.lib.crispy_kmer_prepare(self.h, _ptr(buf), _ptr(offs), _ptr(lens),
                                                  len(lens), k))
+
+    def kmer_rebuild(self):
+        self._check(self.lib.crispy_kmer_rebuild(self.h))
+
+    def probe_int32_gops(self) -> float:
+        g = C.c_double()
+        self._check(self.lib.crispy_probe_int32(self.h, C.byref(g)))
+        return g.value
 
     def kmer_run(self, thr: float, mode: int = MODE_BATCHED, dists: bool = True) -> int:
         n = C.c_int64()

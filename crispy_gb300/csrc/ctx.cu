@@ -16,6 +16,26 @@ std::string g_err;  // errors raised before a context exists
 __global__ void probe_kernel(int* p) {
     if (p) *p = 1;
 }
+
+// Integer-pipe throughput probe: eight independent add/xor chains per
+// thread (IADD3 / LOP3 work, the instruction mix of both hot kernels).
+constexpr int kProbeIters = 4096;
+__global__ void __launch_bounds__(256) int32_probe_kernel(uint32_t seed, uint32_t* sink) {
+    uint32_t x[8], y[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { x[c] = seed + threadIdx.x + c; y[c] = seed ^ (blockIdx.x * 7u + c); }
+    for (int i = 0; i < kProbeIters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            x[c] = x[c] + y[c];
+            y[c] = y[c] ^ x[c];
+        }
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc ^= x[c] ^ y[c];
+    if (acc == 0x9e3779b9u) *sink = acc;   // keeps the chains live
+}
 }  // namespace
 
 namespace crispy {
@@ -200,6 +220,39 @@ const char* crispy_last_error(const crispy_ctx* ctx) {
 int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out) {
     if (!ctx || !out) return CRISPY_E_INPUT;
     *out = ctx->stats;
+    return CRISPY_OK;
+}
+
+int crispy_probe_int32(crispy_ctx* ctx, double* gops) {
+    if (!ctx || !gops) return CRISPY_E_INPUT;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    uint32_t* sink = nullptr;
+    CRISPY_CK(ctx, cudaMalloc(&sink, 4));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, int32_probe_kernel, 256, 0);
+    const int blocks = ctx->sm_count * per_sm * 4;
+    int32_probe_kernel<<<blocks, 256, 0, s>>>(1u, sink);   // warm-up
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a, s);
+        int32_probe_kernel<<<blocks, 256, 0, s>>>(2u + rep, sink);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaError_t e = cudaGetLastError();
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "int32 probe", __FILE__, __LINE__);
+    const double ops = (double)blocks * 256 * kProbeIters * 16;
+    *gops = ops / (best * 1e-3) / 1e9;
     return CRISPY_OK;
 }
 

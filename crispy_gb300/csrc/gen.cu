@@ -433,16 +433,22 @@ WarpFn warp_fn(int c) {
     }
 }
 
+}  // namespace
+
+// Band cells of one pair in O(1): rows i = 1..l2 hold columns
+// max(1, i-kb)..min(l1, i+kb), non-empty for i <= min(l2, l1 + kb).
 int64_t band_cells(int l1, int l2, int band) {
-    const int kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
-    // rows i = 1..l2, columns max(1, i-kb)..min(l1, i+kb)
-    int64_t cells = 0;
-    for (int i = 1; i <= l2; ++i) {
-        const int lo = std::max(1, i - kb), hi = std::min(l1, i + kb);
-        if (hi >= lo) cells += hi - lo + 1;
-    }
-    return cells;
+    const int64_t kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
+    if (l1 <= 0 || l2 <= 0) return 0;
+    const int64_t I = std::min<int64_t>(l2, l1 + kb);
+    const int64_t a = std::min<int64_t>(std::max<int64_t>(l1 - kb, 0), I);  // rows where i+kb <= l1
+    const int64_t sum_hi = a * (a + 1) / 2 + a * kb + (I - a) * l1;
+    const int64_t b = std::min<int64_t>(kb + 1, I);                         // rows where i-kb <= 1
+    const int64_t sum_lo = b + (I * (I + 1) / 2 - b * (b + 1) / 2) - kb * (I - b);
+    return sum_hi - sum_lo + I;
 }
+
+namespace {
 
 }  // namespace
 

@@ -572,6 +572,19 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
                                    cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.gent.ptr, j.h_gent.data(), (size_t)j.ngroups * 4,
                                    cudaMemcpyHostToDevice, s));
+    j.ready = true;   // reads are resident; the entries are built next
+    return crispy_kmer_rebuild(ctx);
+}
+
+// Rebuild the level entries, multiplicities and K = 8 keys from the reads
+// already resident on the device (no host transfer of reads).
+int crispy_kmer_rebuild(crispy_ctx* ctx) {
+    if (!ctx) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_rebuild before kmer_prepare");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const int n = j.n, k = j.k;
     CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 1) * 4, s));
     const size_t hsmem = (size_t)(((1u << (2 * k)) + 1) / 2) * 4;
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -587,7 +600,6 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     CRISPY_CK(ctx, cudaMemcpyAsync(j.h_cntmax.data(), j.cntmax.ptr, (size_t)n * 4,
                                    cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
-    j.ready = true;
     j.nsurv = 0;
     return CRISPY_OK;
 }

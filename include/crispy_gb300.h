@@ -101,6 +101,11 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf,
                         const int64_t* offsets, const int32_t* lengths,
                         int n, int k);
 
+/* Re-run the device-side K-mer structure build from the reads uploaded by
+ * the last crispy_kmer_prepare (no host transfer).  Part of formTuples in
+ * the reference (kmerMain.cpp:117-159). */
+int crispy_kmer_rebuild(crispy_ctx* ctx);
+
 /* All-pairs k-mer distance with the cut threshold and sparse compaction
  * fused into the kernel (kmerKernel.cu:19-51 + writeToFile,
  * kmerMain.cpp:161-203).  Survivors stay on the device, already in the
@@ -166,6 +171,11 @@ typedef struct crispy_stats {
 int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */
 int crispy_set_timing(crispy_ctx* ctx, int enable);
+
+/* Measured integer-pipe throughput of this GPU in Gop/s (32-bit add/xor
+ * lane operations): the roofline denominator of both hot kernels, which
+ * are integer-bound.  No reference counterpart (measurement utility). */
+int crispy_probe_int32(crispy_ctx* ctx, double* gops);
 
 #ifdef __cplusplus
 }
