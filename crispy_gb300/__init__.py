@@ -81,7 +81,23 @@ PROTOTYPES = {
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "crispy_tune_report": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "crispy_ctx_set_mem_cap": (C.c_int, [_P, C.c_size_t]),
+    "crispy_ctx_mem_in_use": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "crispy_ctx_trim": (C.c_int, [_P]),
+    "crispy_server_create": (C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(_P)]),
+    "crispy_server_destroy": (C.c_int, [_P]),
+    "crispy_server_submit": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_float,
+                                       C.c_float, C.POINTER(C.c_uint64)]),
+    "crispy_server_wait": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_int)]),
+    "crispy_server_result": (C.c_int, [_P, C.c_uint64, SINK, _P, _i64p, _i64p]),
+    "crispy_server_cancel": (C.c_int, [_P, C.c_uint64]),
+    "crispy_server_stats": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), _i64p, _i64p]),
+    "crispy_server_stats_reset": (C.c_int, [_P]),
+    "crispy_server_last_error": (C.c_char_p, [_P]),
 }
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
 
 _lib = None
 
@@ -108,6 +124,15 @@ def default_threshold(n: int, user_thr: float = -1.0, stage: int = 0) -> float:
 
 def array_dim(n: int) -> int:
     return int(load_library().crispy_array_dim(n))
+
+
+def tune_report() -> list:
+    """The autotuner's cached choices (list of dicts)."""
+    import json
+
+    buf = C.create_string_buffer(1 << 16)
+    load_library().crispy_tune_report(buf, len(buf))
+    return json.loads(buf.value.decode() or "[]")
 
 
 def read_fasta(path: str, flavour: int = 0):
@@ -171,6 +196,17 @@ class Engine:
     def _check(self, rc: int):
         if rc != OK:
             raise CrispyError(rc, self.lib.crispy_last_error(self.h).decode())
+
+    def set_mem_cap(self, nbytes: int):
+        self._check(self.lib.crispy_ctx_set_mem_cap(self.h, nbytes))
+
+    def mem_in_use(self) -> int:
+        v = C.c_size_t()
+        self._check(self.lib.crispy_ctx_mem_in_use(self.h, C.byref(v)))
+        return v.value
+
+    def trim(self):
+        self._check(self.lib.crispy_ctx_trim(self.h))
 
     def set_stream(self, stream_handle: int | None):
         self._check(self.lib.crispy_ctx_set_stream(self.h, stream_handle))
@@ -254,6 +290,87 @@ class Engine:
         ns = C.c_int64()
         self._check(self.lib.crispy_gen_run_from_kmer(self.h, band, thr, mode, cb, None, C.byref(ns)))
         return chunks
+
+
+class Server:
+    """Continuous-batching job server (crispy_server_* of the C ABI)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, slots: int = 4):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.crispy_server_create(device, budget_bytes, slots, C.byref(h))
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.crispy_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_server_last_error(self.h).decode())
+
+    def submit(self, buf, offs, lens, k=6, band=10, kmer_thr=-1.0, gen_thr=-1.0) -> int:
+        buf = np.ascontiguousarray(buf, np.uint8)
+        offs = np.ascontiguousarray(offs, np.int64)
+        lens = np.ascontiguousarray(lens, np.int32)
+        jid = C.c_uint64()
+        self._check(self.lib.crispy_server_submit(self.h, _ptr(buf), _ptr(offs), _ptr(lens), len(lens),
+                                                  k, band, kmer_thr, gen_thr, C.byref(jid)))
+        return jid.value
+
+    def wait(self, job: int, timeout_ms: int = -1) -> int:
+        st = C.c_int()
+        rc = self.lib.crispy_server_wait(self.h, job, timeout_ms, C.byref(st))
+        if rc == E_TIMEOUT:
+            return st.value
+        self._check(rc)
+        return st.value
+
+    def result(self, job: int):
+        """(kmer survivor count, [(chunk_id, pairs, dists)]) of a finished job."""
+        chunks = []
+
+        def cb(user, chunk_id, pairs, dists, count):
+            p = np.ctypeslib.as_array(C.cast(pairs, C.POINTER(C.c_uint32)), shape=(count, 2)).copy() if count else np.zeros((0, 2), np.uint32)
+            d = np.ctypeslib.as_array(dists, shape=(count,)).copy() if count else np.zeros(0, np.float32)
+            chunks.append((chunk_id, p, d))
+            return 0
+
+        f = SINK(cb)
+        kp = C.c_int64()
+        gp = C.c_int64()
+        self._check(self.lib.crispy_server_result(self.h, job, f, None, C.byref(kp), C.byref(gp)))
+        return kp.value, chunks
+
+    def cancel(self, job: int):
+        self._check(self.lib.crispy_server_cancel(self.h, job))
+
+    def stats(self) -> dict:
+        p50 = C.c_double()
+        p99 = C.c_double()
+        nj = C.c_int64()
+        npairs = C.c_int64()
+        self._check(self.lib.crispy_server_stats(self.h, C.byref(p50), C.byref(p99), C.byref(nj),
+                                                 C.byref(npairs)))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "jobs": nj.value, "pairs": npairs.value}
+
+    def reset_stats(self):
+        self._check(self.lib.crispy_server_stats_reset(self.h))
 
 
 def compute_kmer_dist(fasta: str, k: int = 6, thr: float = -1.0, dists: bool = False,

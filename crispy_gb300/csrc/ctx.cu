@@ -62,10 +62,11 @@ int cuda_fail(crispy_ctx* ctx, cudaError_t e, const char* what, const char* file
 
 int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes) {
     if (bytes <= b.bytes && b.ptr) return CRISPY_OK;
-    if (b.ptr) cudaFree(b.ptr);
-    b.ptr = nullptr;
-    b.bytes = 0;
+    release(ctx, b);
     size_t want = bytes < 256 ? 256 : bytes;
+    if (ctx && ctx->mem_cap && ctx->mem_in_use + want > ctx->mem_cap)
+        return fail(ctx, CRISPY_E_OOM, "device allocation of %zu bytes exceeds the context cap (%zu of %zu in use)",
+                    want, ctx->mem_in_use, ctx->mem_cap);
     cudaError_t e = cudaMalloc(&b.ptr, want);
     if (e != cudaSuccess) {
         b.ptr = nullptr;
@@ -73,7 +74,17 @@ int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes) {
                     cudaGetErrorString(e));
     }
     b.bytes = want;
+    if (ctx) ctx->mem_in_use += want;
     return CRISPY_OK;
+}
+
+void release(crispy_ctx* ctx, DevBuf& b) {
+    if (b.ptr) {
+        cudaFree(b.ptr);
+        if (ctx) ctx->mem_in_use -= b.bytes;
+    }
+    b.ptr = nullptr;
+    b.bytes = 0;
 }
 
 int ensure_host(crispy_ctx* ctx, HostBuf& b, size_t bytes) {
@@ -176,21 +187,42 @@ int crispy_ctx_create(int device, crispy_ctx** out) {
     return CRISPY_OK;
 }
 
-int crispy_ctx_destroy(crispy_ctx* ctx) {
-    if (!ctx) return CRISPY_OK;
+int crispy_ctx_trim(crispy_ctx* ctx) {
+    if (!ctx) return CRISPY_E_INPUT;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     KmerJob& k = ctx->kmer;
     for (DevBuf* b : {&k.seq, &k.off, &k.len, &k.t, &k.gstart, &k.gent, &k.ent, &k.cntmax,
                       &k.hinfo, &k.keys, &k.keys_alt, &k.vals, &k.vals_alt, &k.pairs, &k.dists,
                       &k.counter, &k.mmin, &k.smin, &k.work, &k.sort_tmp})
-        release(*b);
+        release(ctx, *b);
     GenJob& g = ctx->gen;
     for (DevBuf* b : {&g.seq, &g.off, &g.len, &g.woff, &g.packed, &g.pairs, &g.dist, &g.score,
                       &g.ml, &g.al, &g.flags, &g.scan, &g.blocksum, &g.surv_idx, &g.keys,
                       &g.keys_alt, &g.vals, &g.vals_alt, &g.out_pairs, &g.out_dists, &g.order,
-                      &g.buckets, &g.queue, &g.err})
-        release(*b);
+                      &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue})
+        release(ctx, *b);
+    k.ready = false;
+    g.ready = false;
+    return CRISPY_OK;
+}
+
+int crispy_ctx_set_mem_cap(crispy_ctx* ctx, size_t bytes) {
+    if (!ctx) return CRISPY_E_INPUT;
+    ctx->mem_cap = bytes;
+    return CRISPY_OK;
+}
+
+int crispy_ctx_mem_in_use(const crispy_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return CRISPY_E_INPUT;
+    *bytes = ctx->mem_in_use;
+    return CRISPY_OK;
+}
+
+int crispy_ctx_destroy(crispy_ctx* ctx) {
+    if (!ctx) return CRISPY_OK;
+    crispy_ctx_trim(ctx);
+    GenJob& g = ctx->gen;
     release_host(g.h_pairs);
     release_host(g.h_dists);
     for (auto* ev : {&ctx->ev_kmer, &ctx->ev_gen}) {

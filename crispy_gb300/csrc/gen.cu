@@ -30,7 +30,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 
 #include "internal.h"
 
@@ -84,17 +89,19 @@ __device__ __forceinline__ void track(Best& b, int m, uint32_t l, int at) {
     if (m >= b.m) { b.m = m; b.l = l; b.at = at; }
 }
 
-// Largest m over the warp, ties to the largest index `at`; returns the
-// winner's packed ML|AL.
-__device__ __forceinline__ Best warp_best(Best b) {
+// Largest m over a G-lane sub-group, ties to the largest index `at`;
+// returns the winner's packed ML|AL.
+template <int G>
+__device__ __forceinline__ Best group_best(Best b, int lane) {
     const long long mine = (long long)b.m * 4294967296LL + (long long)(unsigned)(b.at + 1);
     long long key = mine;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = G / 2; o > 0; o >>= 1) {
         long long other = __shfl_xor_sync(0xffffffffu, key, o);
         key = other > key ? other : key;
     }
-    const unsigned who = __ballot_sync(0xffffffffu, mine == key);
+    const unsigned group = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const unsigned who = __ballot_sync(0xffffffffu, mine == key) & group;
     const int src = __ffs(who) - 1;
     Best r;
     r.m = (int)(key >> 32);
@@ -112,24 +119,31 @@ struct Lane {
     uint32_t w1[C], w2[C];
 };
 
-// One anti-diagonal step at parity P for all C slots of this lane.
-// kChecked adds the matrix-border logic (boundary cells, cells before the
-// matrix, last-row / last-column tracking).
-template <int C, int P, bool kChecked>
-__device__ __forceinline__ void step(Lane<C>& st, int lane, int s, int kb, int l1, int l2,
-                                     uint32_t band_ok, Best& col, Best& row) {
+// Per-pair values a sub-group holds (the same in all its lanes).
+struct PairCtx {
+    int kb, l1, l2, shift;   // shift = kb & 1: odd bands run one step late
+    uint32_t band_ok;        // bit 2c+P: slot c's parity-P diagonal is in band
+};
+
+// One anti-diagonal step at parity P for all C slots of this lane.  The
+// sub-group's own step is s = t - shift, which makes P = t & 1 for every
+// sub-group of the warp.  kChecked adds the matrix-border logic (boundary
+// cells, cells before the matrix, last-row / last-column tracking).
+template <int G, int C, int P, bool kChecked>
+__device__ __forceinline__ void step(Lane<C>& st, int gl, int s, const PairCtx& pc, Best& col,
+                                     Best& row) {
     int nbM;
     uint32_t nbL;
     if (P == 0) {
         // left = slot q-1 (its gap-left copy), from the previous lane for c = 0
-        nbM = __shfl_up_sync(0xffffffffu, st.cF[C - 1], 1);
-        nbL = __shfl_up_sync(0xffffffffu, st.cL[C - 1], 1);
-        if (lane == 0) nbM = kNeg;
+        nbM = __shfl_up_sync(0xffffffffu, st.cF[C - 1], 1, G);
+        nbL = __shfl_up_sync(0xffffffffu, st.cL[C - 1], 1, G);
+        if (gl == 0) nbM = kNeg;
     } else {
         // up = slot q+1 (its gap-up copy), from the next lane for c = C-1
-        nbM = __shfl_down_sync(0xffffffffu, st.cU[0], 1);
-        nbL = __shfl_down_sync(0xffffffffu, st.cL[0], 1);
-        if (lane == 31) nbM = kNeg;
+        nbM = __shfl_down_sync(0xffffffffu, st.cU[0], 1, G);
+        nbL = __shfl_down_sync(0xffffffffu, st.cL[0], 1, G);
+        if (gl == G - 1) nbM = kNeg;
     }
     int nM[C], nU[C], nF[C];
     uint32_t nL[C];
@@ -148,28 +162,30 @@ __device__ __forceinline__ void step(Lane<C>& st, int lane, int s, int kb, int l
         }
         const bool match = (st.w1[c] ^ st.w2[c]) < 0x40000000u;
         const int md = st.pM[c] + (match ? kMatch : kMismatch);
-        const int mx = max(md, max(upM, lfM));
-        const bool isD = mx == md;
-        const bool isU = upM >= lfM;
+        // max with predicate: isU = up >= left (up wins ties over left),
+        // isD = diag >= max(up, left) (diag wins every tie)
+        bool isU, isD;
+        const int mul = __vibmax_s32(upM, lfM, &isU);
+        const int mx = __vibmax_s32(md, mul, &isD);
         const uint32_t lpred = isU ? upL : lfL;
         uint32_t l = isD ? st.pL[c] + (match ? 0x1u : 0x10001u) : lpred + 0x10001u;
         int pu = isD ? kGO : (isU ? kGE : 0);
         int pf = isD ? kGO : (isU ? 0 : kGE);
         int m = mx;
-        const int q = lane * C + c;
-        const int d = 2 * q - kb + P;
+        const int q = (gl * C + c);
+        const int d = 2 * q - pc.kb + P;
         if (kChecked) {
             const int i = (s + d) >> 1, j = (s - d) >> 1;
-            if (!((band_ok >> (2 * c + P)) & 1u) || i < 0 || j < 0) {
+            if (!((pc.band_ok >> (2 * c + P)) & 1u) || i < 0 || j < 0) {
                 m = kNeg; pu = 0; pf = 0; l = 0;
             } else if (i == 0 || j == 0) {
                 m = 0; pu = 0; pf = 0; l = (uint32_t)(i + j);
             } else {
-                if (i == l2 && j <= l1) track(col, m, l, j);
-                if (j == l1 && i <= l2) track(row, m, l, i);
+                if (i == pc.l2 && j <= pc.l1) track(col, m, l, j);
+                if (j == pc.l1 && i <= pc.l2) track(row, m, l, i);
             }
         } else {
-            if (!((band_ok >> (2 * c + P)) & 1u)) { m = kNeg; pu = 0; pf = 0; l = 0; }
+            if (!((pc.band_ok >> (2 * c + P)) & 1u)) { m = kNeg; pu = 0; pf = 0; l = 0; }
         }
         nM[c] = m; nU[c] = m + pu; nF[c] = m + pf; nL[c] = l;
     }
@@ -186,66 +202,79 @@ __device__ __forceinline__ void step(Lane<C>& st, int lane, int s, int kb, int l
 // loaded at the block start cover every position the block touches.
 constexpr int kBlockSteps = 30;
 
-template <int C, int P0, bool kChecked>
-__device__ __forceinline__ void block_steps(Lane<C>& st, int lane, int s0, int kb, int l1, int l2,
-                                            uint32_t band_ok, Best& col, Best& row) {
+template <int G, int C, bool kChecked>
+__device__ __forceinline__ void block_steps(Lane<C>& st, int gl, int s0, const PairCtx& pc,
+                                            Best& col, Best& row) {
 #pragma unroll 3
     for (int t = 0; t < kBlockSteps; t += 2) {
-        step<C, P0, kChecked>(st, lane, s0 + t, kb, l1, l2, band_ok, col, row);
-        step<C, P0 ^ 1, kChecked>(st, lane, s0 + t + 1, kb, l1, l2, band_ok, col, row);
+        step<G, C, 0, kChecked>(st, gl, s0 + t, pc, col, row);
+        step<G, C, 1, kChecked>(st, gl, s0 + t + 1, pc, col, row);
     }
 }
 
-template <int C, int P0>
-__device__ void align_sweep(Lane<C>& st, const uint32_t* sm1, const uint32_t* sm2, int lane,
-                            int kb, int l1, int l2, Best& col, Best& row) {
-    uint32_t band_ok = 0;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        const int q = lane * C + c;
-        if (2 * q - kb <= kb) band_ok |= 1u << (2 * c);          // parity 0 diagonal in band
-        if (2 * q - kb + 1 <= kb) band_ok |= 1u << (2 * c + 1);  // parity 1 diagonal in band
-    }
-    const int s_end = l1 + l2;
-    const int clean_hi = 2 * min(l1, l2) - kb - 1;
-    for (int s0 = 0; s0 <= s_end; s0 += kBlockSteps) {
+template <int G, int C>
+__device__ void align_sweep(Lane<C>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
+                            const PairCtx& pc, int t_end, Best& col, Best& row) {
+    const int clean_hi = 2 * min(pc.l1, pc.l2) - pc.kb - 1;
+    for (int t0 = 0; t0 <= t_end; t0 += kBlockSteps) {
+        const int s0 = t0 - pc.shift;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            const int d = 2 * (lane * C + c) - kb + P0;
+            const int d = 2 * (gl * C + c) - pc.kb;   // parity 0 at the block start
             const int i = (s0 + d) >> 1, j = (s0 - d) >> 1;
             st.w2[c] = window_at(sm2, i - 1);
             st.w1[c] = window_at(sm1, j - 1);
         }
-        if (s0 >= kb + 2 && s0 + kBlockSteps - 1 < clean_hi)
-            block_steps<C, P0, false>(st, lane, s0, kb, l1, l2, band_ok, col, row);
+        const bool clean = s0 >= pc.kb + 2 && s0 + kBlockSteps - 1 < clean_hi;
+        if (__all_sync(0xffffffffu, clean))
+            block_steps<G, C, false>(st, gl, s0, pc, col, row);
         else
-            block_steps<C, P0, true>(st, lane, s0, kb, l1, l2, band_ok, col, row);
+            block_steps<G, C, true>(st, gl, s0, pc, col, row);
     }
 }
 
-template <int C>
+// One pair per G-lane sub-group (32/G pairs per warp), C band slots per
+// lane, so a pair with kBand + 1 <= G*C slots fits.
+template <int G, int C>
 __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
-    __shared__ uint32_t smem[kGenWarps][2][kSmWords];
+    constexpr int kPerWarp = 32 / G;
+    __shared__ uint32_t smem[kGenWarps][kPerWarp][2][kSmWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* sm1 = smem[warp][0];
-    uint32_t* sm2 = smem[warp][1];
-    int64_t item = a.queue ? -1 : (int64_t)blockIdx.x * kGenWarps + warp;
-    const int64_t stride = (int64_t)gridDim.x * kGenWarps;
+    const int sub = lane / G, gl = lane % G;
+    uint32_t* sm1 = smem[warp][sub][0];
+    uint32_t* sm2 = smem[warp][sub][1];
+    int64_t base = a.queue ? -1 : ((int64_t)blockIdx.x * kGenWarps + warp) * kPerWarp;
+    const int64_t stride = (int64_t)gridDim.x * kGenWarps * kPerWarp;
     for (;;) {
         if (a.queue) {
             unsigned w = 0;
-            if (lane == 0) w = atomicAdd(a.queue, 1u);
-            item = __shfl_sync(0xffffffffu, w, 0);
+            if (lane == 0) w = atomicAdd(a.queue, (unsigned)kPerWarp);
+            base = __shfl_sync(0xffffffffu, w, 0);
         }
-        if (item >= a.count) break;
-        const int64_t p = a.order ? (int64_t)a.order[item] : item;
-        const int2 pr = a.pairs[p];
-        const int l1 = a.len[pr.x], l2 = a.len[pr.y];
-        const int kb = kband_of(l1, l2, a.band);
-        const int nw1 = (l1 + 15) >> 4, nw2 = (l2 + 15) >> 4;
-        const uint32_t* g1 = a.packed + a.woff[pr.x];
-        const uint32_t* g2 = a.packed + a.woff[pr.y];
-        for (int k = lane; k < kSmWords; k += 32) {
+        if (base >= a.count) break;
+        const int64_t item = base + sub;
+        const bool valid = item < a.count;
+        int64_t p = -1;
+        PairCtx pc{0, 0, 0, 0, 0};
+        int2 pr = make_int2(0, 0);
+        if (valid) {
+            p = a.order ? (int64_t)a.order[item] : item;
+            pr = a.pairs[p];
+            pc.l1 = a.len[pr.x];
+            pc.l2 = a.len[pr.y];
+            pc.kb = kband_of(pc.l1, pc.l2, a.band);
+        }
+        pc.shift = pc.kb & 1;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int q = gl * C + c;
+            if (valid && 2 * q - pc.kb <= pc.kb) pc.band_ok |= 1u << (2 * c);
+            if (valid && 2 * q - pc.kb + 1 <= pc.kb) pc.band_ok |= 1u << (2 * c + 1);
+        }
+        const int nw1 = (pc.l1 + 15) >> 4, nw2 = (pc.l2 + 15) >> 4;
+        const uint32_t* g1 = a.packed + (valid ? a.woff[pr.x] : 0);
+        const uint32_t* g2 = a.packed + (valid ? a.woff[pr.y] : 0);
+        for (int k = gl; k < kSmWords; k += G) {
             sm1[k] = k < nw1 ? g1[k] : 0u;
             sm2[k] = k < nw2 ? g2[k] : 0u;
         }
@@ -257,11 +286,11 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
             st.pM[c] = kNeg; st.pL[c] = 0;
         }
         Best col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
-        if (kb & 1) align_sweep<C, 1>(st, sm1, sm2, lane, kb, l1, l2, col, row);
-        else align_sweep<C, 0>(st, sm1, sm2, lane, kb, l1, l2, col, row);
-        col = warp_best(col);
-        row = warp_best(row);
-        if (lane == 0) {
+        const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)(pc.l1 + pc.l2 + pc.shift));
+        align_sweep<G, C>(st, sm1, sm2, gl, pc, t_end, col, row);
+        col = group_best<G>(col, lane);
+        row = group_best<G>(row, lane);
+        if (gl == 0 && valid) {
             const bool use_col = col.m > row.m;   // genKernel.cu:765-768
             const uint32_t l = use_col ? col.l : row.l;
             const int mlv = (int)(l >> 16), alv = (int)(l & 0xffffu);
@@ -271,7 +300,7 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
             if (a.al) a.al[p] = alv;
         }
         __syncwarp();
-        if (!a.queue) item += stride;
+        if (!a.queue) base += stride;
     }
 }
 
@@ -408,29 +437,139 @@ __global__ void gen_gather_kernel(const int2* __restrict__ pairs, const uint32_t
     out_dists[i] = __uint_as_float(keys[i]);
 }
 
-int slots_per_lane(int kb) { return (kb + 1 + 31) / 32; }
+// Register-resident shapes (sub-group lanes G, band slots per lane C).
+// Every one serves a pair with kBand + 1 <= G * C.
+struct Shape {
+    int g, c;
+};
+constexpr Shape kShapes[] = {{8, 1},  {8, 2},  {8, 4},  {16, 1}, {16, 2}, {16, 3}, {16, 4},
+                             {16, 6}, {32, 1}, {32, 2}, {32, 3}, {32, 4}, {32, 6}, {32, 8}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-// register-resident widths compiled; wider bands use gen_wide_kernel
-int bucket_c(int c) {
-    if (c <= 1) return 1;
-    if (c <= 2) return 2;
-    if (c <= 3) return 3;
-    if (c <= 4) return 4;
-    if (c <= 6) return 6;
-    if (c <= 8) return 8;
+// Pairs are binned by band slots; bin 0 is the wide-band kernel.
+constexpr int kBinSlots[] = {0, 8, 16, 32, 48, 64, 96, 128, 192, 256};
+constexpr int kNumBins = sizeof(kBinSlots) / sizeof(kBinSlots[0]);
+// untuned shape per bin (the plain form always uses it)
+constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 5, 6, 7, 11, 12, 13};
+
+int bin_for_slots(int slots) {
+    for (int b = 1; b < kNumBins; ++b)
+        if (kBinSlots[b] >= slots) return b;
     return 0;
 }
 
 using WarpFn = void (*)(GenArgs);
-WarpFn warp_fn(int c) {
-    switch (c) {
-        case 1: return gen_warp_kernel<1>;
-        case 2: return gen_warp_kernel<2>;
-        case 3: return gen_warp_kernel<3>;
-        case 4: return gen_warp_kernel<4>;
-        case 6: return gen_warp_kernel<6>;
-        default: return gen_warp_kernel<8>;
+WarpFn shape_fn(int shape) {
+    switch (shape) {
+        case 0: return gen_warp_kernel<8, 1>;
+        case 1: return gen_warp_kernel<8, 2>;
+        case 2: return gen_warp_kernel<8, 4>;
+        case 3: return gen_warp_kernel<16, 1>;
+        case 4: return gen_warp_kernel<16, 2>;
+        case 5: return gen_warp_kernel<16, 3>;
+        case 6: return gen_warp_kernel<16, 4>;
+        case 7: return gen_warp_kernel<16, 6>;
+        case 8: return gen_warp_kernel<32, 1>;
+        case 9: return gen_warp_kernel<32, 2>;
+        case 10: return gen_warp_kernel<32, 3>;
+        case 11: return gen_warp_kernel<32, 4>;
+        case 12: return gen_warp_kernel<32, 6>;
+        default: return gen_warp_kernel<32, 8>;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: for each bin of a batched run, every shape that covers the bin
+// without wasting more than half its slots is timed (CUDA events) on a
+// strided sample of the bin's pairs; the fastest is cached per (band, bin,
+// length bucket, SM count) for the life of the process.  Any shape gives the
+// same bits, so tuning only picks speed.
+// ---------------------------------------------------------------------------
+struct TuneKey {
+    int band, bin, len_bucket, sms;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(band, bin, len_bucket, sms) < std::tie(o.band, o.bin, o.len_bucket, o.sms);
+    }
+};
+struct TuneEntry {
+    int shape;
+    float ms_best, ms_default;
+    int64_t sample;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tuned;
+
+bool autotune_enabled() {
+    const char* e = std::getenv("CRISPY_AUTOTUNE");
+    return !(e && e[0] == '0');
+}
+
+int launch_shape(crispy_ctx* ctx, cudaStream_t s, int shape, GenArgs a, bool timed) {
+    WarpFn fn = shape_fn(shape);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGenThreads, 0);
+    const int64_t per_block = (int64_t)kGenWarps * (32 / kShapes[shape].g);
+    const int blocks = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
+                                              (a.count + per_block - 1) / per_block);
+    if (timed) ev_begin(ctx, ctx->ev_gen, s);
+    fn<<<std::max(blocks, 1), kGenThreads, 0, s>>>(a);
+    if (timed) ev_end(ctx, ctx->ev_gen, s);
+    count_launch(ctx);
+    return CRISPY_OK;
+}
+
+int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, int len_bucket,
+               const GenArgs& a, const std::vector<uint32_t>& host_order, int64_t first,
+               int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf) {
+    const int dflt = kDefaultShape[bin];
+    if (!autotune_enabled() || n_items < 4096) return dflt;
+    const TuneKey key{band, bin, len_bucket, ctx->sm_count};
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) return it->second.shape;
+    }
+    // strided sample of the bin (keeps its length spread)
+    const int64_t want = std::min<int64_t>(n_items, 24576);
+    std::vector<uint32_t> samp(want);
+    for (int64_t i = 0; i < want; ++i) samp[i] = host_order[first + i * n_items / want];
+    CRISPY_TRY(ensure(ctx, sample_buf, (size_t)want * 4));
+    CRISPY_TRY(ensure(ctx, queue_buf, 64 * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(sample_buf.ptr, samp.data(), (size_t)want * 4, cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = dflt;
+    float best_ms = 1e30f, dflt_ms = 0;
+    const int need = kBinSlots[bin];
+    int qslot = 0;
+    for (int sh = 0; sh < kNumShapes; ++sh) {
+        const int slots = kShapes[sh].g * kShapes[sh].c;
+        if (slots < need || slots > 2 * need) continue;
+        float ms = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            GenArgs t = a;
+            t.order = sample_buf.as<uint32_t>();
+            t.count = want;
+            t.queue = queue_buf.as<unsigned int>() + (qslot++ % 64);
+            CRISPY_CK(ctx, cudaMemsetAsync(t.queue, 0, 4, s));
+            cudaEventRecord(e0, s);
+            launch_shape(ctx, s, sh, t, false);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float m = 0;
+            cudaEventElapsedTime(&m, e0, e1);
+            ms = std::min(ms, m);
+        }
+        if (sh == dflt) dflt_ms = ms;
+        if (ms < best_ms) { best_ms = ms; best = sh; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CRISPY_CK(ctx, cudaGetLastError());
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tuned[key] = TuneEntry{best, best_ms, dflt_ms, want};
+    return best;
 }
 
 }  // namespace
@@ -467,12 +606,14 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     GenJob& g = ctx->gen;
     if (count <= 0) return CRISPY_OK;
     std::vector<uint8_t> cls(count);
+    std::vector<uint16_t> span(count);   // l1 + l2, the pair's step count
     int kbmax = 0;
     int64_t cells = 0;
     for (int64_t p = 0; p < count; ++p) {
         const int l1 = g.h_len[h_pairs[2 * p]], l2 = g.h_len[h_pairs[2 * p + 1]];
         const int kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
-        cls[p] = (uint8_t)bucket_c(slots_per_lane(kb));
+        cls[p] = (uint8_t)bin_for_slots(kb + 1);
+        span[p] = (uint16_t)(l1 + l2);
         if (cls[p] == 0) kbmax = std::max(kbmax, kb);
         cells += band_cells(l1, l2, band);
     }
@@ -485,7 +626,6 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     base.pairs = d_pairs;
     base.band = band;
     base.dist = d_dist; base.score = d_score; base.ml = d_ml; base.al = d_al;
-    const int wpb = kGenWarps;
     auto launch_wide = [&](const GenArgs& ga, const uint32_t* order, int64_t n_items) -> int {
         const int rs = 2 * kbmax + 3;
         const int threads = 128;
@@ -512,6 +652,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
                 if (cls[p] == 0) wide = true;
                 cmax = std::max<int>(cmax, cls[p]);
             }
+            const int shape = kDefaultShape[cmax];
             GenArgs a = base;
             a.pairs = d_pairs + w0;
             a.count = n_items;
@@ -523,60 +664,52 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
                 CRISPY_TRY(launch_wide(a, nullptr, n_items));
                 continue;
             }
-            const int blocks = (int)std::min<int64_t>((n_items + wpb - 1) / wpb, (int64_t)ctx->sm_count * 8);
-            ev_begin(ctx, ctx->ev_gen, s);
-            warp_fn(cmax)<<<blocks, kGenThreads, 0, s>>>(a);
-            ev_end(ctx, ctx->ev_gen, s);
-            count_launch(ctx);
+            CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
             ctx->stats.gen_launches++;
         }
         CRISPY_CK(ctx, cudaGetLastError());
         return CRISPY_OK;
     }
-    // batched: bucket order (counting sort by class, longest pairs first inside
-    // a class so the persistent queue drains evenly)
-    const int classes[7] = {1, 2, 3, 4, 6, 8, 0};
+    // batched: bucket order -- band-slot bin first, then longest pairs first
+    // inside a bin, so the sub-groups of a warp get pairs of similar length
+    // and the persistent queue drains evenly
     std::vector<uint32_t> order(count);
-    std::vector<int64_t> start(8, 0);
+    for (int64_t p = 0; p < count; ++p) order[p] = (uint32_t)p;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const int cx = cls[x] == 0 ? kNumBins : cls[x], cy = cls[y] == 0 ? kNumBins : cls[y];
+        if (cx != cy) return cx < cy;
+        return span[x] > span[y];
+    });
+    std::vector<int64_t> start(kNumBins + 2, 0);   // by bin, wide last
     {
-        std::vector<int64_t> cnt(9, 0);
-        for (int64_t p = 0; p < count; ++p) cnt[cls[p]]++;
         int64_t at = 0;
-        for (int ci = 0; ci < 7; ++ci) {
+        for (int ci = 1; ci <= kNumBins; ++ci) {
             start[ci] = at;
-            at += cnt[classes[ci]];
+            const int want = ci == kNumBins ? 0 : ci;
+            while (at < count && cls[order[at]] == want) ++at;
         }
-        start[7] = at;
-        std::vector<int64_t> fill(start.begin(), start.end());
-        std::vector<int> slot(9, -1);
-        for (int ci = 0; ci < 7; ++ci) slot[classes[ci]] = ci;
-        for (int64_t p = 0; p < count; ++p) order[fill[slot[cls[p]]]++] = (uint32_t)p;
+        start[kNumBins + 1] = at;
     }
     CRISPY_TRY(ensure(ctx, g.order, (size_t)count * 4));
     CRISPY_TRY(ensure(ctx, g.queue, 64));
     CRISPY_CK(ctx, cudaMemcpyAsync(g.order.ptr, order.data(), (size_t)count * 4, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemsetAsync(g.queue.ptr, 0, 64, s));
-    for (int ci = 0; ci < 7; ++ci) {
+    for (int ci = 1; ci <= kNumBins; ++ci) {
         const int64_t n_items = start[ci + 1] - start[ci];
         if (n_items == 0) continue;
         const uint32_t* ord = g.order.as<uint32_t>() + start[ci];
-        if (classes[ci] == 0) {
+        if (ci == kNumBins) {
             CRISPY_TRY(launch_wide(base, ord, n_items));
             continue;
         }
+        const int len_bucket = span[order[start[ci]]] / 128;
         GenArgs a = base;
+        const int shape = pick_shape(ctx, s, band, ci, len_bucket, a, order, start[ci], n_items,
+                                     g.tune_sample, g.tune_queue);
         a.order = ord;
         a.count = n_items;
         a.queue = g.queue.as<unsigned int>() + ci;
-        int per_sm = 1;
-        WarpFn fn = warp_fn(classes[ci]);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGenThreads, 0);
-        const int blocks = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
-                                                  (n_items + wpb - 1) / wpb);
-        ev_begin(ctx, ctx->ev_gen, s);
-        fn<<<blocks, kGenThreads, 0, s>>>(a);
-        ev_end(ctx, ctx->ev_gen, s);
-        count_launch(ctx);
+        CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
         ctx->stats.gen_launches++;
     }
     CRISPY_CK(ctx, cudaGetLastError());
@@ -779,6 +912,32 @@ int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int ba
     ctx->stats.gen_survivors = ns;
     if (nsurvivors) *nsurvivors = ns;
     return CRISPY_OK;
+}
+
+int crispy_tune_report(char* buf, size_t len) {
+    if (!buf || len == 0) return CRISPY_E_INPUT;
+    std::string out = "[";
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        bool first = true;
+        for (auto& kv : g_tuned) {
+            char item[256];
+            const Shape sh = kShapes[kv.second.shape];
+            snprintf(item, sizeof item,
+                     "%s{\"stage\": \"gen\", \"band\": %d, \"band_slots\": %d, \"len_bucket\": %d, "
+                     "\"sms\": %d, \"lanes_per_pair\": %d, \"slots_per_lane\": %d, "
+                     "\"pairs_per_block\": %d, \"sample\": %lld, \"ms\": %.4f, \"default_ms\": %.4f}",
+                     first ? "" : ", ", kv.first.band, kBinSlots[kv.first.bin], kv.first.len_bucket,
+                     kv.first.sms, sh.g, sh.c, kGenWarps * (32 / sh.g), (long long)kv.second.sample,
+                     kv.second.ms_best, kv.second.ms_default);
+            out += item;
+            first = false;
+        }
+    }
+    out += "]";
+    std::strncpy(buf, out.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return out.size() < len ? CRISPY_OK : CRISPY_E_INPUT;
 }
 
 int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, crispy_sink sink,

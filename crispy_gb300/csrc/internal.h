@@ -53,7 +53,7 @@ struct GenJob {
     std::vector<int64_t> h_woff;     // first packed word of each read
     DevBuf seq, off, len, woff, packed;
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
-        vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err;
+        vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue;
     HostBuf h_pairs, h_dists;
 };
 
@@ -77,10 +77,9 @@ struct crispy_ctx {
     crispy::KmerJob kmer;
     crispy::GenJob gen;
     crispy::StreamEvents ev_kmer, ev_gen;
+    size_t mem_cap = 0;      // 0 = unlimited
+    size_t mem_in_use = 0;   // bytes held by DevBuf allocations
     cudaEvent_t t_begin = nullptr, t_end = nullptr;
-    // autotuned parameters, keyed by workload shape (see tune.cu)
-    int kmer_chunk_groups = 0;   // column groups per batched work item (0 = auto)
-    int gen_warps_per_block = 0;
 };
 
 namespace crispy {
@@ -90,6 +89,7 @@ int cuda_fail(crispy_ctx* ctx, cudaError_t e, const char* what, const char* file
 int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes);
 int ensure_host(crispy_ctx* ctx, HostBuf& b, size_t bytes);
 void release(DevBuf& b);
+void release(crispy_ctx* ctx, DevBuf& b);
 void release_host(HostBuf& b);
 
 // Event pair around a launch, when timing is enabled.

@@ -12,23 +12,27 @@
 //   * min(a, b) = sum_{t>=1} [a >= t][b >= t].  Every read becomes a list of
 //     T "level entries" (t-1)*4^K + kmer, one per occurrence, where t is the
 //     occurrence rank of that K-mer in the read.  Then
-//         m(a, b) = #{ entries e of b : P_a[e] }   with P_a = entry set of a.
+//         m(a, b) = #{ entries e of b : e in entries(a) }.
 //   * A block owns 32 row reads and keeps their entry sets in shared memory
 //     as bit planes: word P[e] has bit r set iff row read r holds entry e.
 //     One 32-bit shared load answers one column entry for 32 row reads.
+//     Levels 1..levels live in dense planes (4^K words each); the rare
+//     entries of higher level go to a small open-addressing hash table in
+//     shared memory, so the footprint stays fixed whatever the reads hold.
 //   * A warp owns 32 column reads (one per lane) and streams their entries
-//     from an interleaved layout (entry e of the 32 reads of a group is one
-//     128-byte line), gathers P[e], and adds the word into 32 bit-sliced
-//     counters with a Harley-Seal carry-save tree (LOP3 work only).
+//     from an interleaved layout (four consecutive entries of the 32 reads
+//     of a group form one 512-byte line, one uint4 per lane), gathers P[e],
+//     and adds the word into 32 bit-sliced counters with a Harley-Seal
+//     carry-save tree (LOP3 work only).  The next 16 entries are in flight
+//     while the current 16 are reduced.
 //   * The threshold is an integer test m >= mmin[min(Ta, Tb)], with mmin
 //     tabulated on the host from the reference's float expression (the pass
 //     predicate is monotone in m), first as a bit-sliced compare against a
 //     per-lane lower bound, then exactly for the few candidates.  Survivors
 //     leave through warp-aggregated atomics as (stage, row, col) sort keys;
 //     one stable radix sort restores the reference's stage order.
-//   * Rows whose K-mer multiplicity exceeds the shared-memory level budget,
-//     and K = 8 (whose reference count is not the min-sum, see
-//     kmer_dense_kernel), run through an exact dense-table kernel.
+//   * K = 8 (65,536 bins per level) and row groups whose high-level entries
+//     would overflow the hash run through an exact dense-table kernel.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,9 +46,11 @@ namespace crispy {
 namespace {
 
 constexpr uint32_t kSentinel = 0xFFFFFFFFu;
-constexpr int kTileThreads = 256;
+constexpr int kTileThreads = 512;
 constexpr int kTileWarps = kTileThreads / 32;
-constexpr int kSmemBudget = 200 * 1024;
+constexpr int kHashSlots = 1024;        // high-level entries of one row group
+constexpr int kHashMaxKeys = 512;       // load factor <= 1/2 keeps probes short
+constexpr int kPlaneBudget = 96 * 1024; // dense level planes per block
 
 __device__ __forceinline__ uint32_t sym2(uint8_t c) {
     // A=0 G=1 T=2 C=3, everything else 0 (kmerMain.cpp:137-152)
@@ -57,39 +63,51 @@ __device__ __forceinline__ uint32_t kmer_at(const uint8_t* s, int p, int K) {
     return v;
 }
 
+// Entry e of lane l inside a group block: four consecutive entries of one
+// lane are one uint4, and the 32 lanes' uint4 of the same quad are adjacent.
+__device__ __forceinline__ int64_t ent_at(int e, int lane) {
+    return (int64_t)(e >> 2) * 128 + lane * 4 + (e & 3);
+}
+
 // ---------------------------------------------------------------------------
 // Preparation: one block per read.  Occurrence ranks come from a shared
 // histogram with two 16-bit counters per word (counts <= 2048), so K = 8
 // (65,536 bins) fits in 128 KB.  Writes the read's level entries into its
-// lane of the group's interleaved block, its largest multiplicity, and for
-// K = 8 the (largest K-mer >= 0x8000, its count) key used by the quirk.
+// lane of the group's interleaved block, its largest multiplicity, its count
+// of entries above the dense levels, and for K = 8 the (largest K-mer >=
+// 0x8000, its count) key used by the quirk.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) kmer_prep_kernel(
     const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
-    const int32_t* __restrict__ tcount, int n, int K, const int64_t* __restrict__ gstart,
-    const int32_t* __restrict__ gent, uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax,
+    const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
+    const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
+    uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
     uint32_t* __restrict__ hinfo) {
     extern __shared__ uint32_t hist[];
-    __shared__ int s_max;
+    __shared__ int s_max, s_high;
     __shared__ uint32_t s_hmax;
     const uint32_t K4 = 1u << (2 * K);
     const int hwords = (int)((K4 + 1) / 2);
     for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; }
+        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_high = 0; }
         __syncthreads();
         const int T = tcount[r];
         const uint8_t* s = seq + off[r];
-        uint32_t* dst = ent + gstart[r >> 5] + (r & 31);
+        uint32_t* dst = ent + gstart[r >> 5];
+        const int lane = r & 31;
         const int E = gent[r >> 5];
+        int high = 0;
         for (int p = threadIdx.x; p < T; p += blockDim.x) {
             const uint32_t v = kmer_at(s, p, K);
             const uint32_t sh = (v & 1u) * 16u;
             const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
             const uint32_t t = (old >> sh) & 0xFFFFu;
-            dst[(int64_t)p * 32] = t * K4 + v;
+            dst[ent_at(p, lane)] = t * K4 + v;
+            high += (int)t >= dense_levels;
         }
-        for (int p = T + threadIdx.x; p < E; p += blockDim.x) dst[(int64_t)p * 32] = kSentinel;
+        for (int p = T + threadIdx.x; p < E; p += blockDim.x) dst[ent_at(p, lane)] = kSentinel;
+        atomicAdd(&s_high, high);
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
@@ -104,6 +122,7 @@ __global__ void __launch_bounds__(256) kmer_prep_kernel(
         __syncthreads();
         if (threadIdx.x == 0) {
             cntmax[r] = s_max;
+            nhigh[r] = s_high;
             uint32_t info = 0;
             if (K == 8 && s_hmax >= 0x8000u) {
                 const uint32_t c = (hist[s_hmax >> 1] >> ((s_hmax & 1u) * 16u)) & 0xFFFFu;
@@ -122,12 +141,12 @@ struct TileArgs {
     const int64_t* gstart;
     const int32_t* gent;
     const int32_t* tcount;
-    const int32_t* cntmax;
+    const uint8_t* dense_group;   // row groups the dense kernel takes instead
     const uint16_t* mmin;
     const uint16_t* smin;
     int n;
     uint32_t K4;
-    int levels_cap;   // level planes that fit the dynamic shared memory
+    int levels;                    // dense level planes in shared memory
     int A, stage_dim;
     unsigned long long* counter;
     uint64_t* keys;
@@ -135,8 +154,8 @@ struct TileArgs {
     int64_t cap;
     // plain: one rectangle of rows x cols (one reference stage)
     int r_lo, r_hi, c_lo, c_hi;
-    // batched: work queue of (row group, first col group, end col group)
-    const int4* items;
+    // batched: work queue over row groups (all their columns)
+    const int* items;
     int nitems;
     unsigned int* queue_head;
 };
@@ -157,31 +176,60 @@ __device__ __forceinline__ uint64_t stage_key(int r, int c, int n, int A, int sd
 }
 
 // Survivor emission with one atomic per warp.  All 32 lanes call it.
-__device__ __forceinline__ void emit(const TileArgs& a, bool pass, int r, int c, int m, int mn) {
+__device__ __forceinline__ void emit(unsigned long long* counter, uint64_t* keys, uint32_t* vals,
+                                     int64_t cap, int n, int A, int sd, bool pass, int r, int c,
+                                     int m, int mn) {
     const unsigned pm = __ballot_sync(0xffffffffu, pass);
     if (!pm) return;
     const int lane = threadIdx.x & 31;
     unsigned long long base = 0;
     const int leader = __ffs(pm) - 1;
-    if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(pm));
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(pm));
     base = __shfl_sync(0xffffffffu, base, leader);
     if (pass) {
         const unsigned long long idx = base + __popc(pm & ((1u << lane) - 1u));
-        if (idx < (unsigned long long)a.cap) {
-            a.keys[idx] = stage_key(r, c, a.n, a.A, a.stage_dim);
+        if (idx < (unsigned long long)cap) {
+            keys[idx] = stage_key(r, c, n, A, sd);
             // kmerKernel.cu:47: 1.0f - (float)matches / min(T1, T2), IEEE
             const float d = __fsub_rn(1.0f, __fdiv_rn((float)m, (float)mn));
-            a.vals[idx] = __float_as_uint(d);
+            vals[idx] = __float_as_uint(d);
         }
     }
 }
 
+__device__ __forceinline__ uint32_t hash_slot(uint32_t key) {
+    return (key * 0x9E3779B1u) >> (32 - 10);   // kHashSlots = 1024
+}
+
+// Row bits of a high-level entry (absent -> 0).  Rare path.
+__device__ __noinline__ uint32_t hash_find(const uint32_t* hkeys, const uint32_t* hmask,
+                                           uint32_t key) {
+    uint32_t h = hash_slot(key);
+    for (int probe = 0; probe < kHashSlots; ++probe) {
+        const uint32_t k = hkeys[h];
+        if (k == key) return hmask[h];
+        if (k == kSentinel) return 0u;
+        h = (h + 1) & (kHashSlots - 1);
+    }
+    return 0u;
+}
+
+__device__ __forceinline__ uint32_t lookup(const uint32_t* __restrict__ P, uint32_t limit,
+                                           const uint32_t* hkeys, const uint32_t* hmask,
+                                           bool any_high, uint32_t idx) {
+    if (idx < limit) return P[idx];
+    if (!any_high || idx == kSentinel) return 0u;
+    return hash_find(hkeys, hmask, idx);
+}
+
 template <int B>
-__device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P, uint32_t limit,
+__device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
+                             const uint32_t* hkeys, const uint32_t* hmask, bool any_high,
                              int rg, uint32_t rows_ok, int t_min, const int* s_rowT, int cg0,
                              int cg1) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rg * 32;
+    const uint32_t limit = (uint32_t)a.levels * a.K4;
     for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
         const int c = cg * 32 + lane;
         const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
@@ -193,17 +241,28 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P, 
         }
         if (!__any_sync(0xffffffffu, vmask)) continue;
         const int E = a.gent[cg];
-        const uint32_t* __restrict__ ep = a.ent + a.gstart[cg] + lane;
+        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.ent + a.gstart[cg]) + lane;
         uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
         uint32_t S[B - 4];
 #pragma unroll
         for (int k = 0; k < B - 4; ++k) S[k] = 0;
+        uint4 cur[4], nxt[4];
+        if (E > 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cur[q] = __ldg(ep + q * 32);
+        }
         for (int e = 0; e < E; e += 16) {
+            if (e + 16 < E) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) nxt[q] = __ldg(ep + ((e + 16) / 4 + q) * 32);
+            }
             uint32_t w[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const uint32_t idx = __ldg(ep + (int64_t)(e + q) * 32);
-                w[q] = idx < limit ? P[idx] : 0u;
+            for (int q = 0; q < 4; ++q) {
+                w[4 * q + 0] = lookup(P, limit, hkeys, hmask, any_high, cur[q].x);
+                w[4 * q + 1] = lookup(P, limit, hkeys, hmask, any_high, cur[q].y);
+                w[4 * q + 2] = lookup(P, limit, hkeys, hmask, any_high, cur[q].z);
+                w[4 * q + 3] = lookup(P, limit, hkeys, hmask, any_high, cur[q].w);
             }
             uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
             csa(twosA, ones, w[0], w[1]);
@@ -228,6 +287,8 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P, 
                 S[k] ^= carry;
                 carry = t;
             }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
         }
         // bit planes X[k] of the 32 per-row counts
         uint32_t X[B];
@@ -275,85 +336,90 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P, 
                 mn = min(s_rowT[b], tc);
                 pass = m >= (int)a.mmin[mn];
             }
-            emit(a, pass, r, c, m, mn);
+            emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
         }
     }
 }
 
 template <int B>
-__global__ void __launch_bounds__(kTileThreads) kmer_tile_kernel(TileArgs a) {
+__global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) {
     extern __shared__ __align__(16) uint32_t P[];
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots];
     __shared__ int s_rowT[32];
-    __shared__ int s_cm[32];
     __shared__ int s_item[4];
-    __shared__ int s_L, s_tmin;
+    __shared__ int s_tmin, s_any_high;
     __shared__ uint32_t s_rows_ok;
     const bool queued = a.items != nullptr;
-    int cur_rg = -1, cur_L = 0;
-    for (int it = queued ? -1 : 0;; ) {
-        // ---- fetch work ----
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int it = 0;; ++it) {
+        // ---- fetch work: one row group with all its column groups ----
         if (threadIdx.x == 0) {
             if (queued) {
                 const unsigned w = atomicAdd(a.queue_head, 1u);
-                if ((int)w < a.nitems) {
-                    const int4 q = a.items[w];
-                    s_item[0] = q.x; s_item[1] = q.y; s_item[2] = q.z; s_item[3] = 1;
-                } else {
-                    s_item[3] = 0;
+                s_item[3] = (int)w < a.nitems;
+                if (s_item[3]) {
+                    s_item[0] = a.items[w];
+                    s_item[1] = s_item[0];
+                    s_item[2] = (a.n + 31) / 32;
                 }
             } else {
                 s_item[0] = a.r_lo / 32 + blockIdx.x;
                 s_item[1] = a.c_lo / 32;
                 s_item[2] = (a.c_hi + 31) / 32;
-                s_item[3] = it == 0 ? 1 : 0;
+                s_item[3] = it == 0;
             }
         }
         __syncthreads();
         if (!s_item[3]) break;
         const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
-        ++it;
+        __syncthreads();   // every thread has read s_item
+        if (a.dense_group[rg]) continue;   // taken by kmer_dense_kernel (uniform)
         const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
-        if (rg != cur_rg) {
-            // ---- row group set-up: multiplicities, lengths, planes ----
-            if (threadIdx.x < 32) {
-                const int r = rg * 32 + threadIdx.x;
-                const bool ok = r >= rlo && r < rhi;
-                const int tr = ok ? a.tcount[r] : INT_MAX;
-                const int cm = ok ? a.cntmax[r] : 0;
-                s_rowT[threadIdx.x] = tr;
-                s_cm[threadIdx.x] = cm;
-                const unsigned okm = __ballot_sync(0xffffffffu, ok);
-                const int L = __reduce_max_sync(0xffffffffu, (unsigned)cm);
-                const int tm = __reduce_min_sync(0xffffffffu, (unsigned)tr);
-                if (threadIdx.x == 0) { s_L = L; s_tmin = tm; s_rows_ok = okm; }
-            }
-            __syncthreads();
-            cur_rg = rg;
-            cur_L = s_L;
-            if (cur_L > a.levels_cap) {   // handled by kmer_dense_kernel
-                __syncthreads();
-                continue;
-            }
-            const int words = cur_L * (int)a.K4;
-            uint4* P4 = reinterpret_cast<uint4*>(P);
-            for (int i = threadIdx.x; i < (words + 3) / 4; i += kTileThreads)
-                P4[i] = make_uint4(0, 0, 0, 0);
-            __syncthreads();
-            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-            for (int b = warp; b < 32; b += kTileWarps) {
-                if (!((s_rows_ok >> b) & 1u)) continue;
-                const int r = rg * 32 + b;
-                const uint32_t* src = a.ent + a.gstart[rg] + b;
-                const int T = s_rowT[b];
-                for (int e = lane; e < T; e += 32) atomicOr(&P[src[(int64_t)e * 32]], 1u << b);
-                (void)r;
-            }
-            __syncthreads();
+        // ---- row group set-up ----
+        if (warp == 0) {
+            const int r = rg * 32 + lane;
+            const bool ok = r >= rlo && r < rhi;
+            const int tr = ok ? a.tcount[r] : INT_MAX;
+            s_rowT[lane] = tr;
+            const unsigned okm = __ballot_sync(0xffffffffu, ok);
+            const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
+            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
         }
-        if (cur_L <= a.levels_cap) {
-            tile_columns<B>(a, P, (uint32_t)cur_L * a.K4, rg, s_rows_ok, s_tmin, s_rowT,
-                            max(cg0, rg), cg1);
+        const int words = a.levels * (int)a.K4;
+        uint4* P4 = reinterpret_cast<uint4*>(P);
+        for (int i = threadIdx.x; i < words / 4; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0; }
+        __syncthreads();
+        const uint32_t limit = (uint32_t)words;
+        for (int b = warp; b < 32; b += kTileWarps) {
+            if (!((s_rows_ok >> b) & 1u)) continue;
+            const uint32_t* src = a.ent + a.gstart[rg];
+            const int T = s_rowT[b];
+            const uint32_t bit = 1u << b;
+            for (int e = lane; e < T; e += 32) {
+                const uint32_t idx = src[ent_at(e, b)];
+                if (idx < limit) {
+                    atomicOr(&P[idx], bit);
+                } else {
+                    // high-level entry: open addressing; the host guarantees
+                    // the group holds at most kHashMaxKeys of them
+                    uint32_t h = hash_slot(idx);
+                    for (int probe = 0; probe < kHashSlots; ++probe) {
+                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
+                        if (old == kSentinel || old == idx) {
+                            atomicOr(&hmask[h], bit);
+                            break;
+                        }
+                        h = (h + 1) & (kHashSlots - 1);
+                    }
+                    s_any_high = 1;
+                }
+            }
         }
+        __syncthreads();
+        tile_columns<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
+                        max(cg0, rg), cg1);
         __syncthreads();
     }
 }
@@ -376,14 +442,12 @@ struct DenseArgs {
     const uint32_t* ent;
     const int64_t* gstart;
     const int32_t* tcount;
-    const int32_t* cntmax;
     const uint32_t* hinfo;
     const uint16_t* mmin;
     int n, K;
-    int levels_cap;   // rows of groups whose level need is <= this are skipped
     int r_lo, r_hi, c_lo, c_hi;
     int A, stage_dim;
-    const uint8_t* heavy_group;   // nullptr: every row
+    const uint8_t* dense_group;   // nullptr: every row
     unsigned long long* counter;
     uint64_t* keys;
     uint32_t* vals;
@@ -396,11 +460,8 @@ __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
     const int hwords = (int)((K4 + 1) / 2);
     for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    TileArgs ta{};
-    ta.n = a.n; ta.A = a.A; ta.stage_dim = a.stage_dim; ta.counter = a.counter;
-    ta.keys = a.keys; ta.vals = a.vals; ta.cap = a.cap;
     for (int r = a.r_lo + blockIdx.x; r < a.r_hi && r < a.n; r += gridDim.x) {
-        if (a.heavy_group && !a.heavy_group[r >> 5]) continue;   // uniform per block
+        if (a.dense_group && !a.dense_group[r >> 5]) continue;   // uniform per block
         const int Tr = a.tcount[r];
         const uint8_t* s = a.seq + a.off[r];
         for (int p = threadIdx.x; p < Tr; p += blockDim.x) {
@@ -421,10 +482,11 @@ __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
             bool pass = false;
             if (ok) {
                 const int Tc = a.tcount[c];
-                const uint32_t* ep = a.ent + a.gstart[c >> 5] + (c & 31);
+                const uint32_t* ep = a.ent + a.gstart[c >> 5];
+                const int cl = c & 31;
                 int sum_lo = 0, sum_hi = 0;
                 for (int e = 0; e < Tc; ++e) {
-                    const uint32_t idx = __ldg(ep + (int64_t)e * 32);
+                    const uint32_t idx = __ldg(ep + ent_at(e, cl));
                     const uint32_t t = idx / K4, v = idx - t * K4;
                     const uint32_t cnt = (hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu;
                     const int hit = cnt > t;
@@ -440,7 +502,7 @@ __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
                 mn = min(Tr, Tc);
                 pass = m >= (int)a.mmin[mn];
             }
-            emit(ta, pass, r, c, m, mn);
+            emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
         }
         __syncthreads();
         for (int p = threadIdx.x; p < Tr; p += blockDim.x) hist[kmer_at(s, p, a.K) >> 1] = 0;
@@ -494,18 +556,16 @@ int bits_for(uint64_t v) {
     return b;
 }
 
-int levels_cap_for(int K) {
-    const int per_level = (1 << (2 * K)) * 4;
+// Dense level planes kept in shared memory for K (0: dense kernel only).
+int dense_levels_for(int K) {
     if (K >= 8) return 0;
-    return std::min(16, kSmemBudget / per_level);
+    const int per_level = (1 << (2 * K)) * 4;
+    return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
 
 using TileFn = void (*)(TileArgs);
 TileFn tile_fn_for(int B) {
     switch (B) {
-        case 5: return kmer_tile_kernel<5>;
-        case 6: return kmer_tile_kernel<6>;
-        case 7: return kmer_tile_kernel<7>;
         case 8: return kmer_tile_kernel<8>;
         case 9: return kmer_tile_kernel<9>;
         case 10: return kmer_tile_kernel<10>;
@@ -562,8 +622,8 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
     CRISPY_TRY(ensure(ctx, j.gstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.gent, (size_t)j.ngroups * 4));
-    CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 1) * 4));
-    CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 4) * 4));
+    CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.hinfo, (size_t)n * 4));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
@@ -585,19 +645,22 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     const int n = j.n, k = j.k;
-    CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 1) * 4, s));
+    CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 4) * 4, s));
     const size_t hsmem = (size_t)(((1u << (2 * k)) + 1) / 2) * 4;
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hsmem));
     const int grid = std::min(n, ctx->sm_count * (k >= 8 ? 1 : 8));
+    int32_t* cntmax = j.cntmax.as<int32_t>();
+    int32_t* nhigh = cntmax + n;
     kmer_prep_kernel<<<grid, 256, hsmem, s>>>(j.seq.as<uint8_t>(), j.off.as<int64_t>(),
-                                              j.t.as<int32_t>(), n, k, j.gstart.as<int64_t>(),
-                                              j.gent.as<int32_t>(), j.ent.as<uint32_t>(),
-                                              j.cntmax.as<int32_t>(), j.hinfo.as<uint32_t>());
+                                              j.t.as<int32_t>(), n, k, dense_levels_for(k),
+                                              j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
+                                              j.ent.as<uint32_t>(), cntmax, nhigh,
+                                              j.hinfo.as<uint32_t>());
     count_launch(ctx);
     CRISPY_CK(ctx, cudaGetLastError());
-    j.h_cntmax.resize(n);
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.h_cntmax.data(), j.cntmax.ptr, (size_t)n * 4,
+    j.h_cntmax.resize(2 * (size_t)n);
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.h_cntmax.data(), j.cntmax.ptr, (size_t)n * 8,
                                    cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
     j.nsurv = 0;
@@ -626,27 +689,26 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     CRISPY_CK(ctx, cudaMemcpyAsync(j.mmin.ptr, mmin.data(), mmin.size() * 2, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.smin.ptr, smin.data(), smin.size() * 2, cudaMemcpyHostToDevice, s));
 
-    // level need per 32-read group and the groups the dense kernel must take
-    const int cap_levels = levels_cap_for(K);
-    std::vector<uint8_t> heavy(j.ngroups, 0);
-    int lmax_fast = 1;
-    bool any_heavy = false;
+    // Row groups whose high-level entries exceed the hash go to the dense
+    // kernel; K = 8 sends every group there.
+    const int levels = dense_levels_for(K);
+    std::vector<uint8_t> dense(j.ngroups, 0);
+    bool any_dense = false;
     for (int g = 0; g < j.ngroups; ++g) {
-        int L = 0;
-        for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) L = std::max(L, j.h_cntmax[r]);
-        if (L > cap_levels) { heavy[g] = 1; any_heavy = true; }
-        else lmax_fast = std::max(lmax_fast, L);
+        int64_t high = 0;
+        for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) high += j.h_cntmax[n + r];
+        if (levels == 0 || high > kHashMaxKeys) { dense[g] = 1; any_dense = true; }
     }
-    CRISPY_TRY(ensure(ctx, j.work, (size_t)j.ngroups));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.work.ptr, heavy.data(), j.ngroups, cudaMemcpyHostToDevice, s));
+    const bool fast = levels > 0;
+    CRISPY_TRY(ensure(ctx, j.work, (size_t)j.ngroups + 16));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.work.ptr, dense.data(), j.ngroups, cudaMemcpyHostToDevice, s));
 
     const uint32_t K4 = 1u << (2 * K);
-    const int B = std::max(5, bits_for((uint64_t)j.max_t));
+    const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = tile_fn_for(B);
-    const size_t tsmem = cap_levels > 0 ? (size_t)lmax_fast * K4 * 4 : 0;
+    const size_t tsmem = fast ? (size_t)levels * K4 * 4 : 0;
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
-    if (cap_levels > 0)
-        CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
     int64_t cap = std::max<int64_t>(j.keys.bytes / 8, std::max<int64_t>(1 << 20, 16LL * n));
@@ -660,18 +722,17 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
 
         TileArgs ta{};
         ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
-        ta.tcount = j.t.as<int32_t>(); ta.cntmax = j.cntmax.as<int32_t>();
+        ta.tcount = j.t.as<int32_t>(); ta.dense_group = j.work.as<uint8_t>();
         ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
-        ta.n = n; ta.K4 = K4; ta.levels_cap = cap_levels; ta.A = A; ta.stage_dim = sd;
+        ta.n = n; ta.K4 = K4; ta.levels = levels; ta.A = A; ta.stage_dim = sd;
         ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
         ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
         DenseArgs da{};
         da.seq = j.seq.as<uint8_t>(); da.off = j.off.as<int64_t>(); da.ent = ta.ent; da.gstart = ta.gstart;
-        da.tcount = ta.tcount; da.cntmax = ta.cntmax; da.hinfo = j.hinfo.as<uint32_t>(); da.mmin = ta.mmin;
-        da.n = n; da.K = K; da.levels_cap = cap_levels; da.A = A; da.stage_dim = sd;
-        da.heavy_group = (cap_levels > 0) ? j.work.as<uint8_t>() : nullptr;
+        da.tcount = ta.tcount; da.hinfo = j.hinfo.as<uint32_t>(); da.mmin = ta.mmin;
+        da.n = n; da.K = K; da.A = A; da.stage_dim = sd;
+        da.dense_group = fast ? j.work.as<uint8_t>() : nullptr;
         da.counter = ta.counter; da.keys = ta.keys; da.vals = ta.vals; da.cap = cap;
-        const bool fast = cap_levels > 0;
 
         if (mode == CRISPY_MODE_PLAIN) {
             // One launch per reference stage, round-robin over 8 streams like
@@ -693,7 +754,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                         tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
-                    if (!fast || any_heavy) {
+                    if (any_dense) {
                         DenseArgs d2 = da;
                         d2.r_lo = t2.r_lo; d2.r_hi = t2.r_hi; d2.c_lo = t2.c_lo; d2.c_hi = t2.c_hi;
                         kmer_dense_kernel<<<std::min(t2.r_hi - t2.r_lo, 4 * ctx->sm_count), 256, dsmem, ss>>>(d2);
@@ -712,26 +773,22 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             cudaEventDestroy(fork);
             ctx->stats.kmer_launches += nstages;
         } else {
-            // Batched: one persistent launch over a work queue of (row group,
-            // column-group range) items covering the whole upper triangle.
-            const int cw = ctx->kmer_chunk_groups > 0 ? ctx->kmer_chunk_groups : 64;
-            std::vector<int4> items;
-            if (fast) {
-                for (int rg = 0; rg < j.ngroups; ++rg) {
-                    if (heavy[rg]) continue;
-                    for (int c0 = rg; c0 < j.ngroups; c0 += cw)
-                        items.push_back(make_int4(rg, c0, std::min(j.ngroups, c0 + cw), 0));
-                }
-            }
+            // Batched: one persistent launch over a work queue of row groups
+            // (each with all its columns), longest first.
+            std::vector<int> items;
+            if (fast)
+                for (int rg = 0; rg < j.ngroups; ++rg)
+                    if (!dense[rg]) items.push_back(rg);
             if (!items.empty()) {
-                CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int4) + 64));
-                unsigned int* head = reinterpret_cast<unsigned int*>(j.sort_tmp.as<char>() + items.size() * sizeof(int4));
-                CRISPY_CK(ctx, cudaMemcpyAsync(j.sort_tmp.ptr, items.data(), items.size() * sizeof(int4),
+                CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int) + 64));
+                int* d_items = j.sort_tmp.as<int>();
+                unsigned int* head = reinterpret_cast<unsigned int*>(j.sort_tmp.as<char>() + items.size() * sizeof(int));
+                CRISPY_CK(ctx, cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(int),
                                                cudaMemcpyHostToDevice, s));
                 CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 4, s));
                 TileArgs t2 = ta;
                 t2.r_lo = 0; t2.r_hi = n; t2.c_lo = 0; t2.c_hi = n;
-                t2.items = j.sort_tmp.as<int4>(); t2.nitems = (int)items.size(); t2.queue_head = head;
+                t2.items = d_items; t2.nitems = (int)items.size(); t2.queue_head = head;
                 int per_sm = 1;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile, kTileThreads, tsmem);
                 per_sm = std::max(1, per_sm);
@@ -742,7 +799,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 count_launch(ctx);
                 ctx->stats.kmer_launches += 1;
             }
-            if (!fast || any_heavy) {
+            if (any_dense) {
                 DenseArgs d2 = da;
                 d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
                 kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);

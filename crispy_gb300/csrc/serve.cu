@@ -1,0 +1,332 @@
+// serve.cu -- continuous batching of clustering jobs on one GPU.
+//
+// The reference runs one process per data set and stage (crispy.sh:19-29);
+// there is no server to mirror.  This one keeps `slots` contexts, each with
+// its own stream and grow-only device buffers, and one worker thread per
+// slot.  Jobs queue in arrival order.  A worker that is free takes the
+// oldest queued job whose memory estimate fits the budget still unclaimed,
+// so a large job at the head does not stall small ones behind it; a job
+// larger than the whole budget fails at submit with CRISPY_E_OOM.  Each job
+// runs prepare -> kmer_run -> gen_prepare -> gen_run_from_kmer on its slot
+// with all intermediates in HBM, so jobs on different slots overlap on the
+// device; results are copied to host memory at completion.  Slots share no
+// device state, which is what keeps a job's result identical alone and in
+// a mix.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "internal.h"
+
+namespace {
+
+using clock_type = std::chrono::steady_clock;
+
+struct Job {
+    uint64_t id = 0;
+    std::string bases;
+    std::vector<int64_t> off;
+    std::vector<int32_t> len;
+    int n = 0, k = 6, band = 10;
+    float kthr = -1, gthr = -1;
+    size_t mem = 0;
+    int state = CRISPY_JOB_QUEUED;
+    int status = CRISPY_OK;
+    std::string err;
+    clock_type::time_point t_submit, t_done;
+    int64_t kmer_pairs = 0, gen_pairs = 0;
+    std::vector<int> chunk_id;
+    std::vector<std::vector<uint32_t>> chunk_pairs;
+    std::vector<std::vector<float>> chunk_dists;
+};
+
+// Device bytes a job needs at its peak (generous; the server only uses it
+// for admission).
+size_t estimate_bytes(const Job& j) {
+    size_t reads = j.bases.size() + (size_t)j.n * 16;
+    int64_t t = 0;
+    int maxlen = 0;
+    for (int i = 0; i < j.n; ++i) {
+        t += std::max(0, j.len[i] - j.k + 1);
+        maxlen = std::max(maxlen, j.len[i]);
+    }
+    const size_t entries = (size_t)(t + 32LL * 16 * ((j.n + 31) / 32)) * 4;
+    const size_t survivors = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 24;
+    const size_t gen = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 48 + reads;
+    return 2 * reads + entries + survivors + gen + (8u << 20);
+}
+
+int sink_to_job(void* user, int chunk, const void* pairs, const float* dists, int64_t count) {
+    Job* j = static_cast<Job*>(user);
+    j->chunk_id.push_back(chunk);
+    const uint32_t* p = static_cast<const uint32_t*>(pairs);
+    j->chunk_pairs.emplace_back(p, p + 2 * count);
+    j->chunk_dists.emplace_back(dists, dists + count);
+    j->gen_pairs += count;
+    return 0;
+}
+
+}  // namespace
+
+struct crispy_server {
+    int device = 0;
+    size_t budget = 0, claimed = 0;
+    std::vector<crispy_ctx*> ctx;
+    std::vector<std::thread> workers;
+    std::mutex mu;
+    std::condition_variable work_cv, done_cv;
+    std::deque<Job*> queue;
+    std::unordered_map<uint64_t, Job*> jobs;
+    bool stopping = false;
+    uint64_t next_id = 1;
+    std::vector<double> latencies_ms;
+    int64_t pairs_done = 0;
+    std::string err;
+
+    Job* take_fitting() {   // caller holds mu
+        for (auto it = queue.begin(); it != queue.end(); ++it) {
+            if (claimed + (*it)->mem <= budget) {
+                Job* j = *it;
+                queue.erase(it);
+                return j;
+            }
+        }
+        return nullptr;
+    }
+
+    void run_job(crispy_ctx* c, Job* j) {
+        int rc = crispy_kmer_prepare(c, j->bases.data(), j->off.data(), j->len.data(), j->n, j->k);
+        const float kt = crispy_default_threshold(j->n, j->kthr, 0);
+        const float gt = crispy_default_threshold(j->n, j->gthr, 1);
+        if (rc == CRISPY_OK) rc = crispy_kmer_run(c, kt, CRISPY_MODE_BATCHED, 0, &j->kmer_pairs);
+        if (rc == CRISPY_OK) rc = crispy_gen_prepare(c, j->bases.data(), j->off.data(), j->len.data(), j->n);
+        int64_t ns = 0;
+        if (rc == CRISPY_OK)
+            rc = crispy_gen_run_from_kmer(c, j->band, gt, CRISPY_MODE_BATCHED, sink_to_job, j, &ns);
+        j->status = rc;
+        if (rc != CRISPY_OK) j->err = crispy_last_error(c);
+    }
+
+    void worker(int slot) {
+        crispy_ctx* c = ctx[slot];
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            Job* j = nullptr;
+            work_cv.wait(lk, [&] { return stopping || (j = take_fitting()) != nullptr; });
+            if (!j) return;   // stopping
+            claimed += j->mem;
+            j->state = CRISPY_JOB_RUNNING;
+            lk.unlock();
+            run_job(c, j);
+            // give memory back when this slot holds more than its share
+            size_t in_use = 0;
+            crispy_ctx_mem_in_use(c, &in_use);
+            if (in_use > budget / ctx.size()) crispy_ctx_trim(c);
+            lk.lock();
+            claimed -= j->mem;
+            j->t_done = clock_type::now();
+            j->state = j->status == CRISPY_OK ? CRISPY_JOB_DONE : CRISPY_JOB_FAILED;
+            if (j->status == CRISPY_OK) {
+                latencies_ms.push_back(
+                    std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count());
+                pairs_done += (int64_t)j->n * (j->n - 1) / 2;
+            }
+            done_cv.notify_all();
+            work_cv.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+int crispy_server_create(int device, size_t hbm_budget_bytes, int slots, crispy_server** out) {
+    if (!out || slots < 1 || slots > 64)
+        return crispy::fail(nullptr, CRISPY_E_INPUT, "server: bad arguments");
+    *out = nullptr;
+    auto* s = new crispy_server();
+    s->device = device;
+    if (hbm_budget_bytes == 0) {
+        size_t free_b = 0, total = 0;
+        cudaSetDevice(device);
+        cudaMemGetInfo(&free_b, &total);
+        hbm_budget_bytes = free_b / 2;
+    }
+    s->budget = hbm_budget_bytes;
+    for (int i = 0; i < slots; ++i) {
+        crispy_ctx* c = nullptr;
+        int rc = crispy_ctx_create(device, &c);
+        if (rc != CRISPY_OK) {
+            for (auto* x : s->ctx) crispy_ctx_destroy(x);
+            delete s;
+            return rc;
+        }
+        s->ctx.push_back(c);
+    }
+    for (int i = 0; i < slots; ++i) s->workers.emplace_back(&crispy_server::worker, s, i);
+    *out = s;
+    return CRISPY_OK;
+}
+
+int crispy_server_destroy(crispy_server* s) {
+    if (!s) return CRISPY_OK;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->stopping = true;
+        for (Job* j : s->queue) j->state = CRISPY_JOB_CANCELLED;
+        s->queue.clear();
+    }
+    s->work_cv.notify_all();
+    for (auto& t : s->workers) t.join();
+    for (auto* c : s->ctx) crispy_ctx_destroy(c);
+    for (auto& kv : s->jobs) delete kv.second;
+    delete s;
+    return CRISPY_OK;
+}
+
+int crispy_server_submit(crispy_server* s, const char* seqbuf, const int64_t* offsets,
+                         const int32_t* lengths, int n, int k, int band, float kmer_thr,
+                         float gen_thr, uint64_t* job_id) {
+    if (!s || !seqbuf || !offsets || !lengths || n <= 0 || !job_id) {
+        if (s) s->err = "submit: NULL or empty read set";
+        return CRISPY_E_INPUT;
+    }
+    auto* j = new Job();
+    int64_t end = 0;
+    for (int i = 0; i < n; ++i) end = std::max(end, offsets[i] + lengths[i]);
+    j->bases.assign(seqbuf, seqbuf + end);
+    j->off.assign(offsets, offsets + n);
+    j->len.assign(lengths, lengths + n);
+    j->n = n;
+    j->k = k;
+    j->band = band <= 0 ? 2 : band;
+    j->kthr = kmer_thr;
+    j->gthr = gen_thr;
+    j->mem = estimate_bytes(*j);
+    j->t_submit = clock_type::now();
+    std::lock_guard<std::mutex> g(s->mu);
+    if (j->mem > s->budget) {
+        s->err = "job needs more device memory than the server budget";
+        delete j;
+        return CRISPY_E_OOM;
+    }
+    j->id = s->next_id++;
+    s->jobs[j->id] = j;
+    s->queue.push_back(j);
+    *job_id = j->id;
+    s->work_cv.notify_one();
+    return CRISPY_OK;
+}
+
+int crispy_server_wait(crispy_server* s, uint64_t id, int timeout_ms, int* state) {
+    if (!s) return CRISPY_E_INPUT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) {
+        s->err = "unknown job id";
+        return CRISPY_E_INPUT;
+    }
+    Job* j = it->second;
+    auto finished = [&] { return j->state >= CRISPY_JOB_DONE; };
+    if (timeout_ms < 0) {
+        s->done_cv.wait(lk, finished);
+    } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished)) {
+        if (state) *state = j->state;
+        return CRISPY_E_TIMEOUT;
+    }
+    if (state) *state = j->state;
+    return CRISPY_OK;
+}
+
+int crispy_server_result(crispy_server* s, uint64_t id, crispy_sink sink, void* user,
+                         int64_t* kmer_pairs, int64_t* gen_pairs) {
+    if (!s) return CRISPY_E_INPUT;
+    Job* j = nullptr;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        auto it = s->jobs.find(id);
+        if (it == s->jobs.end()) {
+            s->err = "unknown job id";
+            return CRISPY_E_INPUT;
+        }
+        j = it->second;
+        if (j->state < CRISPY_JOB_DONE) {
+            s->err = "job not finished";
+            return CRISPY_E_STATE;
+        }
+        s->jobs.erase(it);
+    }
+    int rc = CRISPY_OK;
+    if (j->state == CRISPY_JOB_CANCELLED) {
+        rc = CRISPY_E_STATE;
+        s->err = "job was cancelled";
+    } else if (j->state == CRISPY_JOB_FAILED) {
+        rc = j->status;
+        s->err = j->err;
+    } else {
+        if (kmer_pairs) *kmer_pairs = j->kmer_pairs;
+        if (gen_pairs) *gen_pairs = j->gen_pairs;
+        for (size_t c = 0; c < j->chunk_id.size() && sink; ++c) {
+            if (sink(user, j->chunk_id[c], j->chunk_pairs[c].data(), j->chunk_dists[c].data(),
+                     (int64_t)j->chunk_dists[c].size()) != 0) {
+                rc = CRISPY_E_IO;
+                break;
+            }
+        }
+    }
+    delete j;
+    return rc;
+}
+
+int crispy_server_cancel(crispy_server* s, uint64_t id) {
+    if (!s) return CRISPY_E_INPUT;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return CRISPY_E_INPUT;
+    Job* j = it->second;
+    auto q = std::find(s->queue.begin(), s->queue.end(), j);
+    if (q == s->queue.end()) {
+        s->err = "job already running or finished";
+        return CRISPY_E_STATE;
+    }
+    s->queue.erase(q);
+    j->state = CRISPY_JOB_CANCELLED;
+    s->done_cv.notify_all();
+    return CRISPY_OK;
+}
+
+int crispy_server_stats(crispy_server* s, double* p50, double* p99, int64_t* jobs_done,
+                        int64_t* pairs_done) {
+    if (!s) return CRISPY_E_INPUT;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::vector<double> v(s->latencies_ms);
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) -> double {
+        if (v.empty()) return 0.0;
+        // nearest-rank percentile
+        size_t r = (size_t)std::ceil(q * v.size());
+        return v[std::min(v.size(), std::max<size_t>(r, 1)) - 1];
+    };
+    if (p50) *p50 = pct(0.50);
+    if (p99) *p99 = pct(0.99);
+    if (jobs_done) *jobs_done = (int64_t)v.size();
+    if (pairs_done) *pairs_done = s->pairs_done;
+    return CRISPY_OK;
+}
+
+int crispy_server_stats_reset(crispy_server* s) {
+    if (!s) return CRISPY_E_INPUT;
+    std::lock_guard<std::mutex> g(s->mu);
+    s->latencies_ms.clear();
+    s->pairs_done = 0;
+    return CRISPY_OK;
+}
+
+const char* crispy_server_last_error(const crispy_server* s) { return s ? s->err.c_str() : ""; }
+
+}  // extern "C"

@@ -172,10 +172,71 @@ int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */
 int crispy_set_timing(crispy_ctx* ctx, int enable);
 
+/* The autotuner's choices so far, as a JSON array (one object per tuned
+ * genDist bin: band, band slots, lanes per pair, slots per lane, pairs per
+ * block, sample size, best and untuned times).  Set CRISPY_AUTOTUNE=0 in the
+ * environment to disable tuning.  No reference counterpart. */
+int crispy_tune_report(char* buf, size_t len);
+
 /* Measured integer-pipe throughput of this GPU in Gop/s (32-bit add/xor
  * lane operations): the roofline denominator of both hot kernels, which
  * are integer-bound.  No reference counterpart (measurement utility). */
 int crispy_probe_int32(crispy_ctx* ctx, double* gops);
+
+/* ---- memory cap of one context (device bytes); 0 = unlimited.  An
+ *      allocation that would exceed it fails with CRISPY_E_OOM, exactly as
+ *      an exhausted device would.  The server gives every slot a share of
+ *      its HBM budget this way. ---- */
+int crispy_ctx_set_mem_cap(crispy_ctx* ctx, size_t bytes);
+int crispy_ctx_mem_in_use(const crispy_ctx* ctx, size_t* bytes);
+/* Release every device buffer the context holds (its jobs stay valid only
+ * until the next prepare). */
+int crispy_ctx_trim(crispy_ctx* ctx);
+
+/* ---- serving: continuous batching of whole clustering jobs ----
+ *
+ * No counterpart in the reference (each stage there is one process per data
+ * set, crispy.sh:19-29).  A server owns `slots` contexts on one GPU, each
+ * with its own stream.  Jobs (a read set plus k, band and thresholds) queue
+ * in arrival order; a slot that frees up admits the next job whose memory
+ * estimate fits the HBM budget left, so jobs arriving while others run are
+ * admitted as slots and memory free up and their kernels overlap on the
+ * device.  Each job runs kmerDist -> genDist with every intermediate
+ * resident in HBM, and its result is the same chunk list a lone run gives.
+ * Submit, wait, result and cancel are thread-safe. */
+#define CRISPY_JOB_QUEUED    0
+#define CRISPY_JOB_RUNNING   1
+#define CRISPY_JOB_DONE      2
+#define CRISPY_JOB_FAILED    3
+#define CRISPY_JOB_CANCELLED 4
+
+typedef struct crispy_server crispy_server;
+int crispy_server_create(int device, size_t hbm_budget_bytes, int slots,
+                         crispy_server** out);
+int crispy_server_destroy(crispy_server* srv);
+/* Copies the reads; thresholds outside [0,1] select the stage defaults. */
+int crispy_server_submit(crispy_server* srv, const char* seqbuf,
+                         const int64_t* offsets, const int32_t* lengths,
+                         int n, int k, int band, float kmer_thr, float gen_thr,
+                         uint64_t* job_id);
+/* Waits up to timeout_ms (< 0: forever) for the job to finish; *state gets
+ * its CRISPY_JOB_* state.  CRISPY_E_TIMEOUT when it is still pending. */
+int crispy_server_wait(crispy_server* srv, uint64_t job_id, int timeout_ms,
+                       int* state);
+/* Delivers a finished job's genDist chunks to the sink (chunk order), its
+ * k-mer survivor and genetic survivor counts, then forgets the job.  A
+ * failed job returns its error status. */
+int crispy_server_result(crispy_server* srv, uint64_t job_id, crispy_sink sink,
+                         void* user, int64_t* kmer_pairs, int64_t* gen_pairs);
+/* Cancels a queued job (a running one finishes). */
+int crispy_server_cancel(crispy_server* srv, uint64_t job_id);
+/* Submit-to-finish latency percentiles (ms) over finished jobs, finished
+ * job count and pairs processed (sum of n(n-1)/2). */
+int crispy_server_stats(crispy_server* srv, double* p50_ms, double* p99_ms,
+                        int64_t* jobs_done, int64_t* pairs_done);
+/* Forget the latency samples and pair count gathered so far. */
+int crispy_server_stats_reset(crispy_server* srv);
+const char* crispy_server_last_error(const crispy_server* srv);
 
 #ifdef __cplusplus
 }
