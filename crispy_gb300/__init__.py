@@ -78,6 +78,8 @@ PROTOTYPES = {
     "crispy_gen_run": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
     "crispy_gen_run_from_kmer": (C.c_int, [_P, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
     "crispy_gen_align": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P]),
+    "crispy_gen_align_noalloc": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_int,
+                                           _P, _P, _P, _P, _P]),
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
-CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu"]
+CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu"]
 CXX_SOURCES = ["fasta.cpp"]
 CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp"}
 

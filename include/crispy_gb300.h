@@ -154,6 +154,29 @@ int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs,
                      int band, int mode, float* dist, int32_t* score,
                      int32_t* ml, int32_t* al);
 
+/* Banded NW per pair (as crispy_gen_align) for callers that cannot allocate
+ * device memory: an application that hands all device memory to its own
+ * pool at start-up and forbids allocation later, or a runtime whose memory
+ * accounting must not see foreign allocations.  No counterpart in the
+ * reference.  The caller passes device buffers for everything: the reads as
+ * ASCII bytes back to back (d_seq, d_offsets, d_lengths; n reads, none longer
+ * than max_len <= 2048), the pairs (int32[2*npairs]) and the outputs
+ * (d_dist required; d_score, d_ml, d_al may be NULL), and a cudaStream_t (or
+ * NULL).  The DP rows live in a fixed 8 MiB array inside the library that
+ * every GPU loading it holds until exit; nothing is allocated.  All calls
+ * share that array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device resolves the
+ * array's address (with that device current); make it before any stream
+ * capture.  Returns CRISPY_E_UNSUPPORTED when max_len exceeds 2048 or the
+ * band needs more scratch than the array holds, CRISPY_E_INPUT when a pair
+ * index is outside [0, n) or a read is longer than max_len (the call waits
+ * for its kernel to report this). */
+int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offsets,
+                             const int32_t* d_lengths, int n, int max_len,
+                             const int32_t* d_pairs, int64_t npairs, int band,
+                             float* d_dist, int32_t* d_score, int32_t* d_ml,
+                             int32_t* d_al, void* stream);
+
 /* ---- timing of the last run (CUDA events on the context's stream) ---- */
 typedef struct crispy_stats {
     double kmer_kernel_ms;     /* summed duration of the k-mer tile kernel launches */
