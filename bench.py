@@ -12,8 +12,11 @@ value  = all-pairs count n(n-1)/2 / step time, batched form, reads resident in
 e2e    = the same through the public C ABI with host buffers (reads uploaded
          twice, .kpair pairs fetched to the host and sent back, chunks read
          back), as the drop-in executables do minus disk I/O.
-plain  = the same pipeline with the plain kernels (one launch per reference
-         stage / per load window) for the batched-vs-plain ratio.
+plain  = the same pipeline with the plain from-scratch kernels (one thread
+         per pair, one launch per reference stage / load window);
+staged = the GB300 kernels launched the plain way (per stage / window),
+         which splits the batched-vs-plain ratio into kernel design and
+         scheduling.  All three forms must give identical bits (checked).
 
 --impl reference times the reference's CPU algorithm (the oracle port,
 OpenMP on every host core) on a bounded sample of the same workload.
@@ -256,12 +259,20 @@ def run_ours(args, dist, ws, rank, local):
     clocks.start()
     ms_b, kms_b, gms_b, launches_b, last_b = timed(cg.MODE_BATCHED, args.steps, args.warmup)
     clk = clocks.stop()
-    plain_steps = max(1, min(args.steps, 3))
-    ms_p, kms_p, gms_p, _, last_p = timed(cg.MODE_PLAIN, plain_steps, 1)
+    other_steps = max(1, min(args.steps, 3))
+    ms_s, kms_s, gms_s, _, last_s = timed(cg.MODE_STAGED, other_steps, 1)
+    ms_p, kms_p, gms_p, _, last_p = timed(cg.MODE_PLAIN, other_steps, 1)
 
     kp, chunks, st_k, st_g = last_b
     survivors = sum(len(c[2]) for c in chunks)
-    assert kp == last_p[0] and survivors == sum(len(c[2]) for c in last_p[1]), "plain/batched disagree"
+
+    def same(other):
+        if kp != other[0] or len(chunks) != len(other[1]):
+            return False
+        return all(np.array_equal(a[1], b[1]) and np.array_equal(a[2].view(np.uint32), b[2].view(np.uint32))
+                   for a, b in zip(chunks, other[1]))
+
+    assert same(last_p) and same(last_s), "plain / staged / batched outputs differ"
     cells = st_g["gen_cells"]
     mean_t = float(np.mean(np.maximum(np.array(lens) - k + 1, 0)))
 
@@ -270,6 +281,7 @@ def run_ours(args, dist, ws, rank, local):
     kmer_s = float(np.mean(kms_b)) / 1e3
     gen_s = float(np.mean(gms_b)) / 1e3
     plain_s = float(np.mean(ms_p)) / 1e3
+    staged_s = float(np.mean(ms_s)) / 1e3
 
     # e2e through the public API with host buffers
     def e2e_step():
@@ -323,15 +335,28 @@ def run_ours(args, dist, ws, rank, local):
         "kmer_pairs_per_s": n_pairs / kmer_s, "kmer_survivors": kp,
         "gen_gcups": cells / gen_s / 1e9, "gen_cells": cells, "gen_survivors": survivors,
         "kmer_kernel_ms": kmer_s * 1e3, "gen_kernel_ms": gen_s * 1e3,
-        "plain": {"ms_per_step": plain_s * 1e3, "value": n_pairs / plain_s,
+        "plain": {"kernels": "one thread per pair, launched per reference stage / load window",
+                  "ms_per_step": plain_s * 1e3, "value": n_pairs / plain_s,
                   "kmer_kernel_ms": float(np.mean(kms_p)), "gen_kernel_ms": float(np.mean(gms_p))},
+        "staged": {"kernels": "bit-sliced tiles + warp DP, launched per stage / window",
+                   "ms_per_step": staged_s * 1e3, "value": n_pairs / staged_s,
+                   "kmer_kernel_ms": float(np.mean(kms_s)), "gen_kernel_ms": float(np.mean(gms_s))},
         "batched_over_plain": plain_s / step_s,
+        "batched_over_staged": staged_s / step_s,
+        "outputs_identical_across_forms": True,
         "e2e": {"value": ws * n_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
         "gpu_launches": int(launches_b),
         "roofline": dominant, "roofline_kmer": roof_k, "roofline_gen": roof_g,
         "clocks": clk,
     }
+    try:
+        tune = cg.tune_report()
+    except Exception:   # the report is informative only
+        tune = None
+    line["autotune"] = tune
+    if not args.no_serve:
+        line["serve"] = serve_bench(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as td:
             kpps, gcups, cores, desc, _ = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
@@ -341,6 +366,67 @@ def run_ours(args, dist, ws, rank, local):
                                 "note": "extrapolated to the full workload from the sample rates"}
     eng.close()
     return line
+
+
+def serve_bench(args, local: int) -> dict:
+    """Continuous-batching server on a Poisson stream of clustering jobs.
+
+    Jobs: read counts log-uniform in [500, 50000], lengths N(250, 20), k = 6,
+    band 1/10, default thresholds, 120 GB HBM admission budget.  Saturated
+    throughput comes from a closed loop (all jobs queued at once); latency
+    percentiles from open-loop Poisson arrivals at 50 % and 90 % of it.
+    """
+    import crispy_gb300 as cg
+
+    rng = np.random.default_rng(4242)
+    sizes = np.exp(rng.uniform(np.log(500), np.log(50000), size=args.serve_jobs)).astype(int)
+    pool = []
+    for i, n in enumerate(sizes):
+        spec = synth.ReadSetSpec(int(n), max(4, int(n) // 50), 260, "normal", 250, 20, 6, 9000 + i)
+        pool.append(synth.pack_reads(synth.make_read_set(spec)))
+    pairs = [len(p[2]) * (len(p[2]) - 1) // 2 for p in pool]
+    out = {"jobs": len(pool), "slots": args.serve_slots, "hbm_budget_gb": 120,
+           "reads_per_job": {"min": int(min(len(p[2]) for p in pool)),
+                             "max": int(max(len(p[2]) for p in pool))}}
+    with cg.Server(local, 120 << 30, args.serve_slots) as srv:
+        # warm-up: one small and one large job
+        for p in (pool[int(np.argmin(sizes))], pool[int(np.argmax(sizes))]):
+            j = srv.submit(*p)
+            srv.wait(j)
+            srv.result(j)
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        ids = [srv.submit(*p) for p in pool]
+        for j in ids:
+            srv.wait(j)
+            srv.result(j)
+        sat_s = time.perf_counter() - t0
+        sat = srv.stats()
+        rate = len(pool) / sat_s
+        out["saturated"] = {"jobs_per_s": rate, "pairs_per_s": sum(pairs) / sat_s,
+                            "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"]}
+        for frac in (0.5, 0.9):
+            srv.reset_stats()
+            gaps = rng.exponential(1.0 / (frac * rate), size=len(pool))
+            ids = []
+            t0 = time.perf_counter()
+            nxt = t0
+            for p, g in zip(pool, gaps):
+                nxt += g
+                delay = nxt - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(*p))
+            for j in ids:
+                srv.wait(j)
+                srv.result(j)
+            el = time.perf_counter() - t0
+            st = srv.stats()
+            out[f"load_{int(frac * 100)}"] = {"offered_jobs_per_s": frac * rate,
+                                              "jobs_per_s": len(pool) / el,
+                                              "pairs_per_s": sum(pairs) / el,
+                                              "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"]}
+    return out
 
 
 def _attach_traffic(roof_k, roof_g, n_pairs, cells):
@@ -411,6 +497,9 @@ def main():
                     choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sample-reads", type=int, default=_env_int("CRISPY_CPU_SAMPLE", 6000))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=60)
+    ap.add_argument("--serve-slots", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, ws, rank, local = _dist()

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_PKG, "lib", "libcrispy_gb300.so")
 BIN_DIR = os.path.join(_PKG, "bin")
 
 OK, E_INPUT, E_OOM, E_DEVICE, E_TIMEOUT, E_STATE, E_IO, E_UNSUPPORTED = range(8)
-MODE_PLAIN, MODE_BATCHED = 0, 1
+MODE_PLAIN, MODE_BATCHED, MODE_STAGED = 0, 1, 2
 GEN_WINDOW = 589824
 MAX_READ_LEN = 2048
 MAX_NUM_READS = 1024 * 1024
@@ -46,7 +46,7 @@ class Stats(C.Structure):
                 ("total_ms", C.c_double), ("kmer_pairs", C.c_int64),
                 ("kmer_survivors", C.c_int64), ("gen_pairs", C.c_int64),
                 ("gen_cells", C.c_int64), ("gen_survivors", C.c_int64),
-                ("kernels_launched", C.c_int64)]
+                ("kernels_launched", C.c_int64), ("graph_launches", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -111,8 +111,10 @@ int main(int argc, char** argv) {
     }
     const int64_t npairs = (int64_t)pairs.size() / 2;   // a trailing odd int is ignored, as fread/2 does
     const char* mode_env = std::getenv("CRISPY_MODE");
-    const int mode = (mode_env && !std::strcmp(mode_env, "plain")) ? CRISPY_MODE_PLAIN : CRISPY_MODE_BATCHED;
-    std::printf("USE GPU (GB300 engine, %s)\n", mode == CRISPY_MODE_PLAIN ? "plain" : "batched");
+    const int mode = !mode_env ? CRISPY_MODE_BATCHED
+                     : !std::strcmp(mode_env, "plain") ? CRISPY_MODE_PLAIN
+                     : !std::strcmp(mode_env, "staged") ? CRISPY_MODE_STAGED : CRISPY_MODE_BATCHED;
+    std::printf("USE GPU (GB300 engine, %s)\n", mode == CRISPY_MODE_PLAIN ? "plain" : mode == CRISPY_MODE_STAGED ? "staged" : "batched");
     crispy_ctx* ctx = nullptr;
     int rc = crispy_ctx_create(0, &ctx);
     if (rc != CRISPY_OK) { std::fprintf(stderr, "genDist: %s\n", crispy_last_error(nullptr)); return 255; }

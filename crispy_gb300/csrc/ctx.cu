@@ -145,6 +145,43 @@ double ev_sum_ms(StreamEvents& ev) {
 
 void count_launch(crispy_ctx* ctx, int n) { ctx->stats.kernels_launched += n; }
 
+void graph_clear(crispy_ctx* ctx) {
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+    ctx->graphs.clear();
+}
+
+int graph_run(crispy_ctx* ctx, cudaStream_t s, const std::string& key,
+              const std::function<int()>& enqueue) {
+    if (!ctx->use_graphs) return enqueue();
+    auto it = ctx->graphs.find(key);
+    if (it != ctx->graphs.end()) {
+        CRISPY_CK(ctx, cudaGraphLaunch(it->second.exec, s));
+        count_launch(ctx, it->second.kernels);
+        ctx->stats.graph_launches++;
+        return CRISPY_OK;
+    }
+    if (ctx->graphs.size() >= 64) graph_clear(ctx);
+    const int64_t before = ctx->stats.kernels_launched;
+    CRISPY_CK(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc != CRISPY_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    GraphEntry g;
+    g.kernels = (int)(ctx->stats.kernels_launched - before);
+    const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate", __FILE__, __LINE__);
+    ctx->graphs[key] = g;
+    CRISPY_CK(ctx, cudaGraphLaunch(g.exec, s));
+    ctx->stats.graph_launches++;
+    return CRISPY_OK;
+}
+
 }  // namespace crispy
 
 using namespace crispy;
@@ -191,6 +228,7 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
     if (!ctx) return CRISPY_E_INPUT;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    graph_clear(ctx);   // graphs hold the addresses of the buffers freed below
     KmerJob& k = ctx->kmer;
     for (DevBuf* b : {&k.seq, &k.off, &k.len, &k.t, &k.gstart, &k.gent, &k.ent, &k.cntmax,
                       &k.hinfo, &k.keys, &k.keys_alt, &k.vals, &k.vals_alt, &k.pairs, &k.dists,
@@ -200,7 +238,8 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
     for (DevBuf* b : {&g.seq, &g.off, &g.len, &g.woff, &g.packed, &g.pairs, &g.dist, &g.score,
                       &g.ml, &g.al, &g.flags, &g.scan, &g.blocksum, &g.surv_idx, &g.keys,
                       &g.keys_alt, &g.vals, &g.vals_alt, &g.out_pairs, &g.out_dists, &g.order,
-                      &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue})
+                      &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue, &g.cstats,
+                      &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt})
         release(ctx, *b);
     k.ready = false;
     g.ready = false;

@@ -437,6 +437,21 @@ __global__ void gen_gather_kernel(const int2* __restrict__ pairs, const uint32_t
     out_dists[i] = __uint_as_float(keys[i]);
 }
 
+// Band cells of one pair in O(1): rows i = 1..l2 hold columns
+// max(1, i-kb)..min(l1, i+kb), non-empty for i <= min(l2, l1 + kb).
+__host__ __device__ inline int64_t band_cells_of(int l1, int l2, int band) {
+    const int64_t kb = band >= 2 ? (l1 + l2) / (2 * band) : (l1 > l2 ? l1 : l2);
+    if (l1 <= 0 || l2 <= 0) return 0;
+    const int64_t I = l2 < l1 + kb ? l2 : l1 + kb;
+    int64_t a = l1 - kb > 0 ? l1 - kb : 0;
+    a = a < I ? a : I;
+    const int64_t sum_hi = a * (a + 1) / 2 + a * kb + (I - a) * l1;
+    const int64_t b = kb + 1 < I ? kb + 1 : I;
+    const int64_t sum_lo = b + (I * (I + 1) / 2 - b * (b + 1) / 2) - kb * (I - b);
+    return sum_hi - sum_lo + I;
+}
+
+
 // Register-resident shapes (sub-group lanes G, band slots per lane C).
 // Every one serves a pair with kBand + 1 <= G * C.
 struct Shape {
@@ -449,14 +464,42 @@ constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 // Pairs are binned by band slots; bin 0 is the wide-band kernel.
 constexpr int kBinSlots[] = {0, 8, 16, 32, 48, 64, 96, 128, 192, 256};
 constexpr int kNumBins = sizeof(kBinSlots) / sizeof(kBinSlots[0]);
+__constant__ int c_bin_slots[kNumBins] = {0, 8, 16, 32, 48, 64, 96, 128, 192, 256};
+
+// Per-pair classification for the launch plan, on the device: band-slot
+// bin (wide last), a sort key (bin, then longer pairs first), band cells,
+// the widest band, per-bin counts and the widest bin of each load window.
+// stats: [0] cells, [1] max kBand, [2 + b] pairs of order-bin b (1..10),
+// [16 + w] widest order-bin of window w.
+constexpr int kStatBins = 2, kStatWindows = 16;
+__global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t count,
+                                    const int32_t* __restrict__ len, int band, int nbins,
+                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                    unsigned long long* __restrict__ stats) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long cells = 0;
+    if (p < count) {
+        const int2 pr = pairs[p];
+        const int l1 = len[pr.x], l2 = len[pr.y];
+        const int kb = band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
+        int bin = 0;
+        for (int b = 1; b < nbins; ++b)
+            if (c_bin_slots[b] >= kb + 1) { bin = b; break; }
+        const int ob = bin == 0 ? nbins : bin;   // wide pairs sort last
+        if (keys) {
+            keys[p] = ((uint32_t)ob << 13) | (uint32_t)(8191 - (l1 + l2));
+            vals[p] = (uint32_t)p;
+        }
+        cells = (unsigned long long)band_cells_of(l1, l2, band);
+        atomicMax(&stats[1], (unsigned long long)kb);
+        atomicAdd(&stats[kStatBins + ob], 1ull);
+        atomicMax(&stats[kStatWindows + p / CRISPY_GEN_WINDOW], (unsigned long long)ob);
+    }
+    cells = __reduce_add_sync(0xffffffffu, (unsigned)cells) + 0ull;   // per-warp partial (cells < 2^32 per warp)
+    if ((threadIdx.x & 31) == 0 && cells) atomicAdd(&stats[0], cells);
+}
 // untuned shape per bin (the plain form always uses it)
 constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 5, 6, 7, 11, 12, 13};
-
-int bin_for_slots(int slots) {
-    for (int b = 1; b < kNumBins; ++b)
-        if (kBinSlots[b] >= slots) return b;
-    return 0;
-}
 
 using WarpFn = void (*)(GenArgs);
 WarpFn shape_fn(int shape) {
@@ -486,7 +529,7 @@ WarpFn shape_fn(int shape) {
 // same bits, so tuning only picks speed.
 // ---------------------------------------------------------------------------
 struct TuneKey {
-    int band, bin, len_bucket, sms;
+    int band, bin, len_bucket, sms;   // len_bucket reserved (0)
     bool operator<(const TuneKey& o) const {
         return std::tie(band, bin, len_bucket, sms) < std::tie(o.band, o.bin, o.len_bucket, o.sms);
     }
@@ -518,24 +561,29 @@ int launch_shape(crispy_ctx* ctx, cudaStream_t s, int shape, GenArgs a, bool tim
     return CRISPY_OK;
 }
 
-int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, int len_bucket,
-               const GenArgs& a, const std::vector<uint32_t>& host_order, int64_t first,
-               int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf) {
+__global__ void gather_stride_kernel(const uint32_t* __restrict__ src, int64_t n, int64_t want,
+                                     uint32_t* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < want) dst[i] = src[i * n / want];
+}
+
+int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs& a,
+               const uint32_t* d_order, int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf) {
     const int dflt = kDefaultShape[bin];
     if (!autotune_enabled() || n_items < 4096) return dflt;
-    const TuneKey key{band, bin, len_bucket, ctx->sm_count};
+    const TuneKey key{band, bin, 0, ctx->sm_count};
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tuned.find(key);
         if (it != g_tuned.end()) return it->second.shape;
     }
-    // strided sample of the bin (keeps its length spread)
+    // strided sample of the bin (keeps its length spread), taken on the device
     const int64_t want = std::min<int64_t>(n_items, 24576);
-    std::vector<uint32_t> samp(want);
-    for (int64_t i = 0; i < want; ++i) samp[i] = host_order[first + i * n_items / want];
     CRISPY_TRY(ensure(ctx, sample_buf, (size_t)want * 4));
     CRISPY_TRY(ensure(ctx, queue_buf, 64 * 4));
-    CRISPY_CK(ctx, cudaMemcpyAsync(sample_buf.ptr, samp.data(), (size_t)want * 4, cudaMemcpyHostToDevice, s));
+    gather_stride_kernel<<<(unsigned)((want + 255) / 256), 256, 0, s>>>(d_order, n_items, want,
+                                                                      sample_buf.as<uint32_t>());
+    count_launch(ctx);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -574,50 +622,63 @@ int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, int len_bucke
 
 }  // namespace
 
-// Band cells of one pair in O(1): rows i = 1..l2 hold columns
-// max(1, i-kb)..min(l1, i+kb), non-empty for i <= min(l2, l1 + kb).
-int64_t band_cells(int l1, int l2, int band) {
-    const int64_t kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
-    if (l1 <= 0 || l2 <= 0) return 0;
-    const int64_t I = std::min<int64_t>(l2, l1 + kb);
-    const int64_t a = std::min<int64_t>(std::max<int64_t>(l1 - kb, 0), I);  // rows where i+kb <= l1
-    const int64_t sum_hi = a * (a + 1) / 2 + a * kb + (I - a) * l1;
-    const int64_t b = std::min<int64_t>(kb + 1, I);                         // rows where i-kb <= 1
-    const int64_t sum_lo = b + (I * (I + 1) / 2 - b * (b + 1) / 2) - kb * (I - b);
-    return sum_hi - sum_lo + I;
-}
-
-namespace {
-
-}  // namespace
-
-}  // namespace crispy
-
-namespace crispy {
-
-// Plain: per 589,824-pair load window, one launch of the width the window's
-// widest pair needs (the reference launches per window and stream,
-// genCUDA.cu:156-209).  Batched: pairs bucketed by register width (the
-// length buckets), longest first, one persistent launch per bucket on a
-// device work counter.
+// Launch plan for `count` pairs, computed on the device (no host pass over
+// the pairs): PLAIN = the thread-per-pair kernel per 589,824-pair load
+// window (as the reference launches per window, genCUDA.cu:156-209);
+// STAGED = the warp kernel per window, in the untuned shape the window's
+// widest pair needs; BATCHED = pairs sorted by band-slot bin and, inside a
+// bin, longest first, one persistent launch per bin on a device work
+// counter in the autotuned shape.
 int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t count,
                       int band, int mode, float* d_dist, int32_t* d_score, int32_t* d_ml,
-                      int32_t* d_al, const int32_t* h_pairs) {
+                      int32_t* d_al) {
     GenJob& g = ctx->gen;
     if (count <= 0) return CRISPY_OK;
-    std::vector<uint8_t> cls(count);
-    std::vector<uint16_t> span(count);   // l1 + l2, the pair's step count
-    int kbmax = 0;
-    int64_t cells = 0;
-    for (int64_t p = 0; p < count; ++p) {
-        const int l1 = g.h_len[h_pairs[2 * p]], l2 = g.h_len[h_pairs[2 * p + 1]];
-        const int kb = band >= 2 ? (l1 + l2) / (2 * band) : std::max(l1, l2);
-        cls[p] = (uint8_t)bin_for_slots(kb + 1);
-        span[p] = (uint16_t)(l1 + l2);
-        if (cls[p] == 0) kbmax = std::max(kbmax, kb);
-        cells += band_cells(l1, l2, band);
+    const int64_t nwin = (count + CRISPY_GEN_WINDOW - 1) / CRISPY_GEN_WINDOW;
+    const int nstats = kStatWindows + (int)nwin;
+    const bool sorted = mode == CRISPY_MODE_BATCHED;
+    CRISPY_TRY(ensure(ctx, g.cstats, (size_t)(nstats + kNumBins) * 8));
+    if (sorted) {
+        CRISPY_TRY(ensure(ctx, g.ckeys, (size_t)count * 4));
+        CRISPY_TRY(ensure(ctx, g.ckeys_alt, (size_t)count * 4));
+        CRISPY_TRY(ensure(ctx, g.cvals, (size_t)count * 4));
+        CRISPY_TRY(ensure(ctx, g.cvals_alt, (size_t)count * 4));
     }
-    ctx->stats.gen_cells += cells;
+    unsigned long long* d_stats = g.cstats.as<unsigned long long>();
+    uint32_t* d_order = nullptr;
+    auto classify = [&]() -> int {
+        CRISPY_CK(ctx, cudaMemsetAsync(d_stats, 0, (size_t)nstats * 8, s));
+        gen_classify_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(
+            d_pairs, count, g.len.as<int32_t>(), band, kNumBins,
+            sorted ? g.ckeys.as<uint32_t>() : nullptr, sorted ? g.cvals.as<uint32_t>() : nullptr, d_stats);
+        count_launch(ctx);
+        if (sorted) {
+            uint32_t* sk = nullptr;
+            CRISPY_TRY(sort_u32_payload(ctx, s, g.ckeys.as<uint32_t>(), g.ckeys_alt.as<uint32_t>(),
+                                        g.cvals.as<uint32_t>(), g.cvals_alt.as<uint32_t>(), count, 17, &sk,
+                                        &d_order, g.scan));
+        }
+        CRISPY_CK(ctx, cudaGetLastError());
+        return CRISPY_OK;
+    };
+    if (sorted) {
+        CRISPY_TRY(ensure(ctx, g.scan, sort_tmp_bytes(count)));
+        const std::string key = "gclass," + key_of({(uint64_t)count, (uint64_t)band, (uint64_t)(uintptr_t)d_pairs,
+            (uint64_t)(uintptr_t)g.len.ptr, (uint64_t)(uintptr_t)d_stats, (uint64_t)(uintptr_t)g.ckeys.ptr,
+            (uint64_t)(uintptr_t)g.ckeys_alt.ptr, (uint64_t)(uintptr_t)g.cvals.ptr,
+            (uint64_t)(uintptr_t)g.cvals_alt.ptr, (uint64_t)(uintptr_t)g.scan.ptr});
+        CRISPY_TRY(graph_run(ctx, s, key, classify));
+        // where the 3-pass (17-bit) sort leaves the payload: the alternate
+        // buffer, or the input when there is nothing to sort
+        d_order = count > 1 ? g.cvals_alt.as<uint32_t>() : g.cvals.as<uint32_t>();
+    } else {
+        CRISPY_TRY(classify());
+    }
+    std::vector<unsigned long long> st(nstats);
+    CRISPY_CK(ctx, cudaMemcpyAsync(st.data(), d_stats, (size_t)nstats * 8, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    const int kbmax = (int)st[1];
+    ctx->stats.gen_cells += (int64_t)st[0];
     ctx->stats.gen_pairs += count;
     GenArgs base{};
     base.packed = g.packed.as<uint32_t>();
@@ -642,17 +703,10 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         ctx->stats.gen_launches++;
         return CRISPY_OK;
     };
-    if (mode == CRISPY_MODE_PLAIN) {
-        // wide pairs are rare; plain mode sends every window with one to the wide kernel
-        for (int64_t w0 = 0; w0 < count; w0 += CRISPY_GEN_WINDOW) {
+    if (mode == CRISPY_MODE_PLAIN || mode == CRISPY_MODE_STAGED) {
+        for (int64_t w = 0; w < nwin; ++w) {
+            const int64_t w0 = w * CRISPY_GEN_WINDOW;
             const int64_t n_items = std::min<int64_t>(CRISPY_GEN_WINDOW, count - w0);
-            int cmax = 1;
-            bool wide = false;
-            for (int64_t p = w0; p < w0 + n_items; ++p) {
-                if (cls[p] == 0) wide = true;
-                cmax = std::max<int>(cmax, cls[p]);
-            }
-            const int shape = kDefaultShape[cmax];
             GenArgs a = base;
             a.pairs = d_pairs + w0;
             a.count = n_items;
@@ -660,55 +714,35 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
             a.score = d_score ? d_score + w0 : nullptr;
             a.ml = d_ml ? d_ml + w0 : nullptr;
             a.al = d_al ? d_al + w0 : nullptr;
-            if (wide) {
+            const int ob = (int)st[kStatWindows + w];   // widest order-bin (kNumBins = wide)
+            if (mode == CRISPY_MODE_PLAIN || ob >= kNumBins) {
                 CRISPY_TRY(launch_wide(a, nullptr, n_items));
-                continue;
+            } else {
+                CRISPY_TRY(launch_shape(ctx, s, kDefaultShape[ob], a, true));
+                ctx->stats.gen_launches++;
             }
-            CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
-            ctx->stats.gen_launches++;
         }
         CRISPY_CK(ctx, cudaGetLastError());
         return CRISPY_OK;
     }
-    // batched: bucket order -- band-slot bin first, then longest pairs first
-    // inside a bin, so the sub-groups of a warp get pairs of similar length
-    // and the persistent queue drains evenly
-    std::vector<uint32_t> order(count);
-    for (int64_t p = 0; p < count; ++p) order[p] = (uint32_t)p;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-        const int cx = cls[x] == 0 ? kNumBins : cls[x], cy = cls[y] == 0 ? kNumBins : cls[y];
-        if (cx != cy) return cx < cy;
-        return span[x] > span[y];
-    });
-    std::vector<int64_t> start(kNumBins + 2, 0);   // by bin, wide last
-    {
-        int64_t at = 0;
-        for (int ci = 1; ci <= kNumBins; ++ci) {
-            start[ci] = at;
-            const int want = ci == kNumBins ? 0 : ci;
-            while (at < count && cls[order[at]] == want) ++at;
-        }
-        start[kNumBins + 1] = at;
-    }
-    CRISPY_TRY(ensure(ctx, g.order, (size_t)count * 4));
-    CRISPY_TRY(ensure(ctx, g.queue, 64));
-    CRISPY_CK(ctx, cudaMemcpyAsync(g.order.ptr, order.data(), (size_t)count * 4, cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemsetAsync(g.queue.ptr, 0, 64, s));
-    for (int ci = 1; ci <= kNumBins; ++ci) {
-        const int64_t n_items = start[ci + 1] - start[ci];
+    // BATCHED: bins in ascending width, wide last
+    int64_t at = 0;
+    for (int ob = 1; ob <= kNumBins; ++ob) {
+        const int64_t n_items = (int64_t)st[kStatBins + ob];
         if (n_items == 0) continue;
-        const uint32_t* ord = g.order.as<uint32_t>() + start[ci];
-        if (ci == kNumBins) {
+        const uint32_t* ord = d_order + at;
+        at += n_items;
+        if (ob == kNumBins) {
             CRISPY_TRY(launch_wide(base, ord, n_items));
             continue;
         }
-        const int len_bucket = span[order[start[ci]]] / 128;
         GenArgs a = base;
-        const int shape = pick_shape(ctx, s, band, ci, len_bucket, a, order, start[ci], n_items,
-                                     g.tune_sample, g.tune_queue);
         a.order = ord;
         a.count = n_items;
-        a.queue = g.queue.as<unsigned int>() + ci;
+        const int shape = pick_shape(ctx, s, band, ob, a, ord, n_items, g.tune_sample, g.tune_queue);
+        CRISPY_TRY(ensure(ctx, g.queue, 64 * 4));
+        a.queue = g.queue.as<unsigned int>() + ob;
+        CRISPY_CK(ctx, cudaMemsetAsync(a.queue, 0, 4, s));
         CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
         ctx->stats.gen_launches++;
     }
@@ -733,7 +767,7 @@ int gen_check_pairs(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs) {
 
 // Threshold, windows, chunking, stable sort; delivers chunks to the sink.
 int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npairs, float thr,
-               crispy_sink sink, void* user, int64_t* nsurv) {
+               crispy_sink sink, void* user, int64_t* nsurv, bool use_graph) {
     GenJob& g = ctx->gen;
     *nsurv = 0;
     if (npairs == 0) return CRISPY_OK;
@@ -778,18 +812,31 @@ int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npa
     for (size_t ci = 0; ci < chunks.size(); ++ci) {
         const int64_t b = chunks[ci].first, c = chunks[ci].second;
         const unsigned blocks = (unsigned)((c + 255) / 256);
-        gen_keys_kernel<<<blocks, 256, 0, s>>>(g.dist.as<float>(), g.surv_idx.as<uint32_t>(), b, c,
-                                              g.keys.as<uint32_t>(), g.vals.as<uint32_t>());
-        count_launch(ctx);
-        uint32_t *sk = nullptr, *sv = nullptr;
-        // distances lie in [0, 1]: 30 significant bits
-        CRISPY_TRY(sort_u32_payload(ctx, s, g.keys.as<uint32_t>(), g.keys_alt.as<uint32_t>(),
-                                    g.vals.as<uint32_t>(), g.vals_alt.as<uint32_t>(), c, 32, &sk,
-                                    &sv, g.scan));
-        gen_gather_kernel<<<blocks, 256, 0, s>>>(d_pairs, sk, sv, c, g.out_pairs.as<uint2>(),
-                                                g.out_dists.as<float>());
-        count_launch(ctx);
-        CRISPY_CK(ctx, cudaGetLastError());
+        auto chunk_work = [&]() -> int {
+            gen_keys_kernel<<<blocks, 256, 0, s>>>(g.dist.as<float>(), g.surv_idx.as<uint32_t>(), b, c,
+                                                  g.keys.as<uint32_t>(), g.vals.as<uint32_t>());
+            count_launch(ctx);
+            uint32_t *sk = nullptr, *sv = nullptr;
+            // distances lie in [0, 1]: sorted on their 32-bit patterns
+            CRISPY_TRY(sort_u32_payload(ctx, s, g.keys.as<uint32_t>(), g.keys_alt.as<uint32_t>(),
+                                        g.vals.as<uint32_t>(), g.vals_alt.as<uint32_t>(), c, 32, &sk,
+                                        &sv, g.scan));
+            gen_gather_kernel<<<blocks, 256, 0, s>>>(d_pairs, sk, sv, c, g.out_pairs.as<uint2>(),
+                                                    g.out_dists.as<float>());
+            count_launch(ctx);
+            CRISPY_CK(ctx, cudaGetLastError());
+            return CRISPY_OK;
+        };
+        if (use_graph) {
+            CRISPY_TRY(ensure(ctx, g.scan, sort_tmp_bytes(c)));
+            const std::string key = "gchunk," + key_of({(uint64_t)b, (uint64_t)c, (uint64_t)(uintptr_t)d_pairs,
+                (uint64_t)(uintptr_t)g.dist.ptr, (uint64_t)(uintptr_t)g.surv_idx.ptr, (uint64_t)(uintptr_t)g.keys.ptr,
+                (uint64_t)(uintptr_t)g.keys_alt.ptr, (uint64_t)(uintptr_t)g.vals.ptr, (uint64_t)(uintptr_t)g.vals_alt.ptr,
+                (uint64_t)(uintptr_t)g.scan.ptr, (uint64_t)(uintptr_t)g.out_pairs.ptr, (uint64_t)(uintptr_t)g.out_dists.ptr});
+            CRISPY_TRY(graph_run(ctx, s, key, chunk_work));
+        } else {
+            CRISPY_TRY(chunk_work());
+        }
         if (sink) {
             CRISPY_CK(ctx, cudaMemcpyAsync(g.h_pairs.ptr, g.out_pairs.ptr, (size_t)c * 8, cudaMemcpyDeviceToHost, s));
             CRISPY_CK(ctx, cudaMemcpyAsync(g.h_dists.ptr, g.out_dists.ptr, (size_t)c * 4, cudaMemcpyDeviceToHost, s));
@@ -871,7 +918,7 @@ int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int 
     CRISPY_TRY(ensure(ctx, g.al, (size_t)npairs * 4));
     CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, pairs, (size_t)npairs * 8, cudaMemcpyHostToDevice, s));
     CRISPY_TRY(gen_dispatch_impl(ctx, s, g.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
-                                 g.score.as<int32_t>(), g.ml.as<int32_t>(), g.al.as<int32_t>(), pairs));
+                                 g.score.as<int32_t>(), g.ml.as<int32_t>(), g.al.as<int32_t>()));
     if (dist) CRISPY_CK(ctx, cudaMemcpyAsync(dist, g.dist.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
     if (score) CRISPY_CK(ctx, cudaMemcpyAsync(score, g.score.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
     if (ml) CRISPY_CK(ctx, cudaMemcpyAsync(ml, g.ml.ptr, (size_t)npairs * 4, cudaMemcpyDeviceToHost, s));
@@ -900,8 +947,9 @@ int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int ba
         CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
         CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, pairs, (size_t)npairs * 8, cudaMemcpyHostToDevice, s));
         CRISPY_TRY(gen_dispatch_impl(ctx, s, g.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
-                                     nullptr, nullptr, nullptr, pairs));
-        CRISPY_TRY(gen_finish(ctx, s, g.pairs.as<int2>(), npairs, thr, sink, user, &ns));
+                                     nullptr, nullptr, nullptr));
+        CRISPY_TRY(gen_finish(ctx, s, g.pairs.as<int2>(), npairs, thr, sink, user, &ns,
+                              mode == CRISPY_MODE_BATCHED));
     }
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
@@ -951,11 +999,6 @@ int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, cri
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     const int64_t npairs = k.nsurv;
-    // the bucketing needs read lengths per pair on the host
-    std::vector<int32_t> hp((size_t)npairs * 2);
-    if (npairs > 0)
-        CRISPY_CK(ctx, cudaMemcpyAsync(hp.data(), k.pairs.ptr, (size_t)npairs * 8, cudaMemcpyDeviceToHost, s));
-    CRISPY_CK(ctx, cudaStreamSynchronize(s));
     const crispy_stats kst = ctx->stats;
     ctx->stats = crispy_stats{};
     ctx->ev_gen.used = 0;
@@ -964,8 +1007,9 @@ int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, cri
     if (npairs > 0) {
         CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
         CRISPY_TRY(gen_dispatch_impl(ctx, s, k.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
-                                     nullptr, nullptr, nullptr, hp.data()));
-        CRISPY_TRY(gen_finish(ctx, s, k.pairs.as<int2>(), npairs, thr, sink, user, &ns));
+                                     nullptr, nullptr, nullptr));
+        CRISPY_TRY(gen_finish(ctx, s, k.pairs.as<int2>(), npairs, thr, sink, user, &ns,
+                              mode == CRISPY_MODE_BATCHED));
     }
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));

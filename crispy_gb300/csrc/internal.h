@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -53,8 +55,16 @@ struct GenJob {
     std::vector<int64_t> h_woff;     // first packed word of each read
     DevBuf seq, off, len, woff, packed;
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
-        vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue;
+        vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue,
+        cstats, ckeys, ckeys_alt, cvals, cvals_alt;
     HostBuf h_pairs, h_dists;
+};
+
+// An instantiated CUDA graph of one launch sequence and the number of
+// kernels it holds.
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
 };
 
 struct StreamEvents {
@@ -77,6 +87,8 @@ struct crispy_ctx {
     crispy::KmerJob kmer;
     crispy::GenJob gen;
     crispy::StreamEvents ev_kmer, ev_gen;
+    std::map<std::string, crispy::GraphEntry> graphs;   // captured launch sequences
+    bool use_graphs = true;
     size_t mem_cap = 0;      // 0 = unlimited
     size_t mem_in_use = 0;   // bytes held by DevBuf allocations
     cudaEvent_t t_begin = nullptr, t_end = nullptr;
@@ -100,7 +112,16 @@ double ev_sum_ms(StreamEvents& ev);
 // kernel counter (every launch of this library increments it)
 void count_launch(crispy_ctx* ctx, int n = 1);
 
+// Run a launch sequence through a CUDA graph: the first call with a key
+// captures `enqueue` (which must only enqueue work on s: no host syncs, no
+// allocation) and instantiates it; later calls with the same key replay it.
+// The key must name every size and device address the sequence bakes in.
+int graph_run(crispy_ctx* ctx, cudaStream_t s, const std::string& key,
+              const std::function<int()>& enqueue);
+void graph_clear(crispy_ctx* ctx);
+
 // radix sort / scan helpers (sort.cu)
+size_t sort_tmp_bytes(int64_t n);   // scratch a sort of n items needs
 int sort_u64_payload(crispy_ctx* ctx, cudaStream_t s, uint64_t* keys, uint64_t* keys_alt,
                      uint32_t* vals, uint32_t* vals_alt, int64_t n, int key_bits,
                      bool with_vals, uint64_t** sorted_keys, uint32_t** sorted_vals,
@@ -115,6 +136,15 @@ int compact_flags(crispy_ctx* ctx, cudaStream_t s, const uint8_t* flags, int64_t
                   uint32_t* out_idx, uint32_t* tile_counts, DevBuf& tmp, int64_t* total);
 
 }  // namespace crispy
+
+inline std::string key_of(std::initializer_list<uint64_t> parts) {
+    std::string k;
+    for (uint64_t v : parts) {
+        k += std::to_string(v);
+        k += ',';
+    }
+    return k;
+}
 
 #define CRISPY_CK(ctx, call)                                                        \
     do {                                                                            \

@@ -76,21 +76,33 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // lane of the group's interleaved block, its largest multiplicity, its count
 // of entries above the dense levels, and for K = 8 the (largest K-mer >=
 // 0x8000, its count) key used by the quirk.
+//
+// Entry order inside a read's lane follows a bank schedule: the entry gathered
+// at step e by lane l should sit in shared-memory bank (e + l) mod 32 (an
+// entry's bank is its value mod 32), so the 32 lanes of a warp hit 32
+// different banks.  Each bucket (bank) b fills the steps e = o_b + 32 i with
+// o_b = (b - l) mod 32 while it has entries; entries left over after a
+// bucket's steps are used fill the steps whose bucket ran dry.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) kmer_prep_kernel(
+constexpr int kPrepThreads = 256;
+constexpr int kPrepPer = CRISPY_MAX_READ_LEN / kPrepThreads;   // positions per thread
+
+__global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
     const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
     const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
     uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
     uint32_t* __restrict__ hinfo) {
     extern __shared__ uint32_t hist[];
-    __shared__ int s_max, s_high;
+    __shared__ int s_max, s_high, s_left;
     __shared__ uint32_t s_hmax;
+    __shared__ int s_bcnt[32], s_hole0[32];
     const uint32_t K4 = 1u << (2 * K);
     const int hwords = (int)((K4 + 1) / 2);
     for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_high = 0; }
+        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_high = 0; s_left = 0; }
+        if (threadIdx.x < 32) s_bcnt[threadIdx.x] = 0;
         __syncthreads();
         const int T = tcount[r];
         const uint8_t* s = seq + off[r];
@@ -98,16 +110,59 @@ __global__ void __launch_bounds__(256) kmer_prep_kernel(
         const int lane = r & 31;
         const int E = gent[r >> 5];
         int high = 0;
-        for (int p = threadIdx.x; p < T; p += blockDim.x) {
-            const uint32_t v = kmer_at(s, p, K);
-            const uint32_t sh = (v & 1u) * 16u;
-            const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
-            const uint32_t t = (old >> sh) & 0xFFFFu;
-            dst[ent_at(p, lane)] = t * K4 + v;
-            high += (int)t >= dense_levels;
+        uint32_t val[kPrepPer];
+        int rank[kPrepPer];
+#pragma unroll
+        for (int k = 0; k < kPrepPer; ++k) {
+            const int p = threadIdx.x + k * kPrepThreads;
+            if (p < T) {
+                const uint32_t v = kmer_at(s, p, K);
+                const uint32_t sh = (v & 1u) * 16u;
+                const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
+                const uint32_t t = (old >> sh) & 0xFFFFu;
+                val[k] = t * K4 + v;
+                rank[k] = atomicAdd(&s_bcnt[val[k] & 31u], 1);
+                high += (int)t >= dense_levels;
+            }
         }
         for (int p = T + threadIdx.x; p < E; p += blockDim.x) dst[ent_at(p, lane)] = kSentinel;
         atomicAdd(&s_high, high);
+        __syncthreads();
+        // steps per bucket and the holes they leave, prefix-summed (warp 0)
+        if (threadIdx.x < 32) {
+            const int b = threadIdx.x;
+            const int o = (b - lane) & 31;
+            const int steps = o < T ? (T - 1 - o) / 32 + 1 : 0;
+            const int holes = max(0, steps - s_bcnt[b]);
+            int x = holes;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, d);
+                if (b >= d) x += y;
+            }
+            s_hole0[b] = x - holes;   // exclusive prefix
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kPrepPer; ++k) {
+            const int p = threadIdx.x + k * kPrepThreads;
+            if (p < T) {
+                const int b = (int)(val[k] & 31u);
+                const int o = (b - lane) & 31;
+                const int steps = o < T ? (T - 1 - o) / 32 + 1 : 0;
+                int step;
+                if (rank[k] < steps) {
+                    step = o + 32 * rank[k];
+                } else {
+                    const int j = atomicAdd(&s_left, 1);
+                    int h = 0;
+                    while (h < 31 && s_hole0[h + 1] <= j) ++h;
+                    const int oh = (h - lane) & 31;
+                    step = oh + 32 * (s_bcnt[h] + (j - s_hole0[h]));
+                }
+                dst[ent_at(step, lane)] = val[k];
+            }
+        }
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
@@ -487,7 +542,7 @@ __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
                 int sum_lo = 0, sum_hi = 0;
                 for (int e = 0; e < Tc; ++e) {
                     const uint32_t idx = __ldg(ep + ent_at(e, cl));
-                    const uint32_t t = idx / K4, v = idx - t * K4;
+                    const uint32_t t = idx >> (2 * a.K), v = idx & (K4 - 1u);
                     const uint32_t cnt = (hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu;
                     const int hit = cnt > t;
                     if (v >= 0x8000u) sum_hi += hit; else sum_lo += hit;
@@ -652,7 +707,7 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     const int grid = std::min(n, ctx->sm_count * (k >= 8 ? 1 : 8));
     int32_t* cntmax = j.cntmax.as<int32_t>();
     int32_t* nhigh = cntmax + n;
-    kmer_prep_kernel<<<grid, 256, hsmem, s>>>(j.seq.as<uint8_t>(), j.off.as<int64_t>(),
+    kmer_prep_kernel<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), j.off.as<int64_t>(),
                                               j.t.as<int32_t>(), n, k, dense_levels_for(k),
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
@@ -734,9 +789,13 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         da.dense_group = fast ? j.work.as<uint8_t>() : nullptr;
         da.counter = ta.counter; da.keys = ta.keys; da.vals = ta.vals; da.cap = cap;
 
-        if (mode == CRISPY_MODE_PLAIN) {
+        if (mode == CRISPY_MODE_PLAIN || mode == CRISPY_MODE_STAGED) {
             // One launch per reference stage, round-robin over 8 streams like
-            // the reference's stage loop (kmerCUDA.cu:79-111).
+            // the reference's stage loop (kmerCUDA.cu:79-111).  PLAIN runs the
+            // one-thread-per-pair dense kernel on every row, STAGED the
+            // bit-sliced tile kernel (dense kernel only for its overflow rows).
+            const bool tiles = fast && mode == CRISPY_MODE_STAGED;
+            const bool dense_all = !tiles;
             cudaEvent_t fork;
             CRISPY_CK(ctx, cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
             CRISPY_CK(ctx, cudaEventRecord(fork, s));
@@ -749,13 +808,14 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     TileArgs t2 = ta;
                     t2.r_lo = sx * A; t2.r_hi = std::min(n, sx * A + A);
                     t2.c_lo = sy * A; t2.c_hi = std::min(n, sy * A + A);
-                    if (fast) {
+                    if (tiles) {
                         const int rg0 = t2.r_lo / 32, rg1 = (t2.r_hi - 1) / 32;
                         tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
-                    if (any_dense) {
+                    if (dense_all || any_dense) {
                         DenseArgs d2 = da;
+                        if (dense_all) d2.dense_group = nullptr;
                         d2.r_lo = t2.r_lo; d2.r_hi = t2.r_hi; d2.c_lo = t2.c_lo; d2.c_hi = t2.c_hi;
                         kmer_dense_kernel<<<std::min(t2.r_hi - t2.r_lo, 4 * ctx->sm_count), 256, dsmem, ss>>>(d2);
                         count_launch(ctx);
@@ -793,13 +853,31 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile, kTileThreads, tsmem);
                 per_sm = std::max(1, per_sm);
                 const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)items.size());
+                DenseArgs d2 = da;
+                d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
+                const std::string key = "kmain," + key_of({(uint64_t)(uintptr_t)j.ent.ptr, (uint64_t)(uintptr_t)j.keys.ptr,
+                    (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.counter.ptr, (uint64_t)(uintptr_t)d_items,
+                    (uint64_t)(uintptr_t)j.mmin.ptr, (uint64_t)(uintptr_t)j.smin.ptr, (uint64_t)(uintptr_t)j.t.ptr,
+                    (uint64_t)(uintptr_t)j.gstart.ptr, (uint64_t)(uintptr_t)j.gent.ptr, (uint64_t)(uintptr_t)j.work.ptr,
+                    (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)j.off.ptr, (uint64_t)(uintptr_t)j.hinfo.ptr,
+                    (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
+                    (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A});
                 ev_begin(ctx, ctx->ev_kmer, s);
-                tile<<<grid, kTileThreads, tsmem, s>>>(t2);
+                CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
+                    CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
+                    CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 4, s));
+                    tile<<<grid, kTileThreads, tsmem, s>>>(t2);
+                    count_launch(ctx);
+                    if (any_dense) {
+                        kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
+                        count_launch(ctx);
+                    }
+                    CRISPY_CK(ctx, cudaGetLastError());
+                    return CRISPY_OK;
+                }));
                 ev_end(ctx, ctx->ev_kmer, s);
-                count_launch(ctx);
                 ctx->stats.kmer_launches += 1;
-            }
-            if (any_dense) {
+            } else if (any_dense) {
                 DenseArgs d2 = da;
                 d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
                 kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
@@ -819,18 +897,31 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     }
     // stable order: (stage, row, col)
     const int key_bits = bits_for((uint64_t)nstages * (uint64_t)n * (uint64_t)n);
-    uint64_t* sk = nullptr;
-    uint32_t* sv = nullptr;
-    CRISPY_TRY(sort_u64_payload(ctx, s, j.keys.as<uint64_t>(), j.keys_alt.as<uint64_t>(),
-                                j.vals.as<uint32_t>(), j.vals_alt.as<uint32_t>(), j.nsurv, key_bits,
-                                dists != 0, &sk, &sv, j.sort_tmp));
     CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));
     CRISPY_TRY(ensure(ctx, j.dists, (size_t)std::max<int64_t>(j.nsurv, 1) * 4));
-    if (j.nsurv > 0) {
-        kmer_decode_kernel<<<(unsigned)((j.nsurv + 255) / 256), 256, 0, s>>>(
-            sk, sv, j.nsurv, n, j.pairs.as<int2>(), dists ? j.dists.as<float>() : nullptr);
-        count_launch(ctx);
-        CRISPY_CK(ctx, cudaGetLastError());
+    CRISPY_TRY(ensure(ctx, j.sort_tmp, sort_tmp_bytes(j.nsurv)));
+    auto sort_decode = [&]() -> int {
+        uint64_t* sk = nullptr;
+        uint32_t* sv = nullptr;
+        CRISPY_TRY(sort_u64_payload(ctx, s, j.keys.as<uint64_t>(), j.keys_alt.as<uint64_t>(),
+                                    j.vals.as<uint32_t>(), j.vals_alt.as<uint32_t>(), j.nsurv, key_bits,
+                                    dists != 0, &sk, &sv, j.sort_tmp));
+        if (j.nsurv > 0) {
+            kmer_decode_kernel<<<(unsigned)((j.nsurv + 255) / 256), 256, 0, s>>>(
+                sk, sv, j.nsurv, n, j.pairs.as<int2>(), dists ? j.dists.as<float>() : nullptr);
+            count_launch(ctx);
+            CRISPY_CK(ctx, cudaGetLastError());
+        }
+        return CRISPY_OK;
+    };
+    if (mode == CRISPY_MODE_BATCHED && j.nsurv > 0) {
+        const std::string key = "ksort," + key_of({(uint64_t)j.nsurv, (uint64_t)key_bits, (uint64_t)dists,
+            (uint64_t)n, (uint64_t)(uintptr_t)j.keys.ptr, (uint64_t)(uintptr_t)j.keys_alt.ptr,
+            (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.vals_alt.ptr,
+            (uint64_t)(uintptr_t)j.sort_tmp.ptr, (uint64_t)(uintptr_t)j.pairs.ptr, (uint64_t)(uintptr_t)j.dists.ptr});
+        CRISPY_TRY(graph_run(ctx, s, key, sort_decode));
+    } else {
+        CRISPY_TRY(sort_decode());
     }
     j.have_dists = dists != 0;
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));

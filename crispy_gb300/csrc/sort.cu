@@ -11,6 +11,8 @@
 // which is all genDist needs (distances are ML/AL >= +0.0, never NaN).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.h"
 
 namespace crispy {
@@ -47,7 +49,6 @@ __global__ void __launch_bounds__(kSortThreads) rs_hist(const K* __restrict__ ke
 // to *total when total != nullptr.
 __global__ void __launch_bounds__(1024) scan_exclusive_1blk(uint32_t* __restrict__ v, int64_t m,
                                                             uint32_t* __restrict__ total) {
-    __shared__ uint32_t part[1024];
     __shared__ uint32_t wsum[32];
     const int t = threadIdx.x;
     const int64_t per = (m + 1023) / 1024;
@@ -75,7 +76,6 @@ __global__ void __launch_bounds__(1024) scan_exclusive_1blk(uint32_t* __restrict
     }
     __syncthreads();
     uint32_t excl = x - s + (w > 0 ? wsum[w - 1] : 0u);
-    part[t] = excl;
     if (t == 1023 && total) *total = excl + s;
     uint32_t run = excl;
     for (int64_t i = lo; i < hi; ++i) {
@@ -217,6 +217,11 @@ __global__ void __launch_bounds__(kCmpThreads) cmp_scatter(const uint8_t* __rest
 }
 
 }  // namespace
+
+size_t sort_tmp_bytes(int64_t n) {
+    const int64_t nblocks = (n + kSortTile - 1) / kSortTile;
+    return (size_t)256 * (size_t)std::max<int64_t>(nblocks, 1) * sizeof(uint32_t);
+}
 
 int sort_u64_payload(crispy_ctx* ctx, cudaStream_t s, uint64_t* keys, uint64_t* keys_alt,
                      uint32_t* vals, uint32_t* vals_alt, int64_t n, int key_bits, bool with_vals,

@@ -51,9 +51,21 @@ extern "C" {
 #define CRISPY_MAX_NUM_READS  (1024 * 1024)
 #define CRISPY_GEN_WINDOW     589824   /* genMain.h:24-27: pairs per load window and chunk flush size */
 
-/* ---- run modes ---- */
-#define CRISPY_MODE_PLAIN    0  /* one launch per reference stage (kmer) / per load window (gen) */
-#define CRISPY_MODE_BATCHED  1  /* length-bucketed persistent kernels on a device work queue, CUDA-graph launched */
+/* ---- run modes (all three give identical bits) ----
+ * PLAIN    the plain from-scratch kernels, one thread per pair: kmerDist with
+ *          one block per row read holding its dense count table, genDist with
+ *          band rows in global scratch; launched per reference stage (kmer)
+ *          and per 589,824-pair load window (gen), like the reference.
+ * STAGED   the GB300 kernels (bit-sliced k-mer tiles, warp-cooperative
+ *          anti-diagonal DP) launched the plain way: per stage / per window,
+ *          one fixed band-tile shape per window.
+ * BATCHED  the GB300 kernels as persistent work-queue kernels: row-group
+ *          queue for kmerDist, pairs bucketed by band width and length with
+ *          autotuned lanes-per-pair and band-tile shape for genDist, launch
+ *          sequences replayed as CUDA graphs. */
+#define CRISPY_MODE_PLAIN    0
+#define CRISPY_MODE_BATCHED  1
+#define CRISPY_MODE_STAGED   2
 
 typedef struct crispy_ctx crispy_ctx;
 
@@ -190,6 +202,7 @@ typedef struct crispy_stats {
     int64_t gen_cells;         /* band cells of those pairs */
     int64_t gen_survivors;
     int64_t kernels_launched;  /* every kernel this library launched in the last run */
+    int64_t graph_launches;    /* CUDA graph replays among them (batched form) */
 } crispy_stats;
 int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */

@@ -27,7 +27,7 @@ BIN = cg.BIN_DIR
 def _cases(kind):
     for name, s in MANIFEST["sets"].items():
         for run in s[kind]:
-            for mode in ("batched", "plain"):
+            for mode in ("batched", "staged", "plain"):
                 yield name, run, mode
 
 

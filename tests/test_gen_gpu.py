@@ -38,7 +38,7 @@ def _random_pairs(n, m, seed):
 
 
 @pytest.mark.parametrize("band", [10, 5, 3, 2, 1])
-@pytest.mark.parametrize("mode", [cg.MODE_PLAIN, cg.MODE_BATCHED])
+@pytest.mark.parametrize("mode", [cg.MODE_PLAIN, cg.MODE_STAGED, cg.MODE_BATCHED])
 def test_gen_bands(engine, band, mode):
     reads = _reads(300, 50 + band)
     pairs = _random_pairs(len(reads), 3000, band)
@@ -60,8 +60,8 @@ def test_gen_edge_reads(engine):
     n = len(reads)
     pairs = np.array([(i, j) for i in range(n) for j in range(n)], np.int32)
     for band in (10, 2, 1):
-        _align_check(engine, reads, pairs, band, cg.MODE_BATCHED)
-        _align_check(engine, reads, pairs, band, cg.MODE_PLAIN)
+        for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN):
+            _align_check(engine, reads, pairs, band, mode)
 
 
 def test_gen_run_chunks_small(engine):
@@ -73,7 +73,7 @@ def test_gen_run_chunks_small(engine):
     pairs, _ = engine.kmer_fetch(cnt, False)
     engine.gen_prepare(buf, offs, lens)
     tg = cg.default_threshold(len(reads), -1.0, 1)
-    for mode in (cg.MODE_PLAIN, cg.MODE_BATCHED):
+    for mode in (cg.MODE_PLAIN, cg.MODE_STAGED, cg.MODE_BATCHED, cg.MODE_BATCHED):
         got = engine.gen_run(pairs, 10, tg, mode)
         od, _, _, _ = oracle.gen_all(buf, offs, lens, pairs, 10)
         want = oracle.gen_chunks(pairs, od, tg)

@@ -32,7 +32,7 @@ def _check(engine, reads, k, thr, mode):
     return cnt
 
 
-@pytest.mark.parametrize("mode", [cg.MODE_PLAIN, cg.MODE_BATCHED])
+@pytest.mark.parametrize("mode", [cg.MODE_PLAIN, cg.MODE_STAGED, cg.MODE_BATCHED])
 @pytest.mark.parametrize("k", [4, 5, 6, 7, 8])
 def test_kmer_k_modes(engine, k, mode):
     reads = _reads(400, 100 + k, k=k)
@@ -44,8 +44,8 @@ def test_kmer_k_modes(engine, k, mode):
 def test_kmer_tile_sizes_default_threshold(engine, n):
     reads = _reads(n + n // 10 + 5, 7 + n)[:n]
     t = cg.default_threshold(len(reads), -1.0, 0)
-    _check(engine, reads, 6, t, cg.MODE_BATCHED)
-    _check(engine, reads, 6, t, cg.MODE_PLAIN)
+    for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN):
+        _check(engine, reads, 6, t, mode)
 
 
 def test_kmer_k1_k3(engine):
@@ -65,8 +65,8 @@ def test_kmer_heavy_multiplicity(engine):
         s[10:10 + run] = b"A" * run
         heavy.append(bytes(s))
     reads = synth.preprocess_order(reads[40:] + heavy)
-    _check(engine, reads, 6, 0.5, cg.MODE_BATCHED)
-    _check(engine, reads, 6, 0.5, cg.MODE_PLAIN)
+    for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN):
+        _check(engine, reads, 6, 0.5, mode)
     # long degenerate reads: counts above 255
     long = [b"A" * (400 + i) for i in range(5)] + [b"AC" * (150 + i) for i in range(5)]
     _check(engine, synth.preprocess_order(long + reads[:30]), 6, 0.9, cg.MODE_BATCHED)
@@ -88,7 +88,11 @@ def test_kmer_uneven_lengths(engine):
     t = cg.default_threshold(len(reads), -1.0, 0)
     a = _check(engine, reads, 6, t, cg.MODE_BATCHED)
     b = _check(engine, reads, 6, t, cg.MODE_PLAIN)
-    assert a == b
+    c = _check(engine, reads, 6, t, cg.MODE_STAGED)
+    assert a == b == c
+    # the batched form again: its launch sequences replay as CUDA graphs
+    assert _check(engine, reads, 6, t, cg.MODE_BATCHED) == a
+    assert engine.stats()["graph_launches"] > 0
 
 
 def test_kmer_nonacgt(engine):
