@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -110,28 +111,46 @@ __device__ __forceinline__ Best group_best(Best b, int lane) {
     return r;
 }
 
+// Scores are stored as V = M + 2s on anti-diagonal s = i + j.  All three
+// candidates of a cell then carry the same offset 2s, so the maxima and
+// tie-breaks are those of M, while the diagonal candidate becomes
+// V(s-2) + 9*match and a gap candidate V(s-1) + pen + 2.
+//
+// ML and AL travel packed as (A << 16) | B with A = diagonal moves on the
+// path and B = (i0 + j0) + A + matches, (i0, j0) the boundary cell the path
+// starts from (whose packed value i0 + j0 is the reference's AL there, ML
+// 0).  A diagonal move adds 0x10001 + match, a gap move adds nothing, and at
+// the end ML = (i + j) - B, AL = (i + j) - A.
 template <int C>
 struct Lane {
-    int cM[C], cU[C], cF[C];
+    int cM[C], cU[C], cF[C];   // V and the two gap-penalised copies (+2)
     uint32_t cL[C];
     int pM[C];
     uint32_t pL[C];
-    uint32_t w1[C], w2[C];
+    uint32_t x0[C], x1[C];     // per-slot symbol XOR fields of the block, by parity
+    int cap0[C], cap1[C];      // kNeg for a parity whose diagonal is out of band
 };
 
 // Per-pair values a sub-group holds (the same in all its lanes).
 struct PairCtx {
     int kb, l1, l2, shift;   // shift = kb & 1: odd bands run one step late
-    uint32_t band_ok;        // bit 2c+P: slot c's parity-P diagonal is in band
 };
 
-// One anti-diagonal step at parity P for all C slots of this lane.  The
+// Block kinds.  kClean: no cell of the block touches the matrix border.
+// kTrack: no boundary cell and no cell before the matrix (s >= kBand + 2),
+// but last-row / last-column cells may appear; cells past the matrix are
+// computed and ignored, since no in-matrix cell depends on them.  kFull:
+// boundary cells, cells before the matrix and tracking.
+constexpr int kClean = 0, kTrack = 1, kFull = 2;
+
+// One anti-diagonal step at parity P for all C slots of this lane, the
+// slot's F-th cell of this parity inside the current group of three.  The
 // sub-group's own step is s = t - shift, which makes P = t & 1 for every
-// sub-group of the warp.  kChecked adds the matrix-border logic (boundary
-// cells, cells before the matrix, last-row / last-column tracking).
-template <int G, int C, int P, bool kChecked>
-__device__ __forceinline__ void step(Lane<C>& st, int gl, int s, const PairCtx& pc, Best& col,
-                                     Best& row) {
+// sub-group of the warp.  dbase = 2*gl*C - kBand is the parity-0 diagonal
+// of the lane's first slot.
+template <int G, int C, int P, int F, int kMode>
+__device__ __forceinline__ void step(Lane<C>& st, int gl, int s, int dbase, const PairCtx& pc,
+                                     Best& col, Best& row) {
     int nbM;
     uint32_t nbL;
     if (P == 0) {
@@ -160,55 +179,80 @@ __device__ __forceinline__ void step(Lane<C>& st, int gl, int s, const PairCtx& 
             upL = c < C - 1 ? st.cL[c + 1] : nbL;
             lfM = st.cF[c]; lfL = st.cL[c];
         }
-        const bool match = (st.w1[c] ^ st.w2[c]) < 0x40000000u;
-        const int md = st.pM[c] + (match ? kMatch : kMismatch);
+        const uint32_t xf = P == 0 ? st.x0[c] : st.x1[c];
+        const bool match = (xf & (0xC0000000u >> (2 * F))) == 0u;
+        int md = st.pM[c];
+        if (match) md += kMatch - kMismatch;
         // max with predicate: isU = up >= left (up wins ties over left),
         // isD = diag >= max(up, left) (diag wins every tie)
         bool isU, isD;
         const int mul = __vibmax_s32(upM, lfM, &isU);
         const int mx = __vibmax_s32(md, mul, &isD);
-        const uint32_t lpred = isU ? upL : lfL;
-        uint32_t l = isD ? st.pL[c] + (match ? 0x1u : 0x10001u) : lpred + 0x10001u;
-        int pu = isD ? kGO : (isU ? kGE : 0);
-        int pf = isD ? kGO : (isU ? 0 : kGE);
-        int m = mx;
-        const int q = (gl * C + c);
-        const int d = 2 * q - pc.kb + P;
-        if (kChecked) {
+        uint32_t ld = st.pL[c] + 0x10001u;
+        if (match) ld += 1u;
+        uint32_t l = isD ? ld : (isU ? upL : lfL);
+        int m = min(mx, P == 0 ? st.cap0[c] : st.cap1[c]);
+        const int a = isU ? 2 + kGE : 2;
+        int u = m + a, f = m + (2 + 2 + kGE) - a;
+        if (isD) { u = m + 2 + kGO; f = m + 2 + kGO; }
+        if (kMode == kFull) {
+            const int d = dbase + 2 * c + P;
             const int i = (s + d) >> 1, j = (s - d) >> 1;
-            if (!((pc.band_ok >> (2 * c + P)) & 1u) || i < 0 || j < 0) {
-                m = kNeg; pu = 0; pf = 0; l = 0;
+            if (m == kNeg || i < 0 || j < 0) {
+                m = kNeg; u = kNeg; f = kNeg; l = 0;
             } else if (i == 0 || j == 0) {
-                m = 0; pu = 0; pf = 0; l = (uint32_t)(i + j);
+                m = 2 * s; u = m + 2; f = m + 2; l = (uint32_t)(i + j);
             } else {
-                if (i == pc.l2 && j <= pc.l1) track(col, m, l, j);
-                if (j == pc.l1 && i <= pc.l2) track(row, m, l, i);
+                if (i == pc.l2 && j <= pc.l1) track(col, m - 2 * s, l, j);
+                if (j == pc.l1 && i <= pc.l2) track(row, m - 2 * s, l, i);
             }
-        } else {
-            if (!((pc.band_ok >> (2 * c + P)) & 1u)) { m = kNeg; pu = 0; pf = 0; l = 0; }
         }
-        nM[c] = m; nU[c] = m + pu; nF[c] = m + pf; nL[c] = l;
+        nM[c] = m; nU[c] = u; nF[c] = f; nL[c] = l;
+    }
+    if (kMode == kTrack) {
+        // slot c sits on the last row when x + 2c == 0 (2i = 2*l2) and on
+        // the last column when y - 2c == 0 (2j = 2*l1): once per slot and
+        // parity, so one range test per step guards the rare work
+        const int d0 = dbase + P;
+        const int x = s + d0 - 2 * pc.l2;
+        const int y = s - d0 - 2 * pc.l1;
+        if ((x <= 0 && x > -2 * C) || (y >= 0 && y < 2 * C)) {
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                if (nM[c] == kNeg) continue;   // out of band
+                const int i = (s + d0 + 2 * c) >> 1, j = (s - d0 - 2 * c) >> 1;
+                if (x + 2 * c == 0 && j >= 1 && j <= pc.l1) track(col, nM[c] - 2 * s, nL[c], j);
+                if (y - 2 * c == 0 && i >= 1 && i <= pc.l2) track(row, nM[c] - 2 * s, nL[c], i);
+            }
+        }
     }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         st.pM[c] = st.cM[c]; st.pL[c] = st.cL[c];
         st.cM[c] = nM[c]; st.cU[c] = nU[c]; st.cF[c] = nF[c]; st.cL[c] = nL[c];
-        if (P == 0) st.w2[c] <<= 2; else st.w1[c] <<= 2;
     }
 }
 
-// A block of kBlockSteps steps: each 16-symbol window advances at most 15
-// times inside it (it advances on every other step), so the 16 symbols
-// loaded at the block start cover every position the block touches.
+// A block of kBlockSteps = 30 steps gives each slot 15 cells per parity;
+// the symbols they compare are fields 0..14 of the XOR words built from the
+// 16-symbol windows at the block start.  Groups of six steps test fields
+// F = 0, 1, 2 and then shift the XOR words by three fields.
 constexpr int kBlockSteps = 30;
 
-template <int G, int C, bool kChecked>
+template <int G, int C, int kMode>
 __device__ __forceinline__ void block_steps(Lane<C>& st, int gl, int s0, const PairCtx& pc,
                                             Best& col, Best& row) {
-#pragma unroll 3
-    for (int t = 0; t < kBlockSteps; t += 2) {
-        step<G, C, 0, kChecked>(st, gl, s0 + t, pc, col, row);
-        step<G, C, 1, kChecked>(st, gl, s0 + t + 1, pc, col, row);
+    const int dbase = 2 * gl * C - pc.kb;
+#pragma unroll 1
+    for (int t = 0; t < kBlockSteps; t += 6) {
+        step<G, C, 0, 0, kMode>(st, gl, s0 + t, dbase, pc, col, row);
+        step<G, C, 1, 0, kMode>(st, gl, s0 + t + 1, dbase, pc, col, row);
+        step<G, C, 0, 1, kMode>(st, gl, s0 + t + 2, dbase, pc, col, row);
+        step<G, C, 1, 1, kMode>(st, gl, s0 + t + 3, dbase, pc, col, row);
+        step<G, C, 0, 2, kMode>(st, gl, s0 + t + 4, dbase, pc, col, row);
+        step<G, C, 1, 2, kMode>(st, gl, s0 + t + 5, dbase, pc, col, row);
+#pragma unroll
+        for (int c = 0; c < C; ++c) { st.x0[c] <<= 6; st.x1[c] <<= 6; }
     }
 }
 
@@ -222,15 +266,29 @@ __device__ void align_sweep(Lane<C>& st, const uint32_t* sm1, const uint32_t* sm
         for (int c = 0; c < C; ++c) {
             const int d = 2 * (gl * C + c) - pc.kb;   // parity 0 at the block start
             const int i = (s0 + d) >> 1, j = (s0 - d) >> 1;
-            st.w2[c] = window_at(sm2, i - 1);
-            st.w1[c] = window_at(sm1, j - 1);
+            // parity-0 cells compare read1[j-1+k] with read2[i-1+k],
+            // parity-1 cells read1[j-1+k] with read2[i+k]
+            const uint32_t w2 = window_at(sm2, i - 1);
+            const uint32_t w1 = window_at(sm1, j - 1);
+            st.x0[c] = w1 ^ w2;
+            st.x1[c] = w1 ^ (w2 << 2);
         }
-        const bool clean = s0 >= pc.kb + 2 && s0 + kBlockSteps - 1 < clean_hi;
+        const bool started = s0 >= pc.kb + 2;
+        const bool clean = started && s0 + kBlockSteps - 1 < clean_hi;
         if (__all_sync(0xffffffffu, clean))
-            block_steps<G, C, false>(st, gl, s0, pc, col, row);
+            block_steps<G, C, kClean>(st, gl, s0, pc, col, row);
+        else if (__all_sync(0xffffffffu, started))
+            block_steps<G, C, kTrack>(st, gl, s0, pc, col, row);
         else
-            block_steps<G, C, true>(st, gl, s0, pc, col, row);
+            block_steps<G, C, kFull>(st, gl, s0, pc, col, row);
     }
+}
+
+// Packed (A << 16) | B of the chosen last-row / last-column cell -> ML, AL.
+__device__ __forceinline__ void unpack_mlal(uint32_t l, int ij, int* ml, int* al) {
+    if (ij < 0) { *ml = 0; *al = 0; return; }   // no tracked cell (reference: ML = AL = 0)
+    *ml = ij - (int)(l & 0xffffu);
+    *al = ij - (int)(l >> 16);
 }
 
 // One pair per G-lane sub-group (32/G pairs per warp), C band slots per
@@ -255,7 +313,7 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
         const int64_t item = base + sub;
         const bool valid = item < a.count;
         int64_t p = -1;
-        PairCtx pc{0, 0, 0, 0, 0};
+        PairCtx pc{0, 0, 0, 0};
         int2 pr = make_int2(0, 0);
         if (valid) {
             p = a.order ? (int64_t)a.order[item] : item;
@@ -265,12 +323,6 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
             pc.kb = kband_of(pc.l1, pc.l2, a.band);
         }
         pc.shift = pc.kb & 1;
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const int q = gl * C + c;
-            if (valid && 2 * q - pc.kb <= pc.kb) pc.band_ok |= 1u << (2 * c);
-            if (valid && 2 * q - pc.kb + 1 <= pc.kb) pc.band_ok |= 1u << (2 * c + 1);
-        }
         const int nw1 = (pc.l1 + 15) >> 4, nw2 = (pc.l2 + 15) >> 4;
         const uint32_t* g1 = a.packed + (valid ? a.woff[pr.x] : 0);
         const uint32_t* g2 = a.packed + (valid ? a.woff[pr.y] : 0);
@@ -284,16 +336,28 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
         for (int c = 0; c < C; ++c) {
             st.cM[c] = kNeg; st.cU[c] = kNeg; st.cF[c] = kNeg; st.cL[c] = 0;
             st.pM[c] = kNeg; st.pL[c] = 0;
+            // slot q hosts diagonals 2q - kb (parity 0) and 2q - kb + 1
+            const int q = gl * C + c;
+            st.cap0[c] = valid && 2 * q - pc.kb <= pc.kb ? INT_MAX : kNeg;
+            st.cap1[c] = valid && 2 * q - pc.kb + 1 <= pc.kb ? INT_MAX : kNeg;
         }
         Best col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
-        const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)(pc.l1 + pc.l2 + pc.shift));
+        // the sweep ends at the last in-band cell of the last row or column
+        int s_end = 0;
+        if (valid) {
+            if (max(1, pc.l2 - pc.kb) <= min(pc.l1, pc.l2 + pc.kb)) s_end = pc.l2 + min(pc.l1, pc.l2 + pc.kb);
+            if (max(1, pc.l1 - pc.kb) <= min(pc.l2, pc.l1 + pc.kb))
+                s_end = max(s_end, pc.l1 + min(pc.l2, pc.l1 + pc.kb));
+        }
+        const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)(s_end + pc.shift));
         align_sweep<G, C>(st, sm1, sm2, gl, pc, t_end, col, row);
         col = group_best<G>(col, lane);
         row = group_best<G>(row, lane);
         if (gl == 0 && valid) {
             const bool use_col = col.m > row.m;   // genKernel.cu:765-768
-            const uint32_t l = use_col ? col.l : row.l;
-            const int mlv = (int)(l >> 16), alv = (int)(l & 0xffffu);
+            int mlv, alv;
+            if (use_col) unpack_mlal(col.l, col.at < 0 ? -1 : pc.l2 + col.at, &mlv, &alv);
+            else unpack_mlal(row.l, row.at < 0 ? -1 : row.at + pc.l1, &mlv, &alv);
             a.dist[p] = __fdiv_rn((float)mlv, (float)alv);
             if (a.score) a.score[p] = use_col ? col.m : row.m;
             if (a.ml) a.ml[p] = mlv;

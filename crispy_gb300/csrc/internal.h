@@ -39,7 +39,10 @@ struct KmerJob {
     std::vector<int32_t> h_cntmax;   // largest k-mer multiplicity per read
     std::vector<int64_t> h_gstart;   // first entry of each group
     std::vector<int32_t> h_gent;     // entries per lane in each group (multiple of 16)
-    DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo;
+    std::vector<int64_t> h_tstart;   // tile stream: first entry of each group
+    std::vector<int32_t> h_tgent;    // tile stream: steps per lane in each group
+    int64_t ntent = 0;
+    DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
     // last run's survivors, in stage order
     int64_t nsurv = 0;
     bool have_dists = false;

@@ -21,10 +21,14 @@
 //     shared memory, so the footprint stays fixed whatever the reads hold.
 //   * A warp owns 32 column reads (one per lane) and streams their entries
 //     from an interleaved layout (four consecutive entries of the 32 reads
-//     of a group form one 512-byte line, one uint4 per lane), gathers P[e],
-//     and adds the word into 32 bit-sliced counters with a Harley-Seal
-//     carry-save tree (LOP3 work only).  The next 16 entries are in flight
-//     while the current 16 are reduced.
+//     of a group form one 512-byte line, one uint4 per lane), gathers the
+//     plane word of each, and adds it into 32 bit-sliced counters with a
+//     Harley-Seal carry-save tree (LOP3 work only).  The next 16 entries are
+//     in flight while the current 16 are reduced.  The streamed entries are
+//     precomputed byte offsets into the planes, ordered per 32-read group so
+//     that the 32 lanes of a step hit 32 different banks; high-level entries
+//     and pads point at zero guard words, so the gather has no branch and
+//     the rare high-level entries get a separate hash pass.
 //   * The threshold is an integer test m >= mmin[min(Ta, Tb)], with mmin
 //     tabulated on the host from the reference's float expression (the pass
 //     predicate is monotone in m), first as a bit-sliced compare against a
@@ -77,12 +81,11 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // of entries above the dense levels, and for K = 8 the (largest K-mer >=
 // 0x8000, its count) key used by the quirk.
 //
-// Entry order inside a read's lane follows a bank schedule: the entry gathered
-// at step e by lane l should sit in shared-memory bank (e + l) mod 32 (an
-// entry's bank is its value mod 32), so the 32 lanes of a warp hit 32
-// different banks.  Each bucket (bank) b fills the steps e = o_b + 32 i with
-// o_b = (b - l) mod 32 while it has entries; entries left over after a
-// bucket's steps are used fill the steps whose bucket ran dry.
+// Entry order inside a read's lane: its high-level entries (occurrence rank
+// >= dense_levels) first, then its dense entries grouped by shared-memory
+// bank (an entry's bank is its value mod 32; banks in the order lane,
+// lane+1, ... mod 32), with the per-bank counts written to bcnt.  The tile kernel does not read this order directly: the
+// schedule kernel below turns it into a bank-conflict-avoiding stream.
 // ---------------------------------------------------------------------------
 constexpr int kPrepThreads = 256;
 constexpr int kPrepPer = CRISPY_MAX_READ_LEN / kPrepThreads;   // positions per thread
@@ -92,16 +95,16 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
     const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
     uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
-    uint32_t* __restrict__ hinfo) {
+    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt) {
     extern __shared__ uint32_t hist[];
-    __shared__ int s_max, s_high, s_left;
+    __shared__ int s_max, s_hpos;
     __shared__ uint32_t s_hmax;
-    __shared__ int s_bcnt[32], s_hole0[32];
+    __shared__ int s_bcnt[32], s_bstart[32];
     const uint32_t K4 = 1u << (2 * K);
     const int hwords = (int)((K4 + 1) / 2);
     for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_high = 0; s_left = 0; }
+        if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_hpos = 0; }
         if (threadIdx.x < 32) s_bcnt[threadIdx.x] = 0;
         __syncthreads();
         const int T = tcount[r];
@@ -109,60 +112,47 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
         uint32_t* dst = ent + gstart[r >> 5];
         const int lane = r & 31;
         const int E = gent[r >> 5];
-        int high = 0;
         uint32_t val[kPrepPer];
         int rank[kPrepPer];
 #pragma unroll
         for (int k = 0; k < kPrepPer; ++k) {
             const int p = threadIdx.x + k * kPrepThreads;
+            rank[k] = -1;
             if (p < T) {
                 const uint32_t v = kmer_at(s, p, K);
                 const uint32_t sh = (v & 1u) * 16u;
                 const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
                 const uint32_t t = (old >> sh) & 0xFFFFu;
                 val[k] = t * K4 + v;
-                rank[k] = atomicAdd(&s_bcnt[val[k] & 31u], 1);
-                high += (int)t >= dense_levels;
+                if ((int)t >= dense_levels) {
+                    dst[ent_at(atomicAdd(&s_hpos, 1), lane)] = val[k];
+                } else {
+                    rank[k] = atomicAdd(&s_bcnt[val[k] & 31u], 1);
+                }
             }
         }
         for (int p = T + threadIdx.x; p < E; p += blockDim.x) dst[ent_at(p, lane)] = kSentinel;
-        atomicAdd(&s_high, high);
         __syncthreads();
-        // steps per bucket and the holes they leave, prefix-summed (warp 0)
         if (threadIdx.x < 32) {
-            const int b = threadIdx.x;
-            const int o = (b - lane) & 31;
-            const int steps = o < T ? (T - 1 - o) / 32 + 1 : 0;
-            const int holes = max(0, steps - s_bcnt[b]);
-            int x = holes;
+            // bank order rotated by the lane: at a given position the 32
+            // reads of a group sit in different banks, which keeps the
+            // one-thread-per-column dense kernel free of bank conflicts
+            const int i = threadIdx.x;
+            const int b = (i + lane) & 31;
+            const int c = s_bcnt[b];
+            int x = c;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, x, d);
-                if (b >= d) x += y;
+                if (i >= d) x += y;
             }
-            s_hole0[b] = x - holes;   // exclusive prefix
+            s_bstart[b] = s_hpos + x - c;
+            bcnt[(int64_t)r * 32 + b] = (uint16_t)c;
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kPrepPer; ++k) {
-            const int p = threadIdx.x + k * kPrepThreads;
-            if (p < T) {
-                const int b = (int)(val[k] & 31u);
-                const int o = (b - lane) & 31;
-                const int steps = o < T ? (T - 1 - o) / 32 + 1 : 0;
-                int step;
-                if (rank[k] < steps) {
-                    step = o + 32 * rank[k];
-                } else {
-                    const int j = atomicAdd(&s_left, 1);
-                    int h = 0;
-                    while (h < 31 && s_hole0[h + 1] <= j) ++h;
-                    const int oh = (h - lane) & 31;
-                    step = oh + 32 * (s_bcnt[h] + (j - s_hole0[h]));
-                }
-                dst[ent_at(step, lane)] = val[k];
-            }
-        }
+        for (int k = 0; k < kPrepPer; ++k)
+            if (rank[k] >= 0) dst[ent_at(s_bstart[val[k] & 31u] + rank[k], lane)] = val[k];
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
@@ -177,7 +167,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
         __syncthreads();
         if (threadIdx.x == 0) {
             cntmax[r] = s_max;
-            nhigh[r] = s_high;
+            nhigh[r] = s_hpos;
             uint32_t info = 0;
             if (K == 8 && s_hmax >= 0x8000u) {
                 const uint32_t c = (hist[s_hmax >> 1] >> ((s_hmax & 1u) * 16u)) & 0xFFFFu;
@@ -191,10 +181,158 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Bank schedule of the tile stream: one warp per 32-read group writes, for
+// every step e < Et and lane l, the shared-memory byte offset that lane l
+// gathers at step e.  Lanes of a warp gather at the same time, so the 32
+// offsets of a step should sit in 32 different banks.
+//   * Ideal slots: lane l takes a bank-h entry at every step with
+//     (e + l) mod 32 == h while it has bank-h entries left; the ideal
+//     banks of one step are a rotation, hence all different.
+//   * A lane whose ideal bucket is empty at step e (a hole) takes one of its
+//     surplus entries (buckets with more entries than ideal slots) whose bank
+//     no other lane uses at e; claims are settled by match_any, lowest lane
+//     first, repeated until no lane can claim.
+//   * Remaining holes take a wildcard: a guard word (always zero) in a bank
+//     still free at e.  High-level entries (looked up in the hash by a
+//     separate pass) and the pad steps up to Et are the wildcards.  A lane
+//     out of wildcards places a surplus entry anyway (a bank conflict).
+// Every hole is filled by exactly one surplus entry or wildcard, because
+// holes - surplus = Et - dense entries = wildcards for every lane.
+// ---------------------------------------------------------------------------
+constexpr int kSchedWarps = 4;
+constexpr int kSchedChunk = 16;
+constexpr int kSchedSpare = 24;   // spare steps per group (reads of >= 128 tuples)
+
+__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {   // 0-based; -1 if none
+    for (int i = 0; i < k && m; ++i) m &= m - 1u;
+    return m ? __ffs(m) - 1 : -1;
+}
+
+__global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
+    const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
+    const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
+    const int32_t* __restrict__ tcount, const int32_t* __restrict__ nhigh,
+    const uint16_t* __restrict__ bcnt, int n, int ngroups, uint32_t guard_word,
+    uint32_t* __restrict__ tent) {
+    __shared__ uint16_t s_cnt[kSchedWarps][32][33];
+    __shared__ uint16_t s_ov[kSchedWarps][32][33];
+    __shared__ uint16_t s_next[kSchedWarps][32][33];   // next raw position per bank
+    __shared__ uint8_t s_bank[kSchedWarps][kSchedChunk][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
+        const int r = g * 32 + lane;
+        const int Et = tgent[g];
+        const int nh = r < n ? nhigh[r] : 0;
+        int D = 0;
+        unsigned ovmask = 0;
+        for (int b = 0; b < 32; ++b) {
+            const int c = r < n ? (int)bcnt[(int64_t)r * 32 + b] : 0;
+            const int o = (b - lane) & 31;
+            const int slots = Et > o ? (Et - o + 31) >> 5 : 0;
+            const int ov = max(0, c - slots);
+            s_cnt[w][lane][b] = (uint16_t)c;
+            s_ov[w][lane][b] = (uint16_t)ov;
+            D += c;
+            if (ov) ovmask |= 1u << b;
+        }
+        // first raw position of each bank: the prep kernel's lane-rotated order
+        for (int i = 0, pos = nh; i < 32; ++i) {
+            const int b = (i + lane) & 31;
+            s_next[w][lane][b] = (uint16_t)pos;
+            pos += s_cnt[w][lane][b];
+        }
+        int wild = Et - D;
+        __syncwarp();
+        const uint32_t* src = ent + gstart[g];
+        uint32_t* dst = tent + tstart[g];
+        for (int e0 = 0; e0 < Et; e0 += kSchedChunk) {
+            for (int i = 0; i < kSchedChunk; ++i) {
+                const int e = e0 + i;
+                const int h = (e + lane) & 31;
+                const bool hole = (e >> 5) >= (int)s_cnt[w][lane][h];
+                int bank = hole ? -1 : h;
+                unsigned used = __reduce_or_sync(full, hole ? 0u : (1u << h));
+                bool open = hole;
+                for (int round = 0; round < 32; ++round) {
+                    const unsigned cand = open ? (ovmask & ~used) : 0u;
+                    if (!__any_sync(full, cand != 0u)) break;
+                    const int prop = cand ? __ffs(cand) - 1 : 32 + lane;
+                    const unsigned peers = __match_any_sync(full, prop);
+                    const bool win = cand && lane == __ffs(peers) - 1;
+                    if (win) {
+                        bank = prop;
+                        open = false;
+                        const int left = (int)s_ov[w][lane][prop] - 1;
+                        s_ov[w][lane][prop] = (uint16_t)left;
+                        if (left == 0) ovmask &= ~(1u << prop);
+                    }
+                    used |= __reduce_or_sync(full, win ? (1u << prop) : 0u);
+                }
+                const bool wl = open && wild > 0;
+                const unsigned wm = __ballot_sync(full, wl);
+                if (wl) {
+                    // the k-th wildcard lane takes the k-th free bank
+                    const int fb = nth_set_bit(~used, __popc(wm & lt));
+                    bank = 32 + (fb >= 0 ? fb : 0);
+                    --wild;
+                } else if (open) {
+                    const int b = ovmask ? __ffs(ovmask) - 1 : -1;
+                    if (b >= 0) {
+                        bank = b;
+                        const int left = (int)s_ov[w][lane][b] - 1;
+                        s_ov[w][lane][b] = (uint16_t)left;
+                        if (left == 0) ovmask &= ~(1u << b);
+                    } else {
+                        bank = 32;   // unreachable by the count identity; stays in bounds
+                    }
+                }
+                s_bank[w][i][lane] = (uint8_t)bank;
+            }
+            __syncwarp();
+            // gather the chosen entries: positions first, then the loads
+            const int steps = min(kSchedChunk, Et - e0);
+            uint32_t v[kSchedChunk];
+#pragma unroll
+            for (int i = 0; i < kSchedChunk; ++i) {
+                v[i] = 0xFFFFFFFFu;
+                if (i < steps) {
+                    const int b = s_bank[w][i][lane];
+                    if (b < 32) {
+                        const int p = s_next[w][lane][b];
+                        s_next[w][lane][b] = (uint16_t)(p + 1);
+                        v[i] = (uint32_t)p;
+                    } else {
+                        v[i] = 0x80000000u | (uint32_t)(b - 32);
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kSchedChunk; ++i) {
+                if (i < steps) {
+                    const uint32_t x = v[i];
+                    v[i] = (x & 0x80000000u) ? (guard_word + (x & 31u)) * 4u
+                                             : __ldg(src + ent_at((int)x, lane)) * 4u;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kSchedChunk; ++i)
+                if (i < steps) dst[ent_at(e0 + i, lane)] = v[i];
+            __syncwarp();
+        }
+    }
+}
+
 struct TileArgs {
-    const uint32_t* ent;
+    const uint32_t* ent;           // level entries, high-level ones first per read
     const int64_t* gstart;
     const int32_t* gent;
+    const uint32_t* tent;          // scheduled byte offsets into the planes
+    const int64_t* tstart;
+    const int32_t* tgent;
+    const int32_t* nhigh;
     const int32_t* tcount;
     const uint8_t* dense_group;   // row groups the dense kernel takes instead
     const uint16_t* mmin;
@@ -269,14 +407,6 @@ __device__ __noinline__ uint32_t hash_find(const uint32_t* hkeys, const uint32_t
     return 0u;
 }
 
-__device__ __forceinline__ uint32_t lookup(const uint32_t* __restrict__ P, uint32_t limit,
-                                           const uint32_t* hkeys, const uint32_t* hmask,
-                                           bool any_high, uint32_t idx) {
-    if (idx < limit) return P[idx];
-    if (!any_high || idx == kSentinel) return 0u;
-    return hash_find(hkeys, hmask, idx);
-}
-
 template <int B>
 __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
                              const uint32_t* hkeys, const uint32_t* hmask, bool any_high,
@@ -284,7 +414,7 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
                              int cg1) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rg * 32;
-    const uint32_t limit = (uint32_t)a.levels * a.K4;
+    const char* __restrict__ Pb = reinterpret_cast<const char*>(P);
     for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
         const int c = cg * 32 + lane;
         const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
@@ -295,8 +425,10 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
             vmask &= rows_ok;
         }
         if (!__any_sync(0xffffffffu, vmask)) continue;
-        const int E = a.gent[cg];
-        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.ent + a.gstart[cg]) + lane;
+        // Scheduled stream: every entry is the byte offset of its plane
+        // word; high-level entries and pads point at zero guard words.
+        const int E = a.tgent[cg];
+        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[cg]) + lane;
         uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
         uint32_t S[B - 4];
 #pragma unroll
@@ -314,10 +446,10 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
             uint32_t w[16];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                w[4 * q + 0] = lookup(P, limit, hkeys, hmask, any_high, cur[q].x);
-                w[4 * q + 1] = lookup(P, limit, hkeys, hmask, any_high, cur[q].y);
-                w[4 * q + 2] = lookup(P, limit, hkeys, hmask, any_high, cur[q].z);
-                w[4 * q + 3] = lookup(P, limit, hkeys, hmask, any_high, cur[q].w);
+                w[4 * q + 0] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].x);
+                w[4 * q + 1] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].y);
+                w[4 * q + 2] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].z);
+                w[4 * q + 3] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].w);
             }
             uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
             csa(twosA, ones, w[0], w[1]);
@@ -365,6 +497,15 @@ __device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
         add_at(fours, 2);
         add_at(twos, 1);
         add_at(ones, 0);
+        // High-level entries (rank >= levels) only meet high-level row
+        // entries, which live in the hash; they lead each read's level list.
+        if (any_high) {
+            const int nh = col_ok ? a.nhigh[c] : 0;
+            const int maxh = (int)__reduce_max_sync(0xffffffffu, (unsigned)nh);
+            const uint32_t* __restrict__ rp = a.ent + a.gstart[cg];
+            for (int j = 0; j < maxh; ++j)
+                add_at(j < nh ? hash_find(hkeys, hmask, __ldg(rp + ent_at(j, lane))) : 0u, 0);
+        }
         // candidates: count >= a lower bound of mmin over the lane's pairs
         const int tc = col_ok ? a.tcount[c] : 0;
         const uint32_t lo = a.smin[min(t_min, tc)];
@@ -441,9 +582,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) 
             const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
             if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
         }
-        const int words = a.levels * (int)a.K4;
+        const int words = a.levels * (int)a.K4;   // + 32 zero guard words after the planes
         uint4* P4 = reinterpret_cast<uint4*>(P);
-        for (int i = threadIdx.x; i < words / 4; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < (words + 32) / 4; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
         for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0; }
         __syncthreads();
         const uint32_t limit = (uint32_t)words;
@@ -666,11 +807,18 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     j.h_gent.assign(j.ngroups, 0);
     j.h_gstart.assign(j.ngroups + 1, 0);
     for (int r = 0; r < n; ++r) j.h_gent[r >> 5] = std::max(j.h_gent[r >> 5], j.h_t[r]);
+    j.h_tgent.assign(j.ngroups, 0);
+    j.h_tstart.assign(j.ngroups + 1, 0);
     for (int g = 0; g < j.ngroups; ++g) {
-        j.h_gent[g] = (j.h_gent[g] + 15) / 16 * 16;
+        const int mt = j.h_gent[g];
+        j.h_gent[g] = (mt + 15) / 16 * 16;
         j.h_gstart[g + 1] = j.h_gstart[g] + 32LL * j.h_gent[g];
+        // the tile stream gets spare steps: wildcards for the bank schedule
+        j.h_tgent[g] = (mt + (mt >= 128 ? kSchedSpare : 0) + 15) / 16 * 16;
+        j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * j.h_tgent[g];
     }
     j.nent = j.h_gstart[j.ngroups];
+    j.ntent = j.h_tstart[j.ngroups];
     cudaStream_t s = ctx->stream;
     CRISPY_TRY(ensure(ctx, j.seq, (size_t)end + 16));
     CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
@@ -680,12 +828,20 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 4) * 4));
     CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.hinfo, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 64));
+    CRISPY_TRY(ensure(ctx, j.tstart, (size_t)(j.ngroups + 1) * 8));
+    CRISPY_TRY(ensure(ctx, j.tgent, (size_t)j.ngroups * 4));
+    if (dense_levels_for(k) > 0) CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 4) * 4));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.gstart.ptr, j.h_gstart.data(), (size_t)(j.ngroups + 1) * 8,
                                    cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.gent.ptr, j.h_gent.data(), (size_t)j.ngroups * 4,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
                                    cudaMemcpyHostToDevice, s));
     j.ready = true;   // reads are resident; the entries are built next
     return crispy_kmer_rebuild(ctx);
@@ -711,9 +867,19 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
                                               j.t.as<int32_t>(), n, k, dense_levels_for(k),
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
-                                              j.hinfo.as<uint32_t>());
+                                              j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>());
     count_launch(ctx);
     CRISPY_CK(ctx, cudaGetLastError());
+    const int levels = dense_levels_for(k);
+    if (levels > 0) {
+        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        kmer_sched_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
+            j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
+            j.t.as<int32_t>(), nhigh, j.bcnt.as<uint16_t>(), n, j.ngroups,
+            (uint32_t)levels * (1u << (2 * k)), j.tent.as<uint32_t>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+    }
     j.h_cntmax.resize(2 * (size_t)n);
     CRISPY_CK(ctx, cudaMemcpyAsync(j.h_cntmax.data(), j.cntmax.ptr, (size_t)n * 8,
                                    cudaMemcpyDeviceToHost, s));
@@ -761,7 +927,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = tile_fn_for(B);
-    const size_t tsmem = fast ? (size_t)levels * K4 * 4 : 0;
+    const size_t tsmem = fast ? ((size_t)levels * K4 + 32) * 4 : 0;   // planes + guard words
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
@@ -777,6 +943,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
 
         TileArgs ta{};
         ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
+        ta.tent = j.tent.as<uint32_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
+        ta.nhigh = j.cntmax.as<int32_t>() + n;
         ta.tcount = j.t.as<int32_t>(); ta.dense_group = j.work.as<uint8_t>();
         ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
         ta.n = n; ta.K4 = K4; ta.levels = levels; ta.A = A; ta.stage_dim = sd;
@@ -860,6 +1028,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.mmin.ptr, (uint64_t)(uintptr_t)j.smin.ptr, (uint64_t)(uintptr_t)j.t.ptr,
                     (uint64_t)(uintptr_t)j.gstart.ptr, (uint64_t)(uintptr_t)j.gent.ptr, (uint64_t)(uintptr_t)j.work.ptr,
                     (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)j.off.ptr, (uint64_t)(uintptr_t)j.hinfo.ptr,
+                    (uint64_t)(uintptr_t)j.tent.ptr, (uint64_t)(uintptr_t)j.tstart.ptr, (uint64_t)(uintptr_t)j.tgent.ptr,
+                    (uint64_t)(uintptr_t)j.cntmax.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
                     (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A});
                 ev_begin(ctx, ctx->ev_kmer, s);
