@@ -541,26 +541,39 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                     unsigned long long* __restrict__ stats) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool ok = p < count;
     unsigned long long cells = 0;
-    if (p < count) {
+    int kb = 0, ob = -1;
+    if (ok) {
         const int2 pr = pairs[p];
         const int l1 = len[pr.x], l2 = len[pr.y];
-        const int kb = band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
+        kb = band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
         int bin = 0;
         for (int b = 1; b < nbins; ++b)
             if (c_bin_slots[b] >= kb + 1) { bin = b; break; }
-        const int ob = bin == 0 ? nbins : bin;   // wide pairs sort last
+        ob = bin == 0 ? nbins : bin;   // wide pairs sort last
         if (keys) {
             keys[p] = ((uint32_t)ob << 13) | (uint32_t)(8191 - (l1 + l2));
             vals[p] = (uint32_t)p;
         }
         cells = (unsigned long long)band_cells_of(l1, l2, band);
-        atomicMax(&stats[1], (unsigned long long)kb);
-        atomicAdd(&stats[kStatBins + ob], 1ull);
-        atomicMax(&stats[kStatWindows + p / CRISPY_GEN_WINDOW], (unsigned long long)ob);
     }
-    cells = __reduce_add_sync(0xffffffffu, (unsigned)cells) + 0ull;   // per-warp partial (cells < 2^32 per warp)
-    if ((threadIdx.x & 31) == 0 && cells) atomicAdd(&stats[0], cells);
+    // one atomic per warp and counter: the counters are few and shared by
+    // every pair, so per-pair atomics would serialise
+    cells = __reduce_add_sync(0xffffffffu, (unsigned)cells) + 0ull;   // cells < 2^32 per warp
+    const unsigned kbw = __reduce_max_sync(0xffffffffu, (unsigned)kb);
+    if (lane == 0) {
+        if (cells) atomicAdd(&stats[0], cells);
+        atomicMax(&stats[1], (unsigned long long)kbw);
+    }
+    const unsigned same_bin = __match_any_sync(0xffffffffu, ob);
+    if (ok && lane == __ffs(same_bin) - 1) atomicAdd(&stats[kStatBins + ob], (unsigned long long)__popc(same_bin));
+    const int64_t win = ok ? p / CRISPY_GEN_WINDOW : -1;
+    const unsigned same_win = __match_any_sync(0xffffffffu, (unsigned long long)win);
+    const int obw = __reduce_max_sync(same_win, ob);   // max over the lanes of this window
+    if (ok && lane == __ffs(same_win) - 1)
+        atomicMax(&stats[kStatWindows + win], (unsigned long long)obw);
 }
 // untuned shape per bin (the plain form always uses it)
 constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 5, 6, 7, 11, 12, 13};
