@@ -13,22 +13,24 @@
 //     T "level entries" (t-1)*4^K + kmer, one per occurrence, where t is the
 //     occurrence rank of that K-mer in the read.  Then
 //         m(a, b) = #{ entries e of b : e in entries(a) }.
-//   * A block owns 32 row reads and keeps their entry sets in shared memory
-//     as bit planes: word P[e] has bit r set iff row read r holds entry e.
-//     One 32-bit shared load answers one column entry for 32 row reads.
-//     Levels 1..levels live in dense planes (4^K words each); the rare
-//     entries of higher level go to a small open-addressing hash table in
-//     shared memory, so the footprint stays fixed whatever the reads hold.
+//   * A block owns 64 row reads and keeps their entry sets in shared memory
+//     as bit planes: 64-bit word P[e] has bit r set iff row read r holds
+//     entry e.  One 64-bit shared load answers one column entry for 64 row
+//     reads.  Levels 1..levels live in dense planes (4^K words each, 128 KB
+//     at K = 6); the rare entries of higher level go to a small
+//     open-addressing hash table in shared memory, so the footprint stays
+//     fixed whatever the reads hold.
 //   * A warp owns 32 column reads (one per lane) and streams their entries
-//     from an interleaved layout (four consecutive entries of the 32 reads
-//     of a group form one 512-byte line, one uint4 per lane), gathers the
-//     plane word of each, and adds it into 32 bit-sliced counters with a
-//     Harley-Seal carry-save tree (LOP3 work only).  The next 16 entries are
-//     in flight while the current 16 are reduced.  The streamed entries are
-//     precomputed byte offsets into the planes, ordered per 32-read group so
-//     that the 32 lanes of a step hit 32 different banks; high-level entries
-//     and pads point at zero guard words, so the gather has no branch and
-//     the rare high-level entries get a separate hash pass.
+//     from an interleaved layout (eight consecutive entries of one read in a
+//     uint4, the 32 reads' uint4 of one octet in one 512-byte line), gathers
+//     the plane word of each, and adds its two halves into two sets of 32
+//     bit-sliced counters with Harley-Seal carry-save trees (LOP3 work
+//     only).  The next 16 entries are in flight while the current 16 are
+//     reduced.  The streamed entries are precomputed 16-bit plane word
+//     indices, ordered per 32-read group so that the 16 lanes of a half-warp
+//     hit 16 different double banks; high-level entries and pads index zero
+//     guard words, so the gather has no branch and the rare high-level
+//     entries get a separate hash pass.
 //   * The threshold is an integer test m >= mmin[min(Ta, Tb)], with mmin
 //     tabulated on the host from the reference's float expression (the pass
 //     predicate is monotone in m), first as a bit-sliced compare against a
@@ -52,9 +54,11 @@ namespace {
 constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 constexpr int kTileThreads = 512;
 constexpr int kTileWarps = kTileThreads / 32;
-constexpr int kHashSlots = 1024;        // high-level entries of one row group
-constexpr int kHashMaxKeys = 512;       // load factor <= 1/2 keeps probes short
-constexpr int kPlaneBudget = 96 * 1024; // dense level planes per block
+constexpr int kTileRows = 64;            // row reads per block: one 64-bit plane word
+constexpr int kHashBits = 11;
+constexpr int kHashSlots = 1 << kHashBits;   // high-level entries of one row group
+constexpr int kHashMaxKeys = kHashSlots / 2; // load factor <= 1/2 keeps probes short
+constexpr int kPlaneBudget = 128 * 1024;     // dense level planes per block
 
 __device__ __forceinline__ uint32_t sym2(uint8_t c) {
     // A=0 G=1 T=2 C=3, everything else 0 (kmerMain.cpp:137-152)
@@ -182,23 +186,27 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// Bank schedule of the tile stream: one warp per 32-read group writes, for
-// every step e < Et and lane l, the shared-memory byte offset that lane l
-// gathers at step e.  Lanes of a warp gather at the same time, so the 32
-// offsets of a step should sit in 32 different banks.
-//   * Ideal slots: lane l takes a bank-h entry at every step with
-//     (e + l) mod 32 == h while it has bank-h entries left; the ideal
-//     banks of one step are a rotation, hence all different.
+// Bank schedule of the tile stream.  The tile kernel's plane words are
+// 64-bit (64 row reads), so a warp's gather is served as two half-warps of
+// 16 lanes, and word w sits in double bank w mod 16.  One warp per 32-read
+// group writes, for every step e < Et and lane l, the 16-bit plane word
+// index that lane l gathers at step e, such that the 16 lanes of each half
+// hit 16 different double banks where the counts allow.
+//   * Ideal slots: lane l takes a bucket-h entry (h = word mod 16) at every
+//     step with (e + l) mod 16 == h while it has bucket-h entries left; the
+//     ideal buckets of a half at one step are a rotation, hence different.
 //   * A lane whose ideal bucket is empty at step e (a hole) takes one of its
-//     surplus entries (buckets with more entries than ideal slots) whose bank
-//     no other lane uses at e; claims are settled by match_any, lowest lane
-//     first, repeated until no lane can claim.
-//   * Remaining holes take a wildcard: a guard word (always zero) in a bank
-//     still free at e.  High-level entries (looked up in the hash by a
+//     surplus entries (buckets with more entries than ideal slots) whose
+//     bucket no other lane of its half uses at e; claims are settled by
+//     match_any, lowest lane first, repeated until no lane can claim.
+//   * Remaining holes take a wildcard: a guard word (always zero) in a
+//     bucket still free at e.  High-level entries (looked up in the hash by a
 //     separate pass) and the pad steps up to Et are the wildcards.  A lane
 //     out of wildcards places a surplus entry anyway (a bank conflict).
 // Every hole is filled by exactly one surplus entry or wildcard, because
 // holes - surplus = Et - dense entries = wildcards for every lane.
+// The raw list of a read is grouped by 32-bank (value mod 32), so bucket h
+// draws first on bank h, then on bank h + 16.
 // ---------------------------------------------------------------------------
 constexpr int kSchedWarps = 4;
 constexpr int kSchedChunk = 16;
@@ -212,71 +220,74 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int k) {   // 0-based; -1
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
     const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
-    const int32_t* __restrict__ tcount, const int32_t* __restrict__ nhigh,
-    const uint16_t* __restrict__ bcnt, int n, int ngroups, uint32_t guard_word,
-    uint32_t* __restrict__ tent) {
-    __shared__ uint16_t s_cnt[kSchedWarps][32][33];
-    __shared__ uint16_t s_ov[kSchedWarps][32][33];
-    __shared__ uint16_t s_next[kSchedWarps][32][33];   // next raw position per bank
+    const int32_t* __restrict__ nhigh, const uint16_t* __restrict__ bcnt, int n, int ngroups,
+    uint32_t guard_word, uint16_t* __restrict__ tent) {
+    __shared__ uint16_t s_cnt[kSchedWarps][32][17];    // entries per bucket
+    __shared__ uint16_t s_ov[kSchedWarps][32][17];     // surplus per bucket
+    __shared__ uint16_t s_next[kSchedWarps][32][33];   // next raw position per 32-bank
+    __shared__ uint16_t s_left[kSchedWarps][32][33];   // raw entries left per 32-bank
     __shared__ uint8_t s_bank[kSchedWarps][kSchedChunk][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned full = 0xffffffffu;
-    const unsigned lt = (1u << lane) - 1u;
+    const int hs = lane & 16;                       // this half's bit offset in 32-bit masks
+    const unsigned half_lt = ((1u << lane) - 1u) & (0xFFFFu << hs);
     for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
         const int r = g * 32 + lane;
         const int Et = tgent[g];
         const int nh = r < n ? nhigh[r] : 0;
+        for (int b = 0; b < 32; ++b)
+            s_left[w][lane][b] = r < n ? bcnt[(int64_t)r * 32 + b] : (uint16_t)0;
+        // first raw position of each 32-bank: the prep kernel's lane-rotated order
+        for (int i = 0, pos = nh; i < 32; ++i) {
+            const int b = (i + lane) & 31;
+            s_next[w][lane][b] = (uint16_t)pos;
+            pos += s_left[w][lane][b];
+        }
         int D = 0;
         unsigned ovmask = 0;
-        for (int b = 0; b < 32; ++b) {
-            const int c = r < n ? (int)bcnt[(int64_t)r * 32 + b] : 0;
-            const int o = (b - lane) & 31;
-            const int slots = Et > o ? (Et - o + 31) >> 5 : 0;
+        for (int b = 0; b < 16; ++b) {
+            const int c = s_left[w][lane][b] + s_left[w][lane][b + 16];
+            const int o = (b - lane) & 15;
+            const int slots = Et > o ? (Et - o + 15) >> 4 : 0;
             const int ov = max(0, c - slots);
             s_cnt[w][lane][b] = (uint16_t)c;
             s_ov[w][lane][b] = (uint16_t)ov;
             D += c;
             if (ov) ovmask |= 1u << b;
         }
-        // first raw position of each bank: the prep kernel's lane-rotated order
-        for (int i = 0, pos = nh; i < 32; ++i) {
-            const int b = (i + lane) & 31;
-            s_next[w][lane][b] = (uint16_t)pos;
-            pos += s_cnt[w][lane][b];
-        }
         int wild = Et - D;
         __syncwarp();
         const uint32_t* src = ent + gstart[g];
-        uint32_t* dst = tent + tstart[g];
+        uint4* dst = reinterpret_cast<uint4*>(tent + tstart[g]) + lane;
         for (int e0 = 0; e0 < Et; e0 += kSchedChunk) {
             for (int i = 0; i < kSchedChunk; ++i) {
                 const int e = e0 + i;
-                const int h = (e + lane) & 31;
-                const bool hole = (e >> 5) >= (int)s_cnt[w][lane][h];
+                const int h = (e + lane) & 15;
+                const bool hole = (e >> 4) >= (int)s_cnt[w][lane][h];
                 int bank = hole ? -1 : h;
-                unsigned used = __reduce_or_sync(full, hole ? 0u : (1u << h));
+                unsigned used = __reduce_or_sync(full, hole ? 0u : (1u << (h + hs)));
                 bool open = hole;
-                for (int round = 0; round < 32; ++round) {
-                    const unsigned cand = open ? (ovmask & ~used) : 0u;
+                for (int round = 0; round < 16; ++round) {
+                    const unsigned cand = open ? (ovmask & ~(used >> hs) & 0xFFFFu) : 0u;
                     if (!__any_sync(full, cand != 0u)) break;
-                    const int prop = cand ? __ffs(cand) - 1 : 32 + lane;
+                    const int prop = cand ? hs + __ffs(cand) - 1 : 32 + lane;
                     const unsigned peers = __match_any_sync(full, prop);
                     const bool win = cand && lane == __ffs(peers) - 1;
                     if (win) {
-                        bank = prop;
+                        bank = prop - hs;
                         open = false;
-                        const int left = (int)s_ov[w][lane][prop] - 1;
-                        s_ov[w][lane][prop] = (uint16_t)left;
-                        if (left == 0) ovmask &= ~(1u << prop);
+                        const int left = (int)s_ov[w][lane][bank] - 1;
+                        s_ov[w][lane][bank] = (uint16_t)left;
+                        if (left == 0) ovmask &= ~(1u << bank);
                     }
                     used |= __reduce_or_sync(full, win ? (1u << prop) : 0u);
                 }
                 const bool wl = open && wild > 0;
                 const unsigned wm = __ballot_sync(full, wl);
                 if (wl) {
-                    // the k-th wildcard lane takes the k-th free bank
-                    const int fb = nth_set_bit(~used, __popc(wm & lt));
-                    bank = 32 + (fb >= 0 ? fb : 0);
+                    // the k-th wildcard lane of a half takes the k-th free bucket
+                    const int fb = nth_set_bit(~(used >> hs) & 0xFFFFu, __popc(wm & half_lt));
+                    bank = 16 + (fb >= 0 ? fb : 0);
                     --wild;
                 } else if (open) {
                     const int b = ovmask ? __ffs(ovmask) - 1 : -1;
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
                         s_ov[w][lane][b] = (uint16_t)left;
                         if (left == 0) ovmask &= ~(1u << b);
                     } else {
-                        bank = 32;   // unreachable by the count identity; stays in bounds
+                        bank = 16;   // unreachable by the count identity; stays in bounds
                     }
                 }
                 s_bank[w][i][lane] = (uint8_t)bank;
@@ -297,29 +308,37 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
             uint32_t v[kSchedChunk];
 #pragma unroll
             for (int i = 0; i < kSchedChunk; ++i) {
-                v[i] = 0xFFFFFFFFu;
+                v[i] = 0x80000000u;   // guard word of bucket 0
                 if (i < steps) {
                     const int b = s_bank[w][i][lane];
-                    if (b < 32) {
-                        const int p = s_next[w][lane][b];
-                        s_next[w][lane][b] = (uint16_t)(p + 1);
+                    if (b < 16) {
+                        const int bb = s_left[w][lane][b] ? b : b + 16;
+                        const int p = s_next[w][lane][bb];
+                        s_next[w][lane][bb] = (uint16_t)(p + 1);
+                        s_left[w][lane][bb] = (uint16_t)(s_left[w][lane][bb] - 1);
                         v[i] = (uint32_t)p;
                     } else {
-                        v[i] = 0x80000000u | (uint32_t)(b - 32);
+                        v[i] = 0x80000000u | (uint32_t)(b - 16);
                     }
                 }
             }
 #pragma unroll
             for (int i = 0; i < kSchedChunk; ++i) {
-                if (i < steps) {
-                    const uint32_t x = v[i];
-                    v[i] = (x & 0x80000000u) ? (guard_word + (x & 31u)) * 4u
-                                             : __ldg(src + ent_at((int)x, lane)) * 4u;
+                const uint32_t x = v[i];
+                v[i] = (x & 0x80000000u) ? guard_word + (x & 15u) : __ldg(src + ent_at((int)x, lane));
+            }
+            // two octets of this lane: two uint4 of packed 16-bit word indices
+#pragma unroll
+            for (int o = 0; o < 2; ++o) {
+                if (o * 8 < steps) {
+                    uint4 q;
+                    q.x = (v[8 * o + 0] & 0xFFFFu) | (v[8 * o + 1] << 16);
+                    q.y = (v[8 * o + 2] & 0xFFFFu) | (v[8 * o + 3] << 16);
+                    q.z = (v[8 * o + 4] & 0xFFFFu) | (v[8 * o + 5] << 16);
+                    q.w = (v[8 * o + 6] & 0xFFFFu) | (v[8 * o + 7] << 16);
+                    dst[(int64_t)((e0 >> 3) + o) * 32] = q;
                 }
             }
-#pragma unroll
-            for (int i = 0; i < kSchedChunk; ++i)
-                if (i < steps) dst[ent_at(e0 + i, lane)] = v[i];
             __syncwarp();
         }
     }
@@ -329,12 +348,12 @@ struct TileArgs {
     const uint32_t* ent;           // level entries, high-level ones first per read
     const int64_t* gstart;
     const int32_t* gent;
-    const uint32_t* tent;          // scheduled byte offsets into the planes
-    const int64_t* tstart;
+    const uint16_t* tent;          // scheduled 16-bit plane word indices
+    const int64_t* tstart;         // per 32-read group, in 16-bit units
     const int32_t* tgent;
     const int32_t* nhigh;
     const int32_t* tcount;
-    const uint8_t* dense_group;   // row groups the dense kernel takes instead
+    const uint8_t* dense_group;   // 32-read groups the dense kernel takes as rows
     const uint16_t* mmin;
     const uint16_t* smin;
     int n;
@@ -347,7 +366,7 @@ struct TileArgs {
     int64_t cap;
     // plain: one rectangle of rows x cols (one reference stage)
     int r_lo, r_hi, c_lo, c_hi;
-    // batched: work queue over row groups (all their columns)
+    // batched: work queue over 64-row groups (all their columns)
     const int* items;
     int nitems;
     unsigned int* queue_head;
@@ -391,176 +410,209 @@ __device__ __forceinline__ void emit(unsigned long long* counter, uint64_t* keys
 }
 
 __device__ __forceinline__ uint32_t hash_slot(uint32_t key) {
-    return (key * 0x9E3779B1u) >> (32 - 10);   // kHashSlots = 1024
+    return (key * 0x9E3779B1u) >> (32 - kHashBits);
 }
 
 // Row bits of a high-level entry (absent -> 0).  Rare path.
-__device__ __noinline__ uint32_t hash_find(const uint32_t* hkeys, const uint32_t* hmask,
-                                           uint32_t key) {
+__device__ __noinline__ uint2 hash_find(const uint32_t* hkeys, const uint2* hmask, uint32_t key) {
     uint32_t h = hash_slot(key);
     for (int probe = 0; probe < kHashSlots; ++probe) {
         const uint32_t k = hkeys[h];
         if (k == key) return hmask[h];
-        if (k == kSentinel) return 0u;
+        if (k == kSentinel) return make_uint2(0u, 0u);
         h = (h + 1) & (kHashSlots - 1);
     }
-    return 0u;
+    return make_uint2(0u, 0u);
 }
 
+// Bit-sliced counters of 32 row reads: Harley-Seal levels 1, 2, 4, 8 and
+// the binary count of sixteens above them.
 template <int B>
-__device__ void tile_columns(const TileArgs& a, const uint32_t* __restrict__ P,
-                             const uint32_t* hkeys, const uint32_t* hmask, bool any_high,
-                             int rg, uint32_t rows_ok, int t_min, const int* s_rowT, int cg0,
-                             int cg1) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int r0 = rg * 32;
-    const char* __restrict__ Pb = reinterpret_cast<const char*>(P);
-    for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
-        const int c = cg * 32 + lane;
-        const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
-        uint32_t vmask = 0;
-        if (col_ok) {
-            const int span = c - r0;  // rows r0+b < c  <=>  b < span
-            vmask = span >= 32 ? 0xffffffffu : (span <= 0 ? 0u : ((1u << span) - 1u));
-            vmask &= rows_ok;
-        }
-        if (!__any_sync(0xffffffffu, vmask)) continue;
-        // Scheduled stream: every entry is the byte offset of its plane
-        // word; high-level entries and pads point at zero guard words.
-        const int E = a.tgent[cg];
-        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[cg]) + lane;
-        uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
-        uint32_t S[B - 4];
+struct Counter {
+    uint32_t ones, twos, fours, eights;
+    uint32_t S[B - 4];
+    __device__ __forceinline__ void clear() {
+        ones = twos = fours = eights = 0;
 #pragma unroll
         for (int k = 0; k < B - 4; ++k) S[k] = 0;
-        uint4 cur[4], nxt[4];
-        if (E > 0) {
+    }
+    // add 16 words
+    __device__ __forceinline__ void add16(const uint32_t* w) {
+        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+        csa(twosA, ones, w[0], w[1]);
+        csa(twosB, ones, w[2], w[3]);
+        csa(foursA, twos, twosA, twosB);
+        csa(twosA, ones, w[4], w[5]);
+        csa(twosB, ones, w[6], w[7]);
+        csa(foursB, twos, twosA, twosB);
+        csa(eightsA, fours, foursA, foursB);
+        csa(twosA, ones, w[8], w[9]);
+        csa(twosB, ones, w[10], w[11]);
+        csa(foursA, twos, twosA, twosB);
+        csa(twosA, ones, w[12], w[13]);
+        csa(twosB, ones, w[14], w[15]);
+        csa(foursB, twos, twosA, twosB);
+        csa(eightsB, fours, foursA, foursB);
+        csa(sixteens, eights, eightsA, eightsB);
+        uint32_t carry = sixteens;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) cur[q] = __ldg(ep + q * 32);
+        for (int k = 0; k < B - 4; ++k) {
+            const uint32_t t = S[k] & carry;
+            S[k] ^= carry;
+            carry = t;
         }
-        for (int e = 0; e < E; e += 16) {
-            if (e + 16 < E) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) nxt[q] = __ldg(ep + ((e + 16) / 4 + q) * 32);
-            }
-            uint32_t w[16];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                w[4 * q + 0] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].x);
-                w[4 * q + 1] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].y);
-                w[4 * q + 2] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].z);
-                w[4 * q + 3] = *reinterpret_cast<const uint32_t*>(Pb + cur[q].w);
-            }
-            uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
-            csa(twosA, ones, w[0], w[1]);
-            csa(twosB, ones, w[2], w[3]);
-            csa(foursA, twos, twosA, twosB);
-            csa(twosA, ones, w[4], w[5]);
-            csa(twosB, ones, w[6], w[7]);
-            csa(foursB, twos, twosA, twosB);
-            csa(eightsA, fours, foursA, foursB);
-            csa(twosA, ones, w[8], w[9]);
-            csa(twosB, ones, w[10], w[11]);
-            csa(foursA, twos, twosA, twosB);
-            csa(twosA, ones, w[12], w[13]);
-            csa(twosB, ones, w[14], w[15]);
-            csa(foursB, twos, twosA, twosB);
-            csa(eightsB, fours, foursA, foursB);
-            csa(sixteens, eights, eightsA, eightsB);
-            uint32_t carry = sixteens;
-#pragma unroll
-            for (int k = 0; k < B - 4; ++k) {
-                const uint32_t t = S[k] & carry;
-                S[k] ^= carry;
-                carry = t;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) cur[q] = nxt[q];
-        }
-        // bit planes X[k] of the 32 per-row counts
-        uint32_t X[B];
+    }
+    // bit planes X[k] of the 32 per-row counts
+    __device__ __forceinline__ void planes(uint32_t* X) const {
         X[0] = X[1] = X[2] = X[3] = 0;
 #pragma unroll
         for (int k = 4; k < B; ++k) X[k] = S[k - 4];
-        auto add_at = [&](uint32_t v, int p) {
-            uint32_t carry = v;
+        add_at(X, eights, 3);
+        add_at(X, fours, 2);
+        add_at(X, twos, 1);
+        add_at(X, ones, 0);
+    }
+    __device__ __forceinline__ static void add_at(uint32_t* X, uint32_t v, int p) {
+        uint32_t carry = v;
 #pragma unroll
-            for (int k = 0; k < B; ++k) {
-                if (k >= p) {
-                    const uint32_t t = X[k] & carry;
-                    X[k] ^= carry;
-                    carry = t;
-                }
+        for (int k = 0; k < B; ++k) {
+            if (k >= p) {
+                const uint32_t t = X[k] & carry;
+                X[k] ^= carry;
+                carry = t;
             }
-        };
-        add_at(eights, 3);
-        add_at(fours, 2);
-        add_at(twos, 1);
-        add_at(ones, 0);
+        }
+    }
+};
+
+// Threshold and emission for one 32-row half: candidates by a bit-sliced
+// compare against a lower bound of mmin over the lane's pairs, then the
+// exact test per candidate.
+template <int B>
+__device__ __forceinline__ void finish_half(const TileArgs& a, const uint32_t* X, uint32_t vmask,
+                                            int rbase, int t_min, const int* rowT, int c, int tc) {
+    const uint32_t lo = a.smin[min(t_min, tc)];
+    uint32_t cand = 0;
+    if (vmask && lo < (1u << B)) {
+        uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+        for (int k = B - 1; k >= 0; --k) {
+            const uint32_t bit = 0u - ((lo >> k) & 1u);
+            gt |= eq & X[k] & ~bit;
+            eq &= ~(X[k] ^ bit);
+        }
+        cand = (gt | eq) & vmask;
+    }
+    while (__any_sync(0xffffffffu, cand)) {
+        bool pass = false;
+        int r = 0, m = 0, mn = 1;
+        if (cand) {
+            const int b = __ffs(cand) - 1;
+            cand &= cand - 1;
+#pragma unroll
+            for (int k = 0; k < B; ++k) m |= (int)((X[k] >> b) & 1u) << k;
+            r = rbase + b;
+            mn = min(rowT[b], tc);
+            pass = m >= (int)a.mmin[mn];
+        }
+        emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
+    }
+}
+
+__device__ __forceinline__ uint32_t half_mask(int span) {   // rows b < span
+    return span >= 32 ? 0xffffffffu : (span <= 0 ? 0u : ((1u << span) - 1u));
+}
+
+template <int B>
+__device__ void tile_columns(const TileArgs& a, const uint2* __restrict__ P,
+                             const uint32_t* hkeys, const uint2* hmask, bool any_high, int rg,
+                             uint32_t ok0, uint32_t ok1, int tmin0, int tmin1, const int* s_rowT,
+                             int cg0, int cg1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = rg * kTileRows;
+    for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
+        const int c = cg * 32 + lane;
+        const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
+        uint32_t vm0 = 0, vm1 = 0;
+        if (col_ok) {
+            vm0 = half_mask(c - r0) & ok0;
+            vm1 = half_mask(c - r0 - 32) & ok1;
+        }
+        if (!__any_sync(0xffffffffu, vm0 | vm1)) continue;
+        // Scheduled stream: 16-bit plane word indices, eight per uint4;
+        // high-level entries and pads index zero guard words.
+        const int E = a.tgent[cg];
+        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[cg]) + lane;
+        Counter<B> lo, hi;
+        lo.clear();
+        hi.clear();
+        uint4 cur0, cur1, nxt0, nxt1;
+        if (E > 0) { cur0 = __ldg(ep); cur1 = __ldg(ep + 32); }
+        for (int e = 0; e < E; e += 16) {
+            if (e + 16 < E) {
+                nxt0 = __ldg(ep + ((e + 16) >> 3) * 32);
+                nxt1 = __ldg(ep + ((e + 16) >> 3) * 32 + 32);
+            }
+            const uint32_t x[8] = {cur0.x, cur0.y, cur0.z, cur0.w, cur1.x, cur1.y, cur1.z, cur1.w};
+            uint32_t wl[16], wh[16];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint2 p0 = P[x[k] & 0xFFFFu];
+                const uint2 p1 = P[x[k] >> 16];
+                wl[2 * k] = p0.x; wh[2 * k] = p0.y;
+                wl[2 * k + 1] = p1.x; wh[2 * k + 1] = p1.y;
+            }
+            lo.add16(wl);
+            hi.add16(wh);
+            cur0 = nxt0;
+            cur1 = nxt1;
+        }
+        uint32_t X0[B], X1[B];
+        lo.planes(X0);
+        hi.planes(X1);
         // High-level entries (rank >= levels) only meet high-level row
         // entries, which live in the hash; they lead each read's level list.
         if (any_high) {
             const int nh = col_ok ? a.nhigh[c] : 0;
             const int maxh = (int)__reduce_max_sync(0xffffffffu, (unsigned)nh);
             const uint32_t* __restrict__ rp = a.ent + a.gstart[cg];
-            for (int j = 0; j < maxh; ++j)
-                add_at(j < nh ? hash_find(hkeys, hmask, __ldg(rp + ent_at(j, lane))) : 0u, 0);
+            for (int j = 0; j < maxh; ++j) {
+                const uint2 w = j < nh ? hash_find(hkeys, hmask, __ldg(rp + ent_at(j, lane)))
+                                       : make_uint2(0u, 0u);
+                Counter<B>::add_at(X0, w.x, 0);
+                Counter<B>::add_at(X1, w.y, 0);
+            }
         }
-        // candidates: count >= a lower bound of mmin over the lane's pairs
         const int tc = col_ok ? a.tcount[c] : 0;
-        const uint32_t lo = a.smin[min(t_min, tc)];
-        uint32_t cand = 0;
-        if (vmask && lo < (1u << B)) {
-            uint32_t gt = 0, eq = 0xffffffffu;
-#pragma unroll
-            for (int k = B - 1; k >= 0; --k) {
-                const uint32_t bit = 0u - ((lo >> k) & 1u);
-                gt |= eq & X[k] & ~bit;
-                eq &= ~(X[k] ^ bit);
-            }
-            cand = (gt | eq) & vmask;
-        }
-        while (__any_sync(0xffffffffu, cand)) {
-            bool pass = false;
-            int r = 0, m = 0, mn = 1;
-            if (cand) {
-                const int b = __ffs(cand) - 1;
-                cand &= cand - 1;
-#pragma unroll
-                for (int k = 0; k < B; ++k) m |= (int)((X[k] >> b) & 1u) << k;
-                r = r0 + b;
-                mn = min(s_rowT[b], tc);
-                pass = m >= (int)a.mmin[mn];
-            }
-            emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
-        }
+        finish_half<B>(a, X0, vm0, r0, tmin0, s_rowT, c, tc);
+        finish_half<B>(a, X1, vm1, r0 + 32, tmin1, s_rowT + 32, c, tc);
     }
 }
 
 template <int B>
-__global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) {
-    extern __shared__ __align__(16) uint32_t P[];
+__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile_kernel(TileArgs a) {
+    extern __shared__ __align__(16) uint2 P[];   // levels * K4 plane words + 32 guard words
     __shared__ uint32_t hkeys[kHashSlots];
-    __shared__ uint32_t hmask[kHashSlots];
-    __shared__ int s_rowT[32];
+    __shared__ uint2 hmask[kHashSlots];
+    __shared__ int s_rowT[kTileRows];
     __shared__ int s_item[4];
-    __shared__ int s_tmin, s_any_high;
-    __shared__ uint32_t s_rows_ok;
+    __shared__ int s_tmin[2], s_any_high;
+    __shared__ uint32_t s_rows_ok[2];
     const bool queued = a.items != nullptr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int it = 0;; ++it) {
-        // ---- fetch work: one row group with all its column groups ----
+        // ---- fetch work: one 64-row group with all its column groups ----
         if (threadIdx.x == 0) {
             if (queued) {
                 const unsigned w = atomicAdd(a.queue_head, 1u);
                 s_item[3] = (int)w < a.nitems;
                 if (s_item[3]) {
                     s_item[0] = a.items[w];
-                    s_item[1] = s_item[0];
+                    s_item[1] = 0;
                     s_item[2] = (a.n + 31) / 32;
                 }
             } else {
-                s_item[0] = a.r_lo / 32 + blockIdx.x;
+                s_item[0] = a.r_lo / kTileRows + blockIdx.x;
                 s_item[1] = a.c_lo / 32;
                 s_item[2] = (a.c_hi + 31) / 32;
                 s_item[3] = it == 0;
@@ -570,33 +622,41 @@ __global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) 
         if (!s_item[3]) break;
         const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
         __syncthreads();   // every thread has read s_item
-        if (a.dense_group[rg]) continue;   // taken by kmer_dense_kernel (uniform)
         const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
-        // ---- row group set-up ----
-        if (warp == 0) {
-            const int r = rg * 32 + lane;
-            const bool ok = r >= rlo && r < rhi;
+        // ---- row group set-up: rows of dense 32-read groups are left to
+        // kmer_dense_kernel ----
+        if (warp < 2) {
+            const int r = rg * kTileRows + warp * 32 + lane;
+            const bool ok = r >= rlo && r < rhi && !a.dense_group[r >> 5];
             const int tr = ok ? a.tcount[r] : INT_MAX;
-            s_rowT[lane] = tr;
+            s_rowT[warp * 32 + lane] = tr;
             const unsigned okm = __ballot_sync(0xffffffffu, ok);
             const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
-            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
+            if (lane == 0) { s_tmin[warp] = tm; s_rows_ok[warp] = okm; }
+            if (warp == 0 && lane == 0) s_any_high = 0;
         }
         const int words = a.levels * (int)a.K4;   // + 32 zero guard words after the planes
         uint4* P4 = reinterpret_cast<uint4*>(P);
-        for (int i = threadIdx.x; i < (words + 32) / 4; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
-        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0; }
+        for (int i = threadIdx.x; i < (words + 32) / 2; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) {
+            hkeys[i] = kSentinel;
+            hmask[i] = make_uint2(0u, 0u);
+        }
         __syncthreads();
+        uint32_t* Pw = reinterpret_cast<uint32_t*>(P);
+        uint32_t* hmw = reinterpret_cast<uint32_t*>(hmask);
         const uint32_t limit = (uint32_t)words;
-        for (int b = warp; b < 32; b += kTileWarps) {
-            if (!((s_rows_ok >> b) & 1u)) continue;
-            const uint32_t* src = a.ent + a.gstart[rg];
+        for (int b = warp; b < kTileRows; b += kTileWarps) {
+            if (!((s_rows_ok[b >> 5] >> (b & 31)) & 1u)) continue;
+            const int r = rg * kTileRows + b;
+            const uint32_t* src = a.ent + a.gstart[r >> 5];
             const int T = s_rowT[b];
-            const uint32_t bit = 1u << b;
+            const uint32_t bit = 1u << (b & 31);
+            const int halfw = b >> 5;
             for (int e = lane; e < T; e += 32) {
-                const uint32_t idx = src[ent_at(e, b)];
+                const uint32_t idx = src[ent_at(e, r & 31)];
                 if (idx < limit) {
-                    atomicOr(&P[idx], bit);
+                    atomicOr(&Pw[2 * idx + halfw], bit);
                 } else {
                     // high-level entry: open addressing; the host guarantees
                     // the group holds at most kHashMaxKeys of them
@@ -604,7 +664,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) 
                     for (int probe = 0; probe < kHashSlots; ++probe) {
                         const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
                         if (old == kSentinel || old == idx) {
-                            atomicOr(&hmask[h], bit);
+                            atomicOr(&hmw[2 * h + halfw], bit);
                             break;
                         }
                         h = (h + 1) & (kHashSlots - 1);
@@ -614,8 +674,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kmer_tile_kernel(TileArgs a) 
             }
         }
         __syncthreads();
-        tile_columns<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
-                        max(cg0, rg), cg1);
+        tile_columns<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok[0], s_rows_ok[1],
+                        s_tmin[0], s_tmin[1], s_rowT, max(cg0, 2 * rg), cg1);
         __syncthreads();
     }
 }
@@ -755,7 +815,7 @@ int bits_for(uint64_t v) {
 // Dense level planes kept in shared memory for K (0: dense kernel only).
 int dense_levels_for(int K) {
     if (K >= 8) return 0;
-    const int per_level = (1 << (2 * K)) * 4;
+    const int per_level = (1 << (2 * K)) * 8;   // 64-bit words (64 row reads)
     return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
 
@@ -831,7 +891,7 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 64));
     CRISPY_TRY(ensure(ctx, j.tstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.tgent, (size_t)j.ngroups * 4));
-    if (dense_levels_for(k) > 0) CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 4) * 4));
+    if (dense_levels_for(k) > 0) CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
@@ -875,8 +935,8 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
         const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
         kmer_sched_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
-            j.t.as<int32_t>(), nhigh, j.bcnt.as<uint16_t>(), n, j.ngroups,
-            (uint32_t)levels * (1u << (2 * k)), j.tent.as<uint32_t>());
+            nhigh, j.bcnt.as<uint16_t>(), n, j.ngroups, (uint32_t)levels * (1u << (2 * k)),
+            j.tent.as<uint16_t>());
         count_launch(ctx);
         CRISPY_CK(ctx, cudaGetLastError());
     }
@@ -910,15 +970,19 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     CRISPY_CK(ctx, cudaMemcpyAsync(j.mmin.ptr, mmin.data(), mmin.size() * 2, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.smin.ptr, smin.data(), smin.size() * 2, cudaMemcpyHostToDevice, s));
 
-    // Row groups whose high-level entries exceed the hash go to the dense
-    // kernel; K = 8 sends every group there.
+    // Rows of 64-row groups whose high-level entries exceed the hash go to
+    // the dense kernel (flags per 32-read group); K = 8 sends every group there.
     const int levels = dense_levels_for(K);
+    const int nrg = (n + kTileRows - 1) / kTileRows;
     std::vector<uint8_t> dense(j.ngroups, 0);
     bool any_dense = false;
-    for (int g = 0; g < j.ngroups; ++g) {
+    for (int rg = 0; rg < nrg; ++rg) {
         int64_t high = 0;
-        for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) high += j.h_cntmax[n + r];
-        if (levels == 0 || high > kHashMaxKeys) { dense[g] = 1; any_dense = true; }
+        for (int r = rg * kTileRows; r < std::min(n, rg * kTileRows + kTileRows); ++r) high += j.h_cntmax[n + r];
+        if (levels == 0 || high > kHashMaxKeys) {
+            for (int g = 2 * rg; g < std::min(j.ngroups, 2 * rg + 2); ++g) dense[g] = 1;
+            any_dense = true;
+        }
     }
     const bool fast = levels > 0;
     CRISPY_TRY(ensure(ctx, j.work, (size_t)j.ngroups + 16));
@@ -927,7 +991,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = tile_fn_for(B);
-    const size_t tsmem = fast ? ((size_t)levels * K4 + 32) * 4 : 0;   // planes + guard words
+    const size_t tsmem = fast ? ((size_t)levels * K4 + 32) * 8 : 0;   // planes + guard words
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
@@ -943,7 +1007,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
 
         TileArgs ta{};
         ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
-        ta.tent = j.tent.as<uint32_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
+        ta.tent = j.tent.as<uint16_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
         ta.nhigh = j.cntmax.as<int32_t>() + n;
         ta.tcount = j.t.as<int32_t>(); ta.dense_group = j.work.as<uint8_t>();
         ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
@@ -977,7 +1041,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     t2.r_lo = sx * A; t2.r_hi = std::min(n, sx * A + A);
                     t2.c_lo = sy * A; t2.c_hi = std::min(n, sy * A + A);
                     if (tiles) {
-                        const int rg0 = t2.r_lo / 32, rg1 = (t2.r_hi - 1) / 32;
+                        const int rg0 = t2.r_lo / kTileRows, rg1 = (t2.r_hi - 1) / kTileRows;
                         tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
@@ -1005,8 +1069,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             // (each with all its columns), longest first.
             std::vector<int> items;
             if (fast)
-                for (int rg = 0; rg < j.ngroups; ++rg)
-                    if (!dense[rg]) items.push_back(rg);
+                for (int rg = 0; rg < nrg; ++rg)
+                    if (!dense[2 * rg] || (2 * rg + 1 < j.ngroups && !dense[2 * rg + 1])) items.push_back(rg);
             if (!items.empty()) {
                 CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int) + 64));
                 int* d_items = j.sort_tmp.as<int>();
