@@ -63,6 +63,10 @@ struct GenArgs {
     int32_t* ml;
     int32_t* al;
     unsigned int* queue;     // optional work counter (persistent launch)
+    // All 1.  Adds written as multiply-adds by these run on the FMA pipe;
+    // distinct multipliers keep the compiler from factoring a common
+    // product back into ALU adds.
+    int one[6];
 };
 
 __device__ __forceinline__ int kband_of(int l1, int l2, int band) {
@@ -121,12 +125,16 @@ __device__ __forceinline__ Best group_best(Best b, int lane) {
 // starts from (whose packed value i0 + j0 is the reference's AL there, ML
 // 0).  A diagonal move adds 0x10001 + match, a gap move adds nothing, and at
 // the end ML = (i + j) - B, AL = (i + j) - A.
+// A step at parity P reads the cells of steps s-2 (M[P], L[P]: the
+// diagonal) and s-1 (M[P^1], L[P^1], U, F) and writes its cells over
+// M[P], L[P], U and F.  So the buffers alternate by parity and nothing
+// rotates; U and F update in place, slots ordered so that a neighbour is
+// read before it is overwritten.
 template <int C>
 struct Lane {
-    int cM[C], cU[C], cF[C];   // V and the two gap-penalised copies (+2)
-    uint32_t cL[C];
-    int pM[C];
-    uint32_t pL[C];
+    int M[2][C];               // V by step parity
+    uint32_t L[2][C];          // packed path counters by step parity
+    int U[C], F[C];            // gap-penalised copies (+2) of the last step
     uint32_t x0[C], x1[C];     // per-slot symbol XOR fields of the block, by parity
     int cap0[C], cap1[C];      // kNeg for a parity whose diagonal is out of band
 };
@@ -134,6 +142,7 @@ struct Lane {
 // Per-pair values a sub-group holds (the same in all its lanes).
 struct PairCtx {
     int kb, l1, l2, shift;   // shift = kb & 1: odd bands run one step late
+    const int* one;          // GenArgs::one
 };
 
 // Block kinds.  kClean: no cell of the block touches the matrix border.
@@ -151,50 +160,58 @@ constexpr int kClean = 0, kTrack = 1, kFull = 2;
 template <int G, int C, int P, int F, int kMode>
 __device__ __forceinline__ void step(Lane<C>& st, int gl, int s, int dbase, const PairCtx& pc,
                                      Best& col, Best& row) {
+    constexpr int Q = P ^ 1;   // buffers of the previous step
     int nbM;
     uint32_t nbL;
     if (P == 0) {
         // left = slot q-1 (its gap-left copy), from the previous lane for c = 0
-        nbM = __shfl_up_sync(0xffffffffu, st.cF[C - 1], 1, G);
-        nbL = __shfl_up_sync(0xffffffffu, st.cL[C - 1], 1, G);
+        nbM = __shfl_up_sync(0xffffffffu, st.F[C - 1], 1, G);
+        nbL = __shfl_up_sync(0xffffffffu, st.L[Q][C - 1], 1, G);
         if (gl == 0) nbM = kNeg;
     } else {
         // up = slot q+1 (its gap-up copy), from the next lane for c = C-1
-        nbM = __shfl_down_sync(0xffffffffu, st.cU[0], 1, G);
-        nbL = __shfl_down_sync(0xffffffffu, st.cL[0], 1, G);
+        nbM = __shfl_down_sync(0xffffffffu, st.U[0], 1, G);
+        nbL = __shfl_down_sync(0xffffffffu, st.L[Q][0], 1, G);
         if (gl == G - 1) nbM = kNeg;
     }
-    int nM[C], nU[C], nF[C];
-    uint32_t nL[C];
 #pragma unroll
-    for (int c = 0; c < C; ++c) {
+    for (int k = 0; k < C; ++k) {
+        // parity 0 reads slot c-1, so it runs c downwards; parity 1 reads
+        // slot c+1 and runs upwards
+        const int c = P == 0 ? C - 1 - k : k;
         int upM, lfM;
         uint32_t upL, lfL;
         if (P == 0) {
-            upM = st.cU[c]; upL = st.cL[c];
-            lfM = c > 0 ? st.cF[c - 1] : nbM;
-            lfL = c > 0 ? st.cL[c - 1] : nbL;
+            upM = st.U[c]; upL = st.L[Q][c];
+            lfM = c > 0 ? st.F[c - 1] : nbM;
+            lfL = c > 0 ? st.L[Q][c - 1] : nbL;
         } else {
-            upM = c < C - 1 ? st.cU[c + 1] : nbM;
-            upL = c < C - 1 ? st.cL[c + 1] : nbL;
-            lfM = st.cF[c]; lfL = st.cL[c];
+            upM = c < C - 1 ? st.U[c + 1] : nbM;
+            upL = c < C - 1 ? st.L[Q][c + 1] : nbL;
+            lfM = st.F[c]; lfL = st.L[Q][c];
         }
         const uint32_t xf = P == 0 ? st.x0[c] : st.x1[c];
         const bool match = (xf & (0xC0000000u >> (2 * F))) == 0u;
-        int md = st.pM[c];
-        if (match) md += kMatch - kMismatch;
+        // The ALU pipe carries the compares, maxima and selects; most adds
+        // are multiply-adds by pc.one[] (runtime 1s) so that they issue on
+        // the FMA pipe.
+        const int pM = st.M[P][c];
+        const uint32_t pL = st.L[P][c];
+        int md = pM;
+        if (match) md = pM * pc.one[0] + (kMatch - kMismatch);
         // max with predicate: isU = up >= left (up wins ties over left),
         // isD = diag >= max(up, left) (diag wins every tie)
         bool isU, isD;
         const int mul = __vibmax_s32(upM, lfM, &isU);
         const int mx = __vibmax_s32(md, mul, &isD);
-        uint32_t ld = st.pL[c] + 0x10001u;
-        if (match) ld += 1u;
+        uint32_t ld = pL * (uint32_t)pc.one[1] + 0x10001u;
+        if (match) ld = pL * (uint32_t)pc.one[2] + 0x10002u;
         uint32_t l = isD ? ld : (isU ? upL : lfL);
         int m = min(mx, P == 0 ? st.cap0[c] : st.cap1[c]);
-        const int a = isU ? 2 + kGE : 2;
-        int u = m + a, f = m + (2 + 2 + kGE) - a;
-        if (isD) { u = m + 2 + kGO; f = m + 2 + kGO; }
+        // gap-penalised copies (+2 offset): D -8/-8, U +1/+2, L +2/+1
+        int u = m + 2, f = m + (2 + kGE);
+        if (isU) { u = m * pc.one[3] + (2 + kGE); f = m * pc.one[4] + 2; }
+        if (isD) { u = m * pc.one[5] + (2 + kGO); f = u; }
         if (kMode == kFull) {
             const int d = dbase + 2 * c + P;
             const int i = (s + d) >> 1, j = (s - d) >> 1;
@@ -207,7 +224,7 @@ __device__ __forceinline__ void step(Lane<C>& st, int gl, int s, int dbase, cons
                 if (j == pc.l1 && i <= pc.l2) track(row, m - 2 * s, l, i);
             }
         }
-        nM[c] = m; nU[c] = u; nF[c] = f; nL[c] = l;
+        st.M[P][c] = m; st.L[P][c] = l; st.U[c] = u; st.F[c] = f;
     }
     if (kMode == kTrack) {
         // slot c sits on the last row when x + 2c == 0 (2i = 2*l2) and on
@@ -219,17 +236,13 @@ __device__ __forceinline__ void step(Lane<C>& st, int gl, int s, int dbase, cons
         if ((x <= 0 && x > -2 * C) || (y >= 0 && y < 2 * C)) {
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-                if (nM[c] == kNeg) continue;   // out of band
+                const int m = st.M[P][c];
+                if (m == kNeg) continue;   // out of band
                 const int i = (s + d0 + 2 * c) >> 1, j = (s - d0 - 2 * c) >> 1;
-                if (x + 2 * c == 0 && j >= 1 && j <= pc.l1) track(col, nM[c] - 2 * s, nL[c], j);
-                if (y - 2 * c == 0 && i >= 1 && i <= pc.l2) track(row, nM[c] - 2 * s, nL[c], i);
+                if (x + 2 * c == 0 && j >= 1 && j <= pc.l1) track(col, m - 2 * s, st.L[P][c], j);
+                if (y - 2 * c == 0 && i >= 1 && i <= pc.l2) track(row, m - 2 * s, st.L[P][c], i);
             }
         }
-    }
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        st.pM[c] = st.cM[c]; st.pL[c] = st.cL[c];
-        st.cM[c] = nM[c]; st.cU[c] = nU[c]; st.cF[c] = nF[c]; st.cL[c] = nL[c];
     }
 }
 
@@ -313,7 +326,7 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
         const int64_t item = base + sub;
         const bool valid = item < a.count;
         int64_t p = -1;
-        PairCtx pc{0, 0, 0, 0};
+        PairCtx pc{0, 0, 0, 0, a.one};   // a.one decays to the kernel parameter array
         int2 pr = make_int2(0, 0);
         if (valid) {
             p = a.order ? (int64_t)a.order[item] : item;
@@ -334,8 +347,8 @@ __global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
         Lane<C> st;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            st.cM[c] = kNeg; st.cU[c] = kNeg; st.cF[c] = kNeg; st.cL[c] = 0;
-            st.pM[c] = kNeg; st.pL[c] = 0;
+            st.M[0][c] = kNeg; st.M[1][c] = kNeg; st.U[c] = kNeg; st.F[c] = kNeg;
+            st.L[0][c] = 0; st.L[1][c] = 0;
             // slot q hosts diagonals 2q - kb (parity 0) and 2q - kb + 1
             const int q = gl * C + c;
             st.cap0[c] = valid && 2 * q - pc.kb <= pc.kb ? INT_MAX : kNeg;
@@ -758,6 +771,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     ctx->stats.gen_cells += (int64_t)st[0];
     ctx->stats.gen_pairs += count;
     GenArgs base{};
+    for (int& o : base.one) o = 1;
     base.packed = g.packed.as<uint32_t>();
     base.woff = g.woff.as<int64_t>();
     base.len = g.len.as<int32_t>();
