@@ -370,6 +370,9 @@ struct TileArgs {
     const int* items;
     int nitems;
     unsigned int* queue_head;
+    // 65536 and 8 at run time: index arithmetic written as multiply(-high)
+    // adds by them issues on the FMA pipe, next to the LOP3-bound CSA trees
+    uint32_t k65536, k8;
 };
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
@@ -425,20 +428,20 @@ __device__ __noinline__ uint2 hash_find(const uint32_t* hkeys, const uint2* hmas
     return make_uint2(0u, 0u);
 }
 
-// Bit-sliced counters of 32 row reads: Harley-Seal levels 1, 2, 4, 8 and
-// the binary count of sixteens above them.
+// Bit-sliced counters of 32 row reads: Harley-Seal levels 1, 2, 4, 8, 16
+// and the binary count of thirty-twos above them.
 template <int B>
 struct Counter {
-    uint32_t ones, twos, fours, eights;
-    uint32_t S[B - 4];
+    uint32_t ones, twos, fours, eights, sixteens;
+    uint32_t S[B - 5];
     __device__ __forceinline__ void clear() {
-        ones = twos = fours = eights = 0;
+        ones = twos = fours = eights = sixteens = 0;
 #pragma unroll
-        for (int k = 0; k < B - 4; ++k) S[k] = 0;
+        for (int k = 0; k < B - 5; ++k) S[k] = 0;
     }
-    // add 16 words
-    __device__ __forceinline__ void add16(const uint32_t* w) {
-        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+    // add 16 words; returns the carry out of the eights level (weight 16)
+    __device__ __forceinline__ uint32_t add16(const uint32_t* w) {
+        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
         csa(twosA, ones, w[0], w[1]);
         csa(twosB, ones, w[2], w[3]);
         csa(foursA, twos, twosA, twosB);
@@ -453,20 +456,34 @@ struct Counter {
         csa(twosB, ones, w[14], w[15]);
         csa(foursB, twos, twosA, twosB);
         csa(eightsB, fours, foursA, foursB);
-        csa(sixteens, eights, eightsA, eightsB);
-        uint32_t carry = sixteens;
+        csa(c16, eights, eightsA, eightsB);
+        return c16;
+    }
+    __device__ __forceinline__ void carry32(uint32_t carry) {
 #pragma unroll
-        for (int k = 0; k < B - 4; ++k) {
+        for (int k = 0; k < B - 5; ++k) {
             const uint32_t t = S[k] & carry;
             S[k] ^= carry;
             carry = t;
         }
     }
+    // two batches' sixteens carries: one CSA, one carry chain
+    __device__ __forceinline__ void add_sixteens2(uint32_t a, uint32_t b) {
+        uint32_t c32;
+        csa(c32, sixteens, a, b);
+        carry32(c32);
+    }
+    __device__ __forceinline__ void add_sixteens1(uint32_t a) {
+        const uint32_t c32 = sixteens & a;
+        sixteens ^= a;
+        carry32(c32);
+    }
     // bit planes X[k] of the 32 per-row counts
     __device__ __forceinline__ void planes(uint32_t* X) const {
-        X[0] = X[1] = X[2] = X[3] = 0;
+        X[0] = X[1] = X[2] = X[3] = X[4] = 0;
 #pragma unroll
-        for (int k = 4; k < B; ++k) X[k] = S[k - 4];
+        for (int k = 5; k < B; ++k) X[k] = S[k - 5];
+        add_at(X, sixteens, 4);
         add_at(X, eights, 3);
         add_at(X, fours, 2);
         add_at(X, twos, 1);
@@ -484,6 +501,27 @@ struct Counter {
         }
     }
 };
+
+// Gather the plane words of 16 scheduled entries (two uint4 of 16-bit word
+// indices) and feed both 32-row halves; returns the two sixteens carries.
+template <int B>
+__device__ __forceinline__ void gather16(const char* __restrict__ Pb, uint4 q0, uint4 q1,
+                                         uint32_t k65536, uint32_t k8, Counter<B>& lo,
+                                         Counter<B>& hi, uint32_t& c16lo, uint32_t& c16hi) {
+    const uint32_t x[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+    uint32_t wl[16], wh[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t ih = __umulhi(x[k], k65536);   // x >> 16
+        const uint32_t il = x[k] - ih * k65536;       // x & 0xFFFF
+        const uint2 p0 = *reinterpret_cast<const uint2*>(Pb + il * k8);
+        const uint2 p1 = *reinterpret_cast<const uint2*>(Pb + ih * k8);
+        wl[2 * k] = p0.x; wh[2 * k] = p0.y;
+        wl[2 * k + 1] = p1.x; wh[2 * k + 1] = p1.y;
+    }
+    c16lo = lo.add16(wl);
+    c16hi = hi.add16(wh);
+}
 
 // Threshold and emission for one 32-row half: candidates by a bit-sliced
 // compare against a lower bound of mmin over the lane's pairs, then the
@@ -546,26 +584,33 @@ __device__ void tile_columns(const TileArgs& a, const uint2* __restrict__ P,
         Counter<B> lo, hi;
         lo.clear();
         hi.clear();
-        uint4 cur0, cur1, nxt0, nxt1;
-        if (E > 0) { cur0 = __ldg(ep); cur1 = __ldg(ep + 32); }
-        for (int e = 0; e < E; e += 16) {
-            if (e + 16 < E) {
-                nxt0 = __ldg(ep + ((e + 16) >> 3) * 32);
-                nxt1 = __ldg(ep + ((e + 16) >> 3) * 32 + 32);
+        const char* __restrict__ Pb = reinterpret_cast<const char*>(P);
+        // 32 entries per iteration: two 16-entry batches whose sixteens
+        // carries meet in one CSA; the next batch is always in flight
+        uint4 a0, a1;
+        if (E > 0) { a0 = __ldg(ep); a1 = __ldg(ep + 32); }
+        for (int e = 0; e < E; e += 32) {
+            const bool two = e + 16 < E;
+            uint4 b0, b1;
+            if (two) {
+                b0 = __ldg(ep + ((e + 16) >> 3) * 32);
+                b1 = __ldg(ep + ((e + 16) >> 3) * 32 + 32);
             }
-            const uint32_t x[8] = {cur0.x, cur0.y, cur0.z, cur0.w, cur1.x, cur1.y, cur1.z, cur1.w};
-            uint32_t wl[16], wh[16];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint2 p0 = P[x[k] & 0xFFFFu];
-                const uint2 p1 = P[x[k] >> 16];
-                wl[2 * k] = p0.x; wh[2 * k] = p0.y;
-                wl[2 * k + 1] = p1.x; wh[2 * k + 1] = p1.y;
+            uint32_t la, ha;
+            gather16<B>(Pb, a0, a1, a.k65536, a.k8, lo, hi, la, ha);
+            if (e + 32 < E) {
+                a0 = __ldg(ep + ((e + 32) >> 3) * 32);
+                a1 = __ldg(ep + ((e + 32) >> 3) * 32 + 32);
             }
-            lo.add16(wl);
-            hi.add16(wh);
-            cur0 = nxt0;
-            cur1 = nxt1;
+            if (two) {
+                uint32_t lb, hb;
+                gather16<B>(Pb, b0, b1, a.k65536, a.k8, lo, hi, lb, hb);
+                lo.add_sixteens2(la, lb);
+                hi.add_sixteens2(ha, hb);
+            } else {
+                lo.add_sixteens1(la);
+                hi.add_sixteens1(ha);
+            }
         }
         uint32_t X0[B], X1[B];
         lo.planes(X0);
@@ -1008,6 +1053,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         TileArgs ta{};
         ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
         ta.tent = j.tent.as<uint16_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
+        ta.k65536 = 65536u; ta.k8 = 8u;
         ta.nhigh = j.cntmax.as<int32_t>() + n;
         ta.tcount = j.t.as<int32_t>(); ta.dense_group = j.work.as<uint8_t>();
         ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
