@@ -283,13 +283,21 @@ def run_ours(args, dist, ws, rank, local):
     plain_s = float(np.mean(ms_p)) / 1e3
     staged_s = float(np.mean(ms_s)) / 1e3
 
-    # e2e through the public API with host buffers
+    # e2e through the public API from pinned host buffers: reads up once,
+    # kmerDist survivors handed to genDist in HBM, genDist chunks read back
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return t, v
+    _keep = [pinned(buf), pinned(offs), pinned(lens)]
+    pbuf, poffs, plens = (x[1] for x in _keep)
+
     def e2e_step():
-        eng.kmer_prepare(buf, offs, lens, k)
+        eng.kmer_prepare(pbuf, poffs, plens, k)
         c = eng.kmer_run(thr_k, cg.MODE_BATCHED, False)
-        pairs, _ = eng.kmer_fetch(c, False)
-        eng.gen_prepare(buf, offs, lens)
-        out = eng.gen_run(pairs, band, thr_g, cg.MODE_BATCHED)
+        eng.gen_prepare_from_kmer()
+        out = eng.gen_run_from_kmer(band, thr_g, cg.MODE_BATCHED)
         return c, out
 
     for _ in range(max(1, args.warmup // 2)):
@@ -305,8 +313,9 @@ def run_ours(args, dist, ws, rank, local):
         torch.cuda.synchronize()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = _max_over_ranks(dist, float(np.mean(e2e_ms)) / 1e3)
-    h2d = 2 * (buf.nbytes + offs.nbytes + lens.nbytes) + c * 8
-    d2h = c * 8 + sum(len(o[2]) for o in out) * 12 + n * 4
+    # reads and offsets, per-read tuple counts, lengths and word offsets, per-group layouts
+    h2d = buf.nbytes + offs.nbytes + n * 16 + (n // 32 + 1) * 40
+    d2h = sum(len(o[2]) for o in out) * 12 + n * 8                  # chunks + per-read multiplicities
 
     kmer_ops = n_pairs * 2 * mean_t            # frozen: (Ta + Tb) per pair
     gen_ops = cells * 10                        # frozen: 10 per band cell

@@ -75,6 +75,7 @@ PROTOTYPES = {
     "crispy_kmer_fetch": (C.c_int, [_P, _P, _P, C.c_int64, _i64p]),
     "crispy_kmer_stream": (C.c_int, [_P, SINK, _P]),
     "crispy_gen_prepare": (C.c_int, [_P, _P, _P, _P, C.c_int]),
+    "crispy_gen_prepare_from_kmer": (C.c_int, [_P]),
     "crispy_gen_run": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
     "crispy_gen_run_from_kmer": (C.c_int, [_P, C.c_int, C.c_float, C.c_int, SINK, _P, _i64p]),
     "crispy_gen_align": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P]),
@@ -255,6 +256,10 @@ class Engine:
         offs = np.ascontiguousarray(offs, dtype=np.int64)
         lens = np.ascontiguousarray(lens, dtype=np.int32)
         self._check(self.lib.crispy_gen_prepare(self.h, _ptr(buf), _ptr(offs), _ptr(lens), len(lens)))
+
+    def gen_prepare_from_kmer(self):
+        """Pack the reads the last kmer_prepare left on the device (no second upload)."""
+        self._check(self.lib.crispy_gen_prepare_from_kmer(self.h))
 
     def gen_align(self, pairs: np.ndarray, band: int, mode: int = MODE_BATCHED):
         pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)

@@ -989,6 +989,44 @@ int crispy_gen_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offse
     return CRISPY_OK;
 }
 
+int crispy_gen_prepare_from_kmer(crispy_ctx* ctx) {
+    if (!ctx) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "gen_prepare_from_kmer before kmer_prepare");
+    cudaSetDevice(ctx->device);
+    GenJob& g = ctx->gen;
+    g.ready = false;
+    const int n = j.n;
+    g.n = n;
+    g.h_len.resize(n);
+    g.h_woff.resize(n + 1);
+    int64_t words = 0;
+    g.max_len = 0;
+    for (int r = 0; r < n; ++r) {
+        const int L = j.h_t[r] + j.k - 1;
+        if (L <= 0) return fail(ctx, CRISPY_E_INPUT, "read %d is empty", r);
+        g.h_len[r] = L;
+        g.h_woff[r] = words;
+        words += (L + 15) / 16;
+        g.max_len = std::max(g.max_len, L);
+    }
+    g.h_woff[n] = words;
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, g.len, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, g.woff, (size_t)(n + 1) * 8));
+    CRISPY_TRY(ensure(ctx, g.packed, (size_t)(words + 4) * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.len.ptr, g.h_len.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.woff.ptr, g.h_woff.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    gen_pack_kernel<<<std::min(n, ctx->sm_count * 16), 128, 0, s>>>(
+        j.seq.as<uint8_t>(), j.off.as<int64_t>(), g.len.as<int32_t>(), g.woff.as<int64_t>(), n,
+        g.packed.as<uint32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    g.ready = true;
+    return CRISPY_OK;
+}
+
 int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int band, int mode,
                      float* dist, int32_t* score, int32_t* ml, int32_t* al) {
     if (!ctx) return CRISPY_E_INPUT;

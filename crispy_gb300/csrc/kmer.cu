@@ -836,12 +836,20 @@ inline bool keep_host(float d, float thr) {
 // monotone), so "m >= mmin[t]" is exactly the reference's test.
 void build_mmin(float thr, int max_t, std::vector<uint16_t>& mmin, std::vector<uint16_t>& smin) {
     mmin.assign(max_t + 1, 0xFFFF);
+    auto pass = [thr](int m, int t) {
+        volatile float q = (float)m / (float)t;
+        volatile float d = 1.0f - q;
+        return keep_host(d, thr);
+    };
     for (int t = 0; t <= max_t; ++t) {
-        for (int m = 0; m <= t; ++m) {
-            volatile float q = (float)m / (float)t;
-            volatile float d = 1.0f - q;
-            if (keep_host(d, thr)) { mmin[t] = (uint16_t)m; break; }
+        // smallest passing m in [0, t] by bisection (pass is monotone in m)
+        if (!pass(t, t)) continue;
+        int lo = 0, hi = t;
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            if (pass(mid, t)) hi = mid; else lo = mid + 1;
         }
+        mmin[t] = (uint16_t)lo;
     }
     smin.assign(max_t + 1, 0xFFFF);
     uint16_t run = 0xFFFF;

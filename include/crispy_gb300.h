@@ -141,6 +141,13 @@ int crispy_kmer_stream(crispy_ctx* ctx, crispy_sink sink, void* user);
 int crispy_gen_prepare(crispy_ctx* ctx, const char* seqbuf,
                        const int64_t* offsets, const int32_t* lengths, int n);
 
+/* The same from the reads the last crispy_kmer_prepare left on the device:
+ * no second host upload when one process runs both stages (the reference
+ * runs them as two programs that each parse the FASTA, genMain.cpp:184-277).
+ * Fails with CRISPY_E_STATE without a prepared k-mer job and CRISPY_E_INPUT
+ * for an empty read, as crispy_gen_prepare does. */
+int crispy_gen_prepare_from_kmer(crispy_ctx* ctx);
+
 /* Banded NW distance for every pair, threshold filter, 589,824-pair load
  * windows, chunk flush and stable per-chunk sort by distance
  * (genKernel.cu:707-780, genCUDA.cu:150-254, :17-81).  pairs is

@@ -116,3 +116,30 @@ def test_gen_bad_index_rejected(engine):
     with pytest.raises(cg.CrispyError) as e:
         engine.gen_run(np.array([[0, len(reads)]], np.int32), 10, 0.5)
     assert e.value.code == cg.E_INPUT
+
+
+def test_gen_prepare_from_kmer_matches_upload(engine):
+    # packing the reads left on the device by kmer_prepare gives the same
+    # chunks as a second upload through gen_prepare
+    reads = _reads(700, 83, root=520, dist="uniform", a=300, b=500, cents=25)
+    buf, offs, lens = synth.pack_reads(reads)
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    tg = cg.default_threshold(len(reads), -1.0, 1)
+    engine.kmer_prepare(buf, offs, lens, 6)
+    engine.kmer_run(t, cg.MODE_BATCHED, False)
+    engine.gen_prepare(buf, offs, lens)
+    want = engine.gen_run_from_kmer(10, tg, cg.MODE_BATCHED)
+    engine.kmer_prepare(buf, offs, lens, 6)
+    engine.kmer_run(t, cg.MODE_BATCHED, False)
+    engine.gen_prepare_from_kmer()
+    got = engine.gen_run_from_kmer(10, tg, cg.MODE_BATCHED)
+    assert len(got) == len(want) and sum(len(c[2]) for c in got) > 0
+    for (ci, p, d), (wi, wp, wd) in zip(got, want):
+        assert ci == wi and np.array_equal(p, wp) and np.array_equal(d.view(np.uint32), wd.view(np.uint32))
+
+
+def test_gen_prepare_from_kmer_needs_kmer_job():
+    with cg.Engine(0) as fresh:
+        with pytest.raises(cg.CrispyError) as e:
+            fresh.gen_prepare_from_kmer()
+        assert e.value.code == cg.E_STATE
