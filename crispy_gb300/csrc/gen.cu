@@ -319,7 +319,7 @@ __device__ __forceinline__ void unpack_mlal(uint32_t l, int ij, int* ml, int* al
 // One pair per G-lane sub-group (32/G pairs per warp), C band slots per
 // lane, so a pair with kBand + 1 <= G*C slots fits.
 template <int G, int C>
-__global__ void __launch_bounds__(kGenThreads) gen_warp_kernel(GenArgs a) {
+__global__ void __launch_bounds__(kGenThreads, 3) gen_warp_kernel(GenArgs a) {
     constexpr int kPerWarp = 32 / G;
     __shared__ uint32_t smem[kGenWarps][kPerWarp][2][kSmWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
