@@ -43,6 +43,8 @@ struct KmerJob {
     std::vector<int32_t> h_tgent;    // tile stream: steps per lane in each group
     int64_t ntent = 0;
     DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
+    DevBuf tgentL, nsec;             // K = 8: L-stream steps per group; per-read H/L counts
+    std::vector<int32_t> h_nsec;
     // last run's survivors, in stage order
     int64_t nsurv = 0;
     bool have_dists = false;

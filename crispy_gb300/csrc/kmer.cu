@@ -91,6 +91,17 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // lane+1, ... mod 32), with the per-bank counts written to bcnt.  The tile kernel does not read this order directly: the
 // schedule kernel below turns it into a bank-conflict-avoiding stream.
 // ---------------------------------------------------------------------------
+// Raw-list bucket of a dense level entry: K <= 7, the bank of its 32-bit
+// word index; K = 8, the section (H = K-mer >= 0x8000 first) and the 4-byte
+// bank of its 16-bit plane word.
+__device__ __forceinline__ int prep_bucket(uint32_t val, int K) {
+    if (K == 8) {
+        const uint32_t v = val & 0xFFFFu;
+        return (v >= 0x8000u ? 0 : 32) + (int)((v >> 1) & 31u);
+    }
+    return (int)(val & 31u);
+}
+
 constexpr int kPrepThreads = 256;
 constexpr int kPrepPer = CRISPY_MAX_READ_LEN / kPrepThreads;   // positions per thread
 
@@ -99,17 +110,21 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
     const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
     uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
-    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt) {
+    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt, int32_t* __restrict__ nsec) {
     extern __shared__ uint32_t hist[];
     __shared__ int s_max, s_hpos;
     __shared__ uint32_t s_hmax;
-    __shared__ int s_bcnt[32], s_bstart[32];
+    __shared__ int s_bcnt[64], s_bstart[64];
     const uint32_t K4 = 1u << (2 * K);
     const int hwords = (int)((K4 + 1) / 2);
+    // K = 8: two sections, H (K-mer >= 0x8000) then L, grouped by the 4-byte
+    // bank of a 16-bit plane word; K <= 7: one section, grouped by the bank of
+    // a 32-bit word index (value mod 32)
+    const int nsections = K == 8 ? 2 : 1;
     for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_hpos = 0; }
-        if (threadIdx.x < 32) s_bcnt[threadIdx.x] = 0;
+        if (threadIdx.x < 64) s_bcnt[threadIdx.x] = 0;
         __syncthreads();
         const int T = tcount[r];
         const uint8_t* s = seq + off[r];
@@ -131,7 +146,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
                 if ((int)t >= dense_levels) {
                     dst[ent_at(atomicAdd(&s_hpos, 1), lane)] = val[k];
                 } else {
-                    rank[k] = atomicAdd(&s_bcnt[val[k] & 31u], 1);
+                    rank[k] = atomicAdd(&s_bcnt[prep_bucket(val[k], K)], 1);
                 }
             }
         }
@@ -142,21 +157,27 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
             // reads of a group sit in different banks, which keeps the
             // one-thread-per-column dense kernel free of bank conflicts
             const int i = threadIdx.x;
-            const int b = (i + lane) & 31;
-            const int c = s_bcnt[b];
-            int x = c;
+            int base = s_hpos;
+            for (int sec = 0; sec < nsections; ++sec) {
+                const int b = sec * 32 + ((i + lane) & 31);
+                const int c = s_bcnt[b];
+                int x = c;
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, x, d);
-                if (i >= d) x += y;
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, d);
+                    if (i >= d) x += y;
+                }
+                s_bstart[b] = base + x - c;
+                bcnt[(int64_t)r * (32 * nsections) + b] = (uint16_t)c;
+                const int total = __shfl_sync(0xffffffffu, x, 31);
+                if (nsec && i == 0) nsec[(int64_t)r * 2 + sec] = total;
+                base += total;
             }
-            s_bstart[b] = s_hpos + x - c;
-            bcnt[(int64_t)r * 32 + b] = (uint16_t)c;
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kPrepPer; ++k)
-            if (rank[k] >= 0) dst[ent_at(s_bstart[val[k] & 31u] + rank[k], lane)] = val[k];
+            if (rank[k] >= 0) dst[ent_at(s_bstart[prep_bucket(val[k], K)] + rank[k], lane)] = val[k];
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
@@ -217,130 +238,175 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int k) {   // 0-based; -1
     return m ? __ffs(m) - 1 : -1;
 }
 
+// One tile stream of one 32-read group (warp w of the block, lane = read).
+//   kB = 16: 64-bit plane words, 16 double banks per half-warp; bucket b
+//            draws on the raw bank groups b and b + 16 (value mod 32).
+//   kB = 32: 16-bit plane words, 32 four-byte banks over the whole warp;
+//            bucket b is raw group b of the section.
+// raw_cnt: this lane's 32 raw group counts; pos0: its first raw position
+// of the section; the stream values are the plane word indices
+// (value - vsub), and guard words (always zero) fill the wildcard steps.
+struct SchedSmem {
+    uint16_t cnt[kSchedWarps][32][33];    // entries per bucket
+    uint16_t ov[kSchedWarps][32][33];     // surplus per bucket
+    uint16_t next[kSchedWarps][32][33];   // next raw position per raw group
+    uint16_t left[kSchedWarps][32][33];   // raw entries left per raw group
+    uint8_t bank[kSchedWarps][kSchedChunk][32];
+};
+
+template <int kB>
+__device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const uint16_t* raw_cnt,
+                             int pos0, int Et, const uint32_t* __restrict__ src, uint32_t vsub,
+                             uint32_t guard0, uint16_t* __restrict__ dst_group) {
+    const unsigned full = 0xffffffffu;
+    constexpr unsigned kMask = kB == 32 ? 0xffffffffu : 0xFFFFu;
+    const int hs = kB == 32 ? 0 : (lane & 16);          // this half's bit offset in 32-bit masks
+    const unsigned half_lt = ((1u << lane) - 1u) & (kB == 32 ? 0xffffffffu : (0xFFFFu << hs));
+    for (int b = 0; b < 32; ++b) sm.left[w][lane][b] = active ? raw_cnt[b] : (uint16_t)0;
+    // first raw position of each raw group: the prep kernel's lane-rotated order
+    for (int i = 0, pos = pos0; i < 32; ++i) {
+        const int b = (i + lane) & 31;
+        sm.next[w][lane][b] = (uint16_t)pos;
+        pos += sm.left[w][lane][b];
+    }
+    int D = 0;
+    unsigned ovmask = 0;
+    for (int b = 0; b < kB; ++b) {
+        const int c = kB == 32 ? sm.left[w][lane][b] : sm.left[w][lane][b] + sm.left[w][lane][b + 16];
+        const int o = (b - lane) & (kB - 1);
+        const int slots = Et > o ? (Et - o + kB - 1) / kB : 0;
+        const int ov = max(0, c - slots);
+        sm.cnt[w][lane][b] = (uint16_t)c;
+        sm.ov[w][lane][b] = (uint16_t)ov;
+        D += c;
+        if (ov) ovmask |= 1u << b;
+    }
+    int wild = Et - D;
+    __syncwarp();
+    uint4* dst = reinterpret_cast<uint4*>(dst_group) + lane;
+    for (int e0 = 0; e0 < Et; e0 += kSchedChunk) {
+        for (int i = 0; i < kSchedChunk; ++i) {
+            const int e = e0 + i;
+            const int h = (e + lane) & (kB - 1);
+            const bool hole = (e / kB) >= (int)sm.cnt[w][lane][h];
+            int bank = hole ? -1 : h;
+            unsigned used = __reduce_or_sync(full, hole ? 0u : (1u << (h + hs)));
+            bool open = hole;
+            for (int round = 0; round < kB; ++round) {
+                const unsigned cand = open ? (ovmask & ~(used >> hs) & kMask) : 0u;
+                if (!__any_sync(full, cand != 0u)) break;
+                const int prop = cand ? hs + __ffs(cand) - 1 : 64 + lane;
+                const unsigned peers = __match_any_sync(full, prop);
+                const bool win = cand && lane == __ffs(peers) - 1;
+                if (win) {
+                    bank = prop - hs;
+                    open = false;
+                    const int left = (int)sm.ov[w][lane][bank] - 1;
+                    sm.ov[w][lane][bank] = (uint16_t)left;
+                    if (left == 0) ovmask &= ~(1u << bank);
+                }
+                used |= __reduce_or_sync(full, win ? (1u << prop) : 0u);
+            }
+            const bool wl = open && wild > 0;
+            const unsigned wm = __ballot_sync(full, wl);
+            if (wl) {
+                // the k-th wildcard lane of a half takes the k-th free bucket
+                const int fb = nth_set_bit(~(used >> hs) & kMask, __popc(wm & half_lt));
+                bank = kB + (fb >= 0 ? fb : 0);
+                --wild;
+            } else if (open) {
+                const int b = ovmask ? __ffs(ovmask) - 1 : -1;
+                if (b >= 0) {
+                    bank = b;
+                    const int left = (int)sm.ov[w][lane][b] - 1;
+                    sm.ov[w][lane][b] = (uint16_t)left;
+                    if (left == 0) ovmask &= ~(1u << b);
+                } else {
+                    bank = kB;   // unreachable by the count identity; stays in bounds
+                }
+            }
+            sm.bank[w][i][lane] = (uint8_t)bank;
+        }
+        __syncwarp();
+        // gather the chosen entries: positions first, then the loads
+        uint32_t v[kSchedChunk];
+#pragma unroll
+        for (int i = 0; i < kSchedChunk; ++i) {
+            const int b = sm.bank[w][i][lane];
+            if (b < kB) {
+                const int bb = (kB == 32 || sm.left[w][lane][b]) ? b : b + 16;
+                const int p = sm.next[w][lane][bb];
+                sm.next[w][lane][bb] = (uint16_t)(p + 1);
+                sm.left[w][lane][bb] = (uint16_t)(sm.left[w][lane][bb] - 1);
+                v[i] = (uint32_t)p;
+            } else {
+                v[i] = 0x80000000u | (uint32_t)(b - kB);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kSchedChunk; ++i) {
+            const uint32_t x = v[i];
+            // guard of bucket b: word guard0 + b (64-bit words, double bank b)
+            // or halfword guard0 + 2b (16-bit words, 4-byte bank b)
+            v[i] = (x & 0x80000000u) ? guard0 + (x & 31u) * (kB == 32 ? 2u : 1u)
+                                     : __ldg(src + ent_at((int)x, lane)) - vsub;
+        }
+        // two octets of this lane: two uint4 of packed 16-bit word indices
+#pragma unroll
+        for (int o = 0; o < 2; ++o) {
+            uint4 q;
+            q.x = (v[8 * o + 0] & 0xFFFFu) | (v[8 * o + 1] << 16);
+            q.y = (v[8 * o + 2] & 0xFFFFu) | (v[8 * o + 3] << 16);
+            q.z = (v[8 * o + 4] & 0xFFFFu) | (v[8 * o + 5] << 16);
+            q.w = (v[8 * o + 6] & 0xFFFFu) | (v[8 * o + 7] << 16);
+            dst[(int64_t)((e0 >> 3) + o) * 32] = q;
+        }
+        __syncwarp();
+    }
+}
+
+// K <= 7: one 16-bucket stream per group (64-bit plane words).
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
     const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
     const int32_t* __restrict__ nhigh, const uint16_t* __restrict__ bcnt, int n, int ngroups,
     uint32_t guard_word, uint16_t* __restrict__ tent) {
-    __shared__ uint16_t s_cnt[kSchedWarps][32][17];    // entries per bucket
-    __shared__ uint16_t s_ov[kSchedWarps][32][17];     // surplus per bucket
-    __shared__ uint16_t s_next[kSchedWarps][32][33];   // next raw position per 32-bank
-    __shared__ uint16_t s_left[kSchedWarps][32][33];   // raw entries left per 32-bank
-    __shared__ uint8_t s_bank[kSchedWarps][kSchedChunk][32];
+    __shared__ SchedSmem sm;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned full = 0xffffffffu;
-    const int hs = lane & 16;                       // this half's bit offset in 32-bit masks
-    const unsigned half_lt = ((1u << lane) - 1u) & (0xFFFFu << hs);
     for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
         const int r = g * 32 + lane;
-        const int Et = tgent[g];
-        const int nh = r < n ? nhigh[r] : 0;
-        for (int b = 0; b < 32; ++b)
-            s_left[w][lane][b] = r < n ? bcnt[(int64_t)r * 32 + b] : (uint16_t)0;
-        // first raw position of each 32-bank: the prep kernel's lane-rotated order
-        for (int i = 0, pos = nh; i < 32; ++i) {
-            const int b = (i + lane) & 31;
-            s_next[w][lane][b] = (uint16_t)pos;
-            pos += s_left[w][lane][b];
-        }
-        int D = 0;
-        unsigned ovmask = 0;
-        for (int b = 0; b < 16; ++b) {
-            const int c = s_left[w][lane][b] + s_left[w][lane][b + 16];
-            const int o = (b - lane) & 15;
-            const int slots = Et > o ? (Et - o + 15) >> 4 : 0;
-            const int ov = max(0, c - slots);
-            s_cnt[w][lane][b] = (uint16_t)c;
-            s_ov[w][lane][b] = (uint16_t)ov;
-            D += c;
-            if (ov) ovmask |= 1u << b;
-        }
-        int wild = Et - D;
+        const bool active = r < n;
+        sched_stream<16>(sm, w, lane, active, bcnt + (int64_t)(active ? r : 0) * 32,
+                         active ? nhigh[r] : 0, tgent[g], ent + gstart[g], 0u, guard_word,
+                         tent + tstart[g]);
+    }
+}
+
+// K = 8: an H stream and an L stream per group (16-bit plane words); the H
+// section of a read's raw list follows its high-level entries, the L
+// section follows the H section.  Each stream indexes its own plane
+// (H: K-mer - 0x8000, L: K-mer) whose guard words start at 32768.
+__global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
+    const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
+    const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
+    const int32_t* __restrict__ tgentL, const int32_t* __restrict__ nhigh,
+    const int32_t* __restrict__ nsec, const uint16_t* __restrict__ bcnt, int n, int ngroups,
+    uint16_t* __restrict__ tent) {
+    __shared__ SchedSmem sm;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
+        const int r = g * 32 + lane;
+        const bool active = r < n;
+        const int rr = active ? r : 0;
+        const int nh = active ? nhigh[r] : 0;
+        const int nH = active ? nsec[(int64_t)rr * 2] : 0;
+        const int EtH = tgent[g];
+        sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, EtH, ent + gstart[g],
+                         0x8000u, 32768u, tent + tstart[g]);
         __syncwarp();
-        const uint32_t* src = ent + gstart[g];
-        uint4* dst = reinterpret_cast<uint4*>(tent + tstart[g]) + lane;
-        for (int e0 = 0; e0 < Et; e0 += kSchedChunk) {
-            for (int i = 0; i < kSchedChunk; ++i) {
-                const int e = e0 + i;
-                const int h = (e + lane) & 15;
-                const bool hole = (e >> 4) >= (int)s_cnt[w][lane][h];
-                int bank = hole ? -1 : h;
-                unsigned used = __reduce_or_sync(full, hole ? 0u : (1u << (h + hs)));
-                bool open = hole;
-                for (int round = 0; round < 16; ++round) {
-                    const unsigned cand = open ? (ovmask & ~(used >> hs) & 0xFFFFu) : 0u;
-                    if (!__any_sync(full, cand != 0u)) break;
-                    const int prop = cand ? hs + __ffs(cand) - 1 : 32 + lane;
-                    const unsigned peers = __match_any_sync(full, prop);
-                    const bool win = cand && lane == __ffs(peers) - 1;
-                    if (win) {
-                        bank = prop - hs;
-                        open = false;
-                        const int left = (int)s_ov[w][lane][bank] - 1;
-                        s_ov[w][lane][bank] = (uint16_t)left;
-                        if (left == 0) ovmask &= ~(1u << bank);
-                    }
-                    used |= __reduce_or_sync(full, win ? (1u << prop) : 0u);
-                }
-                const bool wl = open && wild > 0;
-                const unsigned wm = __ballot_sync(full, wl);
-                if (wl) {
-                    // the k-th wildcard lane of a half takes the k-th free bucket
-                    const int fb = nth_set_bit(~(used >> hs) & 0xFFFFu, __popc(wm & half_lt));
-                    bank = 16 + (fb >= 0 ? fb : 0);
-                    --wild;
-                } else if (open) {
-                    const int b = ovmask ? __ffs(ovmask) - 1 : -1;
-                    if (b >= 0) {
-                        bank = b;
-                        const int left = (int)s_ov[w][lane][b] - 1;
-                        s_ov[w][lane][b] = (uint16_t)left;
-                        if (left == 0) ovmask &= ~(1u << b);
-                    } else {
-                        bank = 16;   // unreachable by the count identity; stays in bounds
-                    }
-                }
-                s_bank[w][i][lane] = (uint8_t)bank;
-            }
-            __syncwarp();
-            // gather the chosen entries: positions first, then the loads
-            const int steps = min(kSchedChunk, Et - e0);
-            uint32_t v[kSchedChunk];
-#pragma unroll
-            for (int i = 0; i < kSchedChunk; ++i) {
-                v[i] = 0x80000000u;   // guard word of bucket 0
-                if (i < steps) {
-                    const int b = s_bank[w][i][lane];
-                    if (b < 16) {
-                        const int bb = s_left[w][lane][b] ? b : b + 16;
-                        const int p = s_next[w][lane][bb];
-                        s_next[w][lane][bb] = (uint16_t)(p + 1);
-                        s_left[w][lane][bb] = (uint16_t)(s_left[w][lane][bb] - 1);
-                        v[i] = (uint32_t)p;
-                    } else {
-                        v[i] = 0x80000000u | (uint32_t)(b - 16);
-                    }
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < kSchedChunk; ++i) {
-                const uint32_t x = v[i];
-                v[i] = (x & 0x80000000u) ? guard_word + (x & 15u) : __ldg(src + ent_at((int)x, lane));
-            }
-            // two octets of this lane: two uint4 of packed 16-bit word indices
-#pragma unroll
-            for (int o = 0; o < 2; ++o) {
-                if (o * 8 < steps) {
-                    uint4 q;
-                    q.x = (v[8 * o + 0] & 0xFFFFu) | (v[8 * o + 1] << 16);
-                    q.y = (v[8 * o + 2] & 0xFFFFu) | (v[8 * o + 3] << 16);
-                    q.z = (v[8 * o + 4] & 0xFFFFu) | (v[8 * o + 5] << 16);
-                    q.w = (v[8 * o + 6] & 0xFFFFu) | (v[8 * o + 7] << 16);
-                    dst[(int64_t)((e0 >> 3) + o) * 32] = q;
-                }
-            }
-            __syncwarp();
-        }
+        sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + nH, tgentL[g],
+                         ent + gstart[g], 0u, 32768u, tent + tstart[g] + (int64_t)32 * EtH);
+        __syncwarp();
     }
 }
 
@@ -373,6 +439,10 @@ struct TileArgs {
     // 65536 and 8 at run time: index arithmetic written as multiply(-high)
     // adds by them issues on the FMA pipe, next to the LOP3-bound CSA trees
     uint32_t k65536, k8;
+    // K = 8
+    const int32_t* tgentL;         // L-stream steps per group (H: tgent)
+    const uint32_t* hinfo;         // per read: (largest H K-mer << 16) | its count, 0 if none
+    int ngroups;
 };
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
@@ -726,6 +796,236 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile_kernel(TileArgs a) 
 }
 
 // ---------------------------------------------------------------------------
+// K = 8 tile kernel.  The reference's merge for K = 8 gives
+//     m = minsum(H) + [same] * minsum(L)
+// (H = K-mers >= 0x8000, L = the rest; kmerMain.cpp:275-278 against
+// kmerKernel.cu:37-45), so the two halves are counted apart.  A block owns 16
+// row reads; first occurrences live in two planes of 16-bit words (H: K-mer
+// - 0x8000, L: K-mer; 32,768 words each plus guard words, 128 KB together)
+// and repeated occurrences in a shared hash.  Each lane owns two column
+// reads, one of each of two adjacent 32-read groups, and gathers one 16-bit
+// word per read and step into the low / high half of a 32-bit counter
+// input: 16 rows x 2 columns per LOP3.  An H phase over the groups' H
+// streams and an L phase over their L streams give the two bit-sliced sums;
+// m is formed bit-sliced with the [same] mask per (row, column).
+// ---------------------------------------------------------------------------
+constexpr int kRows8 = 16;
+constexpr int kPlane8 = 32768 + 64;    // 16-bit words per plane: K-mers + guard words
+
+__device__ __noinline__ uint32_t hash_find8(const uint32_t* hkeys, const uint32_t* hmask,
+                                            uint32_t key) {
+    uint32_t h = hash_slot(key);
+    for (int probe = 0; probe < kHashSlots; ++probe) {
+        const uint32_t k = hkeys[h];
+        if (k == key) return hmask[h];
+        if (k == kSentinel) return 0u;
+        h = (h + 1) & (kHashSlots - 1);
+    }
+    return 0u;
+}
+
+// 16 scheduled entries of each of two streams (columns in the low and high
+// half); an exhausted stream reads guard word 32768 (zero).
+template <int B>
+__device__ __forceinline__ uint32_t gather8_16(const uint16_t* __restrict__ plane, uint4 qa0, uint4 qa1,
+                                               uint4 qb0, uint4 qb1, Counter<B>& cnt) {
+    const uint32_t xa[8] = {qa0.x, qa0.y, qa0.z, qa0.w, qa1.x, qa1.y, qa1.z, qa1.w};
+    const uint32_t xb[8] = {qb0.x, qb0.y, qb0.z, qb0.w, qb1.x, qb1.y, qb1.z, qb1.w};
+    uint32_t w[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        w[2 * k] = (uint32_t)plane[xa[k] & 0xFFFFu] | ((uint32_t)plane[xb[k] & 0xFFFFu] << 16);
+        w[2 * k + 1] = (uint32_t)plane[xa[k] >> 16] | ((uint32_t)plane[xb[k] >> 16] << 16);
+    }
+    return cnt.add16(w);
+}
+
+template <int B>
+__device__ __forceinline__ void phase8(const uint16_t* __restrict__ plane, const uint4* epa, int ea,
+                                       const uint4* epb, int eb, uint32_t* X) {
+    const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
+    Counter<B> cnt;
+    cnt.clear();
+    const int E = max(ea, eb);
+    for (int e = 0; e < E; e += 16) {
+        const int o = (e >> 3) * 32;
+        const uint4 a0 = e < ea ? __ldg(epa + o) : guard, a1 = e < ea ? __ldg(epa + o + 32) : guard;
+        const uint4 b0 = e < eb ? __ldg(epb + o) : guard, b1 = e < eb ? __ldg(epb + o + 32) : guard;
+        cnt.add_sixteens1(gather8_16<B>(plane, a0, a1, b0, b1, cnt));
+    }
+    cnt.planes(X);
+}
+
+template <int B>
+__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a) {
+    extern __shared__ __align__(16) uint16_t P8[];   // H plane, then L plane
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots];
+    __shared__ int s_rowT[kRows8];
+    __shared__ uint32_t s_rowH[kRows8];
+    __shared__ int s_item[4];
+    __shared__ int s_tmin, s_any_high;
+    __shared__ uint32_t s_rows_ok;
+    const bool queued = a.items != nullptr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            if (queued) {
+                const unsigned w = atomicAdd(a.queue_head, 1u);
+                s_item[3] = (int)w < a.nitems;
+                if (s_item[3]) {
+                    s_item[0] = a.items[w];
+                    s_item[1] = 0;
+                    s_item[2] = (a.n + 63) / 64;
+                }
+            } else {
+                s_item[0] = a.r_lo / kRows8 + blockIdx.x;
+                s_item[1] = a.c_lo / 64;
+                s_item[2] = (a.c_hi + 63) / 64;
+                s_item[3] = it == 0;
+            }
+        }
+        __syncthreads();
+        if (!s_item[3]) break;
+        const int rg = s_item[0], q0 = s_item[1], q1 = s_item[2];
+        __syncthreads();
+        const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
+        const int r0 = rg * kRows8;
+        if (warp == 0) {
+            const int r = r0 + lane;
+            const bool ok = lane < kRows8 && r >= rlo && r < rhi && !a.dense_group[r >> 5];
+            const int tr = ok ? a.tcount[r] : INT_MAX;
+            if (lane < kRows8) { s_rowT[lane] = tr; s_rowH[lane] = ok ? a.hinfo[r] : 0u; }
+            const unsigned okm = __ballot_sync(full, ok);
+            const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
+            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
+        }
+        uint4* P4 = reinterpret_cast<uint4*>(P8);
+        for (int i = threadIdx.x; i < 2 * kPlane8 / 8; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
+        __syncthreads();
+        uint32_t* P32 = reinterpret_cast<uint32_t*>(P8);
+        for (int b = warp; b < kRows8; b += kTileWarps) {
+            if (!((s_rows_ok >> b) & 1u)) continue;
+            const int r = r0 + b;
+            const uint32_t* src = a.ent + a.gstart[r >> 5];
+            const int T = s_rowT[b];
+            for (int e = lane; e < T; e += 32) {
+                const uint32_t idx = src[ent_at(e, r & 31)];
+                if (idx < 65536u) {
+                    // first occurrence: its plane word (H first)
+                    const uint32_t hw = idx >= 0x8000u ? idx - 0x8000u : (uint32_t)kPlane8 + idx;
+                    atomicOr(&P32[hw >> 1], (1u << b) << ((hw & 1u) * 16u));
+                } else {
+                    uint32_t h = hash_slot(idx);
+                    for (int probe = 0; probe < kHashSlots; ++probe) {
+                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
+                        if (old == kSentinel || old == idx) {
+                            atomicOr(&hmask[h], 1u << b);
+                            break;
+                        }
+                        h = (h + 1) & (kHashSlots - 1);
+                    }
+                    s_any_high = 1;
+                }
+            }
+        }
+        __syncthreads();
+        const bool any_high = s_any_high != 0;
+        const uint32_t rows_ok = s_rows_ok;
+        for (int q = max(q0, r0 / 64) + warp; q < q1; q += kTileWarps) {
+            const int gA = 2 * q, gB = 2 * q + 1;
+            const bool hasB = gB < a.ngroups;
+            const int cA = 64 * q + lane, cB = cA + 32;
+            const bool okA = cA >= a.c_lo && cA < a.c_hi && cA < a.n;
+            const bool okB = cB >= a.c_lo && cB < a.c_hi && cB < a.n;
+            const uint32_t vA = okA ? (half_mask(cA - r0) & rows_ok & 0xFFFFu) : 0u;
+            const uint32_t vB = okB ? (half_mask(cB - r0) & rows_ok & 0xFFFFu) : 0u;
+            const uint32_t vmask = vA | (vB << 16);
+            if (!__any_sync(full, vmask)) continue;
+            const uint4* epAH = reinterpret_cast<const uint4*>(a.tent + a.tstart[gA]) + lane;
+            const uint4* epAL = reinterpret_cast<const uint4*>(a.tent + a.tstart[gA] + 32LL * a.tgent[gA]) + lane;
+            const uint4* epBH = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB]) + lane : epAH;
+            const uint4* epBL = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB] + 32LL * a.tgent[gB]) + lane : epAL;
+            uint32_t XH[B], XL[B];
+            phase8<B>(P8, epAH, a.tgent[gA], epBH, hasB ? a.tgent[gB] : 0, XH);
+            phase8<B>(P8 + kPlane8, epAL, a.tgentL[gA], epBL, hasB ? a.tgentL[gB] : 0, XL);
+            if (any_high) {
+                // repeated occurrences (rank >= 1) lead each read's level list
+                const int nhA = okA ? a.nhigh[cA] : 0, nhB = okB ? a.nhigh[cB] : 0;
+                const int maxh = (int)__reduce_max_sync(full, (unsigned)max(nhA, nhB));
+                const uint32_t* rpA = a.ent + a.gstart[gA];
+                const uint32_t* rpB = hasB ? a.ent + a.gstart[gB] : rpA;
+                for (int j = 0; j < maxh; ++j) {
+                    uint32_t hH = 0, hL = 0;
+                    if (j < nhA) {
+                        const uint32_t key = __ldg(rpA + ent_at(j, lane));
+                        const uint32_t w = hash_find8(hkeys, hmask, key);
+                        if ((key & 0xFFFFu) >= 0x8000u) hH |= w; else hL |= w;
+                    }
+                    if (j < nhB) {
+                        const uint32_t key = __ldg(rpB + ent_at(j, lane));
+                        const uint32_t w = hash_find8(hkeys, hmask, key) << 16;
+                        if ((key & 0xFFFFu) >= 0x8000u) hH |= w; else hL |= w;
+                    }
+                    Counter<B>::add_at(XH, hH, 0);
+                    Counter<B>::add_at(XL, hL, 0);
+                }
+            }
+            // [same] per (row, column), then X = XH + (XL & same), bit-sliced
+            const uint32_t hA = okA ? a.hinfo[cA] : 0u, hB = okB ? a.hinfo[cB] : 0u;
+            uint32_t same = 0;
+#pragma unroll
+            for (int b = 0; b < kRows8; ++b) {
+                const uint32_t hr = s_rowH[b];
+                same |= (uint32_t)((hr == 0u && hA == 0u) || (hr != 0u && hr == hA)) << b;
+                same |= (uint32_t)((hr == 0u && hB == 0u) || (hr != 0u && hr == hB)) << (b + 16);
+            }
+            uint32_t X[B];
+            uint32_t carry = 0;
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                const uint32_t y = XL[k] & same;
+                X[k] = XH[k] ^ y ^ carry;
+                carry = (XH[k] & y) | (carry & (XH[k] ^ y));
+            }
+            // threshold: per half a lower bound of mmin, then exact per candidate
+            const int tcA = okA ? a.tcount[cA] : 0, tcB = okB ? a.tcount[cB] : 0;
+            const uint32_t loA = a.smin[min(s_tmin, tcA)], loB = a.smin[min(s_tmin, tcB)];
+            uint32_t cand = 0;
+            if (vmask && (loA < (1u << B) || loB < (1u << B))) {
+                const uint32_t okbits = (loA < (1u << B) ? 0xFFFFu : 0u) | (loB < (1u << B) ? 0xFFFF0000u : 0u);
+                uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+                for (int k = B - 1; k >= 0; --k) {
+                    const uint32_t bit = (((loA >> k) & 1u) ? 0xFFFFu : 0u) | (((loB >> k) & 1u) ? 0xFFFF0000u : 0u);
+                    gt |= eq & X[k] & ~bit;
+                    eq &= ~(X[k] ^ bit);
+                }
+                cand = (gt | eq) & vmask & okbits;
+            }
+            while (__any_sync(full, cand)) {
+                bool pass = false;
+                int r = 0, c = 0, m = 0, mn = 1;
+                if (cand) {
+                    const int bit = __ffs(cand) - 1;
+                    cand &= cand - 1;
+#pragma unroll
+                    for (int k = 0; k < B; ++k) m |= (int)((X[k] >> bit) & 1u) << k;
+                    r = r0 + (bit & 15);
+                    c = bit < 16 ? cA : cB;
+                    mn = min(s_rowT[bit & 15], bit < 16 ? tcA : tcB);
+                    pass = m >= (int)a.mmin[mn];
+                }
+                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Exact dense-table kernel: one row read per block with its full count
 // table (two 16-bit counts per word) in shared memory; one column per
 // thread walks its level entries (t, kmer) and counts [cnt_row[kmer] > t].
@@ -867,12 +1167,22 @@ int bits_for(uint64_t v) {
 
 // Dense level planes kept in shared memory for K (0: dense kernel only).
 int dense_levels_for(int K) {
-    if (K >= 8) return 0;
+    if (K >= 8) return 1;   // first occurrences in the two 16-bit planes of the K = 8 kernel
     const int per_level = (1 << (2 * K)) * 8;   // 64-bit words (64 row reads)
     return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
 
 using TileFn = void (*)(TileArgs);
+TileFn tile8_fn_for(int B) {
+    switch (B) {
+        case 8: return kmer_tile8_kernel<8>;
+        case 9: return kmer_tile8_kernel<9>;
+        case 10: return kmer_tile8_kernel<10>;
+        case 11: return kmer_tile8_kernel<11>;
+        default: return kmer_tile8_kernel<12>;
+    }
+}
+
 TileFn tile_fn_for(int B) {
     switch (B) {
         case 8: return kmer_tile_kernel<8>;
@@ -941,10 +1251,15 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 4) * 4));
     CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.hinfo, (size_t)n * 4));
-    CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 64));
+    CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 128));
     CRISPY_TRY(ensure(ctx, j.tstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.tgent, (size_t)j.ngroups * 4));
-    if (dense_levels_for(k) > 0) CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
+    if (k == 8) {
+        CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
+        CRISPY_TRY(ensure(ctx, j.nsec, (size_t)n * 8));
+    } else {
+        CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
+    }
     CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
@@ -980,11 +1295,45 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
                                               j.t.as<int32_t>(), n, k, dense_levels_for(k),
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
-                                              j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>());
+                                              j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>(),
+                                              k == 8 ? j.nsec.as<int32_t>() : nullptr);
     count_launch(ctx);
     CRISPY_CK(ctx, cudaGetLastError());
     const int levels = dense_levels_for(k);
-    if (levels > 0) {
+    if (k == 8) {
+        // stream layouts need the per-read H / L counts: one round trip
+        j.h_nsec.resize(2 * (size_t)n);
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_nsec.data(), j.nsec.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+        CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        std::vector<int32_t> tgl(j.ngroups, 0);
+        j.h_tstart.assign(j.ngroups + 1, 0);
+        j.h_tgent.assign(j.ngroups, 0);
+        for (int g = 0; g < j.ngroups; ++g) {
+            int mh = 0, ml = 0;
+            for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) {
+                mh = std::max(mh, j.h_nsec[2 * (size_t)r]);
+                ml = std::max(ml, j.h_nsec[2 * (size_t)r + 1]);
+            }
+            j.h_tgent[g] = (mh + (mh >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
+            tgl[g] = (ml + (ml >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
+            j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * (j.h_tgent[g] + tgl[g]);
+        }
+        j.ntent = j.h_tstart[j.ngroups];
+        CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                       cudaMemcpyHostToDevice, s));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
+                                       cudaMemcpyHostToDevice, s));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.tgentL.ptr, tgl.data(), (size_t)j.ngroups * 4,
+                                       cudaMemcpyHostToDevice, s));
+        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        kmer_sched8_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
+            j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
+            j.tgentL.as<int32_t>(), nhigh, j.nsec.as<int32_t>(), j.bcnt.as<uint16_t>(), n, j.ngroups,
+            j.tent.as<uint16_t>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+    } else if (levels > 0) {
         const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
         kmer_sched_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
@@ -1026,14 +1375,15 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     // Rows of 64-row groups whose high-level entries exceed the hash go to
     // the dense kernel (flags per 32-read group); K = 8 sends every group there.
     const int levels = dense_levels_for(K);
-    const int nrg = (n + kTileRows - 1) / kTileRows;
+    const int rows_blk = K == 8 ? kRows8 : kTileRows;   // row reads per tile block
+    const int nrg = (n + rows_blk - 1) / rows_blk;
     std::vector<uint8_t> dense(j.ngroups, 0);
     bool any_dense = false;
     for (int rg = 0; rg < nrg; ++rg) {
         int64_t high = 0;
-        for (int r = rg * kTileRows; r < std::min(n, rg * kTileRows + kTileRows); ++r) high += j.h_cntmax[n + r];
+        for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); ++r) high += j.h_cntmax[n + r];
         if (levels == 0 || high > kHashMaxKeys) {
-            for (int g = 2 * rg; g < std::min(j.ngroups, 2 * rg + 2); ++g) dense[g] = 1;
+            for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32) dense[r >> 5] = 1;
             any_dense = true;
         }
     }
@@ -1043,8 +1393,9 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
 
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
-    TileFn tile = tile_fn_for(B);
-    const size_t tsmem = fast ? ((size_t)levels * K4 + 32) * 8 : 0;   // planes + guard words
+    TileFn tile = K == 8 ? tile8_fn_for(B) : tile_fn_for(B);
+    const size_t tsmem = !fast ? 0 : K == 8 ? (size_t)2 * kPlane8 * 2     // two 16-bit planes + guards
+                                             : ((size_t)levels * K4 + 32) * 8;   // planes + guard words
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
@@ -1062,6 +1413,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
         ta.tent = j.tent.as<uint16_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
         ta.k65536 = 65536u; ta.k8 = 8u;
+        ta.tgentL = j.tgentL.as<int32_t>(); ta.hinfo = j.hinfo.as<uint32_t>(); ta.ngroups = j.ngroups;
         ta.nhigh = j.cntmax.as<int32_t>() + n;
         ta.tcount = j.t.as<int32_t>(); ta.dense_group = j.work.as<uint8_t>();
         ta.mmin = j.mmin.as<uint16_t>(); ta.smin = j.smin.as<uint16_t>();
@@ -1095,7 +1447,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     t2.r_lo = sx * A; t2.r_hi = std::min(n, sx * A + A);
                     t2.c_lo = sy * A; t2.c_hi = std::min(n, sy * A + A);
                     if (tiles) {
-                        const int rg0 = t2.r_lo / kTileRows, rg1 = (t2.r_hi - 1) / kTileRows;
+                        const int rg0 = t2.r_lo / rows_blk, rg1 = (t2.r_hi - 1) / rows_blk;
                         tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
@@ -1123,8 +1475,12 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             // (each with all its columns), longest first.
             std::vector<int> items;
             if (fast)
-                for (int rg = 0; rg < nrg; ++rg)
-                    if (!dense[2 * rg] || (2 * rg + 1 < j.ngroups && !dense[2 * rg + 1])) items.push_back(rg);
+                for (int rg = 0; rg < nrg; ++rg) {
+                    bool any_rows = false;
+                    for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32)
+                        any_rows |= !dense[r >> 5];
+                    if (any_rows) items.push_back(rg);
+                }
             if (!items.empty()) {
                 CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int) + 64));
                 int* d_items = j.sort_tmp.as<int>();
@@ -1147,7 +1503,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.gstart.ptr, (uint64_t)(uintptr_t)j.gent.ptr, (uint64_t)(uintptr_t)j.work.ptr,
                     (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)j.off.ptr, (uint64_t)(uintptr_t)j.hinfo.ptr,
                     (uint64_t)(uintptr_t)j.tent.ptr, (uint64_t)(uintptr_t)j.tstart.ptr, (uint64_t)(uintptr_t)j.tgent.ptr,
-                    (uint64_t)(uintptr_t)j.cntmax.ptr,
+                    (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
                     (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A});
                 ev_begin(ctx, ctx->ev_kmer, s);

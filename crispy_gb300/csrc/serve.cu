@@ -59,7 +59,7 @@ size_t estimate_bytes(const Job& j) {
     // level entries + the scheduled tile stream (spare steps per group) +
     // per-read bank counts
     const size_t groups = (size_t)(j.n + 31) / 32;
-    const size_t entries = (size_t)(2 * t + 32LL * (16 + 40) * groups) * 4 + (size_t)j.n * 64;
+    const size_t entries = (size_t)(2 * t + 32LL * (16 + 40) * groups) * 4 + (size_t)j.n * 136;
     const size_t survivors = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 24;
     const size_t gen = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 48 + reads;
     return 2 * reads + entries + survivors + gen + (8u << 20);

@@ -11,7 +11,7 @@ import argparse
 import crispy_gb300 as cg
 from crispy_gb300 import synth
 
-WORKLOADS = {"uneven_100k": (6, 10), "plain_20k": (6, 10), "small_1k": (6, 10)}
+WORKLOADS = {"uneven_100k": (6, 10), "plain_20k": (6, 10), "small_1k": (6, 10), "stress_500k": (8, 5)}
 
 
 def main():

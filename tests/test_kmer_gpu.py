@@ -104,3 +104,24 @@ def test_kmer_nonacgt(engine):
         s[80 + i % 20] = ord("a")
         mixed.append(bytes(s))
     _check(engine, synth.preprocess_order(mixed), 6, 0.4, cg.MODE_BATCHED)
+
+
+def test_kmer_k8_quirk_tiles(engine):
+    # K = 8 runs the 16-row tile kernel in the batched and staged forms: H / L
+    # halves of the signed-sort quirk, reads without H K-mers (only A/G, so
+    # [same] holds between two of them), repeated K-mers through the hash,
+    # uneven lengths across group edges
+    rng = np.random.default_rng(88)
+    base = _reads(900, 808, root=520, dist="uniform", a=200, b=500, cents=30, k=8)
+    ag = [bytes(rng.choice(np.frombuffer(b"AG", np.uint8), 150 + (i % 40)).astype(np.uint8).tobytes())
+          for i in range(40)]
+    rep = []
+    for i in range(40):
+        s = bytearray(base[i])
+        s[20:20 + 30 + i] = b"C" * (30 + i)
+        rep.append(bytes(s))
+    reads = synth.preprocess_order(base[40:] + ag + rep)
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    counts = [_check(engine, reads, 8, thr, mode)
+              for thr in (t, 0.7) for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
+    assert counts[0] == counts[1] == counts[2] and counts[3] == counts[4] == counts[5] > 0
