@@ -847,11 +847,15 @@ __device__ __forceinline__ void phase8(const uint16_t* __restrict__ plane, const
     Counter<B> cnt;
     cnt.clear();
     const int E = max(ea, eb);
+    // the next batch's entries are in flight while the current one is reduced
+    uint4 a0 = 0 < ea ? __ldg(epa) : guard, a1 = 0 < ea ? __ldg(epa + 32) : guard;
+    uint4 b0 = 0 < eb ? __ldg(epb) : guard, b1 = 0 < eb ? __ldg(epb + 32) : guard;
     for (int e = 0; e < E; e += 16) {
-        const int o = (e >> 3) * 32;
-        const uint4 a0 = e < ea ? __ldg(epa + o) : guard, a1 = e < ea ? __ldg(epa + o + 32) : guard;
-        const uint4 b0 = e < eb ? __ldg(epb + o) : guard, b1 = e < eb ? __ldg(epb + o + 32) : guard;
+        const int o = ((e + 16) >> 3) * 32;
+        const uint4 na0 = e + 16 < ea ? __ldg(epa + o) : guard, na1 = e + 16 < ea ? __ldg(epa + o + 32) : guard;
+        const uint4 nb0 = e + 16 < eb ? __ldg(epb + o) : guard, nb1 = e + 16 < eb ? __ldg(epb + o + 32) : guard;
         cnt.add_sixteens1(gather8_16<B>(plane, a0, a1, b0, b1, cnt));
+        a0 = na0; a1 = na1; b0 = nb0; b1 = nb1;
     }
     cnt.planes(X);
 }

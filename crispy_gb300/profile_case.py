@@ -1,6 +1,6 @@
 """One pass of the hot path on a named workload, for profiler captures.
 
-    python -m crispy_gb300.profile_case --workload uneven_100k [--stage kmer|gen|both]
+    python -m crispy_gb300.profile_case --workload uneven_100k [--stage kmer|gen|both] [--reads N]
 
 Reads are generated and uploaded first; then one batched kmerDist run and one
 batched genDist run over its survivors, nothing else.  Run it with
@@ -18,9 +18,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="uneven_100k", choices=sorted(WORKLOADS))
     ap.add_argument("--stage", default="both", choices=["kmer", "gen", "both"])
+    ap.add_argument("--reads", type=int, default=0, help="keep the first N reads (0: all)")
     args = ap.parse_args()
     k, band = WORKLOADS[args.workload]
     reads = synth.make_read_set(args.workload)
+    if args.reads:
+        reads = reads[:args.reads]
     buf, offs, lens = synth.pack_reads(reads)
     n = len(lens)
     with cg.Engine(0) as eng:
