@@ -46,7 +46,8 @@ class Stats(C.Structure):
                 ("total_ms", C.c_double), ("kmer_pairs", C.c_int64),
                 ("kmer_survivors", C.c_int64), ("gen_pairs", C.c_int64),
                 ("gen_cells", C.c_int64), ("gen_survivors", C.c_int64),
-                ("kernels_launched", C.c_int64), ("graph_launches", C.c_int64)]
+                ("kernels_launched", C.c_int64), ("graph_launches", C.c_int64),
+                ("kmer_spilled", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

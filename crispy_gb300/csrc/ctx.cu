@@ -232,14 +232,18 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
     KmerJob& k = ctx->kmer;
     for (DevBuf* b : {&k.seq, &k.off, &k.len, &k.t, &k.gstart, &k.gent, &k.ent, &k.cntmax,
                       &k.hinfo, &k.keys, &k.keys_alt, &k.vals, &k.vals_alt, &k.pairs, &k.dists,
-                      &k.counter, &k.mmin, &k.smin, &k.work, &k.sort_tmp})
+                      &k.counter, &k.mmin, &k.smin, &k.work, &k.sort_tmp, &k.tstart, &k.tgent,
+                      &k.tent, &k.bcnt, &k.tgentL, &k.nsec})
         release(ctx, *b);
+    release_host(k.h_spill_pairs);
+    release_host(k.h_spill_dists);
+    k.spilled = false;
     GenJob& g = ctx->gen;
     for (DevBuf* b : {&g.seq, &g.off, &g.len, &g.woff, &g.packed, &g.pairs, &g.dist, &g.score,
                       &g.ml, &g.al, &g.flags, &g.scan, &g.blocksum, &g.surv_idx, &g.keys,
                       &g.keys_alt, &g.vals, &g.vals_alt, &g.out_pairs, &g.out_dists, &g.order,
                       &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue, &g.cstats,
-                      &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt})
+                      &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt, &g.acc_pairs, &g.acc_dists})
         release(ctx, *b);
     k.ready = false;
     g.ready = false;

@@ -526,6 +526,26 @@ __global__ void gen_gather_kernel(const int2* __restrict__ pairs, const uint32_t
     out_dists[i] = __uint_as_float(keys[i]);
 }
 
+// Windowed runs: append one load window's survivors (pair, distance) to the
+// pending chunk, and key a pending chunk by its position for the stable sort.
+__global__ void gen_append_kernel(const int2* __restrict__ pairs, const float* __restrict__ dist,
+                                  const uint32_t* __restrict__ surv, int64_t base, int64_t count,
+                                  int2* __restrict__ acc_pairs, float* __restrict__ acc_dists) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t p = surv[base + i];
+    acc_pairs[i] = pairs[p];
+    acc_dists[i] = dist[p];
+}
+
+__global__ void gen_poskeys_kernel(const float* __restrict__ dist, int64_t count,
+                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    keys[i] = __float_as_uint(dist[i]);
+    vals[i] = (uint32_t)i;
+}
+
 // Band cells of one pair in O(1): rows i = 1..l2 hold columns
 // max(1, i-kb)..min(l1, i+kb), non-empty for i <= min(l2, l1 + kb).
 __host__ __device__ inline int64_t band_cells_of(int l1, int l2, int band) {
@@ -1069,6 +1089,110 @@ int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int 
     return CRISPY_OK;
 }
 
+// Load windows per batch of a windowed run (CRISPY_GEN_BATCH_WINDOWS
+// overrides, for tests).
+int64_t gen_batch_windows() {
+    if (const char* e = std::getenv("CRISPY_GEN_BATCH_WINDOWS")) {
+        const long long v = std::atoll(e);
+        if (v > 0) return v;
+    }
+    return 64;
+}
+
+// genDist over a host-resident pair list of any length, a batch of load
+// windows at a time.  The survivors of each window join a pending chunk on
+// the device, which is flushed (stably sorted by distance, sent to the sink)
+// once it reaches the window size -- the reference's rule
+// (genCUDA.cu:150-254) -- so chunks are those of a one-shot run, and the
+// device holds one batch plus at most two windows of survivors.
+int gen_run_windowed(crispy_ctx* ctx, cudaStream_t s, const int2* host_pairs, int64_t npairs, int band,
+                     int mode, float thr, crispy_sink sink, void* user, int64_t* nsurv) {
+    GenJob& g = ctx->gen;
+    const int64_t W = CRISPY_GEN_WINDOW;
+    const int64_t batch = gen_batch_windows() * W;
+    const int64_t bmax = std::min(batch, npairs);
+    CRISPY_TRY(ensure(ctx, g.pairs, (size_t)bmax * 8));
+    CRISPY_TRY(ensure(ctx, g.dist, (size_t)bmax * 4));
+    CRISPY_TRY(ensure(ctx, g.flags, (size_t)bmax));
+    CRISPY_TRY(ensure(ctx, g.surv_idx, (size_t)bmax * 4));
+    const int64_t ntiles_max = (bmax + kScanTile - 1) / kScanTile;
+    CRISPY_TRY(ensure(ctx, g.blocksum, (size_t)ntiles_max * 4));
+    CRISPY_TRY(ensure(ctx, g.acc_pairs, (size_t)2 * W * 8));
+    CRISPY_TRY(ensure(ctx, g.acc_dists, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure(ctx, g.keys, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure(ctx, g.keys_alt, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure(ctx, g.vals, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure(ctx, g.vals_alt, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure(ctx, g.out_pairs, (size_t)2 * W * 8));
+    CRISPY_TRY(ensure(ctx, g.out_dists, (size_t)2 * W * 4));
+    CRISPY_TRY(ensure_host(ctx, g.h_pairs, (size_t)2 * W * 8));
+    CRISPY_TRY(ensure_host(ctx, g.h_dists, (size_t)2 * W * 4));
+    int64_t pending = 0, total = 0;
+    int chunk = 0;
+    auto flush = [&]() -> int {
+        const int64_t c = pending;
+        const unsigned blocks = (unsigned)((c + 255) / 256);
+        gen_poskeys_kernel<<<blocks, 256, 0, s>>>(g.acc_dists.as<float>(), c, g.keys.as<uint32_t>(),
+                                                 g.vals.as<uint32_t>());
+        count_launch(ctx);
+        uint32_t *sk = nullptr, *sv = nullptr;
+        CRISPY_TRY(ensure(ctx, g.scan, sort_tmp_bytes(c)));
+        CRISPY_TRY(sort_u32_payload(ctx, s, g.keys.as<uint32_t>(), g.keys_alt.as<uint32_t>(), g.vals.as<uint32_t>(),
+                                    g.vals_alt.as<uint32_t>(), c, 32, &sk, &sv, g.scan));
+        gen_gather_kernel<<<blocks, 256, 0, s>>>(g.acc_pairs.as<int2>(), sk, sv, c, g.out_pairs.as<uint2>(),
+                                                g.out_dists.as<float>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+        if (sink) {
+            CRISPY_CK(ctx, cudaMemcpyAsync(g.h_pairs.ptr, g.out_pairs.ptr, (size_t)c * 8, cudaMemcpyDeviceToHost, s));
+            CRISPY_CK(ctx, cudaMemcpyAsync(g.h_dists.ptr, g.out_dists.ptr, (size_t)c * 4, cudaMemcpyDeviceToHost, s));
+            CRISPY_CK(ctx, cudaStreamSynchronize(s));
+            if (sink(user, chunk, g.h_pairs.ptr, g.h_dists.as<float>(), c) != 0)
+                return fail(ctx, CRISPY_E_IO, "sink aborted at chunk %d", chunk);
+        }
+        ++chunk;
+        pending = 0;
+        return CRISPY_OK;
+    };
+    for (int64_t b0 = 0; b0 < npairs; b0 += batch) {
+        const int64_t nb = std::min(batch, npairs - b0);
+        CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, host_pairs + b0, (size_t)nb * 8, cudaMemcpyHostToDevice, s));
+        CRISPY_TRY(gen_dispatch_impl(ctx, s, g.pairs.as<int2>(), nb, band, mode, g.dist.as<float>(), nullptr,
+                                     nullptr, nullptr));
+        gen_flag_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(g.dist.as<float>(), nb, thr,
+                                                                    g.flags.as<uint8_t>());
+        count_launch(ctx);
+        int64_t nsb = 0;
+        CRISPY_TRY(compact_flags(ctx, s, g.flags.as<uint8_t>(), nb, g.surv_idx.as<uint32_t>(),
+                                 g.blocksum.as<uint32_t>(), g.scan, &nsb));
+        const int64_t ntiles = (nb + kScanTile - 1) / kScanTile;
+        std::vector<uint32_t> tile_counts(ntiles);
+        CRISPY_CK(ctx, cudaMemcpyAsync(tile_counts.data(), g.blocksum.ptr, (size_t)ntiles * 4,
+                                       cudaMemcpyDeviceToHost, s));
+        CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        const int64_t tiles_per_window = W / kScanTile;
+        int64_t base = 0;
+        for (int64_t t0 = 0; t0 < ntiles; t0 += tiles_per_window) {
+            int64_t cw = 0;
+            for (int64_t t = t0; t < std::min(ntiles, t0 + tiles_per_window); ++t) cw += tile_counts[t];
+            if (cw > 0) {
+                gen_append_kernel<<<(unsigned)((cw + 255) / 256), 256, 0, s>>>(
+                    g.pairs.as<int2>(), g.dist.as<float>(), g.surv_idx.as<uint32_t>(), base, cw,
+                    g.acc_pairs.as<int2>() + pending, g.acc_dists.as<float>() + pending);
+                count_launch(ctx);
+                pending += cw;
+                base += cw;
+                total += cw;
+            }
+            if (pending >= W) CRISPY_TRY(flush());
+        }
+    }
+    if (pending > 0) CRISPY_TRY(flush());
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    *nsurv = total;
+    return CRISPY_OK;
+}
+
 int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int band, float thr,
                    int mode, crispy_sink sink, void* user, int64_t* nsurvivors) {
     if (!ctx) return CRISPY_E_INPUT;
@@ -1083,7 +1207,11 @@ int crispy_gen_run(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int ba
     ctx->ev_gen.used = 0;
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
     int64_t ns = 0;
-    if (npairs > 0) {
+    if (npairs > gen_batch_windows() * CRISPY_GEN_WINDOW) {
+        // longer than one batch of load windows: bounded device memory
+        CRISPY_TRY(gen_run_windowed(ctx, s, reinterpret_cast<const int2*>(pairs), npairs, band, mode, thr, sink,
+                                    user, &ns));
+    } else if (npairs > 0) {
         CRISPY_TRY(ensure(ctx, g.pairs, (size_t)npairs * 8));
         CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
         CRISPY_CK(ctx, cudaMemcpyAsync(g.pairs.ptr, pairs, (size_t)npairs * 8, cudaMemcpyHostToDevice, s));
@@ -1145,7 +1273,11 @@ int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, cri
     ctx->ev_gen.used = 0;
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
     int64_t ns = 0;
-    if (npairs > 0) {
+    if (k.spilled) {
+        // the k-mer survivors sit in pinned host memory: windowed run
+        CRISPY_TRY(gen_run_windowed(ctx, s, k.h_spill_pairs.as<int2>(), npairs, band, mode, thr, sink, user,
+                                    &ns));
+    } else if (npairs > 0) {
         CRISPY_TRY(ensure(ctx, g.dist, (size_t)npairs * 4));
         CRISPY_TRY(gen_dispatch_impl(ctx, s, k.pairs.as<int2>(), npairs, band, mode, g.dist.as<float>(),
                                      nullptr, nullptr, nullptr));

@@ -45,9 +45,12 @@ struct KmerJob {
     DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
     DevBuf tgentL, nsec;             // K = 8: L-stream steps per group; per-read H/L counts
     std::vector<int32_t> h_nsec;
-    // last run's survivors, in stage order
+    // last run's survivors, in stage order: on the device, or (spilled) in
+    // pinned host memory when they outgrow the device share
     int64_t nsurv = 0;
     bool have_dists = false;
+    bool spilled = false;
+    HostBuf h_spill_pairs, h_spill_dists;
     DevBuf keys, keys_alt, vals, vals_alt, pairs, dists, counter, mmin, smin, work;
     DevBuf sort_tmp;
 };
@@ -61,7 +64,7 @@ struct GenJob {
     DevBuf seq, off, len, woff, packed;
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
         vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue,
-        cstats, ckeys, ckeys_alt, cvals, cvals_alt;
+        cstats, ckeys, ckeys_alt, cvals, cvals_alt, acc_pairs, acc_dists;
     HostBuf h_pairs, h_dists;
 };
 

@@ -43,6 +43,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 
@@ -1176,6 +1177,18 @@ int dense_levels_for(int K) {
     return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
 
+// Survivors a k-mer pass may keep on the device (CRISPY_KMER_DEVICE_PAIRS
+// overrides, for tests): an eighth of the free memory at 40 bytes each.
+int64_t kmer_device_pair_cap() {
+    if (const char* e = std::getenv("CRISPY_KMER_DEVICE_PAIRS")) {
+        const long long v = std::atoll(e);
+        if (v > 0) return v;
+    }
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1LL << 26;
+    return std::max<int64_t>(1LL << 22, (int64_t)(free_b / 8 / 40));
+}
+
 using TileFn = void (*)(TileArgs);
 TileFn tile8_fn_for(int B) {
     switch (B) {
@@ -1404,8 +1417,9 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
-    int64_t cap = std::max<int64_t>(j.keys.bytes / 8, std::max<int64_t>(1 << 20, 16LL * n));
-    for (int attempt = 0; attempt < 3; ++attempt) {
+    // One pass over the rows [rlo, rhi) and all their columns: survivors
+    // (up to cap) as sort keys in j.keys / j.vals, their count in *total.
+    auto run_pass = [&](int rlo, int rhi, int64_t cap, int64_t* total_out) -> int {
         CRISPY_TRY(ensure(ctx, j.keys, (size_t)cap * 8));
         CRISPY_TRY(ensure(ctx, j.keys_alt, (size_t)cap * 8));
         CRISPY_TRY(ensure(ctx, j.vals, (size_t)cap * 4));
@@ -1444,7 +1458,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             for (auto& ss : ctx->side) CRISPY_CK(ctx, cudaStreamWaitEvent(ss, fork, 0));
             ev_begin(ctx, ctx->ev_kmer, s);
             int64_t st = 0;
-            for (int sx = 0; sx < sd; ++sx) {
+            for (int sx = rlo / A; sx * A < rhi; ++sx) {
                 for (int sy = sx; sy < sd; ++sy, ++st) {
                     cudaStream_t ss = ctx->side[st % 8];
                     TileArgs t2 = ta;
@@ -1473,13 +1487,13 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             }
             ev_end(ctx, ctx->ev_kmer, s);
             cudaEventDestroy(fork);
-            ctx->stats.kmer_launches += nstages;
+            ctx->stats.kmer_launches += st;
         } else {
             // Batched: one persistent launch over a work queue of row groups
             // (each with all its columns), longest first.
             std::vector<int> items;
             if (fast)
-                for (int rg = 0; rg < nrg; ++rg) {
+                for (int rg = rlo / rows_blk; rg * rows_blk < rhi; ++rg) {
                     bool any_rows = false;
                     for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32)
                         any_rows |= !dense[r >> 5];
@@ -1500,7 +1514,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 per_sm = std::max(1, per_sm);
                 const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)items.size());
                 DenseArgs d2 = da;
-                d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
+                d2.r_lo = rlo; d2.r_hi = rhi; d2.c_lo = 0; d2.c_hi = n;
                 const std::string key = "kmain," + key_of({(uint64_t)(uintptr_t)j.ent.ptr, (uint64_t)(uintptr_t)j.keys.ptr,
                     (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.counter.ptr, (uint64_t)(uintptr_t)d_items,
                     (uint64_t)(uintptr_t)j.mmin.ptr, (uint64_t)(uintptr_t)j.smin.ptr, (uint64_t)(uintptr_t)j.t.ptr,
@@ -1509,7 +1523,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.tent.ptr, (uint64_t)(uintptr_t)j.tstart.ptr, (uint64_t)(uintptr_t)j.tgent.ptr,
                     (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
-                    (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A});
+                    (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A,
+                    (uint64_t)rlo, (uint64_t)rhi});
                 ev_begin(ctx, ctx->ev_kmer, s);
                 CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
@@ -1517,7 +1532,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     tile<<<grid, kTileThreads, tsmem, s>>>(t2);
                     count_launch(ctx);
                     if (any_dense) {
-                        kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
+                        kmer_dense_kernel<<<std::min(rhi - rlo, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
                         count_launch(ctx);
                     }
                     CRISPY_CK(ctx, cudaGetLastError());
@@ -1527,8 +1542,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 ctx->stats.kmer_launches += 1;
             } else if (any_dense) {
                 DenseArgs d2 = da;
-                d2.r_lo = 0; d2.r_hi = n; d2.c_lo = 0; d2.c_hi = n;
-                kmer_dense_kernel<<<std::min(n, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
+                d2.r_lo = rlo; d2.r_hi = rhi; d2.c_lo = 0; d2.c_hi = n;
+                kmer_dense_kernel<<<std::min(rhi - rlo, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
                 count_launch(ctx);
             }
         }
@@ -1536,18 +1551,11 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         unsigned long long total = 0;
         CRISPY_CK(ctx, cudaMemcpyAsync(&total, j.counter.ptr, 8, cudaMemcpyDeviceToHost, s));
         CRISPY_CK(ctx, cudaStreamSynchronize(s));
-        if ((int64_t)total <= cap) {
-            j.nsurv = (int64_t)total;
-            break;
-        }
-        cap = (int64_t)total + total / 8 + 1024;
-        if (attempt == 2) return fail(ctx, CRISPY_E_STATE, "survivor buffer did not converge");
-    }
+        *total_out = (int64_t)total;
+        return CRISPY_OK;
+    };
     // stable order: (stage, row, col)
     const int key_bits = bits_for((uint64_t)nstages * (uint64_t)n * (uint64_t)n);
-    CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));
-    CRISPY_TRY(ensure(ctx, j.dists, (size_t)std::max<int64_t>(j.nsurv, 1) * 4));
-    CRISPY_TRY(ensure(ctx, j.sort_tmp, sort_tmp_bytes(j.nsurv)));
     auto sort_decode = [&]() -> int {
         uint64_t* sk = nullptr;
         uint32_t* sv = nullptr;
@@ -1562,14 +1570,81 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         }
         return CRISPY_OK;
     };
-    if (mode == CRISPY_MODE_BATCHED && j.nsurv > 0) {
-        const std::string key = "ksort," + key_of({(uint64_t)j.nsurv, (uint64_t)key_bits, (uint64_t)dists,
-            (uint64_t)n, (uint64_t)(uintptr_t)j.keys.ptr, (uint64_t)(uintptr_t)j.keys_alt.ptr,
-            (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.vals_alt.ptr,
-            (uint64_t)(uintptr_t)j.sort_tmp.ptr, (uint64_t)(uintptr_t)j.pairs.ptr, (uint64_t)(uintptr_t)j.dists.ptr});
-        CRISPY_TRY(graph_run(ctx, s, key, sort_decode));
+    // sort + decode the j.nsurv keys of the last pass into j.pairs / j.dists
+    auto finish_pass = [&]() -> int {
+        CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));
+        CRISPY_TRY(ensure(ctx, j.dists, (size_t)std::max<int64_t>(j.nsurv, 1) * 4));
+        CRISPY_TRY(ensure(ctx, j.sort_tmp, sort_tmp_bytes(j.nsurv)));
+        if (mode == CRISPY_MODE_BATCHED && j.nsurv > 0) {
+            const std::string key = "ksort," + key_of({(uint64_t)j.nsurv, (uint64_t)key_bits, (uint64_t)dists,
+                (uint64_t)n, (uint64_t)(uintptr_t)j.keys.ptr, (uint64_t)(uintptr_t)j.keys_alt.ptr,
+                (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.vals_alt.ptr,
+                (uint64_t)(uintptr_t)j.sort_tmp.ptr, (uint64_t)(uintptr_t)j.pairs.ptr, (uint64_t)(uintptr_t)j.dists.ptr});
+            return graph_run(ctx, s, key, sort_decode);
+        }
+        return sort_decode();
+    };
+
+    // Survivors held on the device at once: about 40 bytes each while sorted
+    // (keys, values, their sort copies, pairs, distances).
+    const int64_t dev_cap = kmer_device_pair_cap();
+    int64_t cap = std::min(dev_cap, std::max<int64_t>(j.keys.bytes / 8, std::max<int64_t>(1 << 20, 16LL * n)));
+    int64_t total = 0;
+    j.spilled = false;
+    CRISPY_TRY(run_pass(0, n, cap, &total));
+    if (total > cap && total <= dev_cap) {
+        cap = std::min(dev_cap, total + total / 8 + 1024);
+        CRISPY_TRY(run_pass(0, n, cap, &total));
+        if (total > cap) return fail(ctx, CRISPY_E_STATE, "survivor count changed between passes");
+    }
+    if (total <= cap) {
+        j.nsurv = total;
+        CRISPY_TRY(finish_pass());
     } else {
-        CRISPY_TRY(sort_decode());
+        // Spill: the survivors outgrow the device share.  Stage rows are
+        // processed in ranges whose survivors fit; stage order is row-major
+        // over stage rows, so each range's sorted pairs append in order to
+        // one pinned host list (the count is known from the first pass).
+        if (A % rows_blk != 0) return fail(ctx, CRISPY_E_OOM, "survivor list exceeds the device share");
+        CRISPY_TRY(ensure_host(ctx, j.h_spill_pairs, (size_t)total * 8));
+        if (dists) CRISPY_TRY(ensure_host(ctx, j.h_spill_dists, (size_t)total * 4));
+        // expected survivors per stage row, proportional to its pairs
+        std::vector<double> est(sd);
+        const double per_pair = (double)total / ((double)n * (double)(n - 1) / 2.0);
+        for (int sx = 0; sx < sd; ++sx) {
+            const double r0 = sx * (double)A, r1 = std::min<double>(n, r0 + A);
+            est[sx] = per_pair * ((r1 - r0) * (n - 1) - (r1 * (r1 - 1) - r0 * (r0 - 1)) / 2.0);
+        }
+        int64_t off = 0;
+        for (int sx = 0; sx < sd;) {
+            int sx1 = sx + 1;
+            double acc = est[sx];
+            while (sx1 < sd && acc + est[sx1] <= 0.5 * (double)dev_cap) acc += est[sx1++];
+            int64_t t = 0;
+            CRISPY_TRY(run_pass(sx * A, std::min(n, sx1 * A), dev_cap, &t));
+            if (t > dev_cap) {
+                if (sx1 - sx == 1) return fail(ctx, CRISPY_E_OOM, "one stage row's survivors exceed the device share");
+                for (int q = sx; q < sx1; ++q) est[q] *= 2.0;   // denser than estimated: smaller ranges
+                continue;
+            }
+            if (off + t > total) return fail(ctx, CRISPY_E_STATE, "survivor count changed between passes");
+            j.nsurv = t;
+            CRISPY_TRY(finish_pass());
+            if (t > 0) {
+                CRISPY_CK(ctx, cudaMemcpyAsync(j.h_spill_pairs.as<char>() + off * 8, j.pairs.ptr, (size_t)t * 8,
+                                               cudaMemcpyDeviceToHost, s));
+                if (dists)
+                    CRISPY_CK(ctx, cudaMemcpyAsync(j.h_spill_dists.as<char>() + off * 4, j.dists.ptr,
+                                                   (size_t)t * 4, cudaMemcpyDeviceToHost, s));
+                CRISPY_CK(ctx, cudaStreamSynchronize(s));
+            }
+            off += t;
+            sx = sx1;
+        }
+        if (off != total) return fail(ctx, CRISPY_E_STATE, "survivor count changed between passes");
+        j.nsurv = total;
+        j.spilled = true;
+        ctx->stats.kmer_spilled = 1;
     }
     j.have_dists = dists != 0;
     CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
@@ -1590,6 +1665,12 @@ int crispy_kmer_fetch(crispy_ctx* ctx, int32_t* pairs, float* dists, int64_t cap
     if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_fetch before kmer_run");
     if (dists && !j.have_dists) return fail(ctx, CRISPY_E_STATE, "distances were not kept by kmer_run");
     const int64_t c = std::min(cap, j.nsurv);
+    if (j.spilled) {
+        if (c > 0 && pairs) std::memcpy(pairs, j.h_spill_pairs.ptr, (size_t)c * 8);
+        if (c > 0 && dists) std::memcpy(dists, j.h_spill_dists.ptr, (size_t)c * 4);
+        if (count) *count = c;
+        return CRISPY_OK;
+    }
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     if (c > 0 && pairs)
@@ -1606,6 +1687,15 @@ int crispy_kmer_stream(crispy_ctx* ctx, crispy_sink sink, void* user) {
     KmerJob& j = ctx->kmer;
     if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_stream before kmer_run");
     const int64_t batch = 1 << 20;
+    if (j.spilled) {   // already in host memory
+        for (int64_t at = 0; at < j.nsurv; at += batch) {
+            const int64_t c = std::min(batch, j.nsurv - at);
+            const float* d = j.have_dists ? j.h_spill_dists.as<float>() + at : nullptr;
+            if (sink(user, 0, j.h_spill_pairs.as<char>() + at * 8, d, c) != 0)
+                return fail(ctx, CRISPY_E_IO, "sink aborted");
+        }
+        return CRISPY_OK;
+    }
     std::vector<int32_t> p((size_t)std::min(batch, std::max<int64_t>(j.nsurv, 1)) * 2);
     std::vector<float> d(j.have_dists ? p.size() / 2 : 0);
     cudaStream_t s = ctx->stream;

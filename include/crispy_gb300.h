@@ -210,6 +210,8 @@ typedef struct crispy_stats {
     int64_t gen_survivors;
     int64_t kernels_launched;  /* every kernel this library launched in the last run */
     int64_t graph_launches;    /* CUDA graph replays among them (batched form) */
+    int64_t kmer_spilled;      /* 1 when the last kmer run's survivors outgrew the device
+                                  share and were gathered in pinned host memory */
 } crispy_stats;
 int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */
