@@ -319,7 +319,7 @@ __device__ __forceinline__ void unpack_mlal(uint32_t l, int ij, int* ml, int* al
 // One pair per G-lane sub-group (32/G pairs per warp), C band slots per
 // lane, so a pair with kBand + 1 <= G*C slots fits.
 template <int G, int C>
-__global__ void __launch_bounds__(kGenThreads, 3) gen_warp_kernel(GenArgs a) {
+__global__ void __launch_bounds__(kGenThreads, C <= 3 ? 3 : (C <= 5 ? 2 : 1)) gen_warp_kernel(GenArgs a) {
     constexpr int kPerWarp = 32 / G;
     __shared__ uint32_t smem[kGenWarps][kPerWarp][2][kSmWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -567,18 +567,21 @@ struct Shape {
     int g, c;
 };
 constexpr Shape kShapes[] = {{8, 1},  {8, 2},  {8, 4},  {16, 1}, {16, 2}, {16, 3}, {16, 4},
-                             {16, 6}, {32, 1}, {32, 2}, {32, 3}, {32, 4}, {32, 6}, {32, 8}};
+                             {16, 6}, {32, 1}, {32, 2}, {32, 3}, {32, 4}, {32, 6}, {32, 8},
+                             {8, 5},  {8, 7},  {16, 5}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-// Pairs are binned by band slots; bin 0 is the wide-band kernel.
-constexpr int kBinSlots[] = {0, 8, 16, 32, 48, 64, 96, 128, 192, 256};
+// Pairs are binned by band slots; bin 0 is the wide-band kernel.  Bins are
+// fine where bands are common (kBand 31-79 at band 10 on 300-800 nt reads)
+// so that few slots of a pair sit outside its band.
+constexpr int kBinSlots[] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256};
 constexpr int kNumBins = sizeof(kBinSlots) / sizeof(kBinSlots[0]);
-__constant__ int c_bin_slots[kNumBins] = {0, 8, 16, 32, 48, 64, 96, 128, 192, 256};
+__constant__ int c_bin_slots[kNumBins] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256};
 
 // Per-pair classification for the launch plan, on the device: band-slot
 // bin (wide last), a sort key (bin, then longer pairs first), band cells,
 // the widest band, per-bin counts and the widest bin of each load window.
-// stats: [0] cells, [1] max kBand, [2 + b] pairs of order-bin b (1..10),
+// stats: [0] cells, [1] max kBand, [2 + b] pairs of order-bin b (1..13),
 // [16 + w] widest order-bin of window w.
 constexpr int kStatBins = 2, kStatWindows = 16;
 __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t count,
@@ -621,7 +624,8 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
         atomicMax(&stats[kStatWindows + win], (unsigned long long)obw);
 }
 // untuned shape per bin (the plain form always uses it)
-constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 5, 6, 7, 11, 12, 13};
+constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 14, 5, 15, 6, 16, 7, 11, 12, 13};
+static_assert(kStatBins + kNumBins < kStatWindows, "per-bin counters overlap the window slots");
 
 using WarpFn = void (*)(GenArgs);
 WarpFn shape_fn(int shape) {
@@ -639,7 +643,10 @@ WarpFn shape_fn(int shape) {
         case 10: return gen_warp_kernel<32, 3>;
         case 11: return gen_warp_kernel<32, 4>;
         case 12: return gen_warp_kernel<32, 6>;
-        default: return gen_warp_kernel<32, 8>;
+        case 13: return gen_warp_kernel<32, 8>;
+        case 14: return gen_warp_kernel<8, 5>;
+        case 15: return gen_warp_kernel<8, 7>;
+        default: return gen_warp_kernel<16, 5>;
     }
 }
 

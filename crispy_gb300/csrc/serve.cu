@@ -108,7 +108,7 @@ struct crispy_server {
         const float kt = crispy_default_threshold(j->n, j->kthr, 0);
         const float gt = crispy_default_threshold(j->n, j->gthr, 1);
         if (rc == CRISPY_OK) rc = crispy_kmer_run(c, kt, CRISPY_MODE_BATCHED, 0, &j->kmer_pairs);
-        if (rc == CRISPY_OK) rc = crispy_gen_prepare(c, j->bases.data(), j->off.data(), j->len.data(), j->n);
+        if (rc == CRISPY_OK) rc = crispy_gen_prepare_from_kmer(c);   // reads already on the device
         int64_t ns = 0;
         if (rc == CRISPY_OK)
             rc = crispy_gen_run_from_kmer(c, j->band, gt, CRISPY_MODE_BATCHED, sink_to_job, j, &ns);
