@@ -182,11 +182,16 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
-        for (int p = threadIdx.x; p < T; p += blockDim.x) {
-            const uint32_t v = kmer_at(s, p, K);
-            const int c = (int)((hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu);
-            mx = max(mx, c);
-            if (v >= 0x8000u) hm = max(hm, v);
+#pragma unroll
+        for (int k = 0; k < kPrepPer; ++k) {
+            // this thread's positions are those of the first pass: reuse their K-mers
+            const int p = threadIdx.x + k * kPrepThreads;
+            if (p < T) {
+                const uint32_t v = val[k] & (K4 - 1u);
+                const int c = (int)((hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu);
+                mx = max(mx, c);
+                if (v >= 0x8000u) hm = max(hm, v);
+            }
         }
         atomicMax(&s_max, mx);
         atomicMax(&s_hmax, hm);
@@ -202,7 +207,9 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
             hinfo[r] = info;
         }
         __syncthreads();
-        for (int p = threadIdx.x; p < T; p += blockDim.x) hist[kmer_at(s, p, K) >> 1] = 0;
+#pragma unroll
+        for (int k = 0; k < kPrepPer; ++k)
+            if (threadIdx.x + k * kPrepThreads < T) hist[(val[k] & (K4 - 1u)) >> 1] = 0;
         __syncthreads();
     }
 }

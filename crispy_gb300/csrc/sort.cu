@@ -46,43 +46,63 @@ __global__ void __launch_bounds__(kSortThreads) rs_hist(const K* __restrict__ ke
 }
 
 // Exclusive scan of m uint32 values in place with one block; writes the sum
-// to *total when total != nullptr.
+// to *total when total != nullptr.  The block walks the array in tiles of
+// 4096 values (four consecutive values per thread, coalesced), carrying the
+// running sum from tile to tile.
 __global__ void __launch_bounds__(1024) scan_exclusive_1blk(uint32_t* __restrict__ v, int64_t m,
                                                             uint32_t* __restrict__ total) {
     __shared__ uint32_t wsum[32];
+    __shared__ uint32_t s_carry;
     const int t = threadIdx.x;
-    const int64_t per = (m + 1023) / 1024;
-    const int64_t lo = t * per, hi = lo + per < m ? lo + per : m;
-    uint32_t s = 0;
-    for (int64_t i = lo; i < hi; ++i) s += v[i];
-    // block-wide exclusive scan of s
-    uint32_t x = s;
     const int lane = t & 31, w = t >> 5;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[w] = x;
+    if (t == 0) s_carry = 0;
     __syncthreads();
-    if (w == 0) {
-        uint32_t z = wsum[lane];
+    const bool vec = (reinterpret_cast<uintptr_t>(v) & 15u) == 0;
+    for (int64_t base = 0; base < m; base += 4096) {
+        const int64_t i0 = base + 4 * (int64_t)t;
+        uint32_t a[4];
+        if (vec && i0 + 3 < m) {
+            const uint4 q = *reinterpret_cast<const uint4*>(v + i0);
+            a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) a[k] = i0 + k < m ? v[i0 + k] : 0u;
+        }
+        const uint32_t sum = a[0] + a[1] + a[2] + a[3];
+        uint32_t x = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
-            if (lane >= o) z += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        wsum[lane] = z;
+        if (lane == 31) wsum[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t z = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z;
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        uint32_t run = carry + x - sum + (w > 0 ? wsum[w - 1] : 0u);
+        uint32_t out[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { out[k] = run; run += a[k]; }
+        if (vec && i0 + 3 < m) {
+            *reinterpret_cast<uint4*>(v + i0) = make_uint4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) if (i0 + k < m) v[i0 + k] = out[k];
+        }
+        __syncthreads();   // every thread has read s_carry and wsum
+        if (t == 1023) s_carry = carry + wsum[31];
+        __syncthreads();
     }
-    __syncthreads();
-    uint32_t excl = x - s + (w > 0 ? wsum[w - 1] : 0u);
-    if (t == 1023 && total) *total = excl + s;
-    uint32_t run = excl;
-    for (int64_t i = lo; i < hi; ++i) {
-        uint32_t c = v[i];
-        v[i] = run;
-        run += c;
-    }
+    if (t == 0 && total) *total = s_carry;
 }
 
 template <class K, bool kVals>
