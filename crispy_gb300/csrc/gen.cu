@@ -256,7 +256,7 @@ template <int G, int C, int kMode>
 __device__ __forceinline__ void block_steps(Lane<C>& st, int gl, int s0, const PairCtx& pc,
                                             Best& col, Best& row) {
     const int dbase = 2 * gl * C - pc.kb;
-    if (kMode != kClean) {
+    if constexpr (kMode != kClean) {
         // the rarer border and tracking blocks: a two-step body that always
         // tests field 0 keeps their code small (instruction fetch)
 #pragma unroll 1
@@ -266,18 +266,18 @@ __device__ __forceinline__ void block_steps(Lane<C>& st, int gl, int s0, const P
 #pragma unroll
             for (int c = 0; c < C; ++c) { st.x0[c] <<= 2; st.x1[c] <<= 2; }
         }
-        return;
-    }
+    } else {
 #pragma unroll 1
-    for (int t = 0; t < kBlockSteps; t += 6) {
-        step<G, C, 0, 0, kMode>(st, gl, s0 + t, dbase, pc, col, row);
-        step<G, C, 1, 0, kMode>(st, gl, s0 + t + 1, dbase, pc, col, row);
-        step<G, C, 0, 1, kMode>(st, gl, s0 + t + 2, dbase, pc, col, row);
-        step<G, C, 1, 1, kMode>(st, gl, s0 + t + 3, dbase, pc, col, row);
-        step<G, C, 0, 2, kMode>(st, gl, s0 + t + 4, dbase, pc, col, row);
-        step<G, C, 1, 2, kMode>(st, gl, s0 + t + 5, dbase, pc, col, row);
+        for (int t = 0; t < kBlockSteps; t += 6) {
+            step<G, C, 0, 0, kMode>(st, gl, s0 + t, dbase, pc, col, row);
+            step<G, C, 1, 0, kMode>(st, gl, s0 + t + 1, dbase, pc, col, row);
+            step<G, C, 0, 1, kMode>(st, gl, s0 + t + 2, dbase, pc, col, row);
+            step<G, C, 1, 1, kMode>(st, gl, s0 + t + 3, dbase, pc, col, row);
+            step<G, C, 0, 2, kMode>(st, gl, s0 + t + 4, dbase, pc, col, row);
+            step<G, C, 1, 2, kMode>(st, gl, s0 + t + 5, dbase, pc, col, row);
 #pragma unroll
-        for (int c = 0; c < C; ++c) { st.x0[c] <<= 6; st.x1[c] <<= 6; }
+            for (int c = 0; c < C; ++c) { st.x0[c] <<= 6; st.x1[c] <<= 6; }
+        }
     }
 }
 
