@@ -2,7 +2,7 @@
 
 Everything is compiled in-tree for sm_103a only:
     crispy_gb300/lib/libcrispy_gb300.so
-    crispy_gb300/bin/kmerDist, crispy_gb300/bin/genDist
+    crispy_gb300/bin/kmerDist, crispy_gb300/bin/genDist, crispy_gb300/bin/crispyDist
 Translation units compile in parallel; nothing here needs cmake.
 """
 from __future__ import annotations
@@ -27,7 +27,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
 CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu"]
 CXX_SOURCES = ["fasta.cpp"]
-CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp"}
+CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp"}
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -98,3 +98,62 @@ def test_cli_errors(tmp_path):
     r = subprocess.run([os.path.join(BIN, "genDist"), "-i", fa], stdout=subprocess.PIPE,
                        stderr=subprocess.STDOUT)
     assert r.returncode != 0   # no .kpair next to it
+
+
+def _run(args, cwd=None, mode="batched"):
+    r = subprocess.run(args, env=_env(mode), stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       cwd=cwd)
+    assert r.returncode == 0, r.stdout
+    return r.stdout
+
+
+def _outputs(base):
+    d = os.path.dirname(base)
+    stem = os.path.basename(base)
+    return {f[len(stem):]: open(os.path.join(d, f), "rb").read()
+            for f in sorted(os.listdir(d)) if f.startswith(stem + ".")}
+
+
+def _fused_vs_two(tmp_path, src, k, band, mode):
+    a, b = tmp_path / "two", tmp_path / "fused"
+    a.mkdir(); b.mkdir()
+    fa, fb = str(a / "reads_Clean"), str(b / "reads_Clean")
+    shutil.copy(src, fa)
+    shutil.copy(src, fb)
+    _run([os.path.join(BIN, "kmerDist"), "-i", fa, "-k", str(k), "-d"], mode=mode)
+    _run([os.path.join(BIN, "genDist"), "-i", fa, "-b", str(band)], mode=mode)
+    out = _run([os.path.join(BIN, "crispyDist"), "-i", fb, "-k", str(k), "-b", str(band), "-p", "-d"], mode=mode)
+    want, got = _outputs(fa), _outputs(fb)
+    assert sorted(got) == sorted(want) and ".npair_0" in got
+    for ext in want:
+        assert got[ext] == want[ext], f"{ext} differs"
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(MANIFEST["sets"]))
+@pytest.mark.parametrize("mode", ["batched", "plain"])
+def test_crispydist_matches_two_programs(tmp_path, name, mode):
+    # one process, survivors handed over in HBM: the same files as kmerDist -d
+    # followed by genDist
+    s = MANIFEST["sets"][name]
+    src = os.path.join(GOLD, name, name + "_Clean")
+    _fused_vs_two(tmp_path, src, s["kmer"][0]["k"], s["gen"][0]["band"], mode)
+
+
+def test_crispydist_reads_parsed_differently(tmp_path):
+    # trailing N: kmerDist trims it, genDist keeps it, so the fused tool
+    # uploads genDist's own parse instead of reusing the k-mer stage's reads
+    rng = np.random.default_rng(5)
+    base = "".join(rng.choice(list("ACGT"), 240))
+    lines = []
+    for i in range(60):
+        s = list(base)
+        for p in rng.integers(0, 240, 6):
+            s[p] = rng.choice(list("ACGT"))
+        seq = "".join(s)[: 200 + i % 30]
+        if i % 7 == 0:
+            seq += "NN"
+        lines.append(f">r{i}\n{seq}\n")
+    src = str(tmp_path / "src_Clean")
+    open(src, "w").write("".join(lines))
+    _fused_vs_two(tmp_path, src, 6, 10, "batched")
