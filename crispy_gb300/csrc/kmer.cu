@@ -247,6 +247,10 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int k) {   // 0-based; -1
 }
 
 // One tile stream of one 32-read group (warp w of the block, lane = read).
+// A gather of kB-bucket words is served per set of kB lanes (a wavefront);
+// word w sits in bucket w mod kB.
+//   kB = 8:  128-bit plane words, 8 quad banks per quarter-warp; bucket b
+//            draws on the raw bank groups b, b + 8, b + 16, b + 24.
 //   kB = 16: 64-bit plane words, 16 double banks per half-warp; bucket b
 //            draws on the raw bank groups b and b + 16 (value mod 32).
 //   kB = 32: 16-bit plane words, 32 four-byte banks over the whole warp;
@@ -267,9 +271,10 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
                              int pos0, int Et, const uint32_t* __restrict__ src, uint32_t vsub,
                              uint32_t guard0, uint16_t* __restrict__ dst_group) {
     const unsigned full = 0xffffffffu;
-    constexpr unsigned kMask = kB == 32 ? 0xffffffffu : 0xFFFFu;
-    const int hs = kB == 32 ? 0 : (lane & 16);          // this half's bit offset in 32-bit masks
-    const unsigned half_lt = ((1u << lane) - 1u) & (kB == 32 ? 0xffffffffu : (0xFFFFu << hs));
+    constexpr unsigned kMask = kB == 32 ? 0xffffffffu : (1u << kB) - 1u;
+    constexpr int kSub = 32 / kB;                         // raw groups per bucket
+    const int hs = lane & (32 - kB);                      // this lane set's bit offset in 32-bit masks
+    const unsigned half_lt = ((1u << lane) - 1u) & (kMask << hs);
     for (int b = 0; b < 32; ++b) sm.left[w][lane][b] = active ? raw_cnt[b] : (uint16_t)0;
     // first raw position of each raw group: the prep kernel's lane-rotated order
     for (int i = 0, pos = pos0; i < 32; ++i) {
@@ -280,7 +285,9 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
     int D = 0;
     unsigned ovmask = 0;
     for (int b = 0; b < kB; ++b) {
-        const int c = kB == 32 ? sm.left[w][lane][b] : sm.left[w][lane][b] + sm.left[w][lane][b + 16];
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < kSub; ++i) c += sm.left[w][lane][b + i * kB];
         const int o = (b - lane) & (kB - 1);
         const int slots = Et > o ? (Et - o + kB - 1) / kB : 0;
         const int ov = max(0, c - slots);
@@ -342,7 +349,8 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
         for (int i = 0; i < kSchedChunk; ++i) {
             const int b = sm.bank[w][i][lane];
             if (b < kB) {
-                const int bb = (kB == 32 || sm.left[w][lane][b]) ? b : b + 16;
+                int bb = b;   // first raw group of the bucket with entries left
+                for (int q = 1; q < kSub && !sm.left[w][lane][bb]; ++q) bb = b + q * kB;
                 const int p = sm.next[w][lane][bb];
                 sm.next[w][lane][bb] = (uint16_t)(p + 1);
                 sm.left[w][lane][bb] = (uint16_t)(sm.left[w][lane][bb] - 1);
@@ -354,8 +362,8 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
 #pragma unroll
         for (int i = 0; i < kSchedChunk; ++i) {
             const uint32_t x = v[i];
-            // guard of bucket b: word guard0 + b (64-bit words, double bank b)
-            // or halfword guard0 + 2b (16-bit words, 4-byte bank b)
+            // guard of bucket b: word guard0 + b (128- or 64-bit words, bucket
+            // b) or halfword guard0 + 2b (16-bit words, 4-byte bank b)
             v[i] = (x & 0x80000000u) ? guard0 + (x & 31u) * (kB == 32 ? 2u : 1u)
                                      : __ldg(src + ent_at((int)x, lane)) - vsub;
         }
@@ -373,7 +381,9 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
     }
 }
 
-// K <= 7: one 16-bucket stream per group (64-bit plane words).
+// K <= 7: one stream per group; kB = 8 for 128-bit plane words (K <= 6),
+// 16 for 64-bit plane words (K = 7).
+template <int kB>
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
     const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
@@ -384,7 +394,7 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
     for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
         const int r = g * 32 + lane;
         const bool active = r < n;
-        sched_stream<16>(sm, w, lane, active, bcnt + (int64_t)(active ? r : 0) * 32,
+        sched_stream<kB>(sm, w, lane, active, bcnt + (int64_t)(active ? r : 0) * 32,
                          active ? nhigh[r] : 0, tgent[g], ent + gstart[g], 0u, guard_word,
                          tent + tstart[g]);
     }
@@ -535,6 +545,24 @@ struct Counter {
         csa(foursB, twos, twosA, twosB);
         csa(eightsB, fours, foursA, foursB);
         csa(c16, eights, eightsA, eightsB);
+        return c16;
+    }
+    // add 8 words; returns the carry out of the fours level (weight 8)
+    __device__ __forceinline__ uint32_t add8(const uint32_t* w) {
+        uint32_t twosA, twosB, foursA, foursB, c8;
+        csa(twosA, ones, w[0], w[1]);
+        csa(twosB, ones, w[2], w[3]);
+        csa(foursA, twos, twosA, twosB);
+        csa(twosA, ones, w[4], w[5]);
+        csa(twosB, ones, w[6], w[7]);
+        csa(foursB, twos, twosA, twosB);
+        csa(c8, fours, foursA, foursB);
+        return c8;
+    }
+    // two 8-word carries into the eights level; returns the weight-16 carry
+    __device__ __forceinline__ uint32_t merge_eights(uint32_t a, uint32_t b) {
+        uint32_t c16;
+        csa(c16, eights, a, b);
         return c16;
     }
     __device__ __forceinline__ void carry32(uint32_t carry) {
@@ -799,6 +827,225 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile_kernel(TileArgs a) 
         __syncthreads();
         tile_columns<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok[0], s_rows_ok[1],
                         s_tmin[0], s_tmin[1], s_rowT, max(cg0, 2 * rg), cg1);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 128-row tile kernel (K <= 6).  The same algorithm with 128-bit plane words:
+// one 16-byte shared load answers a column entry for 128 row reads, four
+// 32-row words that feed four sets of bit-sliced counters.  A warp's 16-byte
+// gather is served per quarter-warp, so the stream's schedule spreads the
+// 8 lanes of a quarter over 8 quad banks (word mod 8).  Per row pair this
+// halves the entry stream again and lowers the gather wavefronts against
+// 64-row words (correlated reads spread better over fewer, larger buckets);
+// the price is two dense levels at K = 6 (128 KB), the rarer third and later
+// occurrences going to the hash.
+// ---------------------------------------------------------------------------
+constexpr int kRows128 = 128;
+
+// 8 scheduled entries (one uint4 of 16-bit word indices): their 16-byte plane
+// words, split into the four 32-row words, into the four counters.
+template <int B>
+__device__ __forceinline__ void gather8_128(const char* __restrict__ Pb, uint4 q, uint32_t k65536,
+                                            uint32_t k16, Counter<B>* cnt, uint32_t* c8) {
+    const uint32_t x[4] = {q.x, q.y, q.z, q.w};
+    uint32_t w0[8], w1[8], w2[8], w3[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t ih = __umulhi(x[k], k65536);   // x >> 16
+        const uint32_t il = x[k] - ih * k65536;       // x & 0xFFFF
+        const uint4 p0 = *reinterpret_cast<const uint4*>(Pb + il * k16);
+        const uint4 p1 = *reinterpret_cast<const uint4*>(Pb + ih * k16);
+        w0[2 * k] = p0.x; w1[2 * k] = p0.y; w2[2 * k] = p0.z; w3[2 * k] = p0.w;
+        w0[2 * k + 1] = p1.x; w1[2 * k + 1] = p1.y; w2[2 * k + 1] = p1.z; w3[2 * k + 1] = p1.w;
+    }
+    c8[0] = cnt[0].add8(w0);
+    c8[1] = cnt[1].add8(w1);
+    c8[2] = cnt[2].add8(w2);
+    c8[3] = cnt[3].add8(w3);
+}
+
+// 16 entries (two uint4): the four weight-16 carries
+template <int B>
+__device__ __forceinline__ void gather16_128(const char* __restrict__ Pb, uint4 q0, uint4 q1,
+                                             uint32_t k65536, uint32_t k16, Counter<B>* cnt,
+                                             uint32_t* c16) {
+    uint32_t a8[4], b8[4];
+    gather8_128<B>(Pb, q0, k65536, k16, cnt, a8);
+    gather8_128<B>(Pb, q1, k65536, k16, cnt, b8);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) c16[p] = cnt[p].merge_eights(a8[p], b8[p]);
+}
+
+__device__ __noinline__ uint4 hash_find4(const uint32_t* hkeys, const uint4* hmask, uint32_t key) {
+    uint32_t h = hash_slot(key);
+    for (int probe = 0; probe < kHashSlots; ++probe) {
+        const uint32_t k = hkeys[h];
+        if (k == key) return hmask[h];
+        if (k == kSentinel) return make_uint4(0u, 0u, 0u, 0u);
+        h = (h + 1) & (kHashSlots - 1);
+    }
+    return make_uint4(0u, 0u, 0u, 0u);
+}
+
+template <int B>
+__device__ void tile_columns128(const TileArgs& a, const uint4* __restrict__ P,
+                                const uint32_t* hkeys, const uint4* hmask, bool any_high, int rg,
+                                const uint32_t* s_rows_ok, const int* s_tmin, const int* s_rowT,
+                                int cg0, int cg1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = rg * kRows128;
+    const char* __restrict__ Pb = reinterpret_cast<const char*>(P);
+    for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
+        const int c = cg * 32 + lane;
+        const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
+        uint32_t vm[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) vm[q] = col_ok ? half_mask(c - r0 - 32 * q) & s_rows_ok[q] : 0u;
+        if (!__any_sync(0xffffffffu, vm[0] | vm[1] | vm[2] | vm[3])) continue;
+        const int E = a.tgent[cg];
+        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[cg]) + lane;
+        Counter<B> cnt[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cnt[q].clear();
+        // 32 entries per iteration as two 16-entry batches, each gathered as
+        // two halves of 8 (register budget); the next batch is in flight
+        uint4 a0, a1;
+        if (E > 0) { a0 = __ldg(ep); a1 = __ldg(ep + 32); }
+        for (int e = 0; e < E; e += 32) {
+            const bool two = e + 16 < E;
+            uint4 b0, b1;
+            if (two) {
+                b0 = __ldg(ep + ((e + 16) >> 3) * 32);
+                b1 = __ldg(ep + ((e + 16) >> 3) * 32 + 32);
+            }
+            uint32_t ca[4];
+            gather16_128<B>(Pb, a0, a1, a.k65536, a.k8 * 2u, cnt, ca);
+            if (e + 32 < E) {
+                a0 = __ldg(ep + ((e + 32) >> 3) * 32);
+                a1 = __ldg(ep + ((e + 32) >> 3) * 32 + 32);
+            }
+            if (two) {
+                uint32_t cb[4];
+                gather16_128<B>(Pb, b0, b1, a.k65536, a.k8 * 2u, cnt, cb);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cnt[q].add_sixteens2(ca[q], cb[q]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cnt[q].add_sixteens1(ca[q]);
+            }
+        }
+        uint32_t X[4][B];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cnt[q].planes(X[q]);
+        // rank >= levels: the hash (the entries lead each read's level list)
+        if (any_high) {
+            const int nh = col_ok ? a.nhigh[c] : 0;
+            const int maxh = (int)__reduce_max_sync(0xffffffffu, (unsigned)nh);
+            const uint32_t* __restrict__ rp = a.ent + a.gstart[cg];
+            for (int j = 0; j < maxh; ++j) {
+                const uint4 w = j < nh ? hash_find4(hkeys, hmask, __ldg(rp + ent_at(j, lane)))
+                                       : make_uint4(0u, 0u, 0u, 0u);
+                Counter<B>::add_at(X[0], w.x, 0);
+                Counter<B>::add_at(X[1], w.y, 0);
+                Counter<B>::add_at(X[2], w.z, 0);
+                Counter<B>::add_at(X[3], w.w, 0);
+            }
+        }
+        const int tc = col_ok ? a.tcount[c] : 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            finish_half<B>(a, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs a) {
+    extern __shared__ __align__(16) uint4 P128[];   // levels * K4 plane words + 32 guard words
+    uint4* P = P128;
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint4 hmask[kHashSlots];
+    __shared__ int s_rowT[kRows128];
+    __shared__ int s_item[4];
+    __shared__ int s_tmin[4], s_any_high;
+    __shared__ uint32_t s_rows_ok[4];
+    const bool queued = a.items != nullptr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            if (queued) {
+                const unsigned w = atomicAdd(a.queue_head, 1u);
+                s_item[3] = (int)w < a.nitems;
+                if (s_item[3]) {
+                    s_item[0] = a.items[w];
+                    s_item[1] = 0;
+                    s_item[2] = (a.n + 31) / 32;
+                }
+            } else {
+                s_item[0] = a.r_lo / kRows128 + blockIdx.x;
+                s_item[1] = a.c_lo / 32;
+                s_item[2] = (a.c_hi + 31) / 32;
+                s_item[3] = it == 0;
+            }
+        }
+        __syncthreads();
+        if (!s_item[3]) break;
+        const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
+        __syncthreads();   // every thread has read s_item
+        const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
+        // ---- row group set-up: rows of dense 32-read groups are left to
+        // kmer_dense_kernel ----
+        if (warp < 4) {
+            const int r = rg * kRows128 + warp * 32 + lane;
+            const bool ok = r >= rlo && r < rhi && !a.dense_group[r >> 5];
+            const int tr = ok ? a.tcount[r] : INT_MAX;
+            s_rowT[warp * 32 + lane] = tr;
+            const unsigned okm = __ballot_sync(0xffffffffu, ok);
+            const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
+            if (lane == 0) { s_tmin[warp] = tm; s_rows_ok[warp] = okm; }
+            if (warp == 0 && lane == 0) s_any_high = 0;
+        }
+        const int words = a.levels * (int)a.K4;   // + 32 zero guard words after the planes
+        for (int i = threadIdx.x; i < words + 32; i += kTileThreads) P[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) {
+            hkeys[i] = kSentinel;
+            hmask[i] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
+        uint32_t* Pw = reinterpret_cast<uint32_t*>(P);
+        uint32_t* hmw = reinterpret_cast<uint32_t*>(hmask);
+        const uint32_t limit = (uint32_t)words;
+        for (int b = warp; b < kRows128; b += kTileWarps) {
+            if (!((s_rows_ok[b >> 5] >> (b & 31)) & 1u)) continue;
+            const int r = rg * kRows128 + b;
+            const uint32_t* src = a.ent + a.gstart[r >> 5];
+            const int T = s_rowT[b];
+            const uint32_t bit = 1u << (b & 31);
+            const int quarter = b >> 5;
+            for (int e = lane; e < T; e += 32) {
+                const uint32_t idx = src[ent_at(e, r & 31)];
+                if (idx < limit) {
+                    atomicOr(&Pw[4 * idx + quarter], bit);
+                } else {
+                    // high-level entry: open addressing; the host guarantees
+                    // the group holds at most kHashMaxKeys of them
+                    uint32_t h = hash_slot(idx);
+                    for (int probe = 0; probe < kHashSlots; ++probe) {
+                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
+                        if (old == kSentinel || old == idx) {
+                            atomicOr(&hmw[4 * h + quarter], bit);
+                            break;
+                        }
+                        h = (h + 1) & (kHashSlots - 1);
+                    }
+                    s_any_high = 1;
+                }
+            }
+        }
+        __syncthreads();
+        tile_columns128<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
+                           max(cg0, 4 * rg), cg1);
         __syncthreads();
     }
 }
@@ -1178,9 +1425,13 @@ int bits_for(uint64_t v) {
 }
 
 // Dense level planes kept in shared memory for K (0: dense kernel only).
+// Row reads per tile block: 128-bit plane words for K <= 6, 64-bit for
+// K = 7 (one 16,384-word level fills the budget), 16-bit for K = 8.
+int tile_rows_for(int K) { return K == 8 ? kRows8 : K == 7 ? kTileRows : kRows128; }
+
 int dense_levels_for(int K) {
     if (K >= 8) return 1;   // first occurrences in the two 16-bit planes of the K = 8 kernel
-    const int per_level = (1 << (2 * K)) * 8;   // 64-bit words (64 row reads)
+    const int per_level = (1 << (2 * K)) * (tile_rows_for(K) / 8);   // bytes of one level's words
     return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
 
@@ -1204,6 +1455,16 @@ TileFn tile8_fn_for(int B) {
         case 10: return kmer_tile8_kernel<10>;
         case 11: return kmer_tile8_kernel<11>;
         default: return kmer_tile8_kernel<12>;
+    }
+}
+
+TileFn tile128_fn_for(int B) {
+    switch (B) {
+        case 8: return kmer_tile128_kernel<8>;
+        case 9: return kmer_tile128_kernel<9>;
+        case 10: return kmer_tile128_kernel<10>;
+        case 11: return kmer_tile128_kernel<11>;
+        default: return kmer_tile128_kernel<12>;
     }
 }
 
@@ -1359,7 +1620,8 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
         CRISPY_CK(ctx, cudaGetLastError());
     } else if (levels > 0) {
         const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
-        kmer_sched_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
+        auto sched = tile_rows_for(k) == kRows128 ? kmer_sched_kernel<8> : kmer_sched_kernel<16>;
+        sched<<<sgrid, kSchedWarps * 32, 0, s>>>(
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
             nhigh, j.bcnt.as<uint16_t>(), n, j.ngroups, (uint32_t)levels * (1u << (2 * k)),
             j.tent.as<uint16_t>());
@@ -1399,7 +1661,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     // Rows of 64-row groups whose high-level entries exceed the hash go to
     // the dense kernel (flags per 32-read group); K = 8 sends every group there.
     const int levels = dense_levels_for(K);
-    const int rows_blk = K == 8 ? kRows8 : kTileRows;   // row reads per tile block
+    const int rows_blk = tile_rows_for(K);   // row reads per tile block
     const int nrg = (n + rows_blk - 1) / rows_blk;
     std::vector<uint8_t> dense(j.ngroups, 0);
     bool any_dense = false;
@@ -1417,9 +1679,9 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
 
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
-    TileFn tile = K == 8 ? tile8_fn_for(B) : tile_fn_for(B);
+    TileFn tile = K == 8 ? tile8_fn_for(B) : rows_blk == kRows128 ? tile128_fn_for(B) : tile_fn_for(B);
     const size_t tsmem = !fast ? 0 : K == 8 ? (size_t)2 * kPlane8 * 2     // two 16-bit planes + guards
-                                             : ((size_t)levels * K4 + 32) * 8;   // planes + guard words
+                                             : ((size_t)levels * K4 + 32) * (rows_blk / 8);   // planes + guards
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
