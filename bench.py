@@ -322,7 +322,9 @@ def run_ours(args, dist, ws, rank, local):
 
     kmer_ops = n_pairs * 2 * mean_t            # frozen: (Ta + Tb) per pair
     gen_ops = cells * 10                        # frozen: 10 per band cell
-    roof_k = {"kernel": "kmer_tile_kernel", "bound": "int32", "unit": "Gop/s",
+    tile_kernel = ("kmer_tile8_kernel" if k == 8 else "kmer_tile_kernel" if k == 7
+                   else "kmer_tile128_kernel")
+    roof_k = {"kernel": tile_kernel, "bound": "int32", "unit": "Gop/s",
               "achieved": kmer_ops / kmer_s / 1e9, "peak": int_peak_gops,
               "frac": kmer_ops / kmer_s / 1e9 / int_peak_gops,
               "work_per_unit": f"{2*mean_t:.1f} ops per k-mer pair", "traffic": None,

@@ -983,10 +983,14 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
                     s_item[2] = (a.n + 31) / 32;
                 }
             } else {
+                // one row group per x block; the stage's column groups are
+                // split evenly over the y blocks
+                const int cga = a.c_lo / 32, cgb = (a.c_hi + 31) / 32;
+                const int per = (cgb - cga + (int)gridDim.y - 1) / (int)gridDim.y;
                 s_item[0] = a.r_lo / kRows128 + blockIdx.x;
-                s_item[1] = a.c_lo / 32;
-                s_item[2] = (a.c_hi + 31) / 32;
-                s_item[3] = it == 0;
+                s_item[1] = cga + (int)blockIdx.y * per;
+                s_item[2] = min(cgb, s_item[1] + per);
+                s_item[3] = it == 0 && s_item[1] < s_item[2];
             }
         }
         __syncthreads();
@@ -1734,8 +1738,11 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     t2.r_lo = sx * A; t2.r_hi = std::min(n, sx * A + A);
                     t2.c_lo = sy * A; t2.c_hi = std::min(n, sy * A + A);
                     if (tiles) {
+                        // 128-row blocks split each stage's columns in two, which
+                        // keeps as many blocks per stage as 64-row blocks give
                         const int rg0 = t2.r_lo / rows_blk, rg1 = (t2.r_hi - 1) / rows_blk;
-                        tile<<<rg1 - rg0 + 1, kTileThreads, tsmem, ss>>>(t2);
+                        const dim3 grid(rg1 - rg0 + 1, rows_blk == kRows128 ? 2 : 1);
+                        tile<<<grid, kTileThreads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
                     if (dense_all || any_dense) {
