@@ -374,6 +374,8 @@ def run_ours(args, dist, ws, rank, local):
     line["autotune"] = tune
     if not args.no_serve:
         line["serve"] = serve_bench(args, local)
+    if rank == 0 and not args.no_pre:
+        line["preprocess"] = preprocess_bench(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as td:
             kpps, gcups, cores, desc, _ = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
@@ -383,6 +385,60 @@ def run_ours(args, dist, ws, rank, local):
                                 "note": "extrapolated to the full workload from the sample rates"}
     eng.close()
     return line
+
+
+def preprocess_bench(args, local: int) -> dict:
+    """preprocess (the step before kmerDist) on the workload's raw reads.
+
+    The raw FASTA is the generator's reads before deduplication, 60 columns
+    per line.  Timed per run: the record parse on the host
+    (crispy_raw_load), crispy_preprocess on the GPU (upload, filters, sort,
+    duplicate merge, download of the kept order) and the _Clean / .frq
+    writer; against the oracle's single-threaded restatement of the
+    reference (std::list-style stable sort of strings, fprintf output) on
+    the same file.  Both outputs are compared byte for byte.
+    """
+    import crispy_gb300 as cg
+    import oracle
+
+    reads = synth.generate(synth.WORKLOADS[WORKLOADS[args.workload][0]])
+    out = {"input_reads": len(reads)}
+    with tempfile.TemporaryDirectory() as td:
+        raw_path = os.path.join(td, "raw.fa")
+        with open(raw_path, "wb") as f:
+            for i, s in enumerate(reads):
+                f.write(b">read_%d synthetic\n" % i)
+                for a in range(0, len(s), 60):
+                    f.write(s[a:a + 60] + b"\n")
+        out["input_bytes"] = os.path.getsize(raw_path)
+        eng = cg.Engine(local)
+        times = []
+        for it in range(4):
+            t0 = time.perf_counter()
+            raw = cg.RawReads(raw_path)
+            t1 = time.perf_counter()
+            idx, freq, st = eng.preprocess(raw)
+            t2 = time.perf_counter()
+            raw.write(idx, freq, os.path.join(td, "gpu_Clean"))
+            t3 = time.perf_counter()
+            raw.close()
+            if it:   # the first run is the warm-up
+                times.append((t1 - t0, t2 - t1, t3 - t2, t3 - t0))
+        eng.close()
+        parse_s, dev_s, write_s, e2e_s = (float(np.mean(x)) for x in zip(*times))
+        t0 = time.perf_counter()
+        c = oracle.preprocess(raw_path, os.path.join(td, "cpu_Clean"))
+        cpu_s = time.perf_counter() - t0
+        same = all(open(os.path.join(td, "gpu_Clean" + e), "rb").read() ==
+                   open(os.path.join(td, "cpu_Clean" + e), "rb").read() for e in ("", ".frq"))
+    out.update({"kept_reads": int(st["kept"]), "merges": int(st["merges"]),
+                "e2e_ms": e2e_s * 1e3, "parse_ms": parse_s * 1e3,
+                "device_ms": dev_s * 1e3, "write_ms": write_s * 1e3,
+                "reads_per_s": len(reads) / e2e_s,
+                "cpu_baseline": {"ms": cpu_s * 1e3, "cores": 1, "kind": "port",
+                                 "sample": "the whole raw file"},
+                "outputs_identical": bool(same and c["kept"] == st["kept"])})
+    return out
 
 
 def serve_bench(args, local: int) -> dict:
@@ -520,6 +576,7 @@ def main():
     ap.add_argument("--cpu-sample-reads", type=int, default=_env_int("CRISPY_CPU_SAMPLE", 6000))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-pre", action="store_true")
     ap.add_argument("--serve-jobs", type=int, default=60)
     ap.add_argument("--serve-slots", type=int, default=4)
     args = ap.parse_args()

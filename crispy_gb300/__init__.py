@@ -56,6 +56,21 @@ class Stats(C.Structure):
 _P = C.c_void_p
 _i64p = C.POINTER(C.c_int64)
 
+
+class PreOpts(C.Structure):
+    _fields_ = [("length_check", C.c_int), ("sd_allowed", C.c_double), ("primer", C.c_char_p),
+                ("max_mismatches", C.c_int)]
+
+
+class PreStats(C.Structure):
+    _fields_ = [("length_discards", C.c_int32), ("primer_discards", C.c_int32),
+                ("merges", C.c_int32), ("kept", C.c_int32), ("length_reads", C.c_int32),
+                ("min_len0", C.c_int32), ("max_len0", C.c_int32), ("min_len", C.c_int32),
+                ("max_len", C.c_int32), ("ave_len", C.c_double), ("sd", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
 # name -> (restype, argtypes); exactly the declarations of include/crispy_gb300.h
 PROTOTYPES = {
     "crispy_version": (C.c_char_p, []),
@@ -82,6 +97,17 @@ PROTOTYPES = {
     "crispy_gen_align": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P]),
     "crispy_gen_align_noalloc": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_int,
                                            _P, _P, _P, _P, _P]),
+    "crispy_raw_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+    "crispy_raw_view": (C.c_int, [_P, C.POINTER(C.c_char_p), C.POINTER(_i64p),
+                                  C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.POINTER(C.c_uint8)),
+                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "crispy_raw_label": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_int32)]),
+    "crispy_raw_free": (None, [_P]),
+    "crispy_preprocess": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.POINTER(PreOpts), _P, _P,
+                                    C.POINTER(PreStats)]),
+    "crispy_pre_write": (C.c_int, [_P, _P, _P, C.c_int32, C.c_char_p, C.c_int]),
+    "crispy_kmer_prepare_from_pre": (C.c_int, [_P, _P, C.c_int]),
+    "crispy_gen_prepare_from_pre": (C.c_int, [_P, _P]),
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -167,6 +193,64 @@ def _ptr(a: np.ndarray | None) -> int | None:
     return None if a is None else a.ctypes.data
 
 
+class RawReads:
+    """Records of a raw FASTA / FASTQ file as preprocess's readFile collects
+    them (crispy_raw_load); the handle owns the memory."""
+
+    def __init__(self, path: str, fastq: bool = False):
+        self.lib = load_library()
+        self.fastq = bool(fastq)
+        h = _P()
+        rc = self.lib.crispy_raw_load(path.encode(), 1 if fastq else 0, C.byref(h))
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(None).decode())
+        self.h = h
+        buf = C.c_char_p()
+        off = _i64p()
+        ln = C.POINTER(C.c_int32)()
+        fr = C.POINTER(C.c_uint8)()
+        n = C.c_int32()
+        rec = C.c_int32()
+        self.lib.crispy_raw_view(h, C.byref(buf), C.byref(off), C.byref(ln), C.byref(fr), C.byref(n),
+                                 C.byref(rec))
+        self.n, self.records = n.value, rec.value
+        # views into the handle's memory (valid while it lives)
+        self._buf_addr = C.cast(buf, C.c_void_p).value
+        self.offsets = np.ctypeslib.as_array(off, shape=(self.n,)) if self.n else np.zeros(0, np.int64)
+        self.lengths = np.ctypeslib.as_array(ln, shape=(self.n,)) if self.n else np.zeros(0, np.int32)
+        self.freq = np.ctypeslib.as_array(fr, shape=(self.n,)) if self.n else np.zeros(0, np.uint8)
+
+    def seq(self, i: int) -> bytes:
+        return C.string_at(self._buf_addr + int(self.offsets[i]), int(self.lengths[i]))
+
+    def label(self, i: int) -> bytes:
+        p = C.c_char_p()
+        n = C.c_int32()
+        rc = self.lib.crispy_raw_label(self.h, i, C.byref(p), C.byref(n))
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(None).decode())
+        return C.string_at(C.cast(p, C.c_void_p).value, n.value) if n.value else b""
+
+    def write(self, index: np.ndarray, freq: np.ndarray, out_path: str):
+        index = np.ascontiguousarray(index, dtype=np.int32)
+        freq = np.ascontiguousarray(freq, dtype=np.int32)
+        rc = self.lib.crispy_pre_write(self.h, _ptr(index), _ptr(freq), len(index), out_path.encode(),
+                                       1 if self.fastq else 0)
+        if rc != OK:
+            raise CrispyError(rc, self.lib.crispy_last_error(None).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.crispy_raw_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Engine:
     """One context on one GPU (the C ABI's crispy_ctx)."""
 
@@ -250,6 +334,29 @@ class Engine:
         got = C.c_int64()
         self._check(self.lib.crispy_kmer_fetch(self.h, _ptr(pairs), _ptr(d), count, C.byref(got)))
         return pairs[:got.value], (d[:got.value] if dists else None)
+
+    # ---- preprocess ----
+    def preprocess(self, raw: "RawReads", sd: float | None = None, primer: bytes | None = None,
+                   max_mm: int = 2):
+        """Filters and duplicate merge on the device (crispy_preprocess).
+        Returns (record index, merged frequency, stats dict) in _Clean order."""
+        n = raw.n
+        index = np.empty(max(n, 1), np.int32)
+        freq = np.empty(max(n, 1), np.int32)
+        opts = PreOpts(1 if sd is not None else 0, float(sd if sd is not None else 1.0), primer, int(max_mm))
+        st = PreStats()
+        self._check(self.lib.crispy_preprocess(self.h, raw._buf_addr, _ptr(raw.offsets), _ptr(raw.lengths),
+                                               _ptr(raw.freq), n, C.byref(opts), _ptr(index), _ptr(freq),
+                                               C.byref(st)))
+        k = st.kept
+        return index[:k].copy(), freq[:k].copy(), st.as_dict()
+
+    def kmer_prepare_from_pre(self, raw: "RawReads", k: int = 6):
+        """kmer_prepare on the reads the last preprocess kept (no file, no upload)."""
+        self._check(self.lib.crispy_kmer_prepare_from_pre(self.h, raw.h, k))
+
+    def gen_prepare_from_pre(self, raw: "RawReads"):
+        self._check(self.lib.crispy_gen_prepare_from_pre(self.h, raw.h))
 
     # ---- genDist ----
     def gen_prepare(self, buf: np.ndarray, offs: np.ndarray, lens: np.ndarray):

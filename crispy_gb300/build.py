@@ -2,7 +2,8 @@
 
 Everything is compiled in-tree for sm_103a only:
     crispy_gb300/lib/libcrispy_gb300.so
-    crispy_gb300/bin/kmerDist, crispy_gb300/bin/genDist, crispy_gb300/bin/crispyDist
+    crispy_gb300/bin/kmerDist, crispy_gb300/bin/genDist, crispy_gb300/bin/crispyDist,
+    crispy_gb300/bin/preprocess, crispy_gb300/bin/crispyRun
 Translation units compile in parallel; nothing here needs cmake.
 """
 from __future__ import annotations
@@ -25,9 +26,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
-CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu"]
-CXX_SOURCES = ["fasta.cpp"]
-CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp"}
+CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu", "pre.cu"]
+CXX_SOURCES = ["fasta.cpp", "pre_io.cpp"]
+CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp",
+       "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp"}
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -245,6 +245,12 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
                       &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue, &g.cstats,
                       &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt, &g.acc_pairs, &g.acc_dists})
         release(ctx, *b);
+    PreJob& pj = ctx->pre;
+    for (DevBuf* b : {&pj.seq, &pj.off, &pj.len, &pj.freq, &pj.woff, &pj.pad, &pj.alive, &pj.idx,
+                      &pj.idx_alt, &pj.flags, &pj.pos, &pj.tiles, &pj.out_idx, &pj.out_freq,
+                      &pj.counters, &pj.primer, &pj.tmp, &pj.stage_len, &pj.stage_off})
+        release(ctx, *b);
+    pj.ready = false;
     k.ready = false;
     g.ready = false;
     return CRISPY_OK;

@@ -1066,6 +1066,55 @@ int crispy_gen_prepare_from_kmer(crispy_ctx* ctx) {
     return CRISPY_OK;
 }
 
+// The reads the last crispy_preprocess kept, as genDist reads them back
+// from the _Clean file: a device-to-device copy of the padded reads, then
+// the same packing as gen_prepare.
+int crispy_gen_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw) {
+    if (!ctx) return CRISPY_E_INPUT;
+    cudaSetDevice(ctx->device);
+    GenJob& g = ctx->gen;
+    g.ready = false;
+    const uint8_t* d_bytes;
+    size_t bytes;
+    const int64_t* d_off;
+    std::vector<int32_t> len;
+    CRISPY_TRY(pre_stage_reads(ctx, raw, 1, &d_bytes, &bytes, &d_off, len));
+    const int n = (int)len.size();
+    if (n <= 0) return fail(ctx, CRISPY_E_INPUT, "gen_prepare_from_pre: preprocess kept no read");
+    if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
+    g.n = n;
+    g.h_len = len;
+    g.h_woff.resize(n + 1);
+    int64_t words = 0;
+    g.max_len = 0;
+    for (int r = 0; r < n; ++r) {
+        if (len[r] > CRISPY_MAX_READ_LEN)
+            return fail(ctx, CRISPY_E_UNSUPPORTED, "read %d length %d > %d", r, len[r], CRISPY_MAX_READ_LEN);
+        g.h_woff[r] = words;
+        words += (len[r] + 15) / 16;
+        g.max_len = std::max(g.max_len, len[r]);
+    }
+    g.h_woff[n] = words;
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, g.seq, bytes + 16));
+    CRISPY_TRY(ensure(ctx, g.off, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, g.len, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, g.woff, (size_t)(n + 1) * 8));
+    CRISPY_TRY(ensure(ctx, g.packed, (size_t)(words + 4) * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.seq.ptr, d_bytes, bytes, cudaMemcpyDeviceToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.off.ptr, d_off, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.len.ptr, len.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(g.woff.ptr, g.h_woff.data(), (size_t)(n + 1) * 8, cudaMemcpyHostToDevice, s));
+    gen_pack_kernel<<<std::min(n, ctx->sm_count * 16), 128, 0, s>>>(
+        g.seq.as<uint8_t>(), g.off.as<int64_t>(), g.len.as<int32_t>(), g.woff.as<int64_t>(), n,
+        g.packed.as<uint32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    g.ready = true;
+    return CRISPY_OK;
+}
+
 int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs, int band, int mode,
                      float* dist, int32_t* score, int32_t* ml, int32_t* al) {
     if (!ctx) return CRISPY_E_INPUT;

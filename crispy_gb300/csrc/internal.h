@@ -68,6 +68,17 @@ struct GenJob {
     HostBuf h_pairs, h_dists;
 };
 
+// Device buffers of one preprocess call (raw records, their 16-byte
+// aligned copy, filter flags, sort and merge lists).
+struct PreJob {
+    bool ready = false;   // out_idx holds the last call's kept reads
+    int64_t kept = 0;
+    int32_t n = 0;                 // records of the last call
+    std::vector<int32_t> h_idx;    // kept record indices, _Clean order
+    DevBuf seq, off, len, freq, woff, pad, alive, idx, idx_alt, flags, pos, tiles, out_idx,
+        out_freq, counters, primer, tmp, stage_len, stage_off;
+};
+
 // An instantiated CUDA graph of one launch sequence and the number of
 // kernels it holds.
 struct GraphEntry {
@@ -94,6 +105,7 @@ struct crispy_ctx {
     crispy_stats stats{};
     crispy::KmerJob kmer;
     crispy::GenJob gen;
+    crispy::PreJob pre;
     crispy::StreamEvents ev_kmer, ev_gen;
     std::map<std::string, crispy::GraphEntry> graphs;   // captured launch sequences
     bool use_graphs = true;
@@ -127,6 +139,20 @@ void count_launch(crispy_ctx* ctx, int n = 1);
 int graph_run(crispy_ctx* ctx, cudaStream_t s, const std::string& key,
               const std::function<int()>& enqueue);
 void graph_clear(crispy_ctx* ctx);
+
+// The reads the last crispy_preprocess kept, in _Clean order, as the
+// kmerDist (flavour 0) or genDist (flavour 1) FASTA parser reads them back
+// from the _Clean file (pre.cu).  On success *d_bytes is the device buffer
+// holding them, d_off their byte offsets there (device) and h_len their
+// lengths (host).  CRISPY_E_UNSUPPORTED when a kept read holds a
+// whitespace byte or is longer than 4,094 bytes: the file's lines then
+// split differently and only the file itself gives the stage's reads.
+int pre_stage_reads(crispy_ctx* ctx, const crispy_raw* raw, int flavour, const uint8_t** d_bytes,
+                    size_t* bytes, const int64_t** d_off, std::vector<int32_t>& h_len);
+// Records of a raw handle, and the length of the "> label" line
+// writeToFile gives record i, newline excluded (pre_io.cpp).
+int32_t raw_records(const crispy_raw* r);
+int64_t raw_header_line(const crispy_raw* r, int32_t i);
 
 // radix sort / scan helpers (sort.cu)
 size_t sort_tmp_bytes(int64_t n);   // scratch a sort of n items needs

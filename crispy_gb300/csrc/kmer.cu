@@ -1487,33 +1487,29 @@ TileFn tile_fn_for(int B) {
 
 using namespace crispy;
 
-extern "C" {
+namespace crispy {
+namespace {
 
-int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offsets,
-                        const int32_t* lengths, int n, int k) {
-    if (!ctx) return CRISPY_E_INPUT;
-    if (!seqbuf || !offsets || !lengths || n <= 0)
-        return fail(ctx, CRISPY_E_INPUT, "kmer_prepare: empty or NULL read set");
+// Per-read layout of a K-mer job from the read lengths (host metadata and
+// the device buffers sized for it); the reads themselves come next.
+int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
     if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
     if (k < 1 || k > 8) return fail(ctx, CRISPY_E_UNSUPPORTED, "K = %d outside 1..8", k);
-    cudaSetDevice(ctx->device);
     KmerJob& j = ctx->kmer;
     j.ready = false;
     j.n = n;
     j.k = k;
     j.h_t.resize(n);
-    int64_t end = 0;
     j.max_len = 0;
     j.max_t = 0;
     for (int r = 0; r < n; ++r) {
         if (lengths[r] > CRISPY_MAX_READ_LEN)
             return fail(ctx, CRISPY_E_UNSUPPORTED, "read %d length %d > %d", r, lengths[r], CRISPY_MAX_READ_LEN);
-        if (lengths[r] < k - 1 || offsets[r] < 0)
+        if (lengths[r] < k - 1)
             return fail(ctx, CRISPY_E_INPUT, "read %d length %d shorter than K-1", r, lengths[r]);
         j.h_t[r] = lengths[r] - k + 1;
         j.max_len = std::max(j.max_len, (int)lengths[r]);
         j.max_t = std::max(j.max_t, j.h_t[r]);
-        end = std::max(end, offsets[r] + lengths[r]);
     }
     j.ngroups = (n + 31) / 32;
     j.h_gent.assign(j.ngroups, 0);
@@ -1532,7 +1528,6 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     j.nent = j.h_gstart[j.ngroups];
     j.ntent = j.h_tstart[j.ngroups];
     cudaStream_t s = ctx->stream;
-    CRISPY_TRY(ensure(ctx, j.seq, (size_t)end + 16));
     CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
     CRISPY_TRY(ensure(ctx, j.gstart, (size_t)(j.ngroups + 1) * 8));
@@ -1549,8 +1544,6 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
     } else {
         CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
     }
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.gstart.ptr, j.h_gstart.data(), (size_t)(j.ngroups + 1) * 8,
                                    cudaMemcpyHostToDevice, s));
@@ -1560,7 +1553,56 @@ int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offs
                                    cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
                                    cudaMemcpyHostToDevice, s));
+    return CRISPY_OK;
+}
+
+}  // namespace
+}  // namespace crispy
+
+extern "C" {
+
+int crispy_kmer_prepare(crispy_ctx* ctx, const char* seqbuf, const int64_t* offsets,
+                        const int32_t* lengths, int n, int k) {
+    if (!ctx) return CRISPY_E_INPUT;
+    if (!seqbuf || !offsets || !lengths || n <= 0)
+        return fail(ctx, CRISPY_E_INPUT, "kmer_prepare: empty or NULL read set");
+    cudaSetDevice(ctx->device);
+    ctx->kmer.ready = false;
+    int64_t end = 0;
+    for (int r = 0; r < n; ++r) {
+        if (offsets[r] < 0) return fail(ctx, CRISPY_E_INPUT, "read %d has a negative offset", r);
+        end = std::max(end, offsets[r] + (int64_t)std::max(lengths[r], 0));
+    }
+    CRISPY_TRY(kmer_layout(ctx, lengths, n, k));
+    KmerJob& j = ctx->kmer;
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, j.seq, (size_t)end + 16));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, seqbuf, end, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, offsets, (size_t)n * 8, cudaMemcpyHostToDevice, s));
     j.ready = true;   // reads are resident; the entries are built next
+    return crispy_kmer_rebuild(ctx);
+}
+
+// The reads the last crispy_preprocess kept: a device-to-device copy of the
+// padded reads plus their offsets, then the same build as kmer_prepare.
+int crispy_kmer_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw, int k) {
+    if (!ctx) return CRISPY_E_INPUT;
+    cudaSetDevice(ctx->device);
+    ctx->kmer.ready = false;
+    const uint8_t* d_bytes;
+    size_t bytes;
+    const int64_t* d_off;
+    std::vector<int32_t> len;
+    CRISPY_TRY(pre_stage_reads(ctx, raw, 0, &d_bytes, &bytes, &d_off, len));
+    const int n = (int)len.size();
+    if (n <= 0) return fail(ctx, CRISPY_E_INPUT, "kmer_prepare_from_pre: preprocess kept no read");
+    CRISPY_TRY(kmer_layout(ctx, len.data(), n, k));
+    KmerJob& j = ctx->kmer;
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, j.seq, bytes + 16));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.seq.ptr, d_bytes, bytes, cudaMemcpyDeviceToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.off.ptr, d_off, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+    j.ready = true;
     return crispy_kmer_rebuild(ctx);
 }
 

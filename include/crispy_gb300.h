@@ -196,6 +196,79 @@ int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offsets,
                              float* d_dist, int32_t* d_score, int32_t* d_ml,
                              int32_t* d_al, void* stream);
 
+/* ---- preprocess (replaces bin/preprocess, src/preprocess/preprocess.cpp,
+ *      the step crispy.sh:18 runs before kmerDist) ---- */
+
+/* Records of a raw FASTA (fastq = 0, -f a) or FASTQ (fastq = 1, -f q) file
+ * as readFile (preprocess.cpp:74-242) collects them, in file order: the
+ * sequence (pieces of 4096-byte fgets reads, trailing whitespace and, for
+ * FASTA, trailing characters outside "nNATGCatgc" trimmed per piece and per
+ * read), the label (header line without any whitespace) and the frequency
+ * (1, or 0 for a FASTQ record whose sequence line is empty).  `records` is
+ * readIndex, the count the reference prints as "Total numReads" (it also
+ * counts FASTA headers without a sequence). */
+typedef struct crispy_raw crispy_raw;
+int crispy_raw_load(const char* path, int fastq, crispy_raw** out);
+int crispy_raw_view(const crispy_raw* r, const char** seqbuf, const int64_t** offsets,
+                    const int32_t** lengths, const uint8_t** freq, int32_t* n,
+                    int32_t* records);
+int crispy_raw_label(const crispy_raw* r, int32_t i, const char** label, int32_t* len);
+void crispy_raw_free(crispy_raw* r);
+
+/* Options of preprocess's command line (getCommandOptions,
+ * preprocess.cpp:613-684). */
+typedef struct crispy_pre_opts {
+    int length_check;      /* -s given: processReadLength (preprocess.cpp:322-392) */
+    double sd_allowed;     /* -s value (default 1.0) */
+    const char* primer;    /* -p: the primer (first line of the primer file, trailing
+                              whitespace removed); NULL = no primer check */
+    int max_mismatches;    /* -m (default 2): processPrimer (preprocess.cpp:530-560) */
+} crispy_pre_opts;
+
+typedef struct crispy_pre_stats {
+    int32_t length_discards;   /* processReadLength's return */
+    int32_t primer_discards;   /* processPrimer's return */
+    int32_t merges;            /* mergeReads's return */
+    int32_t kept;              /* reads written to the _Clean file */
+    int32_t length_reads;      /* reads the length statistics cover (0: none) */
+    int32_t min_len0, max_len0;   /* length range before the cut (printed first) */
+    int32_t min_len, max_len;     /* the cut: lengths outside [min_len, max_len] go */
+    double ave_len, sd;
+} crispy_pre_stats;
+
+/* The filters and the duplicate merge of preprocess on the device: length
+ * cut and N/n check, primer check by Smith-Waterman (SWLocalAlignment,
+ * preprocess.cpp:394-527), then mergeReads (preprocess.cpp:244-280): reads
+ * sorted by (length, strcmp), stable, and each run of equal sequences
+ * merged into its last read with the run's summed frequency.  Inputs are
+ * the n records of a raw file (any buffer layout; freq 0 = not a read).
+ * Writes the kept reads in _Clean order: out_index[k] = record index,
+ * out_freq[k] = merged frequency (capacity n each). */
+int crispy_preprocess(crispy_ctx* ctx, const char* seqbuf, const int64_t* offsets,
+                      const int32_t* lengths, const uint8_t* freq, int32_t n,
+                      const crispy_pre_opts* opts, int32_t* out_index, int32_t* out_freq,
+                      crispy_pre_stats* stats);
+
+/* writeToFile (preprocess.cpp:562-601): out_path gets "> <label>\n<seq>\n"
+ * per kept read (FASTA labels lose their first character, the '>'), and
+ * out_path.frq "<label> <freq>\n". */
+int crispy_pre_write(const crispy_raw* r, const int32_t* index, const int32_t* freq,
+                     int32_t kept, const char* out_path, int fastq);
+
+/* The reads the last crispy_preprocess on this context kept, still on the
+ * device, as the next two stages would parse them back from the _Clean file
+ * (kmerDist: kmerMain.cpp:298-397, genDist: genMain.cpp:184-277): no file
+ * round trip and no second upload, the hand-over crispy.sh:18-20 makes
+ * through the file.  `raw` is the handle whose records went into that call.
+ * CRISPY_E_UNSUPPORTED when a kept read holds a whitespace byte, a read is
+ * longer than 4,094 bytes or a header line longer than 4,095: the file's
+ * lines then split into several fgets pieces, and only parsing the written
+ * _Clean file (crispy_reads_load_fasta) gives the stages' reads.
+ * Otherwise equivalent to crispy_kmer_prepare / crispy_gen_prepare on the
+ * parsed _Clean file. */
+int crispy_kmer_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw, int k);
+int crispy_gen_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw);
+
 /* ---- timing of the last run (CUDA events on the context's stream) ---- */
 typedef struct crispy_stats {
     double kmer_kernel_ms;     /* summed duration of the k-mer tile kernel launches */

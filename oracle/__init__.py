@@ -53,6 +53,9 @@ def lib() -> C.CDLL:
         L.oracle_band_cells.restype = C.c_int64
         L.oracle_gen_chunks.argtypes = [P, P, C.c_int64, C.c_float, P, P, P, C.c_int]
         L.oracle_gen_chunks.restype = C.c_int
+        L.oracle_preprocess.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_double,
+                                        C.c_char_p, C.c_int, P]
+        L.oracle_preprocess.restype = C.c_int
         _lib = L
     return _lib
 
@@ -148,3 +151,16 @@ def gen_chunks(pairs, dists, thr: float):
         out.append((c, op[at:at + s].copy(), od[at:at + s].copy()))
         at += s
     return out
+
+
+def preprocess(in_path: str, out_path: str, fastq: bool = False, sd: float | None = None,
+               primer: bytes | None = None, max_mm: int = 2) -> dict:
+    """The oracle's preprocess: writes out_path and out_path.frq, returns the counts."""
+    counts = np.zeros(5, np.int64)
+    rc = lib().oracle_preprocess(in_path.encode(), out_path.encode(), int(fastq),
+                                 int(sd is not None), float(sd if sd is not None else 1.0),
+                                 primer, int(max_mm), counts.ctypes.data)
+    if rc != 0:
+        raise OSError(f"oracle preprocess failed on {in_path} ({rc})")
+    return dict(zip(["records", "length_discards", "primer_discards", "merges", "kept"],
+                    counts.tolist()))

@@ -82,6 +82,16 @@ int oracle_gen_chunks(const int32_t* pairs, const float* dists,
                       int64_t npairs, float thr, uint32_t* out_pairs,
                       float* out_dists, int64_t* chunk_sizes, int max_chunks);
 
+/* preprocess end to end (preprocess.cpp:686-726, oracle_pre.cpp): records
+ * of in_path (fastq: -f q), the -s length filter (length_check, sd), the -p
+ * primer check (primer = the primer sequence, NULL without -p; max_mm =
+ * -m), the duplicate merge, and out_path / out_path.frq.  counts[5] gets
+ * {records, length discards, primer discards, merges, kept}.  Returns 0,
+ * -1 (cannot open input), -2 (not FASTA) or -3 (cannot write output). */
+int oracle_preprocess(const char* in_path, const char* out_path, int fastq,
+                      int length_check, double sd, const char* primer, int max_mm,
+                      int64_t* counts);
+
 #ifdef __cplusplus
 }
 #endif

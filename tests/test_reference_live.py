@@ -129,3 +129,51 @@ def test_fasta_quirks(refbin, tmp_path):
     want = {(int(a), int(b)): float(x) for (a, b), x in zip(gp, gd) if plain[a] and plain[b]}
     got = {(int(a), int(b)): float(x) for (a, b), x in zip(ch[0][1], ch[0][2]) if plain[a] and plain[b]}
     assert want == got
+
+
+def _raw_set(path, seed, n, dup_frac=0.3, noise=True):
+    """A raw FASTA with planted duplicates, N's, lower case and wrapped lines."""
+    reads = synth.generate(synth.ReadSetSpec(n, max(4, n // 60), 260, "normal", 200, 12, 6, seed))
+    rng = np.random.default_rng(seed)
+    reads = reads + [reads[i] for i in rng.integers(0, len(reads), size=int(n * dup_frac))]
+    reads = [bytearray(reads[i]) for i in rng.permutation(len(reads))]
+    if noise:
+        for r in reads:
+            u = rng.random()
+            if u < 0.03:
+                r[rng.integers(0, len(r))] = ord("N")
+            elif u < 0.05:
+                a = rng.integers(0, len(r))
+                r[a:a + 4] = r[a:a + 4].lower()
+    with open(path, "wb") as f:
+        for i, s in enumerate(reads):
+            f.write(b">r%d desc %d\n" % (i, i % 13))
+            for a in range(0, len(s), 70):
+                f.write(bytes(s[a:a + 70]) + b"\n")
+    return bytes(reads[0][:22]).upper()
+
+
+@pytest.mark.parametrize("seed,n,args", [
+    (41, 3000, []),
+    (42, 3000, ["-s", "1.0"]),
+    (43, 2000, ["-s", "1.5", "-m", "3", "-p"]),
+    (44, 2000, ["-m", "1", "-p"]),
+])
+def test_preprocess_oracle_vs_reference(refbin, tmp_path, seed, n, args):
+    d = str(tmp_path)
+    primer = _raw_set(os.path.join(d, "raw.fa"), seed, n)
+    argv = list(args)
+    if argv and argv[-1] == "-p":
+        with open(os.path.join(d, "primer.txt"), "wb") as f:
+            f.write(primer + b"\n")
+        argv.append("primer.txt")
+    p = subprocess.run([os.path.join(refbin, "preprocess"), "-i", "raw.fa"] + argv, cwd=d,
+                       stdout=subprocess.PIPE)
+    assert p.returncode == 1
+    sd = float(argv[argv.index("-s") + 1]) if "-s" in argv else None
+    mm = int(argv[argv.index("-m") + 1]) if "-m" in argv else 2
+    oracle.preprocess(os.path.join(d, "raw.fa"), os.path.join(d, "oracle_out"), sd=sd,
+                      primer=primer if "-p" in argv else None, max_mm=mm)
+    for ext in ("", ".frq"):
+        assert open(os.path.join(d, "oracle_out" + ext), "rb").read() == \
+            open(os.path.join(d, "raw.fa_Clean" + ext), "rb").read()
