@@ -1,6 +1,6 @@
 // crispyDist -- kmerDist and genDist in one process.
 //
-// crispy.sh runs bin/kmerDist and then bin/genDist (crispy.sh:20-21); the two
+// crispy.sh runs bin/kmerDist and then bin/genDist (crispy.sh:19-20); the two
 // talk through <fasta>.kpair on disk.  This executable runs both stages on
 // one device context:
 //   - the k-mer survivors stay in HBM and feed genDist directly;
