@@ -376,6 +376,7 @@ def run_ours(args, dist, ws, rank, local):
         line["serve"] = serve_bench(args, local)
     if rank == 0 and not args.no_pre:
         line["preprocess"] = preprocess_bench(args, local)
+        line["aveclust"] = clust_bench(args, local, chunks, n)
     if rank == 0 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as td:
             kpps, gcups, cores, desc, _ = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
@@ -438,6 +439,47 @@ def preprocess_bench(args, local: int) -> dict:
                 "cpu_baseline": {"ms": cpu_s * 1e3, "cores": 1, "kind": "port",
                                  "sample": "the whole raw file"},
                 "outputs_identical": bool(same and c["kept"] == st["kept"])})
+    return out
+
+
+def clust_bench(args, local: int, chunks, n: int) -> dict:
+    """aveclust (the step after genDist) on genDist's chunks.
+
+    Timed: crispy_aveclust on this workload's chunks, and on the chunks of
+    plain_20k (19,954 reads) beside the oracle's step-by-step restatement of
+    the reference (which scans every node per merge: it would take minutes
+    on 100,000 reads, so the CPU comparison uses the 20k set).  The _Merge
+    files of the engine and the oracle are compared byte for byte.
+    """
+    import crispy_gb300 as cg
+    import oracle
+
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        ch = [(c[1], c[2]) for c in chunks]
+        t0 = time.perf_counter()
+        st = cg.aveclust(ch, n, os.path.join(td, "wl"))
+        out[args.workload] = {"reads": n, "edges": int(sum(len(c[1]) for c in ch)),
+                              "merges": int(st["merges"]), "ms": (time.perf_counter() - t0) * 1e3}
+        reads = synth.make_read_set("plain_20k")
+        buf, offs, lens = synth.pack_reads(reads)
+        m = len(lens)
+        with cg.Engine(local) as eng:
+            eng.kmer_prepare(buf, offs, lens, 6)
+            eng.kmer_run(cg.default_threshold(m, -1.0, 0), cg.MODE_BATCHED, False)
+            eng.gen_prepare_from_kmer()
+            ch20 = [(c[1], c[2]) for c in eng.gen_run_from_kmer(10, cg.default_threshold(m, -1.0, 1))]
+        t0 = time.perf_counter()
+        st20 = cg.aveclust(ch20, m, os.path.join(td, "p20"))
+        ours = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        om = oracle.aveclust(ch20, m, os.path.join(td, "oracle_Merge"))
+        cpu = (time.perf_counter() - t0) * 1e3
+        same = open(os.path.join(td, "p20_Merge"), "rb").read() == open(os.path.join(td, "oracle_Merge"), "rb").read()
+        out["plain_20k"] = {"reads": m, "edges": int(sum(len(c[1]) for c in ch20)), "merges": int(st20["merges"]),
+                            "ms": ours, "cpu_baseline": {"ms": cpu, "cores": 1, "kind": "port",
+                                                         "sample": "the whole 20k-read chunk set"},
+                            "merge_file_identical": bool(same and om == st20["merges"])}
     return out
 
 

@@ -57,6 +57,11 @@ _P = C.c_void_p
 _i64p = C.POINTER(C.c_int64)
 
 
+class ClustStats(C.Structure):
+    _fields_ = [("pairs_read", C.c_int64), ("merges", C.c_int64), ("roots", C.c_int32),
+                ("singletons", C.c_int32), ("end_level", C.c_float), ("report", C.c_char * 2048)]
+
+
 class PreOpts(C.Structure):
     _fields_ = [("length_check", C.c_int), ("sd_allowed", C.c_double), ("primer", C.c_char_p),
                 ("max_mismatches", C.c_int)]
@@ -108,6 +113,8 @@ PROTOTYPES = {
     "crispy_pre_write": (C.c_int, [_P, _P, _P, C.c_int32, C.c_char_p, C.c_int]),
     "crispy_kmer_prepare_from_pre": (C.c_int, [_P, _P, C.c_int]),
     "crispy_gen_prepare_from_pre": (C.c_int, [_P, _P]),
+    "crispy_aveclust": (C.c_int, [C.POINTER(_P), C.POINTER(_P), _P, C.c_int, C.c_int, C.c_float,
+                                  C.c_char_p, C.c_char_p, C.POINTER(ClustStats)]),
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -518,3 +525,23 @@ def compute_gen_dist(fasta: str, band: int = 2, thr: float = -1.0, mode: int = M
         d.astype(np.float32).tofile(f"{fasta}.ndist_{cid}")
         total += len(d)
     return total
+
+
+def aveclust(chunks, num_reads: int, out_base: str, end_level: float = -1.0,
+             edge_out: str | None = None) -> dict:
+    """Average-linkage clustering of genDist chunks [(uint32 pairs[N,2], float32 dists[N])]
+    (crispy_aveclust); writes out_base_Merge, .Cluster, .Cluster_List."""
+    lib = load_library()
+    keep = [(np.ascontiguousarray(p, dtype=np.uint32).reshape(-1, 2), np.ascontiguousarray(d, dtype=np.float32))
+            for p, d in chunks]
+    k = len(keep)
+    pp = (_P * max(k, 1))(*[p.ctypes.data for p, _ in keep])
+    dd = (_P * max(k, 1))(*[d.ctypes.data for _, d in keep])
+    counts = np.array([len(d) for _, d in keep] or [0], np.int64)
+    st = ClustStats()
+    rc = lib.crispy_aveclust(pp, dd, counts.ctypes.data, k, num_reads, end_level, out_base.encode(),
+                             edge_out.encode() if edge_out else None, C.byref(st))
+    if rc != OK:
+        raise CrispyError(rc, lib.crispy_last_error(None).decode())
+    return {"pairs_read": st.pairs_read, "merges": st.merges, "roots": st.roots,
+            "singletons": st.singletons, "end_level": st.end_level, "report": st.report.decode()}

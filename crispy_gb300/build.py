@@ -3,7 +3,7 @@
 Everything is compiled in-tree for sm_103a only:
     crispy_gb300/lib/libcrispy_gb300.so
     crispy_gb300/bin/kmerDist, crispy_gb300/bin/genDist, crispy_gb300/bin/crispyDist,
-    crispy_gb300/bin/preprocess, crispy_gb300/bin/crispyRun
+    crispy_gb300/bin/preprocess, crispy_gb300/bin/crispyRun, crispy_gb300/bin/aveclust
 Translation units compile in parallel; nothing here needs cmake.
 """
 from __future__ import annotations
@@ -27,9 +27,9 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
 CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu", "pre.cu"]
-CXX_SOURCES = ["fasta.cpp", "pre_io.cpp"]
+CXX_SOURCES = ["fasta.cpp", "pre_io.cpp", "clust.cpp"]
 CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp",
-       "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp"}
+       "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp", "aveclust": "cli_clust.cpp"}
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

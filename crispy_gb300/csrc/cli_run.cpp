@@ -1,19 +1,25 @@
-// crispyRun -- the first three steps of crispy.sh in one process.
+// crispyRun -- crispy.sh up to aveclust in one process.
 //
-// crispy.sh:18-20 runs
+// crispy.sh:18-24 runs
 //     ./bin/preprocess -i $INPUT
 //     ./bin/kmerDist  -i $INPUT"_Clean" -k $K
 //     ./bin/genDist   -i $INPUT"_Clean" -b $B
-// as three programs that hand the reads over through the _Clean file and
-// the k-mer survivors through the .kpair file.  This executable writes the
-// same files, byte for byte (<in>_Clean, <in>_Clean.frq, <in>_Clean.kpair,
-// <in>_Clean.npair_<f> / .ndist_<f>), from one device context: the raw
-// records go up once, preprocess keeps its kept reads on the device and
-// both stages start from them (crispy_kmer_prepare_from_pre,
-// crispy_gen_prepare_from_pre), and the k-mer survivors feed genDist in
-// HBM.  When a kept read would come back from the _Clean file split into
-// several lines (whitespace inside a read, very long reads or headers), the
-// stages read the written _Clean file instead, as the programs do.
+//     NUM_READS=`grep '>' $INPUT"_Clean" | wc -l`;  NUM_FILES=`ls ...ndist* | wc -l`
+//     ./bin/aveclust  -i $INPUT"_Clean" -n $NUM_READS -f $NUM_FILES
+// as four programs that hand the reads over through the _Clean file, the
+// k-mer survivors through the .kpair file and the genetic distances through
+// the .npair_N / .ndist_N chunks.  This executable writes the same files
+// (<in>_Clean, .frq, .kpair, .npair_<f> / .ndist_<f>, _Merge byte for byte;
+// .Cluster / .Cluster_List with the same clusters, see crispy_aveclust)
+// from one device context: the raw records go up once, preprocess keeps its
+// kept reads on the device and both stages start from them
+// (crispy_kmer_prepare_from_pre, crispy_gen_prepare_from_pre), the k-mer
+// survivors feed genDist in HBM, and the chunks feed aveclust from memory.
+// When a kept read would come back from the _Clean file split into several
+// lines (whitespace inside a read, very long reads or headers), the stages
+// read the written _Clean file instead, as the programs do.  NUM_FILES is
+// the number of chunks this run wrote (crispy.sh's `ls` would also count
+// chunk files an earlier, larger run left behind).
 //
 //   crispyRun <input file> [K (default 6)] [band (default 10)]
 //
@@ -41,8 +47,18 @@ int write_kmer(void* user, int, const void* pairs, const float*, int64_t count) 
     return std::fwrite(pairs, sizeof(int32_t), (size_t)count * 2, o->pair) != (size_t)count * 2;
 }
 
+struct Chunks {
+    std::string base;
+    std::vector<std::vector<uint32_t>> pairs;
+    std::vector<std::vector<float>> dists;
+};
+
 int write_chunk(void* user, int chunk, const void* pairs, const float* dists, int64_t count) {
-    const std::string& base = *static_cast<const std::string*>(user);
+    Chunks& ck = *static_cast<Chunks*>(user);
+    const std::string& base = ck.base;
+    const uint32_t* pp = static_cast<const uint32_t*>(pairs);
+    ck.pairs.emplace_back(pp, pp + 2 * count);
+    ck.dists.emplace_back(dists, dists + count);
     char suf[32];
     std::snprintf(suf, sizeof suf, "_%d", chunk);
     FILE* fp = std::fopen((base + ".npair" + suf).c_str(), "wb");
@@ -137,7 +153,8 @@ int main(int argc, char** argv) {
     if (rc == CRISPY_OK)
         rc = from_file ? prepare_from_file(ctx, clean, 1, K, &ng) : crispy_gen_prepare_from_pre(ctx, raw);
     const float gthr = crispy_default_threshold(ng, -1.0f, 1);
-    if (rc == CRISPY_OK) rc = crispy_gen_run_from_kmer(ctx, band, gthr, mode, write_chunk, (void*)&clean, &total);
+    Chunks ck{clean, {}, {}};
+    if (rc == CRISPY_OK) rc = crispy_gen_run_from_kmer(ctx, band, gthr, mode, write_chunk, &ck, &total);
     if (rc != CRISPY_OK) {
         std::fprintf(stderr, "crispyRun: %s\n", crispy_last_error(ctx));
         crispy_ctx_destroy(ctx);
@@ -145,6 +162,41 @@ int main(int argc, char** argv) {
         return 255;
     }
     std::printf("%llu\n", (unsigned long long)total);
+
+    // aveclust on the chunks, NUM_READS counted as `grep '>' | wc -l` does:
+    // every header line, plus each line of a read that holds a '>'
+    int64_t num_reads = st.kept;
+    for (int32_t k = 0; k < st.kept; ++k) {
+        const char* p = seq + off[index[k]];
+        const char* e = p + len[index[k]];
+        while (p < e) {
+            const char* nl = static_cast<const char*>(std::memchr(p, '\n', (size_t)(e - p)));
+            const char* le = nl ? nl : e;
+            if (std::memchr(p, '>', (size_t)(le - p))) ++num_reads;
+            p = nl ? nl + 1 : e;
+        }
+    }
+    std::vector<const uint32_t*> cp;
+    std::vector<const float*> cd;
+    std::vector<int64_t> cn;
+    for (size_t c = 0; c < ck.pairs.size(); ++c) {
+        cp.push_back(ck.pairs[c].data());
+        cd.push_back(ck.dists[c].data());
+        cn.push_back((int64_t)ck.dists[c].size());
+    }
+    crispy_clust_stats cs{};
+    if (!cn.empty() && num_reads > 0) {
+        rc = crispy_aveclust(cp.data(), cd.data(), cn.data(), (int)cn.size(), (int)num_reads, -1.0f,
+                             clean.c_str(), nullptr, &cs);
+        if (rc != CRISPY_OK) {
+            std::fprintf(stderr, "crispyRun: %s\n", crispy_last_error(nullptr));
+            crispy_ctx_destroy(ctx);
+            crispy_raw_free(raw);
+            return 255;
+        }
+        std::printf("aveclust: %lld merges, %d clusters, %d singletons\n", (long long)cs.merges, cs.roots,
+                    cs.singletons);
+    }
     crispy_ctx_destroy(ctx);
     crispy_raw_free(raw);
     std::printf("Time taken: %.3f s\n", now() - t0);

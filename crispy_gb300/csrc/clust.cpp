@@ -1,0 +1,504 @@
+// clust.cpp -- aveclust: sparse average-linkage clustering of the genDist
+// chunks (src/aveclust/aveclust.cpp), the step crispy.sh:24 runs after
+// genDist.
+//
+// The reference streams the .npair_N / .ndist_N chunks through a multimap
+// (the smallest distance of all chunk heads first, equal distances in
+// insertion order), absorbs each edge into the link map of the larger of the
+// two current cluster roots, and between batches merges the pair of clusters
+// with the smallest exact average distance while it does not exceed the
+// smallest lower bound of the incomplete ones (lambda bound).  Every
+// decision depends on the exact float values and on the iteration order of
+// the link maps (std::unordered_map: a strict `<` keeps the first minimum
+// met), so this restatement performs the same container operations in the
+// same order.  What changes is only how the work is found:
+//   * addNode scans every active node between two IDs for links to the two
+//     merged clusters (aveclust.cpp:466-520); here a reverse index lists the
+//     holders of each key, visited in the same ascending order;
+//   * min_element over the 2n+1 exact / inexact distances after every merge
+//     (aveclust.cpp:978-986) becomes a tournament tree with the same
+//     leftmost-minimum answer;
+//   * updateTopParent re-labels a whole subtree at every merge
+//     (aveclust.cpp:372-378); here the root of a leaf is found on demand
+//     through the parent links (with path compression), which yields the
+//     same node;
+//   * the parent takes over the larger node's link map by a move, not a
+//     copy (the map is cleared right after), and a computeDist for a link
+//     found by iterating the map uses that entry instead of a second lookup.
+// The _Merge file and the -o edge files are byte-identical to the
+// reference's.  The .Cluster / .Cluster_List lines hold the same clusters;
+// the reference orders them by iterating a hash set of node pointers
+// (aveclust.cpp:244-305), an order this code cannot and does not copy: it
+// visits roots by ascending node ID.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.h"
+
+namespace {
+
+constexpr double kEps = 1e-6;              // EPSILON (aveclust.cpp:18)
+constexpr double kUpperEdges = 2e8;        // UPPER_BOUND_NUM_EDGES (aveclust.cpp:19)
+
+struct Link {
+    unsigned int num = 0;
+    float sum = 0.0f;
+};
+using LinkMap = std::unordered_map<unsigned int, Link>;
+
+struct Node {
+    unsigned int id = 0;
+    int parent = -1, left = -1, right = -1;   // node indices (= IDs)
+    float dist = 0.0f;
+    unsigned int members = 1;
+    LinkMap links;
+};
+
+// Leftmost minimum over a float array with point updates (a min_element
+// that stays current).
+struct MinTree {
+    int n = 1;
+    std::vector<float> v;
+    std::vector<int> t;   // index of the leftmost minimum of each subtree
+    void init(int size, float fill) {
+        n = 1;
+        while (n < size) n <<= 1;
+        v.assign(n, 0.0f);
+        t.assign(2 * n, 0);
+        for (int i = 0; i < n; ++i) v[i] = i < size ? fill : INFINITY;
+        for (int i = 0; i < n; ++i) t[n + i] = i;
+        for (int i = n - 1; i > 0; --i) t[i] = pick(t[2 * i], t[2 * i + 1]);
+    }
+    int pick(int a, int b) const { return v[b] < v[a] ? b : a; }   // ties: the left one
+    void set(int i, float x) {
+        v[i] = x;
+        for (int p = (n + i) >> 1; p; p >>= 1) t[p] = pick(t[2 * p], t[2 * p + 1]);
+    }
+    void fill(float x, int size) {
+        for (int i = 0; i < size; ++i) v[i] = x;
+        for (int i = n - 1; i > 0; --i) t[i] = pick(t[2 * i], t[2 * i + 1]);
+    }
+    int argmin() const { return t[1]; }
+    float min() const { return v[t[1]]; }
+    float operator[](int i) const { return v[i]; }
+};
+
+struct Clusterer {
+    int num_reads;
+    float end_level;
+    float lambda = 0.0f;
+    bool all_loaded = false;
+    unsigned long long total_edges = 0;
+    unsigned int new_id;
+    std::vector<Node> nodes;            // every node ever made, index = ID
+    std::vector<char> active;           // vActiveNodes[i] != 0
+    std::vector<int> exact_node;        // vExactNodes (node ID, -1 = none)
+    MinTree exact, inexact;             // vExactDist, vInexactDist
+    std::vector<std::vector<unsigned int>> holders;   // key -> IDs that may hold it
+    std::vector<int> owner;             // a merged node's link map moved to this node
+    std::vector<int> up;                // root search shortcut (path-compressed parents)
+
+    explicit Clusterer(int n, float level) : num_reads(n), end_level(level), new_id((unsigned)n) {
+        const size_t cap = 2 * (size_t)n + 1;
+        nodes.resize(cap);
+        active.assign(cap, 0);
+        exact_node.assign(cap, -1);
+        holders.resize(cap);
+        owner.assign(cap, -1);
+        up.assign(cap, -1);
+        for (int i = 0; i < n; ++i) {
+            nodes[i].id = (unsigned)i;
+            active[i] = 1;
+        }
+        exact.init((int)cap, 1.0f);
+        inexact.init((int)cap, 1.0f);
+    }
+
+    // topParent: the root of the tree that holds node i
+    int root(int i) {
+        int r = i;
+        while (up[r] >= 0) r = up[r];
+        while (up[i] >= 0) {
+            const int nx = up[i];
+            up[i] = r;
+            i = nx;
+        }
+        return r;
+    }
+
+    Link& link_at(Node& holder, unsigned int key) {
+        auto it = holder.links.find(key);
+        if (it == holder.links.end()) holders[key].push_back(holder.id);
+        return holder.links[key];
+    }
+
+    // absorb (aveclust.cpp:562-590)
+    void absorb(unsigned int a, unsigned int b, float d) {
+        Node& x = nodes[root((int)a)];
+        Node& y = nodes[root((int)b)];
+        if (x.id > y.id) {
+            if (x.links.find(y.id) == x.links.end()) ++total_edges;
+            Link& l = link_at(x, y.id);
+            l.sum += d;
+            ++l.num;
+        } else if (y.id > x.id) {
+            if (y.links.find(x.id) == y.links.end()) ++total_edges;
+            Link& l = link_at(y, x.id);
+            l.sum += d;
+            ++l.num;
+        }
+    }
+
+    // computeDist (aveclust.cpp:381-412), x.id > y.id
+    void compute(Node& x, Node& y) {
+        auto it = x.links.find(y.id);
+        if (it != x.links.end()) compute_link(x, y, it->second);
+    }
+    // the same for a link entry of x already in hand (no second lookup)
+    void compute_link(Node& x, Node& y, const Link& lk) {
+        const unsigned int total = x.members * y.members;
+        const float sum = lk.sum;
+        const unsigned int unlinked = total - lk.num;
+        if (unlinked == 0 || all_loaded) {
+            const float d = (sum + end_level * (float)unlinked) / (float)total;
+            if (d < exact[x.id]) {
+                exact.set((int)x.id, d);
+                exact_node[x.id] = (int)y.id;
+            }
+        } else {
+            const float d = (sum + lambda * (float)unlinked) / (float)total;
+            if (d < inexact[x.id]) inexact.set((int)x.id, d);
+        }
+    }
+
+    // updateMin (aveclust.cpp:414-435)
+    void update_min(Node& x) {
+        exact.set((int)x.id, 1.0f);
+        for (auto& kv : x.links) {
+            Node& t = nodes[kv.first];
+            if (x.id > kv.first) compute_link(x, t, kv.second);
+            else compute(t, x);
+        }
+    }
+
+    // the node whose link map now holds what node i held
+    unsigned int owner_of(unsigned int i) {
+        unsigned int r = i;
+        while (owner[r] >= 0) r = (unsigned)owner[r];
+        while (owner[i] >= 0) {
+            const unsigned int nx = (unsigned)owner[i];
+            owner[i] = (int)r;
+            i = nx;
+        }
+        return r;
+    }
+
+    // IDs in (lo, hi) that hold `key`, ascending
+    std::vector<unsigned int> holders_in(unsigned int key, unsigned int lo, unsigned int hi) {
+        std::vector<unsigned int> out;
+        for (unsigned int h : holders[key]) {
+            const unsigned int i = owner_of(h);
+            if (i > lo && i < hi && active[i] && nodes[i].links.count(key)) out.push_back(i);
+        }
+        std::sort(out.begin(), out.end());
+        out.erase(std::unique(out.begin(), out.end()), out.end());
+        return out;
+    }
+
+    // addNode (aveclust.cpp:439-538), x.id > y.id
+    void add_node(Node& x, Node& y, Node& p, float d) {
+        const unsigned int ix = x.id, iy = y.id;
+        p.left = (int)ix;
+        p.right = (int)iy;
+        x.parent = (int)p.id;
+        y.parent = (int)p.id;
+        up[ix] = (int)p.id;
+        up[iy] = (int)p.id;
+        p.dist = d;
+        p.members = x.members + y.members;
+        x.links.erase(iy);
+        --total_edges;
+        // parentNode->linkMap = nodeX->linkMap: x's map is cleared right
+        // after, so it moves (same table, same iteration order), and the
+        // holders of its keys reach p through owner[]
+        p.links = std::move(x.links);
+        x.links = LinkMap();
+        owner[ix] = (int)p.id;
+        for (auto& kv : y.links) {
+            Link& l = link_at(p, kv.first);
+            l.num += kv.second.num;
+            l.sum += kv.second.sum;
+        }
+        x.links.clear();
+        y.links.clear();
+        // holders of y's key between the two IDs, ascending
+        for (unsigned int i : holders_in(iy, iy, ix)) {
+            Node& t = nodes[i];
+            Link& src = t.links[iy];
+            Link& l = link_at(p, i);
+            l.sum += src.sum;
+            l.num += src.num;
+            t.links.erase(iy);
+            --total_edges;
+        }
+        // holders of x's or y's key above x's ID, ascending; x's first
+        std::vector<unsigned int> hx = holders_in(ix, ix, new_id), hy = holders_in(iy, ix, new_id);
+        std::vector<unsigned int> all;
+        std::merge(hx.begin(), hx.end(), hy.begin(), hy.end(), std::back_inserter(all));
+        all.erase(std::unique(all.begin(), all.end()), all.end());
+        for (unsigned int i : all) {
+            Node& t = nodes[i];
+            auto ax = t.links.find(ix);
+            if (ax != t.links.end()) {
+                const Link src = ax->second;
+                Link& l = link_at(p, i);
+                l.sum += src.sum;
+                l.num += src.num;
+                t.links.erase(ix);
+                --total_edges;
+            }
+            auto ay = t.links.find(iy);
+            if (ay != t.links.end()) {
+                const Link src = ay->second;
+                Link& l = link_at(p, i);
+                l.sum += src.sum;
+                l.num += src.num;
+                t.links.erase(iy);
+                --total_edges;
+            }
+        }
+        total_edges += p.links.size();
+        active[ix] = active[iy] = 0;
+        exact_node[ix] = exact_node[iy] = -1;
+        exact.set((int)ix, 1.0f);
+        exact.set((int)iy, 1.0f);
+        inexact.set((int)ix, 1.0f);
+        inexact.set((int)iy, 1.0f);
+        holders[ix].clear();
+        holders[ix].shrink_to_fit();
+        holders[iy].clear();
+        holders[iy].shrink_to_fit();
+        for (auto& kv : p.links) {
+            Node& t = nodes[kv.first];
+            compute_link(p, t, kv.second);
+            if (exact_node[kv.first] == (int)ix || exact_node[kv.first] == (int)iy) update_min(t);
+        }
+    }
+
+    // merge (aveclust.cpp:541-559)
+    void merge(int a, int b, float d) {
+        Node& p = nodes[new_id];
+        p.id = new_id;
+        active[new_id] = 1;
+        if (nodes[a].id > nodes[b].id) add_node(nodes[a], nodes[b], p, d);
+        else add_node(nodes[b], nodes[a], p, d);
+        ++new_id;
+    }
+
+    // updateAllMin (aveclust.cpp:621-647)
+    void update_all_min() {
+        exact.fill(1.0f, (int)nodes.size());
+        inexact.fill(1.0f, (int)nodes.size());
+        for (size_t i = 0; i < nodes.size(); ++i) {
+            if (!active[i] || nodes[i].links.empty()) continue;
+            Node& x = nodes[i];
+            for (auto& kv : x.links) {
+                Node& y = nodes[kv.first];
+                if (x.id > y.id) compute_link(x, y, kv.second);
+                else compute(y, x);
+            }
+        }
+    }
+};
+
+// One chunk's read position (the multimap holds one head per chunk).
+struct Head {
+    unsigned int x, y, chunk;
+};
+
+void put_level_line(std::string& cl, std::string& cf, float level) {
+    char b[64];
+    std::snprintf(b, sizeof b, " %.6f ", level);
+    cl += b;
+    cf += b;
+}
+
+}  // namespace
+
+extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const* dists, const int64_t* counts,
+                               int nchunks, int num_reads, float end_level, const char* out_base,
+                               const char* edge_out, crispy_clust_stats* stats) {
+    using crispy::fail;
+    if (num_reads < 1 || nchunks < 1 || !pairs || !dists || !counts || !out_base)
+        return fail(nullptr, CRISPY_E_INPUT, "aveclust: need reads, at least one chunk and an output name");
+    for (int c = 0; c < nchunks; ++c) {
+        if (counts[c] < 0 || (counts[c] && (!pairs[c] || !dists[c])))
+            return fail(nullptr, CRISPY_E_INPUT, "aveclust: chunk %d is NULL", c);
+        for (int64_t k = 0; k < 2 * counts[c]; ++k)
+            if (pairs[c][k] >= (uint32_t)num_reads)
+                return fail(nullptr, CRISPY_E_INPUT, "aveclust: chunk %d names read %u of %d", c, pairs[c][k], num_reads);
+    }
+    if (end_level < 0.0f || end_level > 1.0f)   // aveclust.cpp:695-700
+        end_level = (float)(num_reads > 500 ? std::min(1 / std::log2((double)num_reads), 1.0)
+                                            : std::min(1 / std::log10((double)num_reads), 1.0));
+    FILE* fo = nullptr;
+    FILE* fo1 = nullptr;
+    if (edge_out) {
+        fo = std::fopen(edge_out, "w");
+        fo1 = std::fopen((std::string(edge_out) + "_Index1").c_str(), "w");
+        if (!fo || !fo1) {
+            if (fo) std::fclose(fo);
+            if (fo1) std::fclose(fo1);
+            return fail(nullptr, CRISPY_E_IO, "aveclust: cannot open %s", edge_out);
+        }
+    }
+    Clusterer C(num_reads, end_level);
+    std::string merges;
+    std::vector<int64_t> pos((size_t)nchunks, 0);
+    std::multimap<float, Head> heads;
+    unsigned int ix = 0, iy = 0;
+    float dist = 0.0f;
+    // loadAPair: the chunk's next entry into (ix, iy, dist), false at its end
+    auto load = [&](int c) -> bool {
+        if (pos[c] >= counts[c]) return false;
+        ix = pairs[c][2 * pos[c]];
+        iy = pairs[c][2 * pos[c] + 1];
+        dist = dists[c][pos[c]];
+        ++pos[c];
+        return true;
+    };
+    for (int c = 0; c < nchunks; ++c)
+        if (load(c)) heads.insert(std::make_pair(dist, Head{ix, iy, (unsigned)c}));
+    unsigned long long max_edges = (unsigned long long)num_reads;
+    int64_t read_pairs = 0;
+    char line[96];
+    while (!C.all_loaded) {
+        if (C.total_edges < max_edges) {
+            while (C.total_edges <= max_edges && !heads.empty()) {
+                auto it = heads.begin();
+                const int c = (int)it->second.chunk;
+                ix = it->second.x;
+                iy = it->second.y;
+                dist = it->first;
+                ++read_pairs;
+                if (fo) {
+                    std::fprintf(fo, "%d %d %f\n", (int)ix, (int)iy, dist);
+                    std::fprintf(fo1, "%d %d %f\n", (int)ix + 1, (int)iy + 1, dist);
+                }
+                if (dist < C.end_level || std::fabs(dist - C.end_level) < kEps) C.absorb(ix, iy, dist);
+                heads.erase(it);
+                if (load(c)) heads.insert(std::make_pair(dist, Head{ix, iy, (unsigned)c}));
+            }
+            if (dist > C.lambda) C.lambda = dist;
+        } else {
+            max_edges *= 2;
+            if ((double)max_edges > kUpperEdges) C.end_level = C.lambda;
+        }
+        if (heads.empty()) C.all_loaded = true;
+        C.update_all_min();
+        float min_in = C.inexact.min();
+        int mi = C.exact.argmin();
+        float min_ex = C.exact[mi];
+        while (min_ex < 1.0f && (min_ex < min_in || std::fabs(min_ex - min_in) < kEps)) {
+            const int a = C.root(mi);
+            const int b = C.root(C.exact_node[mi]);
+            C.merge(a, b, min_ex);
+            std::snprintf(line, sizeof line, "%d %d %.6f\n", (int)C.nodes[a].id + 1, (int)C.nodes[b].id + 1, min_ex);
+            merges += line;
+            min_in = C.inexact.min();
+            mi = C.exact.argmin();
+            min_ex = C.exact[mi];
+        }
+    }
+    if (fo) { std::fclose(fo); std::fclose(fo1); }
+
+    // roots and singletons (aveclust.cpp:944-955), then printClusters
+    // (aveclust.cpp:244-340): per distance level, the clusters a cut at
+    // that level leaves, members in the reference's depth-first order
+    std::vector<int> roots, orphans;
+    std::vector<char> seen(C.nodes.size(), 0);
+    for (int i = 0; i < num_reads; ++i) {
+        if (C.nodes[i].parent < 0) {
+            orphans.push_back(i);
+            continue;
+        }
+        const int r = C.root(i);
+        if (!seen[r]) { seen[r] = 1; roots.push_back(r); }
+    }
+    std::sort(roots.begin(), roots.end());
+    std::string cl, cf;
+    const float step = C.end_level / 10;
+    std::string report;
+    for (float level = step; level < C.end_level || std::fabs(level - C.end_level) < kEps; level += step) {
+        auto within = [&](int i) { return C.nodes[i].dist < level || std::fabs(C.nodes[i].dist - level) < kEps; };
+        std::vector<int> cut;   // the reference's nodeList, built with push_front
+        for (int r : roots) {
+            if (within(r)) { cut.push_back(r); continue; }
+            std::vector<int> todo{r};
+            while (!todo.empty()) {
+                const int t = todo.back();
+                todo.pop_back();
+                const int lf = C.nodes[t].left, rt = C.nodes[t].right;
+                if (within(lf)) cut.push_back(lf); else todo.push_back(lf);
+                if (within(rt)) cut.push_back(rt); else todo.push_back(rt);
+            }
+        }
+        std::reverse(cut.begin(), cut.end());
+        put_level_line(cl, cf, level);
+        for (int top : cut) {
+            cf += '|';
+            std::vector<int> todo{top};
+            bool first = true;
+            unsigned int size = 0;
+            while (!todo.empty()) {
+                const int t = todo.back();
+                todo.pop_back();
+                const Node& nd = C.nodes[t];
+                if (nd.left < 0 && nd.right < 0) {
+                    std::snprintf(line, sizeof line, first ? "%u" : " %u", nd.id);
+                    cf += line;
+                    first = false;
+                    size += nd.members;
+                }
+                if (nd.right >= 0) todo.push_back(nd.right);
+                if (nd.left >= 0) todo.push_back(nd.left);
+            }
+            std::snprintf(line, sizeof line, "%d ", (int)size);
+            cl += line;
+        }
+        for (int o : orphans) {
+            std::snprintf(line, sizeof line, "|%u", (unsigned)o);
+            cf += line;
+            cl += "1 ";
+        }
+        cf += "|\n";
+        cl += "\n";
+        std::snprintf(line, sizeof line, "Dist: %.6f. numOTUs: %u. numSingletons: %lu\n", level,
+                      (unsigned)(cut.size() + orphans.size()), (unsigned long)orphans.size());
+        report += line;
+    }
+    const std::string base(out_base);
+    struct Out { std::string name; const std::string* body; } outs[] = {
+        {base + "_Merge", &merges}, {base + ".Cluster_List", &cl}, {base + ".Cluster", &cf}};
+    for (auto& o : outs) {
+        FILE* f = std::fopen(o.name.c_str(), "wb");
+        if (!f) return fail(nullptr, CRISPY_E_IO, "aveclust: cannot write %s", o.name.c_str());
+        const bool ok = std::fwrite(o.body->data(), 1, o.body->size(), f) == o.body->size();
+        if (std::fclose(f) != 0 || !ok) return fail(nullptr, CRISPY_E_IO, "aveclust: short write to %s", o.name.c_str());
+    }
+    if (stats) {
+        stats->pairs_read = read_pairs;
+        stats->merges = (int64_t)(C.new_id - (unsigned)num_reads);
+        stats->roots = (int32_t)roots.size();
+        stats->singletons = (int32_t)orphans.size();
+        stats->end_level = C.end_level;
+        std::snprintf(stats->report, sizeof stats->report, "%s", report.c_str());
+    }
+    return CRISPY_OK;
+}

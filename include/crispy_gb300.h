@@ -269,6 +269,33 @@ int crispy_pre_write(const crispy_raw* r, const int32_t* index, const int32_t* f
 int crispy_kmer_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw, int k);
 int crispy_gen_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw);
 
+/* ---- aveclust (replaces bin/aveclust, src/aveclust/aveclust.cpp, the step
+ *      crispy.sh:24 runs after genDist) ---- */
+typedef struct crispy_clust_stats {
+    int64_t pairs_read;   /* edges taken from the chunks */
+    int64_t merges;       /* lines of the _Merge file */
+    int32_t roots;        /* trees of two or more reads */
+    int32_t singletons;   /* reads never merged */
+    float end_level;      /* the final endLevel (lambda once the edge cap was hit) */
+    char report[2048];    /* printClusters' "Dist: ... numOTUs ..." lines */
+} crispy_clust_stats;
+
+/* Sparse average-linkage clustering (aveclust's main loop,
+ * aveclust.cpp:663-1007) over genDist's chunks: chunk c holds counts[c]
+ * pairs (uint32 read indices, pairs[c][2k], pairs[c][2k+1]) and distances
+ * (dists[c][k]) ascending, as <in>.npair_c / <in>.ndist_c.  end_level
+ * outside [0, 1] selects the reference's default (1/log2 n above 500
+ * reads, else 1/log10 n).  Writes <out_base>_Merge (byte-identical to the
+ * reference), <out_base>.Cluster and <out_base>.Cluster_List (the same
+ * clusters per level; the reference orders them by pointer hash, this
+ * function by root ID), and with edge_out the -o files edge_out and
+ * edge_out_Index1.  Host code: the clustering is sequential (each merge
+ * decides the next); it runs in O(edges log n) where the reference scans
+ * all nodes per merge. */
+int crispy_aveclust(const uint32_t* const* pairs, const float* const* dists,
+                    const int64_t* counts, int nchunks, int num_reads, float end_level,
+                    const char* out_base, const char* edge_out, crispy_clust_stats* stats);
+
 /* ---- timing of the last run (CUDA events on the context's stream) ---- */
 typedef struct crispy_stats {
     double kmer_kernel_ms;     /* summed duration of the k-mer tile kernel launches */

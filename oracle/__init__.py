@@ -56,6 +56,9 @@ def lib() -> C.CDLL:
         L.oracle_preprocess.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_double,
                                         C.c_char_p, C.c_int, P]
         L.oracle_preprocess.restype = C.c_int
+        L.oracle_aveclust.argtypes = [C.POINTER(P), C.POINTER(P), P, C.c_int, C.c_int, C.c_float,
+                                      C.c_char_p, P]
+        L.oracle_aveclust.restype = C.c_int
         _lib = L
     return _lib
 
@@ -164,3 +167,19 @@ def preprocess(in_path: str, out_path: str, fastq: bool = False, sd: float | Non
         raise OSError(f"oracle preprocess failed on {in_path} ({rc})")
     return dict(zip(["records", "length_discards", "primer_discards", "merges", "kept"],
                     counts.tolist()))
+
+
+def aveclust(chunks, num_reads: int, merge_path: str, end_level: float = -1.0) -> int:
+    """The oracle's aveclust: writes merge_path (the _Merge lines); returns the merge count."""
+    keep = [(np.ascontiguousarray(p, dtype=np.uint32).reshape(-1, 2), np.ascontiguousarray(d, dtype=np.float32))
+            for p, d in chunks]
+    k = len(keep)
+    pp = (C.c_void_p * max(k, 1))(*[p.ctypes.data for p, _ in keep])
+    dd = (C.c_void_p * max(k, 1))(*[d.ctypes.data for _, d in keep])
+    counts = np.array([len(d) for _, d in keep] or [0], np.int64)
+    m = np.zeros(1, np.int64)
+    rc = lib().oracle_aveclust(pp, dd, counts.ctypes.data, k, num_reads, end_level, merge_path.encode(),
+                               m.ctypes.data)
+    if rc != 0:
+        raise OSError(f"oracle aveclust failed ({rc})")
+    return int(m[0])

@@ -92,6 +92,15 @@ int oracle_preprocess(const char* in_path, const char* out_path, int fastq,
                       int length_check, double sd, const char* primer, int max_mm,
                       int64_t* counts);
 
+/* aveclust's clustering (aveclust.cpp:663-1007, oracle_clust.cpp) over
+ * genDist chunks (pairs[c]: uint32[2*counts[c]], dists[c]: float[counts[c]],
+ * each ascending); writes the _Merge lines to merge_path.  end_level outside
+ * [0,1] selects the default.  Returns 0, -1 (bad arguments) or -3 (cannot
+ * write). */
+int oracle_aveclust(const uint32_t* const* pairs, const float* const* dists,
+                    const int64_t* counts, int nchunks, int num_reads, float end_level,
+                    const char* merge_path, int64_t* merges_out);
+
 #ifdef __cplusplus
 }
 #endif

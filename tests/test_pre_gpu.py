@@ -145,10 +145,15 @@ def _run(cmd, cwd, ok=(0,)):
     return p.stdout
 
 
-def _three_programs(d, name, k, band):
+def _four_programs(d, name, k, band):
+    """crispy.sh:18-24 with the drop-in executables."""
+    clean = name + "_Clean"
     _run([EXE, "-i", name], d, ok=(1,))
-    _run([os.path.join(cg.BIN_DIR, "kmerDist"), "-i", name + "_Clean", "-k", str(k)], d)
-    _run([os.path.join(cg.BIN_DIR, "genDist"), "-i", name + "_Clean", "-b", str(band)], d)
+    _run([os.path.join(cg.BIN_DIR, "kmerDist"), "-i", clean, "-k", str(k)], d)
+    _run([os.path.join(cg.BIN_DIR, "genDist"), "-i", clean, "-b", str(band)], d)
+    num_reads = sum(1 for line in open(os.path.join(d, clean), "rb") if b">" in line)
+    num_files = sum(1 for f in os.listdir(d) if f.startswith(clean + ".ndist"))
+    _run([os.path.join(cg.BIN_DIR, "aveclust"), "-i", clean, "-n", str(num_reads), "-f", str(num_files)], d)
 
 
 def _outputs(d):
@@ -176,7 +181,7 @@ def _whitespace_set(path):
 
 @pytest.mark.parametrize("case,k,band", [
     ("dups", 6, 10), ("dups", 8, 5), ("uneven", 6, 10), ("trailing_n", 7, 2), ("whitespace", 6, 10)])
-def test_crispyrun_matches_three_programs(tmp_path, case, k, band):
+def test_crispyrun_matches_four_programs(tmp_path, case, k, band):
     a, b = tmp_path / "three", tmp_path / "one"
     a.mkdir()
     b.mkdir()
@@ -192,12 +197,12 @@ def test_crispyrun_matches_three_programs(tmp_path, case, k, band):
     else:
         _whitespace_set(raw)
     shutil.copy(raw, os.path.join(str(b), "raw.fa"))
-    _three_programs(str(a), "raw.fa", k, band)
+    _four_programs(str(a), "raw.fa", k, band)
     out = _run([os.path.join(cg.BIN_DIR, "crispyRun"), "raw.fa", str(k), str(band)], str(b))
     assert b"totalNumPairs" in out
     want, got = _outputs(str(a)), _outputs(str(b))
     assert sorted(want) == sorted(got)
-    assert any(".npair_" in f for f in got)
+    assert any(".npair_" in f for f in got) and "raw.fa_Clean_Merge" in got
     for f in want:
         assert got[f] == want[f], f
 
