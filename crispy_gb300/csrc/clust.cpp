@@ -61,31 +61,49 @@ struct Node {
 };
 
 // Leftmost minimum over a float array with point updates (a min_element
-// that stays current).
+// that stays current).  Writes land in the array at once; the tree above
+// them is brought up to date when the minimum is next asked for, so the
+// many updates of one entry between two queries cost one path.
 struct MinTree {
     int n = 1;
     std::vector<float> v;
-    std::vector<int> t;   // index of the leftmost minimum of each subtree
+    std::vector<int> t;          // index of the leftmost minimum of each subtree
+    std::vector<int> pending;    // entries written since the last query
+    std::vector<char> marked;
     void init(int size, float fill) {
         n = 1;
         while (n < size) n <<= 1;
         v.assign(n, 0.0f);
         t.assign(2 * n, 0);
+        marked.assign(n, 0);
+        pending.clear();
         for (int i = 0; i < n; ++i) v[i] = i < size ? fill : INFINITY;
         for (int i = 0; i < n; ++i) t[n + i] = i;
-        for (int i = n - 1; i > 0; --i) t[i] = pick(t[2 * i], t[2 * i + 1]);
+        rebuild();
     }
     int pick(int a, int b) const { return v[b] < v[a] ? b : a; }   // ties: the left one
+    void rebuild() {
+        for (int i = n - 1; i > 0; --i) t[i] = pick(t[2 * i], t[2 * i + 1]);
+        for (int i : pending) marked[i] = 0;
+        pending.clear();
+    }
     void set(int i, float x) {
         v[i] = x;
-        for (int p = (n + i) >> 1; p; p >>= 1) t[p] = pick(t[2 * p], t[2 * p + 1]);
+        if (!marked[i]) { marked[i] = 1; pending.push_back(i); }
     }
     void fill(float x, int size) {
         for (int i = 0; i < size; ++i) v[i] = x;
-        for (int i = n - 1; i > 0; --i) t[i] = pick(t[2 * i], t[2 * i + 1]);
+        rebuild();
     }
-    int argmin() const { return t[1]; }
-    float min() const { return v[t[1]]; }
+    void flush() {
+        for (int i : pending) {
+            marked[i] = 0;
+            for (int p = (n + i) >> 1; p; p >>= 1) t[p] = pick(t[2 * p], t[2 * p + 1]);
+        }
+        pending.clear();
+    }
+    int argmin() { flush(); return t[1]; }
+    float min() { flush(); return v[t[1]]; }
     float operator[](int i) const { return v[i]; }
 };
 
