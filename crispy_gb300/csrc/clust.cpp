@@ -34,7 +34,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <map>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -118,7 +117,11 @@ struct Clusterer {
     std::vector<char> active;           // vActiveNodes[i] != 0
     std::vector<int> exact_node;        // vExactNodes (node ID, -1 = none)
     MinTree exact, inexact;             // vExactDist, vInexactDist
-    std::vector<std::vector<unsigned int>> holders;   // key -> IDs that may hold it
+    // key -> IDs that may hold it: one singly linked list per key in a
+    // shared pool (head[key], then next[] through pool entries)
+    std::vector<int> hold_head;
+    std::vector<unsigned int> hold_id;
+    std::vector<int> hold_next;
     std::vector<int> owner;             // a merged node's link map moved to this node
     std::vector<int> up;                // root search shortcut (path-compressed parents)
 
@@ -127,7 +130,7 @@ struct Clusterer {
         nodes.resize(cap);
         active.assign(cap, 0);
         exact_node.assign(cap, -1);
-        holders.resize(cap);
+        hold_head.assign(cap, -1);
         owner.assign(cap, -1);
         up.assign(cap, -1);
         for (int i = 0; i < n; ++i) {
@@ -150,24 +153,35 @@ struct Clusterer {
         return r;
     }
 
-    Link& link_at(Node& holder, unsigned int key) {
-        auto it = holder.links.find(key);
-        if (it == holder.links.end()) holders[key].push_back(holder.id);
-        return holder.links[key];
+    void add_holder(unsigned int key, unsigned int id) {
+        hold_id.push_back(id);
+        hold_next.push_back(hold_head[key]);
+        hold_head[key] = (int)hold_id.size() - 1;
+    }
+
+    // linkMap[key] (inserting a zero link when absent, at the same place
+    // operator[] would), recording a new holder; *fresh tells whether it
+    // was inserted
+    Link& link_at(Node& holder, unsigned int key, bool* fresh = nullptr) {
+        auto r = holder.links.try_emplace(key);
+        if (r.second) add_holder(key, holder.id);
+        if (fresh) *fresh = r.second;
+        return r.first->second;
     }
 
     // absorb (aveclust.cpp:562-590)
     void absorb(unsigned int a, unsigned int b, float d) {
         Node& x = nodes[root((int)a)];
         Node& y = nodes[root((int)b)];
+        bool fresh = false;
         if (x.id > y.id) {
-            if (x.links.find(y.id) == x.links.end()) ++total_edges;
-            Link& l = link_at(x, y.id);
+            Link& l = link_at(x, y.id, &fresh);
+            if (fresh) ++total_edges;
             l.sum += d;
             ++l.num;
         } else if (y.id > x.id) {
-            if (y.links.find(x.id) == y.links.end()) ++total_edges;
-            Link& l = link_at(y, x.id);
+            Link& l = link_at(y, x.id, &fresh);
+            if (fresh) ++total_edges;
             l.sum += d;
             ++l.num;
         }
@@ -220,8 +234,8 @@ struct Clusterer {
     // IDs in (lo, hi) that hold `key`, ascending
     std::vector<unsigned int> holders_in(unsigned int key, unsigned int lo, unsigned int hi) {
         std::vector<unsigned int> out;
-        for (unsigned int h : holders[key]) {
-            const unsigned int i = owner_of(h);
+        for (int e = hold_head[key]; e >= 0; e = hold_next[e]) {
+            const unsigned int i = owner_of(hold_id[e]);
             if (i > lo && i < hi && active[i] && nodes[i].links.count(key)) out.push_back(i);
         }
         std::sort(out.begin(), out.end());
@@ -298,10 +312,7 @@ struct Clusterer {
         exact.set((int)iy, 1.0f);
         inexact.set((int)ix, 1.0f);
         inexact.set((int)iy, 1.0f);
-        holders[ix].clear();
-        holders[ix].shrink_to_fit();
-        holders[iy].clear();
-        holders[iy].shrink_to_fit();
+        hold_head[ix] = hold_head[iy] = -1;   // the keys die with the two nodes
         for (auto& kv : p.links) {
             Node& t = nodes[kv.first];
             compute_link(p, t, kv.second);
@@ -335,10 +346,26 @@ struct Clusterer {
     }
 };
 
-// One chunk's read position (the multimap holds one head per chunk).
+// The chunk heads in the multimap's order: smallest distance first, equal
+// distances in insertion order (a std::multimap<float, ...> inserts a key
+// after those equal to it).  A binary heap on (distance, insertion number)
+// gives the same order without a node allocation per edge.
 struct Head {
+    float d;
+    unsigned long long seq;
     unsigned int x, y, chunk;
 };
+struct HeadAfter {   // heap order: the head that comes later is "less"
+    bool operator()(const Head& a, const Head& b) const {
+        return a.d > b.d || (a.d == b.d && a.seq > b.seq);
+    }
+};
+
+// Decimal digits of v into the end of buf; returns the first digit.
+char* put_uint(char* end, unsigned long long v) {
+    do { *--end = (char)('0' + v % 10); v /= 10; } while (v);
+    return end;
+}
 
 void put_level_line(std::string& cl, std::string& cf, float level) {
     char b[64];
@@ -379,7 +406,6 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
     Clusterer C(num_reads, end_level);
     std::string merges;
     std::vector<int64_t> pos((size_t)nchunks, 0);
-    std::multimap<float, Head> heads;
     unsigned int ix = 0, iy = 0;
     float dist = 0.0f;
     // loadAPair: the chunk's next entry into (ix, iy, dist), false at its end
@@ -391,27 +417,34 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         ++pos[c];
         return true;
     };
+    std::vector<Head> heads;   // heap under HeadAfter
+    unsigned long long seq = 0;
+    auto push_head = [&](int c) {
+        heads.push_back(Head{dist, seq++, ix, iy, (unsigned)c});
+        std::push_heap(heads.begin(), heads.end(), HeadAfter());
+    };
     for (int c = 0; c < nchunks; ++c)
-        if (load(c)) heads.insert(std::make_pair(dist, Head{ix, iy, (unsigned)c}));
+        if (load(c)) push_head(c);
     unsigned long long max_edges = (unsigned long long)num_reads;
     int64_t read_pairs = 0;
     char line[96];
     while (!C.all_loaded) {
         if (C.total_edges < max_edges) {
             while (C.total_edges <= max_edges && !heads.empty()) {
-                auto it = heads.begin();
-                const int c = (int)it->second.chunk;
-                ix = it->second.x;
-                iy = it->second.y;
-                dist = it->first;
+                std::pop_heap(heads.begin(), heads.end(), HeadAfter());
+                const Head h = heads.back();
+                heads.pop_back();
+                const int c = (int)h.chunk;
+                ix = h.x;
+                iy = h.y;
+                dist = h.d;
                 ++read_pairs;
                 if (fo) {
                     std::fprintf(fo, "%d %d %f\n", (int)ix, (int)iy, dist);
                     std::fprintf(fo1, "%d %d %f\n", (int)ix + 1, (int)iy + 1, dist);
                 }
                 if (dist < C.end_level || std::fabs(dist - C.end_level) < kEps) C.absorb(ix, iy, dist);
-                heads.erase(it);
-                if (load(c)) heads.insert(std::make_pair(dist, Head{ix, iy, (unsigned)c}));
+                if (load(c)) push_head(c);
             }
             if (dist > C.lambda) C.lambda = dist;
         } else {
@@ -479,8 +512,10 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
                 todo.pop_back();
                 const Node& nd = C.nodes[t];
                 if (nd.left < 0 && nd.right < 0) {
-                    std::snprintf(line, sizeof line, first ? "%u" : " %u", nd.id);
-                    cf += line;
+                    char* e = line + sizeof line;
+                    char* b = put_uint(e, nd.id);
+                    if (!first) *--b = ' ';
+                    cf.append(b, (size_t)(e - b));
                     first = false;
                     size += nd.members;
                 }
@@ -491,8 +526,10 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
             cl += line;
         }
         for (int o : orphans) {
-            std::snprintf(line, sizeof line, "|%u", (unsigned)o);
-            cf += line;
+            char* e = line + sizeof line;
+            char* b = put_uint(e, (unsigned)o);
+            *--b = '|';
+            cf.append(b, (size_t)(e - b));
             cl += "1 ";
         }
         cf += "|\n";
