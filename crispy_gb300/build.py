@@ -100,7 +100,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
 
 
 def build_oracle(with_reference: bool | None = None) -> None:
-    """Compile the checker (oracle/) and, where the reference tree exists,
+    """Compile the oracle (oracle/) and, where the reference tree exists,
     the reference's own CPU path into oracle/_ref/."""
     odir = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", odir])

@@ -1,8 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg, always as the checker or the timed CPU
-baseline, never as a substitute for the GPU engine.
+bench.py's CPU-baseline leg, always as the reference results are compared
+with or as the timed CPU baseline, never as a substitute for the GPU engine.
 """
 from __future__ import annotations
 

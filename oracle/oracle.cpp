@@ -1,7 +1,7 @@
 /*
  * oracle.cpp -- CPU restatement of CRiSPy's kmerDist / genDist semantics.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  See oracle.h.  Citations are
+ * TEST INFRASTRUCTURE ONLY (the oracle).  See oracle.h.  Citations are
  * file:line inside the reference project (src/kmerDist, src/genDist).
  *
  * The code is deliberately plain: it follows the reference's CPU loops

@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of CRiSPy's kmerDist and genDist semantics.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA path
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the CUDA path
  * is compared against; nothing in the product (crispy_gb300/, include/) links
  * it, and the product fails loudly instead of falling back to it.  Only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.

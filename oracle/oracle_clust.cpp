@@ -2,8 +2,8 @@
  * oracle_clust.cpp -- CPU restatement of CRiSPy's aveclust
  * (src/aveclust/aveclust.cpp), step for step.
  *
- * TEST INFRASTRUCTURE ONLY (the checker for crispy_aveclust and the timed
- * CPU baseline of bench.py; the product never links it).  Tree nodes live
+ * TEST INFRASTRUCTURE ONLY (what tests compare crispy_aveclust with, and the
+ * timed CPU baseline of bench.py; the product never links it).  Tree nodes live
  * on the heap and point at each other, link maps are std::unordered_map
  * keyed by node ID, every merge scans the active nodes between the two IDs
  * and takes min_element over all exact / inexact distances -- the

@@ -3,8 +3,8 @@
  * (src/preprocess/preprocess.cpp), end to end: records, filters, duplicate
  * merge, output files.
  *
- * TEST INFRASTRUCTURE ONLY (the checker for crispy_preprocess and the
- * preprocess executable; the product never links it).  It follows the
+ * TEST INFRASTRUCTURE ONLY (what tests compare crispy_preprocess and the
+ * preprocess executable with; the product never links it).  It follows the
  * reference's control flow step by step, in plain C++: fgets into a
  * 4096-byte buffer, the same trims, a record list in file order, a stable
  * sort by (length, strcmp), the adjacent-duplicate fold and fprintf output.
