@@ -339,6 +339,8 @@ def run_ours(args, dist, ws, rank, local):
               "peak_source": "measured: crispy_probe_int32 (IADD3/LOP3 chains), this run"}
     dominant = roof_g if gen_s >= kmer_s else roof_k
     _attach_traffic(roof_k, roof_g, n_pairs, cells)
+    _attach_hbm_view(roof_k, kmer_s)
+    _attach_hbm_view(roof_g, gen_s)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -542,6 +544,22 @@ def serve_bench(args, local: int) -> dict:
                                               "pairs_per_s": sum(pairs) / el,
                                               "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"]}
     return out
+
+
+def _attach_hbm_view(roof, seconds):
+    """The same launch against the measured HBM copy bandwidth: its DRAM
+    traffic per launch over its duration.  Shows how far from HBM-bound the
+    kernel is (neither stage is: their binding pipes are integer / L1)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if roof.get("traffic") is None or not os.path.exists(p) or seconds <= 0:
+        return
+    try:
+        peak = float(json.load(open(p))["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return
+    gbs = roof["traffic"] / seconds / 1e9
+    roof["hbm_view"] = {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                        "peak_source": "measured: MEASURED_PEAKS.json hbm_gbs"}
 
 
 def _attach_traffic(roof_k, roof_g, n_pairs, cells):
