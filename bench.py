@@ -633,7 +633,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("CRISPY_BENCH_WORKLOAD", "uneven_100k"),
                     choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-sample-reads", type=int, default=_env_int("CRISPY_CPU_SAMPLE", 6000))
+    ap.add_argument("--cpu-sample-reads", type=int, default=_env_int("CRISPY_CPU_SAMPLE", 12000))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-pre", action="store_true")
