@@ -59,6 +59,9 @@ def lib() -> C.CDLL:
         L.oracle_aveclust.argtypes = [C.POINTER(P), C.POINTER(P), P, C.c_int, C.c_int, C.c_float,
                                       C.c_char_p, P]
         L.oracle_aveclust.restype = C.c_int
+        L.oracle_kmer_rows.argtypes = [P, P, P, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int,
+                                       P, P, C.c_int64]
+        L.oracle_kmer_rows.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -80,6 +83,25 @@ def read_fasta(path: str, flavour: int):
     data = np.frombuffer(C.string_at(buf, total), dtype=np.uint8).copy()
     L.oracle_fasta_free(h)
     return data, offs, lens
+
+
+def kmer_rows(buf, offs, lens, k: int, thr: float, row_lo: int, row_hi: int, nthreads: int = 0):
+    """Survivors of rows [row_lo, row_hi) against all later columns, (row, col) order."""
+    L = lib()
+    buf = np.ascontiguousarray(buf, np.uint8)
+    offs = np.ascontiguousarray(offs, np.int64)
+    lens = np.ascontiguousarray(lens, np.int32)
+    cap = 1 << 16
+    while True:
+        pairs = np.empty((cap, 2), np.int32)
+        d = np.empty(cap, np.float32)
+        tot = L.oracle_kmer_rows(buf.ctypes.data, offs.ctypes.data, lens.ctypes.data, len(lens), k, thr,
+                                 row_lo, row_hi, nthreads, pairs.ctypes.data, d.ctypes.data, cap)
+        if tot < 0:
+            raise ValueError("oracle_kmer_rows failed")
+        if tot <= cap:
+            return pairs[:tot], d[:tot]
+        cap = tot
 
 
 def default_threshold(n: int, user_thr: float, num: int) -> float:

@@ -237,6 +237,52 @@ int64_t oracle_kmer_all(const char* seqbuf, const int64_t* offsets,
     return total;
 }
 
+// Survivors of the rows [row_lo, row_hi) against every later column, in
+// (row, col) order: the same per-pair rule as oracle_kmer_all on a slice of
+// the triangle, for checking full-size runs on a few rows.
+int64_t oracle_kmer_rows(const char* seqbuf, const int64_t* offsets, const int32_t* lengths,
+                         int n, int K, float thr, int row_lo, int row_hi, int nthreads,
+                         int32_t* out_pairs, float* out_dists, int64_t cap) {
+    if (n <= 0 || K < 1 || K > 8 || row_lo < 0 || row_hi > n || row_lo > row_hi) return -1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    std::vector<std::vector<uint16_t>> tup(n);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int r = 0; r < n; ++r) tup[r] = tuples_of(seqbuf + offsets[r], lengths[r], K);
+    const int rows = row_hi - row_lo;
+    std::vector<std::vector<std::pair<int, float>>> rowbuf(rows);
+    for (int i = 0; i < rows; ++i) {
+        const int row = row_lo + i;
+        const int chunks = 64;
+        std::vector<std::vector<std::pair<int, float>>> part(chunks);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int c = 0; c < chunks; ++c) {
+            const int64_t lo = row + 1 + (int64_t)(n - row - 1) * c / chunks;
+            const int64_t hi = row + 1 + (int64_t)(n - row - 1) * (c + 1) / chunks;
+            for (int64_t col = lo; col < hi; ++col) {
+                const int m = merge_count(tup[row], tup[col]);
+                const float d = kmer_dist(m, (int)tup[row].size(), (int)tup[col].size());
+                if (keep(d, thr)) part[c].push_back({(int)col, d});
+            }
+        }
+        for (auto& v : part) rowbuf[i].insert(rowbuf[i].end(), v.begin(), v.end());
+    }
+    int64_t total = 0;
+    for (int i = 0; i < rows; ++i)
+        for (auto& e : rowbuf[i]) {
+            if (total < cap) {
+                out_pairs[2 * total] = row_lo + i;
+                out_pairs[2 * total + 1] = e.first;
+                if (out_dists) out_dists[total] = e.second;
+            }
+            ++total;
+        }
+    return total;
+}
+
 // genCPU.cpp:290-466 (banded) and :81-225 (band <= 1: no band limit, which
 // is the banded recurrence with every cell in band).  Rows i run over read2
 // (pair[1]) and columns j over read1 (pair[0]); symbols are compared as the

@@ -101,6 +101,13 @@ int oracle_aveclust(const uint32_t* const* pairs, const float* const* dists,
                     const int64_t* counts, int nchunks, int num_reads, float end_level,
                     const char* merge_path, int64_t* merges_out);
 
+/* Survivors of rows [row_lo, row_hi) against every later column, in (row,
+ * col) order, with oracle_kmer_all's per-pair rule; returns the total (may
+ * exceed cap) or a negative error. */
+int64_t oracle_kmer_rows(const char* seqbuf, const int64_t* offsets, const int32_t* lengths,
+                         int n, int K, float thr, int row_lo, int row_hi, int nthreads,
+                         int32_t* out_pairs, float* out_dists, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif
