@@ -26,15 +26,38 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
 
+// Anonymous mapping that asks for transparent huge pages: the parse threads
+// then take one fault per 2 MB instead of one per 4 KB.
+struct BigBuf {
+    char* p = nullptr;
+    size_t n = 0;
+    ~BigBuf() { if (p) ::munmap(p, n); }
+    bool alloc(size_t bytes) {
+        n = (bytes + (2u << 20) - 1) & ~(size_t)((2u << 20) - 1);
+        void* m = ::mmap(nullptr, n, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+        if (m == MAP_FAILED) { p = nullptr; n = 0; return false; }
+        p = static_cast<char*>(m);
+#ifdef MADV_HUGEPAGE
+        ::madvise(p, n, MADV_HUGEPAGE);
+#endif
+        return true;
+    }
+};
+
 struct crispy_raw {
     bool fastq = false;
-    std::string bases;
+    std::string bases;   // FASTQ: sequences back to back
+    BigBuf fa_bases;     // FASTA: sequences at their chunk's file offsets
+    const char* data() const { return fa_bases.p ? fa_bases.p : bases.data(); }
     std::vector<int64_t> offsets;
     std::vector<int32_t> lengths;
     std::vector<uint8_t> freq;
@@ -78,6 +101,15 @@ size_t seq_trimmed(const char* p, size_t n) {
     return k ? k : n;
 }
 
+// READ::initialize drops every whitespace byte of the label.
+void push_label(crispy_raw* r, const char* label, size_t label_n) {
+    r->label_off.push_back((int64_t)r->labels.size());
+    int32_t n = 0;
+    for (size_t i = 0; i < label_n; ++i)
+        if (!is_space((unsigned char)label[i])) { r->labels.push_back(label[i]); ++n; }
+    r->label_len.push_back(n);
+}
+
 // A piece as a pointer into the file and its length up to the first NUL.
 struct Piece {
     const char* p;
@@ -85,17 +117,32 @@ struct Piece {
     char raw0;   // first byte of the fgets buffer ('$' at end of file)
 };
 
-// fgets over an in-memory file.
+// fgets over an in-memory file.  `size` is where reading stops: the file's
+// end (end-of-file rules apply) or, for a chunk, the start of its
+// successor's first line (no end-of-file rules: stop_at_size).
 struct PieceReader {
     const char* data;
     size_t size, pos = 0;
     bool eof = false;
+    bool stop_at_size = false;
     bool has_nul = true;   // false: the file holds no NUL byte, skip the per-piece scan
     // false at end of file (the reference's buffer then starts with '$')
     bool next(Piece& pc) {
         if (pos >= size) {
             eof = true;
             return false;
+        }
+        if (stop_at_size) {   // a chunk's last line ends with '\n' right at size
+            const size_t room = std::min(kPieceMax, size - pos);
+            const char* p = data + pos;
+            const void* nl = std::memchr(p, '\n', room);
+            const size_t take = nl ? (size_t)((const char*)nl - p) + 1 : room;
+            pos += take;
+            const void* z = has_nul ? std::memchr(p, '\0', take) : nullptr;
+            pc.p = p;
+            pc.n = z ? (size_t)((const char*)z - p) : take;
+            pc.raw0 = p[0];
+            return true;
         }
         const size_t room = std::min(kPieceMax, size - pos);
         const char* p = data + pos;
@@ -121,54 +168,142 @@ void push(crispy_raw* r, int64_t start, const char* label, size_t label_n, uint8
     r->offsets.push_back(start);
     r->lengths.push_back((int32_t)((int64_t)r->bases.size() - start));
     r->freq.push_back(freq);
-    // READ::initialize drops every whitespace byte of the label
-    r->label_off.push_back((int64_t)r->labels.size());
-    int32_t n = 0;
-    for (size_t i = 0; i < label_n; ++i)
-        if (!is_space((unsigned char)label[i])) { r->labels.push_back(label[i]); ++n; }
-    r->label_len.push_back(n);
+    push_label(r, label, label_n);
 }
 
-// deleteSpacesInSeq on the sequence collected since `start`.
-void trim_tail(crispy_raw* r, int64_t start) {
-    const size_t n = r->bases.size() - (size_t)start;
-    r->bases.resize((size_t)start + seq_trimmed(r->bases.data() + start, n));
-}
+// ---- FASTA: chunks of the file tokenised in parallel, then readFile's
+// state machine over the tokens in order ----
+//
+// Chunks start at a line that begins with '>' (a byte after '\n'), so they
+// cut the file into the same fgets pieces as one sequential pass.  A chunk
+// turns its pieces into tokens:
+//   HEADER  a piece starting with '>' (label = the piece, trailing
+//           whitespace trimmed);
+//   SEQRUN  the sequence pieces between two other tokens, each trimmed and
+//           copied back to back into the sequence buffer at the chunk's own
+//           file offset (trimmed bytes never outrun the raw ones);
+//   DOLLAR  a piece starting with '$', or the failed read at end of file
+//           (the reference's buffer then starts with '$').
+// The state machine then decides records and labels exactly as readFile
+// does: a record is emitted at the next HEADER / DOLLAR when its sequence is
+// not empty, a HEADER without sequence only counts, and DOLLAR ends input.
+struct Tok {
+    uint8_t kind;   // 0 HEADER, 1 SEQRUN, 2 DOLLAR
+    int64_t a, b;   // HEADER: file offset, length; SEQRUN: buffer offset, length
+};
 
-int parse_fasta(PieceReader& in, crispy_raw* r) {
+void tokenise(const char* data, size_t begin, size_t end, bool last, char* out, std::vector<Tok>& toks) {
+    PieceReader in{data, end, begin};
+    in.has_nul = std::memchr(data + begin, '\0', end - begin) != nullptr;   // this chunk's pieces only
+    in.stop_at_size = !last;
     Piece pc{};
-    if (!in.next(pc) || pc.n == 0 || pc.p[0] != '>') return CRISPY_E_INPUT;
-    const char* label = pc.p;
-    size_t label_n = space_trimmed(pc.p, pc.n);
-    int64_t start = (int64_t)r->bases.size();   // first byte of the pending sequence
-    int32_t idx = 0;
-    bool ended = false;
+    int64_t w = (int64_t)begin, run = -1;
+    auto close_run = [&]() {
+        if (run >= 0) toks.push_back(Tok{1, run, w - run});
+        run = -1;
+    };
     while (!in.eof) {
-        if (!in.next(pc)) pc = Piece{"$", 1, '$'};
+        if (!in.next(pc)) {
+            if (last) {   // end of file: the '$' marker
+                close_run();
+                toks.push_back(Tok{2, 0, 0});
+            }
+            break;
+        }
         const size_t k = space_trimmed(pc.p, pc.n);
         const char c0 = pc.n ? pc.p[0] : '\0';
         if (c0 != '>' && c0 != '$') {
-            r->bases.append(pc.p, seq_trimmed(pc.p, k));
+            const size_t k2 = seq_trimmed(pc.p, k);
+            if (run < 0) run = w;
+            std::memcpy(out + w, pc.p, k2);
+            w += (int64_t)k2;
             continue;
         }
-        if ((int64_t)r->bases.size() == start) {   // no sequence collected
-            ++idx;
-            if (pc.raw0 == '$') { ended = true; break; }
-            continue;
+        close_run();
+        if (c0 == '>') toks.push_back(Tok{0, (int64_t)(pc.p - data), (int64_t)k});
+        else toks.push_back(Tok{2, 0, 0});
+    }
+    close_run();
+    // the rest of the chunk's region is never read as sequence; writing it
+    // here keeps every page of the buffer resident before it is uploaded
+    std::memset(out + w, 0, end - (size_t)w);
+}
+
+int parse_fasta(const char* data, size_t size, crispy_raw* r) {
+    if (size == 0 || data[0] != '>') return CRISPY_E_INPUT;
+    // chunk boundaries: the first line start at or after each even cut that
+    // begins with '>'
+    // one chunk per MB, at most one per hardware thread and 16; the
+    // CRISPY_PARSE_CHUNKS environment variable sets the number (tests use it
+    // to cut small files)
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    int want = (int)std::max<size_t>(1, std::min<size_t>(std::min(16u, hw), size >> 20));
+    if (const char* e = std::getenv("CRISPY_PARSE_CHUNKS")) want = std::max(1, std::min(256, std::atoi(e)));
+    std::vector<size_t> cut{0};
+    for (int t = 1; t < want; ++t) {
+        size_t p = std::max(cut.back() + 1, size * (size_t)t / (size_t)want);
+        while (p < size && !(data[p - 1] == '\n' && data[p] == '>')) {
+            const void* nl = std::memchr(data + p, '\n', size - p);   // the next line start, past p
+            p = nl ? (size_t)((const char*)nl - data) + 1 : size;
         }
-        trim_tail(r, start);
-        push(r, start, label, label_n, 1);
-        ++idx;
-        start = (int64_t)r->bases.size();
-        if (pc.raw0 == '$') { ended = true; break; }
-        label = pc.p;
-        label_n = k;
+        if (p >= size) break;
+        cut.push_back(p);
     }
-    if (!ended && (int64_t)r->bases.size() != start) {
-        trim_tail(r, start);
-        push(r, start, label, label_n, 1);
-        ++idx;
+    cut.push_back(size);
+    const int chunks = (int)cut.size() - 1;
+    if (!r->fa_bases.alloc(size + 16)) return CRISPY_E_OOM;
+    std::vector<std::vector<Tok>> toks((size_t)chunks);
+    if (chunks == 1) {
+        tokenise(data, 0, size, true, r->fa_bases.p, toks[0]);
+    } else {
+        std::vector<std::thread> th;
+        for (int c = 0; c < chunks; ++c)
+            th.emplace_back(tokenise, data, cut[c], cut[c + 1], c + 1 == chunks, r->fa_bases.p,
+                            std::ref(toks[c]));
+        for (auto& t : th) t.join();
     }
+    // readFile's loop over the tokens (preprocess.cpp:100-166, 230-236)
+    const char* buf = r->fa_bases.p;
+    const Tok* label = nullptr;
+    int64_t pend = -1, plen = 0;   // the pending sequence (buffer offset, length)
+    int32_t idx = 0;
+    bool ended = false, first = true;
+    auto emit = [&]() {
+        const int64_t n = (int64_t)seq_trimmed(buf + pend, (size_t)plen);   // deleteSpacesInSeq(seq)
+        r->offsets.push_back(pend);
+        r->lengths.push_back((int32_t)n);
+        r->freq.push_back(1);
+        push_label(r, data + label->a, (size_t)label->b);
+        ++idx;
+        pend = -1;
+        plen = 0;
+    };
+    for (int c = 0; c < chunks && !ended; ++c) {
+        for (const Tok& t : toks[c]) {
+            if (first) {   // the first line must be a header (preprocess.cpp:107-118)
+                if (t.kind != 0) return CRISPY_E_INPUT;
+                label = &t;
+                first = false;
+                continue;
+            }
+            if (t.kind == 1) {
+                if (pend < 0) pend = t.a;
+                plen += t.b;
+                continue;
+            }
+            if (plen == 0) {
+                ++idx;
+                pend = -1;
+                if (t.kind == 2) { ended = true; break; }
+                continue;
+            }
+            emit();
+            if (t.kind == 2) { ended = true; break; }
+            label = &t;
+        }
+    }
+    if (first) return CRISPY_E_INPUT;
+    if (!ended && plen > 0) emit();
     r->records = idx;
     return CRISPY_OK;
 }
@@ -231,7 +366,7 @@ int crispy_raw_load(const char* path, int fastq, crispy_raw** out) {
     std::string copy;   // for inputs that cannot be mapped (pipes, special files)
     if (::fstat(fd, &sb) == 0 && S_ISREG(sb.st_mode) && sb.st_size > 0) {
         size = (size_t)sb.st_size;
-        map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE | MAP_POPULATE, fd, 0);
+        map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);   // chunk threads fault their pages in
     }
     if (map != MAP_FAILED) {
         data = static_cast<const char*>(map);
@@ -248,15 +383,21 @@ int crispy_raw_load(const char* path, int fastq, crispy_raw** out) {
     }
     auto* r = new crispy_raw();
     r->fastq = fastq != 0;
-    r->bases.reserve(size);
-    PieceReader in{data, size};
-    in.has_nul = size && std::memchr(data, '\0', size) != nullptr;
-    const int rc = fastq ? parse_fastq(in, r) : parse_fasta(in, r);
+    int rc;
+    if (fastq) {
+        r->bases.reserve(size);
+        PieceReader in{data, size};
+        in.has_nul = size && std::memchr(data, '\0', size) != nullptr;
+        rc = parse_fastq(in, r);
+    } else {
+        rc = parse_fasta(data, size, r);
+    }
     if (map != MAP_FAILED) ::munmap(map, size);
     ::close(fd);
     if (rc != CRISPY_OK) {
         delete r;
-        return crispy::fail(nullptr, rc, "%s is not in FASTA format", path);
+        return rc == CRISPY_E_INPUT ? crispy::fail(nullptr, rc, "%s is not in FASTA format", path)
+                                    : crispy::fail(nullptr, rc, "cannot allocate the records of %s", path);
     }
     *out = r;
     return CRISPY_OK;
@@ -266,7 +407,7 @@ int crispy_raw_view(const crispy_raw* r, const char** seqbuf, const int64_t** of
                     const int32_t** lengths, const uint8_t** freq, int32_t* n,
                     int32_t* records) {
     if (!r) return crispy::fail(nullptr, CRISPY_E_INPUT, "NULL handle");
-    if (seqbuf) *seqbuf = r->bases.data();
+    if (seqbuf) *seqbuf = r->data();
     if (offsets) *offsets = r->offsets.data();
     if (lengths) *lengths = r->lengths.data();
     if (freq) *freq = r->freq.data();
@@ -285,9 +426,11 @@ int crispy_raw_label(const crispy_raw* r, int32_t i, const char** label, int32_t
 
 void crispy_raw_free(crispy_raw* r) { delete r; }
 
-// writeToFile (preprocess.cpp:562-601).  Records are formatted into a
-// 4 MB buffer that is written out whenever it fills (one fwrite per
-// buffer), so no copy of the whole output is ever held.
+// writeToFile (preprocess.cpp:562-601).  Every record's place in the two
+// files is known from the lengths, so the records are formatted into two
+// buffers by up to 16 threads over contiguous ranges of kept reads (the
+// reads are gathered from scattered places of the record buffer), and each
+// file is written with one fwrite.
 int crispy_pre_write(const crispy_raw* r, const int32_t* index, const int32_t* freq,
                      int32_t kept, const char* out_path, int fastq) {
     if (!r || !out_path || kept < 0 || (kept && (!index || !freq)))
@@ -296,6 +439,62 @@ int crispy_pre_write(const crispy_raw* r, const int32_t* index, const int32_t* f
     for (int32_t k = 0; k < kept; ++k)
         if (index[k] < 0 || index[k] >= n)
             return crispy::fail(nullptr, CRISPY_E_INPUT, "record index out of range");
+    auto label_of = [&](int32_t i, size_t* len) -> const char* {
+        const char* lab = r->labels.data() + r->label_off[i];
+        size_t ll = (size_t)r->label_len[i];
+        if (!fastq && ll > 0) { ++lab; --ll; }   // label.substr(1): drop the '>'
+        *len = ll;
+        return lab;
+    };
+    auto digits = [](int64_t v) -> size_t {
+        size_t d = v < 0 ? 2 : 1;
+        for (v = v < 0 ? -v : v; v >= 10; v /= 10) ++d;
+        return d;
+    };
+    std::vector<size_t> so((size_t)kept + 1, 0), fo((size_t)kept + 1, 0);
+    for (int32_t k = 0; k < kept; ++k) {
+        size_t ll;
+        label_of(index[k], &ll);
+        so[k + 1] = so[k] + 2 + ll + 1 + (size_t)r->lengths[index[k]] + 1;   // "> %s\n%s\n"
+        fo[k + 1] = fo[k] + ll + 1 + digits(freq[k]) + 1;                    // "%s %d\n"
+    }
+    std::unique_ptr<char[]> sbuf(new char[so[kept] + 1]), fbuf(new char[fo[kept] + 1]);
+    const char* bases = r->data();
+    auto fill = [&](int32_t k0, int32_t k1) {
+        for (int32_t k = k0; k < k1; ++k) {
+            const int32_t i = index[k];
+            size_t ll;
+            const char* lab = label_of(i, &ll);
+            char* o = sbuf.get() + so[k];
+            *o++ = '>';
+            *o++ = ' ';
+            std::memcpy(o, lab, ll);
+            o += ll;
+            *o++ = '\n';
+            std::memcpy(o, bases + r->offsets[i], (size_t)r->lengths[i]);
+            o += r->lengths[i];
+            *o = '\n';
+            char* q = fbuf.get() + fo[k];
+            std::memcpy(q, lab, ll);
+            q += ll;
+            *q++ = ' ';
+            const size_t d = digits(freq[k]);
+            int64_t v = freq[k];
+            if (v < 0) { q[0] = '-'; v = -v; }
+            for (size_t j = d; j > (freq[k] < 0 ? 1u : 0u); --j) { q[j - 1] = (char)('0' + v % 10); v /= 10; }
+            q[d] = '\n';
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(16u, hw), (int64_t)kept / 4096));
+    if (nt == 1) {
+        fill(0, kept);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back(fill, (int32_t)((int64_t)kept * t / nt), (int32_t)((int64_t)kept * (t + 1) / nt));
+        for (auto& x : th) x.join();
+    }
     const std::string fname = std::string(out_path) + ".frq";
     FILE* fout = std::fopen(out_path, "wb");
     FILE* ff = std::fopen(fname.c_str(), "wb");
@@ -304,51 +503,8 @@ int crispy_pre_write(const crispy_raw* r, const int32_t* index, const int32_t* f
         if (ff) std::fclose(ff);
         return crispy::fail(nullptr, CRISPY_E_IO, "cannot open output files %s / %s", out_path, fname.c_str());
     }
-    constexpr size_t kChunk = 4u << 20;
-    struct Out {
-        FILE* f;
-        std::vector<char> buf;
-        size_t used = 0;
-    };
-    Out so{fout, std::vector<char>(kChunk)}, fo{ff, std::vector<char>(kChunk)};
-    bool ok = true;
-    auto put = [&](Out& o, const char* p, size_t len) {
-        if (o.used + len > kChunk) {
-            ok = ok && std::fwrite(o.buf.data(), 1, o.used, o.f) == o.used;
-            o.used = 0;
-            if (len > kChunk) {   // a read longer than the buffer goes out directly
-                ok = ok && std::fwrite(p, 1, len, o.f) == len;
-                return;
-            }
-        }
-        std::memcpy(o.buf.data() + o.used, p, len);
-        o.used += len;
-    };
-    char num[16];
-    for (int32_t k = 0; k < kept && ok; ++k) {
-        const int32_t i = index[k];
-        const char* lab = r->labels.data() + r->label_off[i];
-        size_t ll = (size_t)r->label_len[i];
-        if (!fastq && ll > 0) { ++lab; --ll; }   // label.substr(1): drop the '>'
-        put(so, "> ", 2);
-        put(so, lab, ll);
-        put(so, "\n", 1);
-        put(so, r->bases.data() + r->offsets[i], (size_t)r->lengths[i]);
-        put(so, "\n", 1);
-        put(fo, lab, ll);
-        // " %d\n"
-        char* e = num + sizeof num;
-        *--e = '\n';
-        int64_t v = freq[k];
-        const bool neg = v < 0;
-        if (neg) v = -v;
-        do { *--e = (char)('0' + v % 10); v /= 10; } while (v);
-        if (neg) *--e = '-';
-        *--e = ' ';
-        put(fo, e, (size_t)(num + sizeof num - e));
-    }
-    if (ok && so.used) ok = std::fwrite(so.buf.data(), 1, so.used, fout) == so.used;
-    if (ok && fo.used) ok = std::fwrite(fo.buf.data(), 1, fo.used, ff) == fo.used;
+    bool ok = std::fwrite(sbuf.get(), 1, so[kept], fout) == so[kept];
+    ok = std::fwrite(fbuf.get(), 1, fo[kept], ff) == fo[kept] && ok;
     ok = (std::fclose(fout) == 0) && ok;
     ok = (std::fclose(ff) == 0) && ok;
     return ok ? CRISPY_OK : crispy::fail(nullptr, CRISPY_E_IO, "short write to %s", out_path);

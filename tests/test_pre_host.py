@@ -102,6 +102,78 @@ def test_engine_host_parse_and_write(tmp_path, name):
     assert open(out + ".frq", "rb").read() == open(str(d / case["output"]) + ".frq", "rb").read()
 
 
+@pytest.mark.parametrize("chunks", [2, 3, 7, 64])
+@pytest.mark.parametrize("name", sorted(n for n, c in MANIFEST.items()
+                                        if "-s" not in c["args"] and "-p" not in c["args"]
+                                        and "-f" not in c["args"]))
+def test_engine_parse_in_chunks(tmp_path, monkeypatch, name, chunks):
+    """The FASTA parser cut into several chunks (parsed in parallel, then
+    stitched) reads the same records as in one pass."""
+    case = MANIFEST[name]
+    d = _case_dir(tmp_path, name)
+    monkeypatch.setenv("CRISPY_PARSE_CHUNKS", str(chunks))
+    raw = cg.RawReads(str(d / case["input"]))
+    monkeypatch.delenv("CRISPY_PARSE_CHUNKS")
+    one = cg.RawReads(str(d / case["input"]))
+    assert raw.records == one.records == case["total"] and raw.n == one.n
+    for i in range(raw.n):
+        assert raw.seq(i) == one.seq(i) and raw.label(i) == one.label(i)
+    index, freq = _host_sort_merge(raw)
+    out = str(d / "engine_out")
+    raw.write(index, freq, out)
+    assert open(out, "rb").read() == open(d / case["output"], "rb").read()
+
+
+def _boundary_fasta(rng):
+    """Records whose shapes meet chunk cuts: empty records, blank and
+    whitespace lines, a header longer than one fgets piece, lines of
+    exactly 4095 bytes, a '$' line late in the file."""
+    out = bytearray()
+    for i in range(400):
+        kind = i % 9
+        out += b">rec_%d some words\n" % i
+        if kind == 1:
+            continue                                   # header without sequence
+        s = rng.choice(np.frombuffer(b"ACGTNacgt", np.uint8), size=int(rng.integers(1, 300))).tobytes()
+        if kind == 2:
+            out += s[:50] + b"\n\n" + s[50:] + b"\n"    # blank line inside
+        elif kind == 3:
+            out += s + b"  \t\n   \n"                  # trailing whitespace lines
+        elif kind == 4:
+            out += b"C" * 4095 + b"\n" + s + b"\n"      # a line of exactly one piece
+        elif kind == 5 and i % 2:
+            out = out[:-1] + b"H" * 4200 + b"\n" + s + b"\n"   # header beyond one piece
+        else:
+            out += s + b"XX\n"
+    return bytes(out)
+
+
+@pytest.mark.parametrize("chunks", [1, 2, 5, 13, 40])
+def test_parse_chunk_boundaries_vs_oracle(tmp_path, monkeypatch, chunks):
+    rng = np.random.default_rng(chunks)
+    p = tmp_path / "b.fa"
+    p.write_bytes(_boundary_fasta(rng))
+    monkeypatch.setenv("CRISPY_PARSE_CHUNKS", str(chunks))
+    raw = cg.RawReads(str(p))
+    index, freq = _host_sort_merge(raw)
+    raw.write(index, freq, str(tmp_path / "eng"))
+    c = oracle.preprocess(str(p), str(tmp_path / "ora"))
+    assert raw.records == c["records"]
+    for e in ("", ".frq"):
+        assert open(str(tmp_path / "eng") + e, "rb").read() == open(str(tmp_path / "ora") + e, "rb").read()
+    # a '$' line ends the input in every chunking
+    q = tmp_path / "d.fa"
+    data = _boundary_fasta(rng)
+    cut = data.index(b">rec_300 ")
+    q.write_bytes(data[:cut] + b"$ stop\n" + data[cut:])
+    raw = cg.RawReads(str(q))
+    index, freq = _host_sort_merge(raw)
+    raw.write(index, freq, str(tmp_path / "eng2"))
+    c = oracle.preprocess(str(q), str(tmp_path / "ora2"))
+    assert raw.records == c["records"]
+    assert open(str(tmp_path / "eng2"), "rb").read() == open(str(tmp_path / "ora2"), "rb").read()
+
+
 def test_raw_load_errors(tmp_path):
     with pytest.raises(cg.CrispyError):
         cg.RawReads(str(tmp_path / "missing.fa"))
