@@ -11,6 +11,8 @@
 //   * an empty line inside a record contributes its '\n' to the sequence
 //     (it only has whitespace, and whitespace-only pieces are not trimmed);
 //   * a piece whose first byte is '$' is taken as end of input.
+// The scan itself (parallel chunks cut at header lines, then the loop over
+// their tokens) is shared with preprocess's reader (pre_io.cpp).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -20,72 +22,24 @@
 #include "internal.h"
 
 struct crispy_reads {
-    std::string bases;
+    crispy::FastaBuffer buf;   // each read at its chunk's offset
     std::vector<int64_t> offsets;
     std::vector<int32_t> lengths;
     int32_t max_len = 0;
 };
-
-namespace {
-
-constexpr size_t kPiece = 4096;  // kmerMain.h:24 / genMain.h:22 BUF_SIZE
-
-const char* kSpace = " \n\r\t\v\f\b";
-
-void rstrip_set_complement(std::string& s, const char* keep) {
-    size_t last = s.find_last_of(keep);
-    if (last != std::string::npos) s.erase(last + 1);
-}
-
-void rstrip_space(std::string& s) {
-    size_t last = s.find_last_not_of(kSpace);
-    if (last != std::string::npos) s.erase(last + 1);
-}
-
-}  // namespace
 
 extern "C" {
 
 int crispy_reads_load_fasta(const char* path, int flavour, crispy_reads** out) {
     if (!out || !path) return crispy::fail(nullptr, CRISPY_E_INPUT, "NULL argument");
     *out = nullptr;
-    FILE* fp = std::fopen(path, "rb");
-    if (!fp) return crispy::fail(nullptr, CRISPY_E_IO, "cannot open read file %s", path);
-    const char* keep = flavour ? "nNATGCatgc" : "ATGCatgc";
-    char piece[kPiece];
-    if (!std::fgets(piece, kPiece, fp) || piece[0] != '>') {
-        std::fclose(fp);
-        return crispy::fail(nullptr, CRISPY_E_INPUT, "%s is not in FASTA format", path);
-    }
     auto* r = new crispy_reads();
-    std::string pending;
-    auto emit = [&]() {
-        rstrip_set_complement(pending, keep);
-        r->offsets.push_back((int64_t)r->bases.size());
-        r->lengths.push_back((int32_t)pending.size());
-        r->max_len = std::max<int32_t>(r->max_len, (int32_t)pending.size());
-        r->bases.append(pending);
-        pending.clear();
-    };
-    enum { kMore, kEnd } state = kMore;
-    while (state == kMore && !std::feof(fp)) {
-        piece[0] = '$';  // stays '$' when fgets reaches end of file
-        if (!std::fgets(piece, kPiece, fp)) { /* piece keeps the '$' marker */ }
-        std::string s(piece);
-        rstrip_space(s);
-        const bool header_or_end = (s[0] == '>' || s[0] == '$');
-        if (!header_or_end) {
-            rstrip_set_complement(s, keep);
-            pending += s;
-        } else if (!pending.empty()) {
-            emit();
-            if (piece[0] == '$') state = kEnd;
-        } else if (piece[0] == '$') {
-            state = kEnd;
-        }
+    const int rc = crispy::scan_stage_fasta(path, flavour, r->buf, r->offsets, r->lengths);
+    if (rc != CRISPY_OK) {
+        delete r;
+        return rc;
     }
-    if (state == kMore && !pending.empty()) emit();
-    std::fclose(fp);
+    for (int32_t l : r->lengths) r->max_len = std::max(r->max_len, l);
     *out = r;
     return CRISPY_OK;
 }
@@ -93,7 +47,7 @@ int crispy_reads_load_fasta(const char* path, int flavour, crispy_reads** out) {
 int crispy_reads_view(const crispy_reads* r, const char** seqbuf, const int64_t** offsets,
                       const int32_t** lengths, int32_t* n, int32_t* max_len) {
     if (!r) return CRISPY_E_INPUT;
-    if (seqbuf) *seqbuf = r->bases.data();
+    if (seqbuf) *seqbuf = r->buf.p;
     if (offsets) *offsets = r->offsets.data();
     if (lengths) *lengths = r->lengths.data();
     if (n) *n = (int32_t)r->lengths.size();

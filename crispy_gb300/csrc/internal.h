@@ -149,6 +149,24 @@ void graph_clear(crispy_ctx* ctx);
 // split differently and only the file itself gives the stage's reads.
 int pre_stage_reads(crispy_ctx* ctx, const crispy_raw* raw, int flavour, const uint8_t** d_bytes,
                     size_t* bytes, const int64_t** d_off, std::vector<int32_t>& h_len);
+// Read buffer of the FASTA scans: an anonymous mapping with transparent
+// huge pages (pre_io.cpp).
+struct FastaBuffer {
+    char* p = nullptr;
+    size_t n = 0;
+    FastaBuffer() = default;
+    FastaBuffer(const FastaBuffer&) = delete;
+    FastaBuffer& operator=(const FastaBuffer&) = delete;
+    ~FastaBuffer();
+    bool alloc(size_t bytes);
+};
+
+// The reads of a FASTA file as kmerDist (flavour 0, kmerMain.cpp:298-397)
+// or genDist (flavour 1, genMain.cpp:184-277) parse it, scanned in parallel
+// chunks (pre_io.cpp): each read at buf.p + offsets[i], lengths[i] bytes.
+int scan_stage_fasta(const char* path, int flavour, FastaBuffer& buf, std::vector<int64_t>& offsets,
+                     std::vector<int32_t>& lengths);
+
 // Records of a raw handle, and the length of the "> label" line
 // writeToFile gives record i, newline excluded (pre_io.cpp).
 int32_t raw_records(const crispy_raw* r);

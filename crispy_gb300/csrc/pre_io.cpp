@@ -35,28 +35,34 @@
 
 #include "internal.h"
 
-// Anonymous mapping that asks for transparent huge pages: the parse threads
-// then take one fault per 2 MB instead of one per 4 KB.
-struct BigBuf {
-    char* p = nullptr;
-    size_t n = 0;
-    ~BigBuf() { if (p) ::munmap(p, n); }
-    bool alloc(size_t bytes) {
-        n = (bytes + (2u << 20) - 1) & ~(size_t)((2u << 20) - 1);
-        void* m = ::mmap(nullptr, n, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-        if (m == MAP_FAILED) { p = nullptr; n = 0; return false; }
-        p = static_cast<char*>(m);
-#ifdef MADV_HUGEPAGE
-        ::madvise(p, n, MADV_HUGEPAGE);
-#endif
-        return true;
+namespace crispy {
+
+// An anonymous mapping that asks for transparent huge pages: the parse
+// threads then take one fault per 2 MB instead of one per 4 KB.
+FastaBuffer::~FastaBuffer() {
+    if (p) ::munmap(p, n);
+}
+bool FastaBuffer::alloc(size_t bytes) {
+    n = (bytes + (2u << 20) - 1) & ~(size_t)((2u << 20) - 1);
+    void* m = ::mmap(nullptr, n, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (m == MAP_FAILED) {
+        p = nullptr;
+        n = 0;
+        return false;
     }
-};
+    p = static_cast<char*>(m);
+#ifdef MADV_HUGEPAGE
+    ::madvise(p, n, MADV_HUGEPAGE);
+#endif
+    return true;
+}
+
+}  // namespace crispy
 
 struct crispy_raw {
     bool fastq = false;
-    std::string bases;   // FASTQ: sequences back to back
-    BigBuf fa_bases;     // FASTA: sequences at their chunk's file offsets
+    std::string bases;                // FASTQ: sequences back to back
+    crispy::FastaBuffer fa_bases;     // FASTA: sequences at their chunk's file offsets
     const char* data() const { return fa_bases.p ? fa_bases.p : bases.data(); }
     std::vector<int64_t> offsets;
     std::vector<int32_t> lengths;
@@ -75,15 +81,16 @@ constexpr size_t kPieceMax = 4095;   // fgets(buf, BUF_SIZE = 4096, ...) (prepro
 bool trim_space_char(unsigned char c) {
     return c == '\n' || c == '\r' || c == ' ' || c == '\t' || c == '\v' || c == '\f' || c == '\b';
 }
-// deleteSpacesInSeq (preprocess.cpp:65-71) cuts after the last of these
-bool seq_keep_char(unsigned char c) {
-    switch (c) {
-        case 'n': case 'N': case 'A': case 'T': case 'G': case 'C': case 'a': case 't': case 'g': case 'c':
-            return true;
-        default:
-            return false;
+// The letters a sequence piece is cut back to: deleteSpacesInSeq's
+// "nNATGCatgc" (preprocess.cpp:65-71, genMain.cpp:175-181) or kmerDist's
+// "ATGCatgc" (kmerMain.cpp:289-295).
+struct KeepSet {
+    bool in[256] = {};
+    explicit KeepSet(const char* letters) {
+        for (const char* c = letters; *c; ++c) in[(unsigned char)*c] = true;
     }
-}
+};
+const KeepSet kPreKeep("nNATGCatgc");
 bool is_space(unsigned char c) {   // isspace in the "C" locale
     return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
 }
@@ -94,10 +101,10 @@ size_t space_trimmed(const char* p, size_t n) {
     while (k > 0 && trim_space_char((unsigned char)p[k - 1])) --k;
     return k ? k : n;
 }
-// Length after deleteSpacesInSeq: cut after the last base letter, if any.
-size_t seq_trimmed(const char* p, size_t n) {
+// Length after deleteSpacesInSeq: cut after the last kept letter, if any.
+size_t seq_trimmed(const char* p, size_t n, const KeepSet& keep) {
     size_t k = n;
-    while (k > 0 && !seq_keep_char((unsigned char)p[k - 1])) --k;
+    while (k > 0 && !keep.in[(unsigned char)p[k - 1]]) --k;
     return k ? k : n;
 }
 
@@ -192,7 +199,8 @@ struct Tok {
     int64_t a, b;   // HEADER: file offset, length; SEQRUN: buffer offset, length
 };
 
-void tokenise(const char* data, size_t begin, size_t end, bool last, char* out, std::vector<Tok>& toks) {
+void tokenise(const char* data, size_t begin, size_t end, bool last, const KeepSet* keep, char* out,
+              std::vector<Tok>& toks) {
     PieceReader in{data, end, begin};
     in.has_nul = std::memchr(data + begin, '\0', end - begin) != nullptr;   // this chunk's pieces only
     in.stop_at_size = !last;
@@ -213,7 +221,7 @@ void tokenise(const char* data, size_t begin, size_t end, bool last, char* out, 
         const size_t k = space_trimmed(pc.p, pc.n);
         const char c0 = pc.n ? pc.p[0] : '\0';
         if (c0 != '>' && c0 != '$') {
-            const size_t k2 = seq_trimmed(pc.p, k);
+            const size_t k2 = seq_trimmed(pc.p, k, *keep);
             if (run < 0) run = w;
             std::memcpy(out + w, pc.p, k2);
             w += (int64_t)k2;
@@ -229,13 +237,17 @@ void tokenise(const char* data, size_t begin, size_t end, bool last, char* out, 
     std::memset(out + w, 0, end - (size_t)w);
 }
 
-int parse_fasta(const char* data, size_t size, crispy_raw* r) {
+// The FASTA records of data[0, size): sequences into buf (at their chunk's
+// offsets), their offsets and lengths; with labels != NULL also the label
+// of each record (whitespace removed); *records = readIndex.
+int scan_fasta(const char* data, size_t size, const KeepSet& keep, crispy::FastaBuffer& buf,
+               std::vector<int64_t>& offsets, std::vector<int32_t>& lengths, crispy_raw* labels,
+               int32_t* records) {
     if (size == 0 || data[0] != '>') return CRISPY_E_INPUT;
     // chunk boundaries: the first line start at or after each even cut that
-    // begins with '>'
-    // one chunk per MB, at most one per hardware thread and 16; the
-    // CRISPY_PARSE_CHUNKS environment variable sets the number (tests use it
-    // to cut small files)
+    // begins with '>'; one chunk per MB, at most one per hardware thread and
+    // 16 (the CRISPY_PARSE_CHUNKS environment variable sets the number:
+    // tests use it to cut small files)
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     int want = (int)std::max<size_t>(1, std::min<size_t>(std::min(16u, hw), size >> 20));
     if (const char* e = std::getenv("CRISPY_PARSE_CHUNKS")) want = std::max(1, std::min(256, std::atoi(e)));
@@ -251,29 +263,27 @@ int parse_fasta(const char* data, size_t size, crispy_raw* r) {
     }
     cut.push_back(size);
     const int chunks = (int)cut.size() - 1;
-    if (!r->fa_bases.alloc(size + 16)) return CRISPY_E_OOM;
+    if (!buf.alloc(size + 16)) return CRISPY_E_OOM;
     std::vector<std::vector<Tok>> toks((size_t)chunks);
     if (chunks == 1) {
-        tokenise(data, 0, size, true, r->fa_bases.p, toks[0]);
+        tokenise(data, 0, size, true, &keep, buf.p, toks[0]);
     } else {
         std::vector<std::thread> th;
         for (int c = 0; c < chunks; ++c)
-            th.emplace_back(tokenise, data, cut[c], cut[c + 1], c + 1 == chunks, r->fa_bases.p,
-                            std::ref(toks[c]));
+            th.emplace_back(tokenise, data, cut[c], cut[c + 1], c + 1 == chunks, &keep, buf.p, std::ref(toks[c]));
         for (auto& t : th) t.join();
     }
-    // readFile's loop over the tokens (preprocess.cpp:100-166, 230-236)
-    const char* buf = r->fa_bases.p;
+    // readFile's loop over the tokens (preprocess.cpp:100-166, 230-236; the
+    // stages' readFile, kmerMain.cpp:298-397, runs the same loop)
     const Tok* label = nullptr;
     int64_t pend = -1, plen = 0;   // the pending sequence (buffer offset, length)
     int32_t idx = 0;
     bool ended = false, first = true;
     auto emit = [&]() {
-        const int64_t n = (int64_t)seq_trimmed(buf + pend, (size_t)plen);   // deleteSpacesInSeq(seq)
-        r->offsets.push_back(pend);
-        r->lengths.push_back((int32_t)n);
-        r->freq.push_back(1);
-        push_label(r, data + label->a, (size_t)label->b);
+        const int64_t n = (int64_t)seq_trimmed(buf.p + pend, (size_t)plen, keep);   // deleteSpacesInSeq(seq)
+        offsets.push_back(pend);
+        lengths.push_back((int32_t)n);
+        if (labels) push_label(labels, data + label->a, (size_t)label->b);
         ++idx;
         pend = -1;
         plen = 0;
@@ -304,9 +314,48 @@ int parse_fasta(const char* data, size_t size, crispy_raw* r) {
     }
     if (first) return CRISPY_E_INPUT;
     if (!ended && plen > 0) emit();
-    r->records = idx;
+    *records = idx;
     return CRISPY_OK;
 }
+
+int parse_fasta(const char* data, size_t size, crispy_raw* r) {
+    const int rc = scan_fasta(data, size, kPreKeep, r->fa_bases, r->offsets, r->lengths, r, &r->records);
+    r->freq.assign(r->offsets.size(), 1);
+    return rc;
+}
+
+// The file mapped read-only (or read, where it cannot be mapped).
+struct MappedFile {
+    const char* data = nullptr;
+    size_t size = 0;
+    void* map = MAP_FAILED;
+    int fd = -1;
+    std::string copy;
+    int open(const char* path) {
+        fd = ::open(path, O_RDONLY);
+        if (fd < 0) return CRISPY_E_IO;
+        struct stat sb;
+        if (::fstat(fd, &sb) == 0 && S_ISREG(sb.st_mode) && sb.st_size > 0) {
+            size = (size_t)sb.st_size;
+            map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);   // chunk threads fault their pages in
+        }
+        if (map != MAP_FAILED) {
+            data = static_cast<const char*>(map);
+            return CRISPY_OK;
+        }
+        char b[1 << 16];
+        ssize_t got;
+        while ((got = ::read(fd, b, sizeof b)) > 0) copy.append(b, (size_t)got);
+        if (got < 0) return CRISPY_E_IO;
+        data = copy.data();
+        size = copy.size();
+        return CRISPY_OK;
+    }
+    ~MappedFile() {
+        if (map != MAP_FAILED) ::munmap(map, size);
+        if (fd >= 0) ::close(fd);
+    }
+};
 
 int parse_fastq(PieceReader& in, crispy_raw* r) {
     Piece pc{}, lab{};
@@ -343,6 +392,19 @@ int parse_fastq(PieceReader& in, crispy_raw* r) {
 
 namespace crispy {
 
+int scan_stage_fasta(const char* path, int flavour, FastaBuffer& buf, std::vector<int64_t>& offsets,
+                     std::vector<int32_t>& lengths) {
+    static const KeepSet kmer_keep("ATGCatgc"), gen_keep("nNATGCatgc");
+    MappedFile f;
+    if (f.open(path) != CRISPY_OK) return fail(nullptr, CRISPY_E_IO, "cannot open read file %s", path);
+    int32_t records = 0;
+    const int rc = scan_fasta(f.data, f.size, flavour ? gen_keep : kmer_keep, buf, offsets, lengths, nullptr,
+                              &records);
+    if (rc == CRISPY_E_INPUT) return fail(nullptr, rc, "%s is not in FASTA format", path);
+    if (rc != CRISPY_OK) return fail(nullptr, rc, "cannot allocate the reads of %s", path);
+    return CRISPY_OK;
+}
+
 int32_t raw_records(const crispy_raw* r) { return (int32_t)r->lengths.size(); }
 
 int64_t raw_header_line(const crispy_raw* r, int32_t i) {
@@ -357,43 +419,19 @@ extern "C" {
 int crispy_raw_load(const char* path, int fastq, crispy_raw** out) {
     if (!out || !path) return crispy::fail(nullptr, CRISPY_E_INPUT, "NULL argument");
     *out = nullptr;
-    const int fd = ::open(path, O_RDONLY);
-    if (fd < 0) return crispy::fail(nullptr, CRISPY_E_IO, "cannot open read file %s", path);
-    struct stat sb;
-    const char* data = nullptr;
-    size_t size = 0;
-    void* map = MAP_FAILED;
-    std::string copy;   // for inputs that cannot be mapped (pipes, special files)
-    if (::fstat(fd, &sb) == 0 && S_ISREG(sb.st_mode) && sb.st_size > 0) {
-        size = (size_t)sb.st_size;
-        map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);   // chunk threads fault their pages in
-    }
-    if (map != MAP_FAILED) {
-        data = static_cast<const char*>(map);
-    } else {
-        char buf[1 << 16];
-        ssize_t got;
-        while ((got = ::read(fd, buf, sizeof buf)) > 0) copy.append(buf, (size_t)got);
-        if (got < 0) {
-            ::close(fd);
-            return crispy::fail(nullptr, CRISPY_E_IO, "cannot read %s", path);
-        }
-        data = copy.data();
-        size = copy.size();
-    }
+    MappedFile f;
+    if (f.open(path) != CRISPY_OK) return crispy::fail(nullptr, CRISPY_E_IO, "cannot open read file %s", path);
     auto* r = new crispy_raw();
     r->fastq = fastq != 0;
     int rc;
     if (fastq) {
-        r->bases.reserve(size);
-        PieceReader in{data, size};
-        in.has_nul = size && std::memchr(data, '\0', size) != nullptr;
+        r->bases.reserve(f.size);
+        PieceReader in{f.data, f.size};
+        in.has_nul = f.size && std::memchr(f.data, '\0', f.size) != nullptr;
         rc = parse_fastq(in, r);
     } else {
-        rc = parse_fasta(data, size, r);
+        rc = parse_fasta(f.data, f.size, r);
     }
-    if (map != MAP_FAILED) ::munmap(map, size);
-    ::close(fd);
     if (rc != CRISPY_OK) {
         delete r;
         return rc == CRISPY_E_INPUT ? crispy::fail(nullptr, rc, "%s is not in FASTA format", path)

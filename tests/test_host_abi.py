@@ -69,15 +69,24 @@ FASTA_CASES = {
 }
 
 
+def _reads_of(parsed):
+    data, offs, lens = parsed
+    return [data[o:o + l].tobytes() for o, l in zip(offs.tolist(), lens.tolist())]
+
+
+@pytest.mark.parametrize("chunks", [None, "3", "9"])
 @pytest.mark.parametrize("case", sorted(FASTA_CASES))
 @pytest.mark.parametrize("flavour", [0, 1])
-def test_fasta_parser_matches_oracle(tmp_path, case, flavour):
+def test_fasta_parser_matches_oracle(tmp_path, monkeypatch, case, flavour, chunks):
+    """Same reads as the oracle's parse, also when the file is scanned in
+    several chunks (CRISPY_PARSE_CHUNKS) and the reads sit at chunk offsets."""
     p = str(tmp_path / case)
-    _write(p, FASTA_CASES[case])
+    _write(p, FASTA_CASES[case] * 7)
+    if chunks:
+        monkeypatch.setenv("CRISPY_PARSE_CHUNKS", chunks)
     a = cg.read_fasta(p, flavour)
     b = oracle.read_fasta(p, flavour)
-    for x, y in zip(a, b):
-        assert np.array_equal(x, y)
+    assert _reads_of(a) == _reads_of(b)
 
 
 def test_fasta_not_fasta(tmp_path):
