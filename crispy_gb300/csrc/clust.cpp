@@ -35,6 +35,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -330,19 +331,49 @@ struct Clusterer {
         ++new_id;
     }
 
-    // updateAllMin (aveclust.cpp:621-647)
+    // updateAllMin (aveclust.cpp:621-647).  A node's links are keyed by
+    // smaller IDs, so computeDist only ever writes the node's own exact /
+    // inexact entries: the nodes are independent and run on up to 16
+    // threads, each node in its own link-map order, and the minimum trees
+    // are rebuilt once at the end.
     void update_all_min() {
-        exact.fill(1.0f, (int)nodes.size());
-        inexact.fill(1.0f, (int)nodes.size());
-        for (size_t i = 0; i < nodes.size(); ++i) {
-            if (!active[i] || nodes[i].links.empty()) continue;
-            Node& x = nodes[i];
-            for (auto& kv : x.links) {
-                Node& y = nodes[kv.first];
-                if (x.id > y.id) compute_link(x, y, kv.second);
-                else compute(y, x);
+        const int64_t total = (int64_t)nodes.size();
+        for (int64_t i = 0; i < total; ++i) { exact.v[i] = 1.0f; inexact.v[i] = 1.0f; }
+        auto range = [&](int64_t lo, int64_t hi) {
+            for (int64_t i = lo; i < hi; ++i) {
+                if (!active[i] || nodes[i].links.empty()) continue;
+                Node& x = nodes[i];
+                float ex = 1.0f, in = 1.0f;
+                int exn = exact_node[i];
+                for (auto& kv : x.links) {
+                    if (kv.first >= x.id) continue;   // links are keyed by smaller IDs
+                    const Node& y = nodes[kv.first];
+                    const unsigned int tot = x.members * y.members;
+                    const unsigned int unlinked = tot - kv.second.num;
+                    if (unlinked == 0 || all_loaded) {
+                        const float d = (kv.second.sum + end_level * (float)unlinked) / (float)tot;
+                        if (d < ex) { ex = d; exn = (int)y.id; }
+                    } else {
+                        const float d = (kv.second.sum + lambda * (float)unlinked) / (float)tot;
+                        if (d < in) in = d;
+                    }
+                }
+                exact.v[i] = ex;
+                inexact.v[i] = in;
+                exact_node[i] = exn;
             }
+        };
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(16u, hw), total / 16384));
+        if (nt == 1) {
+            range(0, total);
+        } else {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nt; ++t) th.emplace_back(range, total * t / nt, total * (t + 1) / nt);
+            for (auto& x : th) x.join();
         }
+        exact.rebuild();
+        inexact.rebuild();
     }
 };
 
@@ -483,10 +514,19 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         if (!seen[r]) { seen[r] = 1; roots.push_back(r); }
     }
     std::sort(roots.begin(), roots.end());
-    std::string cl, cf;
+    // the levels as the reference's float loop visits them, then one thread
+    // per level (each reads the finished trees only)
     const float step = C.end_level / 10;
-    std::string report;
-    for (float level = step; level < C.end_level || std::fabs(level - C.end_level) < kEps; level += step) {
+    std::vector<float> levels;
+    for (float level = step; level < C.end_level || std::fabs(level - C.end_level) < kEps; level += step)
+        levels.push_back(level);
+    const size_t nl = levels.size();
+    std::vector<std::string> cls(nl), cfs(nl), reps(nl);
+    auto one_level = [&](size_t li) {
+        const float level = levels[li];
+        std::string& cl = cls[li];
+        std::string& cf = cfs[li];
+        char buf[96];
         auto within = [&](int i) { return C.nodes[i].dist < level || std::fabs(C.nodes[i].dist - level) < kEps; };
         std::vector<int> cut;   // the reference's nodeList, built with push_front
         for (int r : roots) {
@@ -502,9 +542,10 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         }
         std::reverse(cut.begin(), cut.end());
         put_level_line(cl, cf, level);
+        std::vector<int> todo;
         for (int top : cut) {
             cf += '|';
-            std::vector<int> todo{top};
+            todo.assign(1, top);
             bool first = true;
             unsigned int size = 0;
             while (!todo.empty()) {
@@ -512,7 +553,7 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
                 todo.pop_back();
                 const Node& nd = C.nodes[t];
                 if (nd.left < 0 && nd.right < 0) {
-                    char* e = line + sizeof line;
+                    char* e = buf + sizeof buf;
                     char* b = put_uint(e, nd.id);
                     if (!first) *--b = ' ';
                     cf.append(b, (size_t)(e - b));
@@ -522,11 +563,13 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
                 if (nd.right >= 0) todo.push_back(nd.right);
                 if (nd.left >= 0) todo.push_back(nd.left);
             }
-            std::snprintf(line, sizeof line, "%d ", (int)size);
-            cl += line;
+            char* e = buf + sizeof buf;
+            *--e = ' ';
+            char* b = put_uint(e, size);   // "%d " of an unsigned count below 2^31
+            cl.append(b, (size_t)(buf + sizeof buf - b));
         }
         for (int o : orphans) {
-            char* e = line + sizeof line;
+            char* e = buf + sizeof buf;
             char* b = put_uint(e, (unsigned)o);
             *--b = '|';
             cf.append(b, (size_t)(e - b));
@@ -534,9 +577,20 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         }
         cf += "|\n";
         cl += "\n";
-        std::snprintf(line, sizeof line, "Dist: %.6f. numOTUs: %u. numSingletons: %lu\n", level,
+        std::snprintf(buf, sizeof buf, "Dist: %.6f. numOTUs: %u. numSingletons: %lu\n", level,
                       (unsigned)(cut.size() + orphans.size()), (unsigned long)orphans.size());
-        report += line;
+        reps[li] = buf;
+    };
+    {
+        std::vector<std::thread> th;
+        for (size_t li = 0; li < nl; ++li) th.emplace_back(one_level, li);
+        for (auto& t : th) t.join();
+    }
+    std::string cl, cf, report;
+    for (size_t li = 0; li < nl; ++li) {
+        cl += cls[li];
+        cf += cfs[li];
+        report += reps[li];
     }
     const std::string base(out_base);
     struct Out { std::string name; const std::string* body; } outs[] = {
