@@ -386,6 +386,7 @@ def run_ours(args, dist, ws, rank, local):
     if rank == 0 and not args.no_pre:
         line["preprocess"] = preprocess_bench(args, local)
         line["aveclust"] = clust_bench(args, local, chunks, n)
+        line["crispy_run"] = run_bench(args)
     if rank == 0 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as td:
             kpps, gcups, cores, desc, _ = _cpu_sample(reads, k, band, args.cpu_sample_reads, td)
@@ -489,6 +490,39 @@ def clust_bench(args, local: int, chunks, n: int) -> dict:
                             "ms": ours, "cpu_baseline": {"ms": cpu, "cores": 1, "kind": "port",
                                                          "sample": "the whole 20k-read chunk set"},
                             "merge_file_identical": bool(same and om == st20["merges"])}
+    return out
+
+
+def run_bench(args) -> dict:
+    """crispyRun: crispy.sh from the raw FASTA through aveclust in one
+    process (preprocess, kmerDist, genDist, aveclust; every file written).
+    Wall time of the executable on the workload's raw reads, best of 2 after
+    one warm-up, and the time it prints itself."""
+    import subprocess as sp
+
+    import crispy_gb300 as cg
+
+    reads = synth.generate(synth.WORKLOADS[WORKLOADS[args.workload][0]])
+    _, k, band = WORKLOADS[args.workload]
+    out = {"input_reads": len(reads), "k": k, "band": band}
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "raw.fa"), "wb") as f:
+            for i, s in enumerate(reads):
+                f.write(b">read_%d synthetic\n" % i)
+                for a in range(0, len(s), 60):
+                    f.write(s[a:a + 60] + b"\n")
+        walls = []
+        for it in range(3):
+            t0 = time.perf_counter()
+            p = sp.run([os.path.join(cg.BIN_DIR, "crispyRun"), "raw.fa", str(k), str(band)], cwd=td,
+                       stdout=sp.PIPE, stderr=sp.STDOUT)
+            if p.returncode != 0:
+                return {"error": p.stdout.decode(errors="replace")[-300:]}
+            if it:
+                walls.append(time.perf_counter() - t0)
+        files = sorted(f for f in os.listdir(td) if f != "raw.fa")
+        out.update({"wall_ms": min(walls) * 1e3, "files": files,
+                    "stdout_tail": p.stdout.decode(errors="replace").strip().splitlines()[-3:]})
     return out
 
 
