@@ -45,6 +45,11 @@ struct KmerJob {
     DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
     DevBuf tgentL, nsec;             // K = 8: L-stream steps per group; per-read H/L counts
     std::vector<int32_t> h_nsec;
+    // K = 8 read order: per-read arrays above (t, cntmax, hinfo, entries)
+    // are by position in it; perm maps position -> read ID, offp holds the
+    // offsets by position, t0 the tuple counts by read ID
+    DevBuf t0, offp, perm;
+    std::vector<int32_t> h_perm;
     // last run's survivors, in stage order: on the device, or (spilled) in
     // pinned host memory when they outgrow the device share
     int64_t nsurv = 0;

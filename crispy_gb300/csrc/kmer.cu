@@ -215,6 +215,54 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
 }
 
 // ---------------------------------------------------------------------------
+// K = 8 read order.  The tile kernel adds a pair's L half only where both
+// reads have the same H key (largest H K-mer and its count, or no H K-mer).
+// Sorting the reads by (H key, tuple count) puts reads of one key next to
+// one another, so that most warps of the tile kernel hold no pair with
+// [same] and skip their L phase; the tuple count keeps the 32-read groups'
+// padding small.  One warp per read finds the largest H K-mer, then counts
+// it; the sort key is (H key << tbits) | T, the payload the read index.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) kmer_hkey_kernel(const uint8_t* __restrict__ seq,
+                                                        const int64_t* __restrict__ off,
+                                                        const int32_t* __restrict__ tcount, int n,
+                                                        int tbits, uint64_t* __restrict__ keys,
+                                                        uint32_t* __restrict__ idx) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < n; r += nw) {
+        const int T = tcount[r];
+        const uint8_t* s = seq + off[r];
+        uint32_t hm = 0;
+        for (int p = lane; p < T; p += 32) {
+            const uint32_t v = kmer_at(s, p, 8);
+            if (v >= 0x8000u) hm = max(hm, v);
+        }
+        hm = __reduce_max_sync(full, hm);
+        uint32_t c = 0;
+        if (hm != 0u)
+            for (int p = lane; p < T; p += 32) c += kmer_at(s, p, 8) == hm;
+        c = __reduce_add_sync(full, c);
+        if (lane == 0) {
+            const uint32_t key = hm != 0u ? (hm << 16) | (c & 0xFFFFu) : 0u;
+            keys[r] = ((uint64_t)key << tbits) | (uint32_t)T;
+            idx[r] = (uint32_t)r;
+        }
+    }
+}
+
+__global__ void kmer_gather_off_kernel(const int64_t* __restrict__ off, const uint32_t* __restrict__ perm,
+                                       int n, int64_t* __restrict__ offp, int32_t* __restrict__ permi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t r = perm[i];
+        offp[i] = off[r];
+        permi[i] = (int32_t)r;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Bank schedule of the tile stream.  The tile kernel's plane words are
 // 64-bit (64 row reads), so a warp's gather is served as two half-warps of
 // 16 lanes, and word w sits in double bank w mod 16.  One warp per 32-read
@@ -461,6 +509,10 @@ struct TileArgs {
     const int32_t* tgentL;         // L-stream steps per group (H: tgent)
     const uint32_t* hinfo;         // per read: (largest H K-mer << 16) | its count, 0 if none
     int ngroups;
+    // read order of the job (position -> read ID), nullptr: identity; with
+    // an order, pairs are kept whose lower read ID lies in [olo, ohi)
+    const int32_t* perm;
+    int olo, ohi;
 };
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
@@ -479,9 +531,19 @@ __device__ __forceinline__ uint64_t stage_key(int r, int c, int n, int A, int sd
 }
 
 // Survivor emission with one atomic per warp.  All 32 lanes call it.
+// (r, c) are positions in the job's read order; with a read order (perm !=
+// nullptr, K = 8) they map back to the caller's read IDs, the pair is
+// reordered so that the lower ID comes first, and only pairs whose lower ID
+// lies in [olo, ohi) are kept (the stage rows of one pass).
 __device__ __forceinline__ void emit(unsigned long long* counter, uint64_t* keys, uint32_t* vals,
-                                     int64_t cap, int n, int A, int sd, bool pass, int r, int c,
-                                     int m, int mn) {
+                                     int64_t cap, int n, int A, int sd, const int32_t* perm,
+                                     int olo, int ohi, bool pass, int r, int c, int m, int mn) {
+    if (perm != nullptr && pass) {
+        const int pr = __ldg(perm + r), pc = __ldg(perm + c);
+        r = min(pr, pc);
+        c = max(pr, pc);
+        pass = r >= olo && r < ohi;
+    }
     const unsigned pm = __ballot_sync(0xffffffffu, pass);
     if (!pm) return;
     const int lane = threadIdx.x & 31;
@@ -659,7 +721,7 @@ __device__ __forceinline__ void finish_half(const TileArgs& a, const uint32_t* X
             mn = min(rowT[b], tc);
             pass = m >= (int)a.mmin[mn];
         }
-        emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
+        emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
     }
 }
 
@@ -1211,9 +1273,25 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
             const uint4* epAL = reinterpret_cast<const uint4*>(a.tent + a.tstart[gA] + 32LL * a.tgent[gA]) + lane;
             const uint4* epBH = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB]) + lane : epAH;
             const uint4* epBL = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB] + 32LL * a.tgent[gB]) + lane : epAL;
+            // [same] per (row, column): the L sums count only where it holds
+            const uint32_t hA = okA ? a.hinfo[cA] : 0u, hB = okB ? a.hinfo[cB] : 0u;
+            uint32_t same = 0;
+#pragma unroll
+            for (int b = 0; b < kRows8; ++b) {
+                const uint32_t hr = s_rowH[b];
+                same |= (uint32_t)((hr == 0u && hA == 0u) || (hr != 0u && hr == hA)) << b;
+                same |= (uint32_t)((hr == 0u && hB == 0u) || (hr != 0u && hr == hB)) << (b + 16);
+            }
             uint32_t XH[B], XL[B];
             phase8<B>(P8, epAH, a.tgent[gA], epBH, hasB ? a.tgent[gB] : 0, XH);
-            phase8<B>(P8 + kPlane8, epAL, a.tgentL[gA], epBL, hasB ? a.tgentL[gB] : 0, XL);
+            // a warp none of whose pairs has [same] skips the L phase (reads
+            // ordered by their H key make most warps like that)
+            if (__any_sync(full, same & vmask)) {
+                phase8<B>(P8 + kPlane8, epAL, a.tgentL[gA], epBL, hasB ? a.tgentL[gB] : 0, XL);
+            } else {
+#pragma unroll
+                for (int k = 0; k < B; ++k) XL[k] = 0u;
+            }
             if (any_high) {
                 // repeated occurrences (rank >= 1) lead each read's level list
                 const int nhA = okA ? a.nhigh[cA] : 0, nhB = okB ? a.nhigh[cB] : 0;
@@ -1236,15 +1314,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                     Counter<B>::add_at(XL, hL, 0);
                 }
             }
-            // [same] per (row, column), then X = XH + (XL & same), bit-sliced
-            const uint32_t hA = okA ? a.hinfo[cA] : 0u, hB = okB ? a.hinfo[cB] : 0u;
-            uint32_t same = 0;
-#pragma unroll
-            for (int b = 0; b < kRows8; ++b) {
-                const uint32_t hr = s_rowH[b];
-                same |= (uint32_t)((hr == 0u && hA == 0u) || (hr != 0u && hr == hA)) << b;
-                same |= (uint32_t)((hr == 0u && hB == 0u) || (hr != 0u && hr == hB)) << (b + 16);
-            }
+            // X = XH + (XL & same), bit-sliced
             uint32_t X[B];
             uint32_t carry = 0;
 #pragma unroll
@@ -1281,7 +1351,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                     mn = min(s_rowT[bit & 15], bit < 16 ? tcA : tcB);
                     pass = m >= (int)a.mmin[mn];
                 }
-                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
+                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
             }
         }
         __syncthreads();
@@ -1316,6 +1386,8 @@ struct DenseArgs {
     uint64_t* keys;
     uint32_t* vals;
     int64_t cap;
+    const int32_t* perm;          // as in TileArgs
+    int olo, ohi;
 };
 
 __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
@@ -1366,7 +1438,7 @@ __global__ void __launch_bounds__(256) kmer_dense_kernel(DenseArgs a) {
                 mn = min(Tr, Tc);
                 pass = m >= (int)a.mmin[mn];
             }
-            emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, pass, r, c, m, mn);
+            emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
         }
         __syncthreads();
         for (int p = threadIdx.x; p < Tr; p += blockDim.x) hist[kmer_at(s, p, a.K) >> 1] = 0;
@@ -1490,8 +1562,44 @@ using namespace crispy;
 namespace crispy {
 namespace {
 
+// Group layout of the reads in the job's read order (tuple counts t[]):
+// entries per lane and first entry of each 32-read group, uploaded with t.
+int kmer_groups(crispy_ctx* ctx, const int32_t* t) {
+    KmerJob& j = ctx->kmer;
+    const int n = j.n;
+    j.h_gent.assign(j.ngroups, 0);
+    j.h_gstart.assign(j.ngroups + 1, 0);
+    for (int r = 0; r < n; ++r) j.h_gent[r >> 5] = std::max(j.h_gent[r >> 5], t[r]);
+    j.h_tgent.assign(j.ngroups, 0);
+    j.h_tstart.assign(j.ngroups + 1, 0);
+    for (int g = 0; g < j.ngroups; ++g) {
+        const int mt = j.h_gent[g];
+        j.h_gent[g] = (mt + 15) / 16 * 16;
+        j.h_gstart[g + 1] = j.h_gstart[g] + 32LL * j.h_gent[g];
+        // the tile stream gets spare steps: wildcards for the bank schedule
+        j.h_tgent[g] = (mt + (mt >= 128 ? kSchedSpare : 0) + 15) / 16 * 16;
+        j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * j.h_tgent[g];
+    }
+    j.nent = j.h_gstart[j.ngroups];
+    j.ntent = j.h_tstart[j.ngroups];
+    cudaStream_t s = ctx->stream;
+    CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 4) * 4));
+    if (j.k != 8) CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, t, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.gstart.ptr, j.h_gstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.gent.ptr, j.h_gent.data(), (size_t)j.ngroups * 4,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                   cudaMemcpyHostToDevice, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
+                                   cudaMemcpyHostToDevice, s));
+    return CRISPY_OK;
+}
+
 // Per-read layout of a K-mer job from the read lengths (host metadata and
-// the device buffers sized for it); the reads themselves come next.
+// the device buffers sized for it); the reads themselves come next.  K = 8
+// jobs get their group layout at rebuild, in the read order built there.
 int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
     if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
     if (k < 1 || k > 8) return fail(ctx, CRISPY_E_UNSUPPORTED, "K = %d outside 1..8", k);
@@ -1512,48 +1620,60 @@ int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
         j.max_t = std::max(j.max_t, j.h_t[r]);
     }
     j.ngroups = (n + 31) / 32;
-    j.h_gent.assign(j.ngroups, 0);
-    j.h_gstart.assign(j.ngroups + 1, 0);
-    for (int r = 0; r < n; ++r) j.h_gent[r >> 5] = std::max(j.h_gent[r >> 5], j.h_t[r]);
-    j.h_tgent.assign(j.ngroups, 0);
-    j.h_tstart.assign(j.ngroups + 1, 0);
-    for (int g = 0; g < j.ngroups; ++g) {
-        const int mt = j.h_gent[g];
-        j.h_gent[g] = (mt + 15) / 16 * 16;
-        j.h_gstart[g + 1] = j.h_gstart[g] + 32LL * j.h_gent[g];
-        // the tile stream gets spare steps: wildcards for the bank schedule
-        j.h_tgent[g] = (mt + (mt >= 128 ? kSchedSpare : 0) + 15) / 16 * 16;
-        j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * j.h_tgent[g];
-    }
-    j.nent = j.h_gstart[j.ngroups];
-    j.ntent = j.h_tstart[j.ngroups];
-    cudaStream_t s = ctx->stream;
     CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
     CRISPY_TRY(ensure(ctx, j.gstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.gent, (size_t)j.ngroups * 4));
-    CRISPY_TRY(ensure(ctx, j.ent, (size_t)std::max<int64_t>(j.nent, 4) * 4));
     CRISPY_TRY(ensure(ctx, j.cntmax, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.hinfo, (size_t)n * 4));
     CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 128));
     CRISPY_TRY(ensure(ctx, j.tstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.tgent, (size_t)j.ngroups * 4));
-    if (k == 8) {
-        CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
-        CRISPY_TRY(ensure(ctx, j.nsec, (size_t)n * 8));
-    } else {
-        CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
-    }
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.t.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.gstart.ptr, j.h_gstart.data(), (size_t)(j.ngroups + 1) * 8,
-                                   cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.gent.ptr, j.h_gent.data(), (size_t)j.ngroups * 4,
-                                   cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
-                                   cudaMemcpyHostToDevice, s));
-    CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
-                                   cudaMemcpyHostToDevice, s));
+    if (k != 8) return kmer_groups(ctx, j.h_t.data());
+    CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
+    CRISPY_TRY(ensure(ctx, j.nsec, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, j.t0, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.offp, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, j.perm, (size_t)n * 4));
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.t0.ptr, j.h_t.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
     return CRISPY_OK;
+}
+
+// K = 8 read order (kmer_hkey_kernel): the sorted order as perm (position ->
+// read ID) and the reads' offsets in that order, then the group layout.
+int kmer_order(crispy_ctx* ctx) {
+    KmerJob& j = ctx->kmer;
+    const int n = j.n;
+    cudaStream_t s = ctx->stream;
+    const int tbits = std::max(1, bits_for((uint64_t)j.max_t));
+    CRISPY_TRY(ensure(ctx, j.keys, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, j.keys_alt, (size_t)n * 8));
+    CRISPY_TRY(ensure(ctx, j.vals, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.vals_alt, (size_t)n * 4));
+    CRISPY_TRY(ensure(ctx, j.sort_tmp, sort_tmp_bytes(n)));
+    kmer_hkey_kernel<<<std::min((n + 7) / 8, ctx->sm_count * 16), 256, 0, s>>>(
+        j.seq.as<uint8_t>(), j.off.as<int64_t>(), j.t0.as<int32_t>(), n, tbits, j.keys.as<uint64_t>(),
+        j.vals.as<uint32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    uint64_t* sk = nullptr;
+    uint32_t* sv = nullptr;
+    CRISPY_TRY(sort_u64_payload(ctx, s, j.keys.as<uint64_t>(), j.keys_alt.as<uint64_t>(), j.vals.as<uint32_t>(),
+                                j.vals_alt.as<uint32_t>(), n, 32 + tbits, true, &sk, &sv, j.sort_tmp));
+    kmer_gather_off_kernel<<<(n + 255) / 256, 256, 0, s>>>(j.off.as<int64_t>(), sv, n, j.offp.as<int64_t>(),
+                                                           j.perm.as<int32_t>());
+    count_launch(ctx);
+    CRISPY_CK(ctx, cudaGetLastError());
+    j.h_perm.resize(n);
+    CRISPY_CK(ctx, cudaMemcpyAsync(j.h_perm.data(), j.perm.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    std::vector<int32_t> tp(n);
+    for (int i = 0; i < n; ++i) {
+        const int32_t r = j.h_perm[i];
+        if (r < 0 || r >= n) return fail(ctx, CRISPY_E_STATE, "read order is not a permutation");
+        tp[i] = j.h_t[r];
+    }
+    return kmer_groups(ctx, tp.data());
 }
 
 }  // namespace
@@ -1615,6 +1735,9 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     const int n = j.n, k = j.k;
+    // K = 8: entries and streams are laid out in the read order
+    if (k == 8) CRISPY_TRY(kmer_order(ctx));
+    const int64_t* loff = k == 8 ? j.offp.as<int64_t>() : j.off.as<int64_t>();
     CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 4) * 4, s));
     const size_t hsmem = (size_t)(((1u << (2 * k)) + 1) / 2) * 4;
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1622,7 +1745,7 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     const int grid = std::min(n, ctx->sm_count * (k >= 8 ? 1 : 8));
     int32_t* cntmax = j.cntmax.as<int32_t>();
     int32_t* nhigh = cntmax + n;
-    kmer_prep_kernel<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), j.off.as<int64_t>(),
+    kmer_prep_kernel<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), loff,
                                               j.t.as<int32_t>(), n, k, dense_levels_for(k),
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
@@ -1732,9 +1855,16 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
-    // One pass over the rows [rlo, rhi) and all their columns: survivors
-    // (up to cap) as sort keys in j.keys / j.vals, their count in *total.
-    auto run_pass = [&](int rlo, int rhi, int64_t cap, int64_t* total_out) -> int {
+    // K = 8 jobs hold their reads in the read order built at rebuild: the
+    // kernels run over positions, emit() maps them back to read IDs.
+    const int32_t* perm = K == 8 ? j.perm.as<int32_t>() : nullptr;
+    const int64_t* loff = K == 8 ? j.offp.as<int64_t>() : j.off.as<int64_t>();
+    // One pass over the pairs whose lower read ID lies in [olo, ohi):
+    // survivors (up to cap) as sort keys in j.keys / j.vals, their count in
+    // *total.  Without a read order the kernels cover the rows [olo, ohi);
+    // with one they cover every row and emit() keeps the range.
+    auto run_pass = [&](int olo, int ohi, int64_t cap, int64_t* total_out) -> int {
+        const int rlo = perm ? 0 : olo, rhi = perm ? n : ohi;
         CRISPY_TRY(ensure(ctx, j.keys, (size_t)cap * 8));
         CRISPY_TRY(ensure(ctx, j.keys_alt, (size_t)cap * 8));
         CRISPY_TRY(ensure(ctx, j.vals, (size_t)cap * 4));
@@ -1753,8 +1883,10 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         ta.n = n; ta.K4 = K4; ta.levels = levels; ta.A = A; ta.stage_dim = sd;
         ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
         ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
+        ta.perm = perm; ta.olo = olo; ta.ohi = ohi;
         DenseArgs da{};
-        da.seq = j.seq.as<uint8_t>(); da.off = j.off.as<int64_t>(); da.ent = ta.ent; da.gstart = ta.gstart;
+        da.perm = perm; da.olo = olo; da.ohi = ohi;
+        da.seq = j.seq.as<uint8_t>(); da.off = loff; da.ent = ta.ent; da.gstart = ta.gstart;
         da.tcount = ta.tcount; da.hinfo = j.hinfo.as<uint32_t>(); da.mmin = ta.mmin;
         da.n = n; da.K = K; da.A = A; da.stage_dim = sd;
         da.dense_group = fast ? j.work.as<uint8_t>() : nullptr;
@@ -1837,7 +1969,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.counter.ptr, (uint64_t)(uintptr_t)d_items,
                     (uint64_t)(uintptr_t)j.mmin.ptr, (uint64_t)(uintptr_t)j.smin.ptr, (uint64_t)(uintptr_t)j.t.ptr,
                     (uint64_t)(uintptr_t)j.gstart.ptr, (uint64_t)(uintptr_t)j.gent.ptr, (uint64_t)(uintptr_t)j.work.ptr,
-                    (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)j.off.ptr, (uint64_t)(uintptr_t)j.hinfo.ptr,
+                    (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)loff, (uint64_t)(uintptr_t)j.hinfo.ptr,
+                    (uint64_t)(uintptr_t)perm, (uint64_t)olo, (uint64_t)ohi,
                     (uint64_t)(uintptr_t)j.tent.ptr, (uint64_t)(uintptr_t)j.tstart.ptr, (uint64_t)(uintptr_t)j.tgent.ptr,
                     (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
@@ -1923,7 +2056,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         // processed in ranges whose survivors fit; stage order is row-major
         // over stage rows, so each range's sorted pairs append in order to
         // one pinned host list (the count is known from the first pass).
-        if (A % rows_blk != 0) return fail(ctx, CRISPY_E_OOM, "survivor list exceeds the device share");
+        if (!perm && A % rows_blk != 0) return fail(ctx, CRISPY_E_OOM, "survivor list exceeds the device share");
         CRISPY_TRY(ensure_host(ctx, j.h_spill_pairs, (size_t)total * 8));
         if (dists) CRISPY_TRY(ensure_host(ctx, j.h_spill_dists, (size_t)total * 4));
         // expected survivors per stage row, proportional to its pairs

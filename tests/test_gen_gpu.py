@@ -118,18 +118,20 @@ def test_gen_bad_index_rejected(engine):
     assert e.value.code == cg.E_INPUT
 
 
-def test_gen_prepare_from_kmer_matches_upload(engine):
+@pytest.mark.parametrize("k", [6, 8])
+def test_gen_prepare_from_kmer_matches_upload(engine, k):
     # packing the reads left on the device by kmer_prepare gives the same
-    # chunks as a second upload through gen_prepare
+    # chunks as a second upload through gen_prepare (K = 8 jobs hold their
+    # reads in a read order of their own; genDist takes them by read ID)
     reads = _reads(700, 83, root=520, dist="uniform", a=300, b=500, cents=25)
     buf, offs, lens = synth.pack_reads(reads)
-    t = cg.default_threshold(len(reads), -1.0, 0)
+    t = cg.default_threshold(len(reads), -1.0, 0) if k == 6 else 0.7
     tg = cg.default_threshold(len(reads), -1.0, 1)
-    engine.kmer_prepare(buf, offs, lens, 6)
+    engine.kmer_prepare(buf, offs, lens, k)
     engine.kmer_run(t, cg.MODE_BATCHED, False)
     engine.gen_prepare(buf, offs, lens)
     want = engine.gen_run_from_kmer(10, tg, cg.MODE_BATCHED)
-    engine.kmer_prepare(buf, offs, lens, 6)
+    engine.kmer_prepare(buf, offs, lens, k)
     engine.kmer_run(t, cg.MODE_BATCHED, False)
     engine.gen_prepare_from_kmer()
     got = engine.gen_run_from_kmer(10, tg, cg.MODE_BATCHED)
