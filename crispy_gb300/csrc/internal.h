@@ -50,6 +50,10 @@ struct KmerJob {
     // offsets by position, t0 the tuple counts by read ID
     DevBuf t0, offp, perm;
     std::vector<int32_t> h_perm;
+    // K = 8: H key per position and the run of equal keys holding it
+    std::vector<uint32_t> h_hinfo;
+    std::vector<int32_t> h_run_lo, h_run_hi;
+    bool hkeys_ordered = false;
     // last run's survivors, in stage order: on the device, or (spilled) in
     // pinned host memory when they outgrow the device share
     int64_t nsurv = 0;

@@ -97,8 +97,10 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // bank of its 16-bit plane word.
 __device__ __forceinline__ int prep_bucket(uint32_t val, int K) {
     if (K == 8) {
+        // H: bank of a 32-bit plane word (K-mer - 0x8000); L: 4-byte bank
+        // of a 16-bit plane word
         const uint32_t v = val & 0xFFFFu;
-        return (v >= 0x8000u ? 0 : 32) + (int)((v >> 1) & 31u);
+        return v >= 0x8000u ? (int)(v & 31u) : 32 + (int)((v >> 1) & 31u);
     }
     return (int)(val & 31u);
 }
@@ -317,7 +319,7 @@ struct SchedSmem {
 template <int kB>
 __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const uint16_t* raw_cnt,
                              int pos0, int Et, const uint32_t* __restrict__ src, uint32_t vsub,
-                             uint32_t guard0, uint16_t* __restrict__ dst_group) {
+                             uint32_t guard0, uint32_t gstride, uint16_t* __restrict__ dst_group) {
     const unsigned full = 0xffffffffu;
     constexpr unsigned kMask = kB == 32 ? 0xffffffffu : (1u << kB) - 1u;
     constexpr int kSub = 32 / kB;                         // raw groups per bucket
@@ -410,9 +412,9 @@ __device__ void sched_stream(SchedSmem& sm, int w, int lane, bool active, const 
 #pragma unroll
         for (int i = 0; i < kSchedChunk; ++i) {
             const uint32_t x = v[i];
-            // guard of bucket b: word guard0 + b (128- or 64-bit words, bucket
-            // b) or halfword guard0 + 2b (16-bit words, 4-byte bank b)
-            v[i] = (x & 0x80000000u) ? guard0 + (x & 31u) * (kB == 32 ? 2u : 1u)
+            // guard of bucket b: word guard0 + b (128-, 64- or 32-bit words,
+            // bucket b) or halfword guard0 + 2b (16-bit words, 4-byte bank b)
+            v[i] = (x & 0x80000000u) ? guard0 + (x & 31u) * gstride
                                      : __ldg(src + ent_at((int)x, lane)) - vsub;
         }
         // two octets of this lane: two uint4 of packed 16-bit word indices
@@ -443,15 +445,16 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
         const int r = g * 32 + lane;
         const bool active = r < n;
         sched_stream<kB>(sm, w, lane, active, bcnt + (int64_t)(active ? r : 0) * 32,
-                         active ? nhigh[r] : 0, tgent[g], ent + gstart[g], 0u, guard_word,
+                         active ? nhigh[r] : 0, tgent[g], ent + gstart[g], 0u, guard_word, 1u,
                          tent + tstart[g]);
     }
 }
 
-// K = 8: an H stream and an L stream per group (16-bit plane words); the H
-// section of a read's raw list follows its high-level entries, the L
-// section follows the H section.  Each stream indexes its own plane
-// (H: K-mer - 0x8000, L: K-mer) whose guard words start at 32768.
+// K = 8: an H stream and an L stream per group; the H section of a read's
+// raw list follows its high-level entries, the L section follows the H
+// section.  Each stream indexes its own plane whose guard words start at
+// 32768: H: K-mer - 0x8000, 32-bit words (bank = word mod 32); L: K-mer,
+// 16-bit words (bank = word / 2 mod 32).
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
     const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
@@ -468,10 +471,10 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
         const int nH = active ? nsec[(int64_t)rr * 2] : 0;
         const int EtH = tgent[g];
         sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, EtH, ent + gstart[g],
-                         0x8000u, 32768u, tent + tstart[g]);
+                         0x8000u, 32768u, 1u, tent + tstart[g]);
         __syncwarp();
         sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + nH, tgentL[g],
-                         ent + gstart[g], 0u, 32768u, tent + tstart[g] + (int64_t)32 * EtH);
+                         ent + gstart[g], 0u, 32768u, 2u, tent + tstart[g] + (int64_t)32 * EtH);
         __syncwarp();
     }
 }
@@ -513,6 +516,12 @@ struct TileArgs {
     // an order, pairs are kept whose lower read ID lies in [olo, ohi)
     const int32_t* perm;
     int olo, ohi;
+    // K = 8 batched split: per item the 64-read column groups [x, y) of the
+    // 16-row kernel, which then keeps only pairs with [same]; the per-read
+    // H / L entry counts (H-only kernel)
+    const int2* item_q;
+    int same_only;
+    const int32_t* nsec;
 };
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
@@ -1121,9 +1130,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
 //     m = minsum(H) + [same] * minsum(L)
 // (H = K-mers >= 0x8000, L = the rest; kmerMain.cpp:275-278 against
 // kmerKernel.cu:37-45), so the two halves are counted apart.  A block owns 16
-// row reads; first occurrences live in two planes of 16-bit words (H: K-mer
-// - 0x8000, L: K-mer; 32,768 words each plus guard words, 128 KB together)
-// and repeated occurrences in a shared hash.  Each lane owns two column
+// row reads; first occurrences live in two planes (H: K-mer - 0x8000, 32-bit
+// words of which the low 16 bits are used, so that the H stream's schedule
+// by 32-bit banks serves both K = 8 kernels; L: K-mer, 16-bit words; 32,768
+// words each plus guard words, 192 KB together) and repeated occurrences in
+// a shared hash.  Each lane owns two column
 // reads, one of each of two adjacent 32-read groups, and gathers one 16-bit
 // word per read and step into the low / high half of a 32-bit counter
 // input: 16 rows x 2 columns per LOP3.  An H phase over the groups' H
@@ -1131,7 +1142,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
 // m is formed bit-sliced with the [same] mask per (row, column).
 // ---------------------------------------------------------------------------
 constexpr int kRows8 = 16;
-constexpr int kPlane8 = 32768 + 64;    // 16-bit words per plane: K-mers + guard words
+constexpr int kPlane8 = 32768 + 64;    // 16-bit L plane words: K-mers + guard words
+constexpr int kPlaneH = 32768 + 32;    // 32-bit H plane words: K-mers + guard words
+constexpr size_t kSmem8 = (size_t)kPlaneH * 4 + (size_t)kPlane8 * 2;
 
 __device__ __noinline__ uint32_t hash_find8(const uint32_t* hkeys, const uint32_t* hmask,
                                             uint32_t key) {
@@ -1146,9 +1159,10 @@ __device__ __noinline__ uint32_t hash_find8(const uint32_t* hkeys, const uint32_
 }
 
 // 16 scheduled entries of each of two streams (columns in the low and high
-// half); an exhausted stream reads guard word 32768 (zero).
-template <int B>
-__device__ __forceinline__ uint32_t gather8_16(const uint16_t* __restrict__ plane, uint4 qa0, uint4 qa1,
+// half); an exhausted stream reads guard word 32768 (zero).  W: the plane's
+// word type (only the low 16 bits are set).
+template <int B, typename W>
+__device__ __forceinline__ uint32_t gather8_16(const W* __restrict__ plane, uint4 qa0, uint4 qa1,
                                                uint4 qb0, uint4 qb1, Counter<B>& cnt) {
     const uint32_t xa[8] = {qa0.x, qa0.y, qa0.z, qa0.w, qa1.x, qa1.y, qa1.z, qa1.w};
     const uint32_t xb[8] = {qb0.x, qb0.y, qb0.z, qb0.w, qb1.x, qb1.y, qb1.z, qb1.w};
@@ -1161,8 +1175,8 @@ __device__ __forceinline__ uint32_t gather8_16(const uint16_t* __restrict__ plan
     return cnt.add16(w);
 }
 
-template <int B>
-__device__ __forceinline__ void phase8(const uint16_t* __restrict__ plane, const uint4* epa, int ea,
+template <int B, typename W>
+__device__ __forceinline__ void phase8(const W* __restrict__ plane, const uint4* epa, int ea,
                                        const uint4* epb, int eb, uint32_t* X) {
     const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
     Counter<B> cnt;
@@ -1175,7 +1189,7 @@ __device__ __forceinline__ void phase8(const uint16_t* __restrict__ plane, const
         const int o = ((e + 16) >> 3) * 32;
         const uint4 na0 = e + 16 < ea ? __ldg(epa + o) : guard, na1 = e + 16 < ea ? __ldg(epa + o + 32) : guard;
         const uint4 nb0 = e + 16 < eb ? __ldg(epb + o) : guard, nb1 = e + 16 < eb ? __ldg(epb + o + 32) : guard;
-        cnt.add_sixteens1(gather8_16<B>(plane, a0, a1, b0, b1, cnt));
+        cnt.add_sixteens1(gather8_16<B, W>(plane, a0, a1, b0, b1, cnt));
         a0 = na0; a1 = na1; b0 = nb0; b1 = nb1;
     }
     cnt.planes(X);
@@ -1183,7 +1197,7 @@ __device__ __forceinline__ void phase8(const uint16_t* __restrict__ plane, const
 
 template <int B>
 __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a) {
-    extern __shared__ __align__(16) uint16_t P8[];   // H plane, then L plane
+    extern __shared__ __align__(16) uint32_t PH[];   // H plane (32-bit words), then L plane (16-bit)
     __shared__ uint32_t hkeys[kHashSlots];
     __shared__ uint32_t hmask[kHashSlots];
     __shared__ int s_rowT[kRows8];
@@ -1201,8 +1215,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                 s_item[3] = (int)w < a.nitems;
                 if (s_item[3]) {
                     s_item[0] = a.items[w];
-                    s_item[1] = 0;
-                    s_item[2] = (a.n + 63) / 64;
+                    s_item[1] = a.item_q ? a.item_q[w].x : 0;
+                    s_item[2] = a.item_q ? a.item_q[w].y : (a.n + 63) / 64;
                 }
             } else {
                 s_item[0] = a.r_lo / kRows8 + blockIdx.x;
@@ -1226,11 +1240,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
             const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
             if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
         }
-        uint4* P4 = reinterpret_cast<uint4*>(P8);
-        for (int i = threadIdx.x; i < 2 * kPlane8 / 8; i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        uint4* P4 = reinterpret_cast<uint4*>(PH);
+        for (int i = threadIdx.x; i < (int)(kSmem8 / 16); i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
         for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
         __syncthreads();
-        uint32_t* P32 = reinterpret_cast<uint32_t*>(P8);
+        uint32_t* PL32 = PH + kPlaneH;
         for (int b = warp; b < kRows8; b += kTileWarps) {
             if (!((s_rows_ok >> b) & 1u)) continue;
             const int r = r0 + b;
@@ -1239,9 +1253,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
             for (int e = lane; e < T; e += 32) {
                 const uint32_t idx = src[ent_at(e, r & 31)];
                 if (idx < 65536u) {
-                    // first occurrence: its plane word (H first)
-                    const uint32_t hw = idx >= 0x8000u ? idx - 0x8000u : (uint32_t)kPlane8 + idx;
-                    atomicOr(&P32[hw >> 1], (1u << b) << ((hw & 1u) * 16u));
+                    // first occurrence: its plane word
+                    if (idx >= 0x8000u) atomicOr(&PH[idx - 0x8000u], 1u << b);
+                    else atomicOr(&PL32[idx >> 1], (1u << b) << ((idx & 1u) * 16u));
                 } else {
                     uint32_t h = hash_slot(idx);
                     for (int probe = 0; probe < kHashSlots; ++probe) {
@@ -1282,12 +1296,16 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                 same |= (uint32_t)((hr == 0u && hA == 0u) || (hr != 0u && hr == hA)) << b;
                 same |= (uint32_t)((hr == 0u && hB == 0u) || (hr != 0u && hr == hB)) << (b + 16);
             }
+            // same_only: the H-only kernel has taken the pairs without [same]
+            const uint32_t keep = a.same_only ? same : 0xffffffffu;
+            if (a.same_only && !__any_sync(full, same & vmask)) continue;
             uint32_t XH[B], XL[B];
-            phase8<B>(P8, epAH, a.tgent[gA], epBH, hasB ? a.tgent[gB] : 0, XH);
+            phase8<B, uint32_t>(PH, epAH, a.tgent[gA], epBH, hasB ? a.tgent[gB] : 0, XH);
             // a warp none of whose pairs has [same] skips the L phase (reads
             // ordered by their H key make most warps like that)
             if (__any_sync(full, same & vmask)) {
-                phase8<B>(P8 + kPlane8, epAL, a.tgentL[gA], epBL, hasB ? a.tgentL[gB] : 0, XL);
+                phase8<B, uint16_t>(reinterpret_cast<const uint16_t*>(PH + kPlaneH), epAL, a.tgentL[gA], epBL,
+                                    hasB ? a.tgentL[gB] : 0, XL);
             } else {
 #pragma unroll
                 for (int k = 0; k < B; ++k) XL[k] = 0u;
@@ -1336,7 +1354,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                     gt |= eq & X[k] & ~bit;
                     eq &= ~(X[k] ^ bit);
                 }
-                cand = (gt | eq) & vmask & okbits;
+                cand = (gt | eq) & vmask & okbits & keep;
             }
             while (__any_sync(full, cand)) {
                 bool pass = false;
@@ -1349,6 +1367,170 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
                     r = r0 + (bit & 15);
                     c = bit < 16 ? cA : cB;
                     mn = min(s_rowT[bit & 15], bit < 16 ? tcA : tcB);
+                    pass = m >= (int)a.mmin[mn];
+                }
+                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K = 8 H-only tile kernel (batched form).  With the reads in their H-key
+// order, a pair has [same] only inside one key group, so m = minsum(H) for
+// every pair outside the groups.  This kernel takes exactly those pairs; the
+// 16-row kernel above takes each row block's same-key column range.  A
+// block owns 32 row reads: first H occurrences live in one plane of 32-bit
+// words (32,768 plus 32 guard words, 128 KB), repeated H occurrences in the
+// shared hash.  A lane owns one column read and gathers one 32-bit word per
+// step: 32 rows per LOP3 and one shared load per step.
+// ---------------------------------------------------------------------------
+constexpr int kRows8H = 32;
+constexpr size_t kSmem8H = (size_t)kPlaneH * 4;
+
+template <int B>
+__device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, const uint4* ep, int E,
+                                        uint32_t* X) {
+    const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
+    Counter<B> cnt;
+    cnt.clear();
+    uint4 a0 = 0 < E ? __ldg(ep) : guard, a1 = 0 < E ? __ldg(ep + 32) : guard;
+    for (int e = 0; e < E; e += 16) {
+        const int o = ((e + 16) >> 3) * 32;
+        const uint4 n0 = e + 16 < E ? __ldg(ep + o) : guard, n1 = e + 16 < E ? __ldg(ep + o + 32) : guard;
+        const uint32_t x[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        uint32_t w[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            w[2 * k] = plane[x[k] & 0xFFFFu];
+            w[2 * k + 1] = plane[x[k] >> 16];
+        }
+        cnt.add_sixteens1(cnt.add16(w));
+        a0 = n0; a1 = n1;
+    }
+    cnt.planes(X);
+}
+
+template <int B>
+__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8h_kernel(TileArgs a) {
+    extern __shared__ __align__(16) uint32_t PH[];
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots];
+    __shared__ int s_rowT[kRows8H];
+    __shared__ uint32_t s_keyv[kRows8H], s_keym[kRows8H];
+    __shared__ int s_item, s_tmin, s_any_high, s_nkeys;
+    __shared__ uint32_t s_rows_ok;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned w = atomicAdd(a.queue_head, 1u);
+            s_item = (int)w < a.nitems ? a.items[w] : -1;
+        }
+        __syncthreads();
+        const int rg = s_item;
+        if (rg < 0) break;
+        const int r0 = rg * kRows8H;
+        if (warp == 0) {
+            const int r = r0 + lane;
+            const bool ok = r < a.n && !a.dense_group[rg];
+            const int tr = ok ? a.tcount[r] : INT_MAX;
+            const uint32_t hr = ok ? a.hinfo[r] : 0u;
+            s_rowT[lane] = tr;
+            const unsigned okm = __ballot_sync(full, ok);
+            const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
+            // the rows' distinct H keys, each with its row mask
+            const unsigned rowsk = __match_any_sync(full, hr) & okm;
+            const bool leader = ok && lane == __ffs(rowsk) - 1;
+            const unsigned lm = __ballot_sync(full, leader);
+            if (leader) {
+                const int k = __popc(lm & ((1u << lane) - 1u));
+                s_keyv[k] = hr;
+                s_keym[k] = rowsk;
+            }
+            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; s_nkeys = __popc(lm); }
+        }
+        uint4* P4 = reinterpret_cast<uint4*>(PH);
+        for (int i = threadIdx.x; i < (int)(kSmem8H / 16); i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
+        __syncthreads();
+        const uint32_t* src = a.ent + a.gstart[rg];
+        for (int b = warp; b < kRows8H; b += kTileWarps) {
+            if (!((s_rows_ok >> b) & 1u)) continue;
+            const int r = r0 + b;
+            // high-level entries, then the H section of the read's list
+            const int eh = a.nhigh[r] + a.nsec[2 * (int64_t)r];
+            for (int e = lane; e < eh; e += 32) {
+                const uint32_t idx = src[ent_at(e, b)];
+                if (idx < 65536u) {
+                    if (idx >= 0x8000u) atomicOr(&PH[idx - 0x8000u], 1u << b);
+                } else if ((idx & 0xFFFFu) >= 0x8000u) {
+                    uint32_t h = hash_slot(idx);
+                    for (int probe = 0; probe < kHashSlots; ++probe) {
+                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
+                        if (old == kSentinel || old == idx) {
+                            atomicOr(&hmask[h], 1u << b);
+                            break;
+                        }
+                        h = (h + 1) & (kHashSlots - 1);
+                    }
+                    s_any_high = 1;
+                }
+            }
+        }
+        __syncthreads();
+        const bool any_high = s_any_high != 0;
+        const uint32_t rows_ok = s_rows_ok;
+        const int nkeys = s_nkeys;
+        for (int q = rg + warp; q < a.ngroups; q += kTileWarps) {
+            const int c = 32 * q + lane;
+            const bool okc = c < a.n;
+            const uint32_t hc = okc ? a.hinfo[c] : 0u;
+            uint32_t same = 0;
+            for (int k = 0; k < nkeys; ++k) same |= s_keyv[k] == hc ? s_keym[k] : 0u;
+            const uint32_t vmask = okc ? (half_mask(c - r0) & rows_ok & ~same) : 0u;
+            if (!__any_sync(full, vmask)) continue;
+            uint32_t X[B];
+            phase8h<B>(PH, reinterpret_cast<const uint4*>(a.tent + a.tstart[q]) + lane, a.tgent[q], X);
+            if (any_high) {
+                // repeated H occurrences (rank >= 1) lead the column's list
+                const int nh = okc ? a.nhigh[c] : 0;
+                const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
+                const uint32_t* rp = a.ent + a.gstart[q];
+                for (int j = 0; j < maxh; ++j) {
+                    uint32_t w = 0;
+                    if (j < nh) {
+                        const uint32_t key = __ldg(rp + ent_at(j, lane));
+                        if ((key & 0xFFFFu) >= 0x8000u) w = hash_find8(hkeys, hmask, key);
+                    }
+                    Counter<B>::add_at(X, w, 0);
+                }
+            }
+            // threshold: a lower bound of mmin per column, then exact per candidate
+            const int tc = okc ? a.tcount[c] : 0;
+            const uint32_t lo = a.smin[min(s_tmin, tc)];
+            uint32_t cand = 0;
+            if (vmask && lo < (1u << B)) {
+                uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+                for (int k = B - 1; k >= 0; --k) {
+                    const uint32_t bit = ((lo >> k) & 1u) ? 0xffffffffu : 0u;
+                    gt |= eq & X[k] & ~bit;
+                    eq &= ~(X[k] ^ bit);
+                }
+                cand = (gt | eq) & vmask;
+            }
+            while (__any_sync(full, cand)) {
+                bool pass = false;
+                int r = 0, m = 0, mn = 1;
+                if (cand) {
+                    const int bit = __ffs(cand) - 1;
+                    cand &= cand - 1;
+#pragma unroll
+                    for (int k = 0; k < B; ++k) m |= (int)((X[k] >> bit) & 1u) << k;
+                    r = r0 + bit;
+                    mn = min(s_rowT[bit], tc);
                     pass = m >= (int)a.mmin[mn];
                 }
                 emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
@@ -1531,6 +1713,16 @@ TileFn tile8_fn_for(int B) {
         case 10: return kmer_tile8_kernel<10>;
         case 11: return kmer_tile8_kernel<11>;
         default: return kmer_tile8_kernel<12>;
+    }
+}
+
+TileFn tile8h_fn_for(int B) {
+    switch (B) {
+        case 8: return kmer_tile8h_kernel<8>;
+        case 9: return kmer_tile8h_kernel<9>;
+        case 10: return kmer_tile8h_kernel<10>;
+        case 11: return kmer_tile8h_kernel<11>;
+        default: return kmer_tile8h_kernel<12>;
     }
 }
 
@@ -1736,6 +1928,7 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     cudaStream_t s = ctx->stream;
     const int n = j.n, k = j.k;
     // K = 8: entries and streams are laid out in the read order
+    j.hkeys_ordered = false;
     if (k == 8) CRISPY_TRY(kmer_order(ctx));
     const int64_t* loff = k == 8 ? j.offp.as<int64_t>() : j.off.as<int64_t>();
     CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 4) * 4, s));
@@ -1758,7 +1951,21 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
         // stream layouts need the per-read H / L counts: one round trip
         j.h_nsec.resize(2 * (size_t)n);
         CRISPY_CK(ctx, cudaMemcpyAsync(j.h_nsec.data(), j.nsec.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+        j.h_hinfo.resize(n);
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_hinfo.data(), j.hinfo.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
         CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        // runs of equal H keys along the positions; the batched split needs
+        // each key in one run (keys ascending, as the read order sorts them)
+        j.h_run_lo.resize(n);
+        j.h_run_hi.resize(n);
+        j.hkeys_ordered = true;
+        for (int i = 0; i < n;) {
+            int e = i + 1;
+            while (e < n && j.h_hinfo[e] == j.h_hinfo[i]) ++e;
+            if (e < n && j.h_hinfo[e] < j.h_hinfo[i]) j.hkeys_ordered = false;
+            for (int q = i; q < e; ++q) { j.h_run_lo[q] = i; j.h_run_hi[q] = e; }
+            i = e;
+        }
         std::vector<int32_t> tgl(j.ngroups, 0);
         j.h_tstart.assign(j.ngroups + 1, 0);
         j.h_tgent.assign(j.ngroups, 0);
@@ -1831,14 +2038,17 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     // the dense kernel (flags per 32-read group); K = 8 sends every group there.
     const int levels = dense_levels_for(K);
     const int rows_blk = tile_rows_for(K);   // row reads per tile block
-    const int nrg = (n + rows_blk - 1) / rows_blk;
+    // the hash of a K = 8 block holds the high-level entries of up to 32 rows
+    // (H-only kernel), so K = 8 decides per 32-read group
+    const int hash_blk = K == 8 ? kRows8H : rows_blk;
+    const int nrg = (n + hash_blk - 1) / hash_blk;
     std::vector<uint8_t> dense(j.ngroups, 0);
     bool any_dense = false;
     for (int rg = 0; rg < nrg; ++rg) {
         int64_t high = 0;
-        for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); ++r) high += j.h_cntmax[n + r];
+        for (int r = rg * hash_blk; r < std::min(n, rg * hash_blk + hash_blk); ++r) high += j.h_cntmax[n + r];
         if (levels == 0 || high > kHashMaxKeys) {
-            for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32) dense[r >> 5] = 1;
+            for (int r = rg * hash_blk; r < std::min(n, rg * hash_blk + hash_blk); r += 32) dense[r >> 5] = 1;
             any_dense = true;
         }
     }
@@ -1849,10 +2059,16 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = K == 8 ? tile8_fn_for(B) : rows_blk == kRows128 ? tile128_fn_for(B) : tile_fn_for(B);
-    const size_t tsmem = !fast ? 0 : K == 8 ? (size_t)2 * kPlane8 * 2     // two 16-bit planes + guards
+    const size_t tsmem = !fast ? 0 : K == 8 ? kSmem8     // H and L planes + guards
                                              : ((size_t)levels * K4 + 32) * (rows_blk / 8);   // planes + guards
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    // K = 8 batched: the H-only kernel over all row groups plus the 16-row
+    // kernel over each row block's same-key column range (the H keys must be
+    // in order along the positions, as the read order makes them)
+    const bool split8 = fast && K == 8 && mode == CRISPY_MODE_BATCHED && j.hkeys_ordered;
+    TileFn tile_h = split8 ? tile8h_fn_for(B) : nullptr;
+    if (split8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8H));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
     // K = 8 jobs hold their reads in the read order built at rebuild: the
@@ -1884,6 +2100,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
         ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
         ta.perm = perm; ta.olo = olo; ta.ohi = ohi;
+        ta.nsec = K == 8 ? j.nsec.as<int32_t>() : nullptr;
         DenseArgs da{};
         da.perm = perm; da.olo = olo; da.ohi = ohi;
         da.seq = j.seq.as<uint8_t>(); da.off = loff; da.ent = ta.ent; da.gstart = ta.gstart;
@@ -1939,49 +2156,87 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             cudaEventDestroy(fork);
             ctx->stats.kmer_launches += st;
         } else {
-            // Batched: one persistent launch over a work queue of row groups
-            // (each with all its columns), longest first.
-            std::vector<int> items;
-            if (fast)
+            // Batched: persistent launches over work queues of row groups
+            // (each with all its columns), longest first.  K = 8 split: the
+            // H-only kernel over the 32-row groups, then the 16-row kernel
+            // over each 16-row block's same-key column range.
+            std::vector<int> items, items_s;
+            std::vector<int2> q_s;
+            if (split8) {
+                for (int g = 0; g < j.ngroups; ++g)
+                    if (!dense[g]) items.push_back(g);
+                for (int rb = 0; rb * kRows8 < n; ++rb) {
+                    const int r0 = rb * kRows8, r1 = std::min(n, r0 + kRows8);
+                    if (dense[r0 >> 5]) continue;
+                    // columns of the keys of rows r0 .. r1-1: one range, the keys being in order
+                    const int q0 = std::max(r0 / 64, j.h_run_lo[r0] / 64);
+                    const int q1 = (j.h_run_hi[r1 - 1] + 63) / 64;
+                    if (q1 > q0) {
+                        items_s.push_back(rb);
+                        q_s.push_back(make_int2(q0, q1));
+                    }
+                }
+            } else if (fast) {
                 for (int rg = rlo / rows_blk; rg * rows_blk < rhi; ++rg) {
                     bool any_rows = false;
                     for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32)
                         any_rows |= !dense[r >> 5];
                     if (any_rows) items.push_back(rg);
                 }
-            if (!items.empty()) {
-                CRISPY_TRY(ensure(ctx, j.sort_tmp, items.size() * sizeof(int) + 64));
-                int* d_items = j.sort_tmp.as<int>();
-                unsigned int* head = reinterpret_cast<unsigned int*>(j.sort_tmp.as<char>() + items.size() * sizeof(int));
-                CRISPY_CK(ctx, cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(int),
-                                               cudaMemcpyHostToDevice, s));
-                CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 4, s));
+            }
+            if (!items.empty() || !items_s.empty()) {
+                const size_t nh = items.size(), ns = items_s.size();
+                CRISPY_TRY(ensure(ctx, j.sort_tmp, ns * sizeof(int2) + (nh + ns) * sizeof(int) + 64));
+                int2* d_q = j.sort_tmp.as<int2>();
+                int* d_items = reinterpret_cast<int*>(d_q + ns);
+                int* d_items_s = d_items + nh;
+                unsigned int* head = reinterpret_cast<unsigned int*>(d_items_s + ns);
+                if (nh) CRISPY_CK(ctx, cudaMemcpyAsync(d_items, items.data(), nh * sizeof(int), cudaMemcpyHostToDevice, s));
+                if (ns) {
+                    CRISPY_CK(ctx, cudaMemcpyAsync(d_items_s, items_s.data(), ns * sizeof(int), cudaMemcpyHostToDevice, s));
+                    CRISPY_CK(ctx, cudaMemcpyAsync(d_q, q_s.data(), ns * sizeof(int2), cudaMemcpyHostToDevice, s));
+                }
+                CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 8, s));
+                const TileFn main_fn = split8 ? tile_h : tile;
+                const size_t main_smem = split8 ? kSmem8H : tsmem;
                 TileArgs t2 = ta;
                 t2.r_lo = 0; t2.r_hi = n; t2.c_lo = 0; t2.c_hi = n;
-                t2.items = d_items; t2.nitems = (int)items.size(); t2.queue_head = head;
-                int per_sm = 1;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile, kTileThreads, tsmem);
+                t2.items = d_items; t2.nitems = (int)nh; t2.queue_head = head;
+                TileArgs t3 = t2;
+                t3.items = d_items_s; t3.nitems = (int)ns; t3.queue_head = head + 1;
+                t3.item_q = d_q; t3.same_only = 1;
+                int per_sm = 1, per_sm_s = 1;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, main_fn, kTileThreads, main_smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, tile, kTileThreads, tsmem);
                 per_sm = std::max(1, per_sm);
-                const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)items.size());
+                per_sm_s = std::max(1, per_sm_s);
+                const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)nh);
+                const int grid_s = (int)std::min<int64_t>((int64_t)per_sm_s * ctx->sm_count, (int64_t)ns);
                 DenseArgs d2 = da;
                 d2.r_lo = rlo; d2.r_hi = rhi; d2.c_lo = 0; d2.c_hi = n;
                 const std::string key = "kmain," + key_of({(uint64_t)(uintptr_t)j.ent.ptr, (uint64_t)(uintptr_t)j.keys.ptr,
-                    (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.counter.ptr, (uint64_t)(uintptr_t)d_items,
+                    (uint64_t)(uintptr_t)j.vals.ptr, (uint64_t)(uintptr_t)j.counter.ptr, (uint64_t)(uintptr_t)d_q,
                     (uint64_t)(uintptr_t)j.mmin.ptr, (uint64_t)(uintptr_t)j.smin.ptr, (uint64_t)(uintptr_t)j.t.ptr,
                     (uint64_t)(uintptr_t)j.gstart.ptr, (uint64_t)(uintptr_t)j.gent.ptr, (uint64_t)(uintptr_t)j.work.ptr,
                     (uint64_t)(uintptr_t)j.seq.ptr, (uint64_t)(uintptr_t)loff, (uint64_t)(uintptr_t)j.hinfo.ptr,
                     (uint64_t)(uintptr_t)perm, (uint64_t)olo, (uint64_t)ohi,
                     (uint64_t)(uintptr_t)j.tent.ptr, (uint64_t)(uintptr_t)j.tstart.ptr, (uint64_t)(uintptr_t)j.tgent.ptr,
-                    (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr,
-                    (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap,
-                    (uint64_t)items.size(), (uint64_t)grid, (uint64_t)any_dense, (uint64_t)A,
+                    (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr, (uint64_t)(uintptr_t)j.nsec.ptr,
+                    (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap, (uint64_t)split8,
+                    (uint64_t)nh, (uint64_t)ns, (uint64_t)grid, (uint64_t)grid_s, (uint64_t)any_dense, (uint64_t)A,
                     (uint64_t)rlo, (uint64_t)rhi});
                 ev_begin(ctx, ctx->ev_kmer, s);
                 CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
-                    CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 4, s));
-                    tile<<<grid, kTileThreads, tsmem, s>>>(t2);
-                    count_launch(ctx);
+                    CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 8, s));
+                    if (nh) {
+                        main_fn<<<grid, kTileThreads, main_smem, s>>>(t2);
+                        count_launch(ctx);
+                    }
+                    if (ns) {
+                        tile<<<grid_s, kTileThreads, tsmem, s>>>(t3);
+                        count_launch(ctx);
+                    }
                     if (any_dense) {
                         kmer_dense_kernel<<<std::min(rhi - rlo, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
                         count_launch(ctx);
