@@ -1142,6 +1142,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
 // m is formed bit-sliced with the [same] mask per (row, column).
 // ---------------------------------------------------------------------------
 constexpr int kRows8 = 16;
+constexpr int kTile8Threads = 1024;
+constexpr int kTile8Warps = kTile8Threads / 32;
 constexpr int kPlane8 = 32768 + 64;    // 16-bit L plane words: K-mers + guard words
 constexpr int kPlaneH = 32768 + 32;    // 32-bit H plane words: K-mers + guard words
 constexpr size_t kSmem8 = (size_t)kPlaneH * 4 + (size_t)kPlane8 * 2;
@@ -1196,7 +1198,7 @@ __device__ __forceinline__ void phase8(const W* __restrict__ plane, const uint4*
 }
 
 template <int B>
-__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a) {
+__global__ void __launch_bounds__(kTile8Threads, 1) kmer_tile8_kernel(TileArgs a) {
     extern __shared__ __align__(16) uint32_t PH[];   // H plane (32-bit words), then L plane (16-bit)
     __shared__ uint32_t hkeys[kHashSlots];
     __shared__ uint32_t hmask[kHashSlots];
@@ -1241,11 +1243,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
             if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
         }
         uint4* P4 = reinterpret_cast<uint4*>(PH);
-        for (int i = threadIdx.x; i < (int)(kSmem8 / 16); i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
-        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
+        for (int i = threadIdx.x; i < (int)(kSmem8 / 16); i += kTile8Threads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTile8Threads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
         __syncthreads();
         uint32_t* PL32 = PH + kPlaneH;
-        for (int b = warp; b < kRows8; b += kTileWarps) {
+        for (int b = warp; b < kRows8; b += kTile8Warps) {
             if (!((s_rows_ok >> b) & 1u)) continue;
             const int r = r0 + b;
             const uint32_t* src = a.ent + a.gstart[r >> 5];
@@ -1273,7 +1275,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
         __syncthreads();
         const bool any_high = s_any_high != 0;
         const uint32_t rows_ok = s_rows_ok;
-        for (int q = max(q0, r0 / 64) + warp; q < q1; q += kTileWarps) {
+        for (int q = max(q0, r0 / 64) + warp; q < q1; q += kTile8Warps) {
             const int gA = 2 * q, gB = 2 * q + 1;
             const bool hasB = gB < a.ngroups;
             const int cA = 64 * q + lane, cB = cA + 32;
@@ -1388,6 +1390,22 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8_kernel(TileArgs a)
 // ---------------------------------------------------------------------------
 constexpr int kRows8H = 32;
 constexpr size_t kSmem8H = (size_t)kPlaneH * 4;
+constexpr int kTile8HThreads = 1024;   // 32 warps: the stream loads' latency is hidden by warps
+constexpr int kTile8HWarps = kTile8HThreads / 32;
+constexpr int kDepth8H = 1;   // batches of 16 stream entries in flight ahead of the one reduced
+
+template <int B>
+__device__ __forceinline__ void gather8h_16(const uint32_t* __restrict__ plane, uint4 q0, uint4 q1,
+                                            Counter<B>& cnt) {
+    const uint32_t x[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+    uint32_t w[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        w[2 * k] = plane[x[k] & 0xFFFFu];
+        w[2 * k + 1] = plane[x[k] >> 16];
+    }
+    cnt.add_sixteens1(cnt.add16(w));
+}
 
 template <int B>
 __device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, const uint4* ep, int E,
@@ -1395,25 +1413,29 @@ __device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, cons
     const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
     Counter<B> cnt;
     cnt.clear();
-    uint4 a0 = 0 < E ? __ldg(ep) : guard, a1 = 0 < E ? __ldg(ep + 32) : guard;
-    for (int e = 0; e < E; e += 16) {
-        const int o = ((e + 16) >> 3) * 32;
-        const uint4 n0 = e + 16 < E ? __ldg(ep + o) : guard, n1 = e + 16 < E ? __ldg(ep + o + 32) : guard;
-        const uint32_t x[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        uint32_t w[16];
+    // batch i (16 entries) is the uint4 pair at ep + 64 i, ep + 64 i + 32
+    uint4 q[kDepth8H + 1][2];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            w[2 * k] = plane[x[k] & 0xFFFFu];
-            w[2 * k + 1] = plane[x[k] >> 16];
-        }
-        cnt.add_sixteens1(cnt.add16(w));
-        a0 = n0; a1 = n1;
+    for (int d = 0; d <= kDepth8H; ++d) {
+        const bool in = 16 * d < E;
+        q[d][0] = in ? __ldg(ep + 64 * d) : guard;
+        q[d][1] = in ? __ldg(ep + 64 * d + 32) : guard;
+    }
+    for (int e = 0; e < E; e += 16) {
+        const int en = e + 16 * (kDepth8H + 1);
+        const int o = (en >> 3) * 32;
+        const uint4 n0 = en < E ? __ldg(ep + o) : guard, n1 = en < E ? __ldg(ep + o + 32) : guard;
+        gather8h_16<B>(plane, q[0][0], q[0][1], cnt);
+#pragma unroll
+        for (int d = 0; d < kDepth8H; ++d) { q[d][0] = q[d + 1][0]; q[d][1] = q[d + 1][1]; }
+        q[kDepth8H][0] = n0;
+        q[kDepth8H][1] = n1;
     }
     cnt.planes(X);
 }
 
 template <int B>
-__global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8h_kernel(TileArgs a) {
+__global__ void __launch_bounds__(kTile8HThreads, 1) kmer_tile8h_kernel(TileArgs a) {
     extern __shared__ __align__(16) uint32_t PH[];
     __shared__ uint32_t hkeys[kHashSlots];
     __shared__ uint32_t hmask[kHashSlots];
@@ -1452,11 +1474,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8h_kernel(TileArgs a
             if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; s_nkeys = __popc(lm); }
         }
         uint4* P4 = reinterpret_cast<uint4*>(PH);
-        for (int i = threadIdx.x; i < (int)(kSmem8H / 16); i += kTileThreads) P4[i] = make_uint4(0, 0, 0, 0);
-        for (int i = threadIdx.x; i < kHashSlots; i += kTileThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
+        for (int i = threadIdx.x; i < (int)(kSmem8H / 16); i += kTile8HThreads) P4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < kHashSlots; i += kTile8HThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
         __syncthreads();
         const uint32_t* src = a.ent + a.gstart[rg];
-        for (int b = warp; b < kRows8H; b += kTileWarps) {
+        for (int b = warp; b < kRows8H; b += kTile8HWarps) {
             if (!((s_rows_ok >> b) & 1u)) continue;
             const int r = r0 + b;
             // high-level entries, then the H section of the read's list
@@ -1483,7 +1505,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile8h_kernel(TileArgs a
         const bool any_high = s_any_high != 0;
         const uint32_t rows_ok = s_rows_ok;
         const int nkeys = s_nkeys;
-        for (int q = rg + warp; q < a.ngroups; q += kTileWarps) {
+        for (int q = rg + warp; q < a.ngroups; q += kTile8HWarps) {
             const int c = 32 * q + lane;
             const bool okc = c < a.n;
             const uint32_t hc = okc ? a.hinfo[c] : 0u;
@@ -2059,6 +2081,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = K == 8 ? tile8_fn_for(B) : rows_blk == kRows128 ? tile128_fn_for(B) : tile_fn_for(B);
+    const int tile_threads = K == 8 ? kTile8Threads : kTileThreads;
     const size_t tsmem = !fast ? 0 : K == 8 ? kSmem8     // H and L planes + guards
                                              : ((size_t)levels * K4 + 32) * (rows_blk / 8);   // planes + guards
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
@@ -2133,7 +2156,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                         // keeps as many blocks per stage as 64-row blocks give
                         const int rg0 = t2.r_lo / rows_blk, rg1 = (t2.r_hi - 1) / rows_blk;
                         const dim3 grid(rg1 - rg0 + 1, rows_blk == kRows128 ? 2 : 1);
-                        tile<<<grid, kTileThreads, tsmem, ss>>>(t2);
+                        tile<<<grid, tile_threads, tsmem, ss>>>(t2);
                         count_launch(ctx);
                     }
                     if (dense_all || any_dense) {
@@ -2206,8 +2229,9 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 t3.items = d_items_s; t3.nitems = (int)ns; t3.queue_head = head + 1;
                 t3.item_q = d_q; t3.same_only = 1;
                 int per_sm = 1, per_sm_s = 1;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, main_fn, kTileThreads, main_smem);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, tile, kTileThreads, tsmem);
+                const int main_threads = split8 ? kTile8HThreads : tile_threads;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, main_fn, main_threads, main_smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, tile, tile_threads, tsmem);
                 per_sm = std::max(1, per_sm);
                 per_sm_s = std::max(1, per_sm_s);
                 const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)nh);
@@ -2230,11 +2254,11 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
                     CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 8, s));
                     if (nh) {
-                        main_fn<<<grid, kTileThreads, main_smem, s>>>(t2);
+                        main_fn<<<grid, main_threads, main_smem, s>>>(t2);
                         count_launch(ctx);
                     }
                     if (ns) {
-                        tile<<<grid_s, kTileThreads, tsmem, s>>>(t3);
+                        tile<<<grid_s, tile_threads, tsmem, s>>>(t3);
                         count_launch(ctx);
                     }
                     if (any_dense) {
