@@ -322,7 +322,7 @@ def run_ours(args, dist, ws, rank, local):
 
     kmer_ops = n_pairs * 2 * mean_t            # frozen: (Ta + Tb) per pair
     gen_ops = cells * 10                        # frozen: 10 per band cell
-    tile_kernel = ("kmer_tile8_kernel" if k == 8 else "kmer_tile_kernel" if k == 7
+    tile_kernel = ("kmer_tile8h_kernel + kmer_tile8_kernel" if k == 8 else "kmer_tile_kernel" if k == 7
                    else "kmer_tile128_kernel")
     roof_k = {"kernel": tile_kernel, "bound": "int32", "unit": "Gop/s",
               "achieved": kmer_ops / kmer_s / 1e9, "peak": int_peak_gops,
@@ -345,7 +345,7 @@ def run_ours(args, dist, ws, rank, local):
         "achieved": n_pairs * dense_ops / kmer_s / 1e9, "peak": int_peak_gops,
         "frac": n_pairs * dense_ops / kmer_s / 1e9 / int_peak_gops}
     dominant = roof_g if gen_s >= kmer_s else roof_k
-    _attach_traffic(roof_k, roof_g, n_pairs, cells)
+    _attach_traffic(roof_k, roof_g, n_pairs, cells, k)
     _attach_hbm_view(roof_k, kmer_s)
     _attach_hbm_view(roof_g, gen_s)
 
@@ -603,8 +603,9 @@ def _attach_hbm_view(roof, seconds):
                         "peak_source": "measured: MEASURED_PEAKS.json hbm_gbs"}
 
 
-def _attach_traffic(roof_k, roof_g, n_pairs, cells):
-    """DRAM bytes per launch from a committed ncu summary, scaled by units."""
+def _attach_traffic(roof_k, roof_g, n_pairs, cells, k):
+    """DRAM bytes per launch from a committed ncu summary, scaled by units
+    (k = 8 has kmerDist figures of its own, from the stress set)."""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.exists(p):
         return
@@ -612,15 +613,16 @@ def _attach_traffic(roof_k, roof_g, n_pairs, cells):
         t = json.load(open(p))
     except (OSError, ValueError):
         return
-    if "kmer_bytes_per_pair" in t:
-        roof_k["traffic"] = t["kmer_bytes_per_pair"] * n_pairs
-        roof_k["traffic_source"] = t.get("source")
+    tk = t.get("k8", t) if k == 8 else t
+    if "kmer_bytes_per_pair" in tk:
+        roof_k["traffic"] = tk["kmer_bytes_per_pair"] * n_pairs
+        roof_k["traffic_source"] = tk.get("source")
     if "gen_bytes_per_cell" in t:
         roof_g["traffic"] = t["gen_bytes_per_cell"] * cells
         roof_g["traffic_source"] = t.get("source")
     # the hardware pipe each kernel saturates, from the same ncu captures
-    if "kmer_binding_pipe" in t:
-        roof_k["ncu_binding_pipe"] = t["kmer_binding_pipe"]
+    if "kmer_binding_pipe" in tk:
+        roof_k["ncu_binding_pipe"] = tk["kmer_binding_pipe"]
     if "gen_binding_pipe" in t:
         roof_g["ncu_binding_pipe"] = t["gen_binding_pipe"]
 

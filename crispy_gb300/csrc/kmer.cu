@@ -1790,8 +1790,11 @@ int kmer_groups(crispy_ctx* ctx, const int32_t* t) {
         const int mt = j.h_gent[g];
         j.h_gent[g] = (mt + 15) / 16 * 16;
         j.h_gstart[g + 1] = j.h_gstart[g] + 32LL * j.h_gent[g];
-        // the tile stream gets spare steps: wildcards for the bank schedule
-        j.h_tgent[g] = (mt + (mt >= 128 ? kSchedSpare : 0) + 15) / 16 * 16;
+        // K = 7: spare steps give the bank schedule wildcards; the 128-row
+        // kernel (K <= 6) gains more from the steps saved than it loses to
+        // the conflicts left
+        const int spare = tile_rows_for(j.k) == kRows128 || mt < 128 ? 0 : kSchedSpare;
+        j.h_tgent[g] = (mt + spare + 15) / 16 * 16;
         j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * j.h_tgent[g];
     }
     j.nent = j.h_gstart[j.ngroups];
@@ -1997,7 +2000,9 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
                 mh = std::max(mh, j.h_nsec[2 * (size_t)r]);
                 ml = std::max(ml, j.h_nsec[2 * (size_t)r + 1]);
             }
-            j.h_tgent[g] = (mh + (mh >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
+            // no spare steps for H: the H-only kernel is issue-bound, a bank
+            // conflict costs it less than a step
+            j.h_tgent[g] = (mh + 15) / 16 * 16;
             tgl[g] = (ml + (ml >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
             j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * (j.h_tgent[g] + tgl[g]);
         }
