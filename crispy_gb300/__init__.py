@@ -115,6 +115,7 @@ PROTOTYPES = {
     "crispy_gen_prepare_from_pre": (C.c_int, [_P, _P]),
     "crispy_aveclust": (C.c_int, [C.POINTER(_P), C.POINTER(_P), _P, C.c_int, C.c_int, C.c_float,
                                   C.c_char_p, C.c_char_p, C.POINTER(ClustStats)]),
+    "crispy_sparsecut": (C.c_int, [C.c_char_p, C.c_int, _P, C.c_int, C.POINTER(ClustStats)]),
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
@@ -545,3 +546,16 @@ def aveclust(chunks, num_reads: int, out_base: str, end_level: float = -1.0,
         raise CrispyError(rc, lib.crispy_last_error(None).decode())
     return {"pairs_read": st.pairs_read, "merges": st.merges, "roots": st.roots,
             "singletons": st.singletons, "end_level": st.end_level, "report": st.report.decode()}
+
+
+def sparsecut(in_base: str, num_reads: int, cutoffs) -> dict:
+    """Clusters of the dendrogram in_base_Merge at each cutoff distance
+    (crispy_sparsecut); writes in_base.Cluster and in_base.Cluster_List."""
+    lib = load_library()
+    cut = np.ascontiguousarray(cutoffs, dtype=np.float32).reshape(-1)
+    st = ClustStats()
+    rc = lib.crispy_sparsecut(in_base.encode(), num_reads, cut.ctypes.data if len(cut) else None, len(cut),
+                              C.byref(st))
+    if rc != OK:
+        raise CrispyError(rc, lib.crispy_last_error(None).decode())
+    return {"merges": st.merges, "roots": st.roots, "singletons": st.singletons, "report": st.report.decode()}

@@ -29,7 +29,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu", "pre.cu"]
 CXX_SOURCES = ["fasta.cpp", "pre_io.cpp", "clust.cpp"]
 CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp",
-       "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp", "aveclust": "cli_clust.cpp"}
+       "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp", "aveclust": "cli_clust.cpp",
+       "sparsecut": "cli_cut.cpp"}
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -1,4 +1,4 @@
-// crispyRun -- crispy.sh up to aveclust in one process.
+// crispyRun -- crispy.sh in one process (the R changepoint step excepted).
 //
 // crispy.sh:18-24 runs
 //     ./bin/preprocess -i $INPUT
@@ -6,7 +6,10 @@
 //     ./bin/genDist   -i $INPUT"_Clean" -b $B
 //     NUM_READS=`grep '>' $INPUT"_Clean" | wc -l`;  NUM_FILES=`ls ...ndist* | wc -l`
 //     ./bin/aveclust  -i $INPUT"_Clean" -n $NUM_READS -f $NUM_FILES
-// as four programs that hand the reads over through the _Clean file, the
+// and crispy.sh:26-29 then cuts the dendrogram at the changepoint's cutoffs
+//     R ... crispy_changepoint.r --args $INPUT"_Clean_Merge"   (-> optimal_cutoff.txt)
+//     ./bin/sparsecut -i $INPUT"_Clean" -n $NUM_READS -c optimal_cutoff.txt
+// as separate programs that hand the reads over through the _Clean file, the
 // k-mer survivors through the .kpair file and the genetic distances through
 // the .npair_N / .ndist_N chunks.  This executable writes the same files
 // (<in>_Clean, .frq, .kpair, .npair_<f> / .ndist_<f>, _Merge byte for byte;
@@ -21,10 +24,13 @@
 // the number of chunks this run wrote (crispy.sh's `ls` would also count
 // chunk files an earlier, larger run left behind).
 //
-//   crispyRun <input file> [K (default 6)] [band (default 10)]
+//   crispyRun <input file> [K (default 6)] [band (default 10)] [cutoff file]
 //
-// The arguments and their defaults are crispy.sh's (crispy.sh:1-16); the
-// thresholds are the stages' defaults.  CRISPY_MODE selects the form as for
+// The first three arguments and their defaults are crispy.sh's
+// (crispy.sh:1-16); the thresholds are the stages' defaults.  R is not part
+// of this engine: given a cutoff file (as the changepoint step writes it),
+// the sparsecut step runs on it and rewrites .Cluster / .Cluster_List with
+// the clusters at those cutoffs (crispy_sparsecut).  CRISPY_MODE selects the form as for
 // kmerDist / genDist.  No reference counterpart as a single program.
 #include <sys/time.h>
 
@@ -34,6 +40,7 @@
 #include <string>
 #include <vector>
 
+#include "cli_common.h"
 #include "crispy_gb300.h"
 
 namespace {
@@ -98,7 +105,7 @@ int prepare_from_file(crispy_ctx* ctx, const std::string& clean, int flavour, in
 int main(int argc, char** argv) {
     const double t0 = now();
     if (argc < 2 || !std::strcmp(argv[1], "-h")) {
-        std::printf("Correct syntax: crispyRun <input file name> [k value] [band value]\n");
+        std::printf("Correct syntax: crispyRun <input file name> [k value] [band value] [cutoff file]\n");
         return 255;
     }
     const std::string in = argv[1];
@@ -196,6 +203,20 @@ int main(int argc, char** argv) {
         }
         std::printf("aveclust: %lld merges, %d clusters, %d singletons\n", (long long)cs.merges, cs.roots,
                     cs.singletons);
+    }
+    if (argc > 4 && !cn.empty() && num_reads > 0) {
+        // sparsecut on the _Merge file aveclust wrote (crispy.sh:29)
+        std::vector<float> cutoffs;
+        const std::string err = crispy_cli::read_cutoffs(argv[4], cutoffs, false);
+        crispy_clust_stats ss{};
+        if (!err.empty() || crispy_sparsecut(clean.c_str(), (int)num_reads, cutoffs.data(),
+                                             (int)cutoffs.size(), &ss) != CRISPY_OK) {
+            std::fprintf(stderr, "crispyRun: %s\n", err.empty() ? crispy_last_error(nullptr) : err.c_str());
+            crispy_ctx_destroy(ctx);
+            crispy_raw_free(raw);
+            return 255;
+        }
+        std::printf("sparsecut: %d cutoffs\n%s", (int)cutoffs.size(), ss.report);
     }
     crispy_ctx_destroy(ctx);
     crispy_raw_free(raw);

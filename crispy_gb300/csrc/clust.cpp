@@ -405,6 +405,102 @@ void put_level_line(std::string& cl, std::string& cf, float level) {
     cf += b;
 }
 
+// printClusters (aveclust.cpp:244-340; sparsecut.cpp:146-272 is the same
+// function with EPSILON 1e-5): per distance level, the clusters a cut at
+// that level leaves (a node is kept whole when its dist is below the level
+// or within eps of it), each with its leaves in the reference's depth-first
+// order, then the singletons.  Roots are visited by ascending node ID (the
+// reference iterates a hash set of node pointers).  One thread per level;
+// each reads the finished tree only.  NodeT: id, left, right (-1: none),
+// dist, members.
+template <typename NodeT>
+void cluster_levels(const std::vector<NodeT>& nodes, const std::vector<int>& roots,
+                    const std::vector<int>& orphans, const std::vector<float>& levels, double eps,
+                    std::string& cl_out, std::string& cf_out, std::string& report) {
+    const size_t nl = levels.size();
+    std::vector<std::string> cls(nl), cfs(nl), reps(nl);
+    auto one_level = [&](size_t li) {
+        const float level = levels[li];
+        std::string& cl = cls[li];
+        std::string& cf = cfs[li];
+        char buf[96];
+        auto within = [&](int i) { return nodes[i].dist < level || std::fabs(nodes[i].dist - level) < eps; };
+        std::vector<int> cut;   // the reference's nodeList, built with push_front
+        for (int r : roots) {
+            if (within(r)) { cut.push_back(r); continue; }
+            std::vector<int> todo{r};
+            while (!todo.empty()) {
+                const int t = todo.back();
+                todo.pop_back();
+                const int lf = nodes[t].left, rt = nodes[t].right;
+                if (within(lf)) cut.push_back(lf); else todo.push_back(lf);
+                if (within(rt)) cut.push_back(rt); else todo.push_back(rt);
+            }
+        }
+        std::reverse(cut.begin(), cut.end());
+        put_level_line(cl, cf, level);
+        std::vector<int> todo;
+        for (int top : cut) {
+            cf += '|';
+            todo.assign(1, top);
+            bool first = true;
+            unsigned int size = 0;
+            while (!todo.empty()) {
+                const int t = todo.back();
+                todo.pop_back();
+                const NodeT& nd = nodes[t];
+                if (nd.left < 0 && nd.right < 0) {
+                    char* e = buf + sizeof buf;
+                    char* b = put_uint(e, nd.id);
+                    if (!first) *--b = ' ';
+                    cf.append(b, (size_t)(e - b));
+                    first = false;
+                    size += nd.members;
+                }
+                if (nd.right >= 0) todo.push_back(nd.right);
+                if (nd.left >= 0) todo.push_back(nd.left);
+            }
+            char* e = buf + sizeof buf;
+            *--e = ' ';
+            char* b = put_uint(e, size);   // "%d " of an unsigned count below 2^31
+            cl.append(b, (size_t)(buf + sizeof buf - b));
+        }
+        for (int o : orphans) {
+            char* e = buf + sizeof buf;
+            char* b = put_uint(e, (unsigned)o);
+            *--b = '|';
+            cf.append(b, (size_t)(e - b));
+            cl += "1 ";
+        }
+        cf += "|\n";
+        cl += "\n";
+        std::snprintf(buf, sizeof buf, "Dist: %.6f. numOTUs: %u. numSingletons: %lu\n", level,
+                      (unsigned)(cut.size() + orphans.size()), (unsigned long)orphans.size());
+        reps[li] = buf;
+    };
+    {
+        std::vector<std::thread> th;
+        for (size_t li = 0; li < nl; ++li) th.emplace_back(one_level, li);
+        for (auto& t : th) t.join();
+    }
+    for (size_t li = 0; li < nl; ++li) {
+        cl_out += cls[li];
+        cf_out += cfs[li];
+        report += reps[li];
+    }
+}
+
+int write_files(const char* who, const std::string* names, const std::string* const* bodies, int n) {
+    for (int i = 0; i < n; ++i) {
+        FILE* f = std::fopen(names[i].c_str(), "wb");
+        if (!f) return crispy::fail(nullptr, CRISPY_E_IO, "%s: cannot write %s", who, names[i].c_str());
+        const bool ok = std::fwrite(bodies[i]->data(), 1, bodies[i]->size(), f) == bodies[i]->size();
+        if (std::fclose(f) != 0 || !ok)
+            return crispy::fail(nullptr, CRISPY_E_IO, "%s: short write to %s", who, names[i].c_str());
+    }
+    return CRISPY_OK;
+}
+
 }  // namespace
 
 extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const* dists, const int64_t* counts,
@@ -500,9 +596,8 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
     }
     if (fo) { std::fclose(fo); std::fclose(fo1); }
 
-    // roots and singletons (aveclust.cpp:944-955), then printClusters
-    // (aveclust.cpp:244-340): per distance level, the clusters a cut at
-    // that level leaves, members in the reference's depth-first order
+    // roots and singletons (aveclust.cpp:944-955), then printClusters at
+    // the levels the reference's float loop visits
     std::vector<int> roots, orphans;
     std::vector<char> seen(C.nodes.size(), 0);
     for (int i = 0; i < num_reads; ++i) {
@@ -514,99 +609,105 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         if (!seen[r]) { seen[r] = 1; roots.push_back(r); }
     }
     std::sort(roots.begin(), roots.end());
-    // the levels as the reference's float loop visits them, then one thread
-    // per level (each reads the finished trees only)
     const float step = C.end_level / 10;
     std::vector<float> levels;
     for (float level = step; level < C.end_level || std::fabs(level - C.end_level) < kEps; level += step)
         levels.push_back(level);
-    const size_t nl = levels.size();
-    std::vector<std::string> cls(nl), cfs(nl), reps(nl);
-    auto one_level = [&](size_t li) {
-        const float level = levels[li];
-        std::string& cl = cls[li];
-        std::string& cf = cfs[li];
-        char buf[96];
-        auto within = [&](int i) { return C.nodes[i].dist < level || std::fabs(C.nodes[i].dist - level) < kEps; };
-        std::vector<int> cut;   // the reference's nodeList, built with push_front
-        for (int r : roots) {
-            if (within(r)) { cut.push_back(r); continue; }
-            std::vector<int> todo{r};
-            while (!todo.empty()) {
-                const int t = todo.back();
-                todo.pop_back();
-                const int lf = C.nodes[t].left, rt = C.nodes[t].right;
-                if (within(lf)) cut.push_back(lf); else todo.push_back(lf);
-                if (within(rt)) cut.push_back(rt); else todo.push_back(rt);
-            }
-        }
-        std::reverse(cut.begin(), cut.end());
-        put_level_line(cl, cf, level);
-        std::vector<int> todo;
-        for (int top : cut) {
-            cf += '|';
-            todo.assign(1, top);
-            bool first = true;
-            unsigned int size = 0;
-            while (!todo.empty()) {
-                const int t = todo.back();
-                todo.pop_back();
-                const Node& nd = C.nodes[t];
-                if (nd.left < 0 && nd.right < 0) {
-                    char* e = buf + sizeof buf;
-                    char* b = put_uint(e, nd.id);
-                    if (!first) *--b = ' ';
-                    cf.append(b, (size_t)(e - b));
-                    first = false;
-                    size += nd.members;
-                }
-                if (nd.right >= 0) todo.push_back(nd.right);
-                if (nd.left >= 0) todo.push_back(nd.left);
-            }
-            char* e = buf + sizeof buf;
-            *--e = ' ';
-            char* b = put_uint(e, size);   // "%d " of an unsigned count below 2^31
-            cl.append(b, (size_t)(buf + sizeof buf - b));
-        }
-        for (int o : orphans) {
-            char* e = buf + sizeof buf;
-            char* b = put_uint(e, (unsigned)o);
-            *--b = '|';
-            cf.append(b, (size_t)(e - b));
-            cl += "1 ";
-        }
-        cf += "|\n";
-        cl += "\n";
-        std::snprintf(buf, sizeof buf, "Dist: %.6f. numOTUs: %u. numSingletons: %lu\n", level,
-                      (unsigned)(cut.size() + orphans.size()), (unsigned long)orphans.size());
-        reps[li] = buf;
-    };
-    {
-        std::vector<std::thread> th;
-        for (size_t li = 0; li < nl; ++li) th.emplace_back(one_level, li);
-        for (auto& t : th) t.join();
-    }
     std::string cl, cf, report;
-    for (size_t li = 0; li < nl; ++li) {
-        cl += cls[li];
-        cf += cfs[li];
-        report += reps[li];
-    }
+    cluster_levels(C.nodes, roots, orphans, levels, kEps, cl, cf, report);
     const std::string base(out_base);
-    struct Out { std::string name; const std::string* body; } outs[] = {
-        {base + "_Merge", &merges}, {base + ".Cluster_List", &cl}, {base + ".Cluster", &cf}};
-    for (auto& o : outs) {
-        FILE* f = std::fopen(o.name.c_str(), "wb");
-        if (!f) return fail(nullptr, CRISPY_E_IO, "aveclust: cannot write %s", o.name.c_str());
-        const bool ok = std::fwrite(o.body->data(), 1, o.body->size(), f) == o.body->size();
-        if (std::fclose(f) != 0 || !ok) return fail(nullptr, CRISPY_E_IO, "aveclust: short write to %s", o.name.c_str());
-    }
+    const std::string names[] = {base + "_Merge", base + ".Cluster_List", base + ".Cluster"};
+    const std::string* bodies[] = {&merges, &cl, &cf};
+    CRISPY_TRY(write_files("aveclust", names, bodies, 3));
     if (stats) {
         stats->pairs_read = read_pairs;
         stats->merges = (int64_t)(C.new_id - (unsigned)num_reads);
         stats->roots = (int32_t)roots.size();
         stats->singletons = (int32_t)orphans.size();
         stats->end_level = C.end_level;
+        std::snprintf(stats->report, sizeof stats->report, "%s", report.c_str());
+    }
+    return CRISPY_OK;
+}
+
+namespace {
+
+constexpr double kCutEps = 1e-5;   // EPSILON (sparsecut.cpp:18)
+
+struct CutNode {
+    unsigned int id = 0;
+    int parent = -1, left = -1, right = -1;
+    float dist = 0.0f;
+    unsigned int members = 1;
+};
+
+}  // namespace
+
+// sparsecut (src/sparsecut/sparsecut.cpp, the step crispy.sh:29 runs after
+// the changepoint cutoffs): rebuild the dendrogram from <in_base>_Merge
+// (sparsecut.cpp:361-367: "%d %d %f" lines of 1-based node IDs; merge k
+// creates node num_reads + k with the larger-ID child on the left,
+// sparsecut.cpp:283-315) and print the clusters at each cutoff.  Merge
+// lines that do not join two current clusters are refused (the reference
+// does not check them).
+extern "C" int crispy_sparsecut(const char* in_base, int num_reads, const float* cutoffs, int ncutoffs,
+                                crispy_clust_stats* stats) {
+    using crispy::fail;
+    if (!in_base || num_reads < 1 || ncutoffs < 0 || (ncutoffs > 0 && !cutoffs))
+        return fail(nullptr, CRISPY_E_INPUT, "sparsecut: need an input name, reads and the cutoffs");
+    const std::string base(in_base);
+    const std::string merge_name = base + "_Merge";
+    FILE* f = std::fopen(merge_name.c_str(), "r");
+    if (!f) return fail(nullptr, CRISPY_E_IO, "sparsecut: cannot open %s", merge_name.c_str());
+    std::vector<CutNode> nodes((size_t)2 * num_reads);
+    for (int i = 0; i < num_reads; ++i) nodes[i].id = (unsigned)i;
+    int new_id = num_reads;
+    int idx = 0, idy = 0;
+    float dist = 0.0f;
+    while (std::fscanf(f, "%d %d %f", &idx, &idy, &dist) == 3) {
+        const int a = idx - 1, b = idy - 1;
+        if (new_id >= 2 * num_reads || a < 0 || b < 0 || a >= new_id || b >= new_id || a == b ||
+            nodes[a].parent >= 0 || nodes[b].parent >= 0) {
+            std::fclose(f);
+            return fail(nullptr, CRISPY_E_INPUT, "sparsecut: %s merges %d and %d, not two current clusters",
+                        merge_name.c_str(), idx, idy);
+        }
+        CutNode& p = nodes[new_id];
+        p.id = (unsigned)new_id;
+        const int x = std::max(a, b), y = std::min(a, b);   // addNode(nodeX, nodeY): larger ID left
+        p.left = x;
+        p.right = y;
+        p.dist = dist;
+        p.members = nodes[x].members + nodes[y].members;
+        nodes[x].parent = nodes[y].parent = new_id;
+        ++new_id;
+    }
+    std::fclose(f);
+    // each leaf's top node: parents come after their children
+    std::vector<int> top(new_id);
+    for (int i = new_id - 1; i >= 0; --i) top[i] = nodes[i].parent < 0 ? i : top[nodes[i].parent];
+    std::vector<int> roots, orphans;
+    std::vector<char> seen(new_id, 0);
+    for (int i = 0; i < num_reads; ++i) {
+        if (nodes[i].parent < 0) {
+            orphans.push_back(i);
+            continue;
+        }
+        if (!seen[top[i]]) { seen[top[i]] = 1; roots.push_back(top[i]); }
+    }
+    std::sort(roots.begin(), roots.end());
+    std::string cl, cf, report;
+    cluster_levels(nodes, roots, orphans, std::vector<float>(cutoffs, cutoffs + ncutoffs), kCutEps, cl, cf,
+                   report);
+    const std::string names[] = {base + ".Cluster_List", base + ".Cluster"};
+    const std::string* bodies[] = {&cl, &cf};
+    CRISPY_TRY(write_files("sparsecut", names, bodies, 2));
+    if (stats) {
+        stats->pairs_read = 0;
+        stats->merges = (int64_t)(new_id - num_reads);
+        stats->roots = (int32_t)roots.size();
+        stats->singletons = (int32_t)orphans.size();
+        stats->end_level = ncutoffs > 0 ? cutoffs[ncutoffs - 1] : 0.0f;
         std::snprintf(stats->report, sizeof stats->report, "%s", report.c_str());
     }
     return CRISPY_OK;

@@ -296,6 +296,19 @@ int crispy_aveclust(const uint32_t* const* pairs, const float* const* dists,
                     const int64_t* counts, int nchunks, int num_reads, float end_level,
                     const char* out_base, const char* edge_out, crispy_clust_stats* stats);
 
+/* ---- sparsecut (replaces bin/sparsecut, src/sparsecut/sparsecut.cpp, the
+ *      step crispy.sh:29 runs with the changepoint's cutoff file) ---- */
+/* Reads the dendrogram <in_base>_Merge (as aveclust writes it: one
+ * "idX idY dist" line per merge, 1-based node IDs) and writes
+ * <in_base>.Cluster and <in_base>.Cluster_List with the clusters a cut at
+ * each of the ncutoffs distances leaves (sparsecut.cpp:317-410; EPSILON
+ * 1e-5).  Clusters are those of the reference; it orders them by pointer
+ * hash, this function by root ID.  stats: merges read, roots, singletons,
+ * and the "Dist: ... numOTUs ..." report lines.  A merge line that does not
+ * join two current clusters is CRISPY_E_INPUT. */
+int crispy_sparsecut(const char* in_base, int num_reads, const float* cutoffs, int ncutoffs,
+                     crispy_clust_stats* stats);
+
 /* ---- timing of the last run (CUDA events on the context's stream) ---- */
 typedef struct crispy_stats {
     double kmer_kernel_ms;     /* summed duration of the k-mer tile kernel launches */

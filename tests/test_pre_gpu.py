@@ -145,7 +145,7 @@ def _run(cmd, cwd, ok=(0,)):
     return p.stdout
 
 
-def _four_programs(d, name, k, band):
+def _four_programs(d, name, k, band, cut=None):
     """crispy.sh:18-24 with the drop-in executables."""
     clean = name + "_Clean"
     _run([EXE, "-i", name], d, ok=(1,))
@@ -154,6 +154,8 @@ def _four_programs(d, name, k, band):
     num_reads = sum(1 for line in open(os.path.join(d, clean), "rb") if b">" in line)
     num_files = sum(1 for f in os.listdir(d) if f.startswith(clean + ".ndist"))
     _run([os.path.join(cg.BIN_DIR, "aveclust"), "-i", clean, "-n", str(num_reads), "-f", str(num_files)], d)
+    if cut:
+        _run([os.path.join(cg.BIN_DIR, "sparsecut"), "-i", clean, "-n", str(num_reads), "-c", cut], d)
 
 
 def _outputs(d):
@@ -197,9 +199,20 @@ def test_crispyrun_matches_four_programs(tmp_path, case, k, band):
     else:
         _whitespace_set(raw)
     shutil.copy(raw, os.path.join(str(b), "raw.fa"))
-    _four_programs(str(a), "raw.fa", k, band)
-    out = _run([os.path.join(cg.BIN_DIR, "crispyRun"), "raw.fa", str(k), str(band)], str(b))
+    # with a cutoff file (the changepoint step's output) the sparsecut step
+    # runs too, and rewrites .Cluster / .Cluster_List at those cutoffs
+    cut = None
+    if case in ("dups", "uneven") and k == 6:
+        cut = "cut.txt"
+        for d in (a, b):
+            open(os.path.join(str(d), cut), "w").write("0.01\n0.02\n0.03\n0.05\n")
+    _four_programs(str(a), "raw.fa", k, band, cut)
+    out = _run([os.path.join(cg.BIN_DIR, "crispyRun"), "raw.fa", str(k), str(band)] + ([cut] if cut else []),
+               str(b))
     assert b"totalNumPairs" in out
+    if cut:
+        assert b"sparsecut: 4 cutoffs" in out
+        assert open(os.path.join(str(b), "raw.fa_Clean.Cluster_List")).read().startswith(" 0.010000 ")
     want, got = _outputs(str(a)), _outputs(str(b))
     assert sorted(want) == sorted(got)
     assert any(".npair_" in f for f in got) and "raw.fa_Clean_Merge" in got
