@@ -1392,11 +1392,12 @@ constexpr int kRows8H = 32;
 constexpr size_t kSmem8H = (size_t)kPlaneH * 4;
 constexpr int kTile8HThreads = 1024;   // 32 warps: the stream loads' latency is hidden by warps
 constexpr int kTile8HWarps = kTile8HThreads / 32;
-constexpr int kDepth8H = 1;   // batches of 16 stream entries in flight ahead of the one reduced
 
+// 16 scheduled entries of one stream: their plane words into the counter;
+// returns the weight-16 carry.
 template <int B>
-__device__ __forceinline__ void gather8h_16(const uint32_t* __restrict__ plane, uint4 q0, uint4 q1,
-                                            Counter<B>& cnt) {
+__device__ __forceinline__ uint32_t gather8h_c16(const uint32_t* __restrict__ plane, uint4 q0, uint4 q1,
+                                                 Counter<B>& cnt) {
     const uint32_t x[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
     uint32_t w[16];
 #pragma unroll
@@ -1404,32 +1405,29 @@ __device__ __forceinline__ void gather8h_16(const uint32_t* __restrict__ plane, 
         w[2 * k] = plane[x[k] & 0xFFFFu];
         w[2 * k + 1] = plane[x[k] >> 16];
     }
-    cnt.add_sixteens1(cnt.add16(w));
+    return cnt.add16(w);
 }
 
+// A column's H stream (E steps, a multiple of 16) against the plane: two
+// 16-entry batches per carry chain, the next pair's first batch in flight.
+// E is the column group's step count, the same for every lane, so the
+// second batch's branch does not diverge.
 template <int B>
 __device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, const uint4* ep, int E,
                                         uint32_t* X) {
     const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
     Counter<B> cnt;
     cnt.clear();
-    // batch i (16 entries) is the uint4 pair at ep + 64 i, ep + 64 i + 32
-    uint4 q[kDepth8H + 1][2];
-#pragma unroll
-    for (int d = 0; d <= kDepth8H; ++d) {
-        const bool in = 16 * d < E;
-        q[d][0] = in ? __ldg(ep + 64 * d) : guard;
-        q[d][1] = in ? __ldg(ep + 64 * d + 32) : guard;
-    }
-    for (int e = 0; e < E; e += 16) {
-        const int en = e + 16 * (kDepth8H + 1);
-        const int o = (en >> 3) * 32;
-        const uint4 n0 = en < E ? __ldg(ep + o) : guard, n1 = en < E ? __ldg(ep + o + 32) : guard;
-        gather8h_16<B>(plane, q[0][0], q[0][1], cnt);
-#pragma unroll
-        for (int d = 0; d < kDepth8H; ++d) { q[d][0] = q[d + 1][0]; q[d][1] = q[d + 1][1]; }
-        q[kDepth8H][0] = n0;
-        q[kDepth8H][1] = n1;
+    uint4 a0 = 0 < E ? __ldg(ep) : guard, a1 = 0 < E ? __ldg(ep + 32) : guard;
+    for (int e = 0; e < E; e += 32) {
+        const bool two = e + 16 < E;
+        const int ob = ((e + 16) >> 3) * 32, on = ((e + 32) >> 3) * 32;
+        const uint4 b0 = two ? __ldg(ep + ob) : guard, b1 = two ? __ldg(ep + ob + 32) : guard;
+        const uint4 n0 = e + 32 < E ? __ldg(ep + on) : guard, n1 = e + 32 < E ? __ldg(ep + on + 32) : guard;
+        const uint32_t ca = gather8h_c16<B>(plane, a0, a1, cnt);
+        if (two) cnt.add_sixteens2(ca, gather8h_c16<B>(plane, b0, b1, cnt));
+        else cnt.add_sixteens1(ca);
+        a0 = n0; a1 = n1;
     }
     cnt.planes(X);
 }
