@@ -125,3 +125,32 @@ def test_kmer_k8_quirk_tiles(engine):
     counts = [_check(engine, reads, 8, thr, mode)
               for thr in (t, 0.7) for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
     assert counts[0] == counts[1] == counts[2] and counts[3] == counts[4] == counts[5] > 0
+
+
+@pytest.mark.parametrize("kind", ["no_h", "one_key", "random"])
+def test_kmer_k8_key_groups(engine, kind):
+    # K = 8 orders the reads by H key and splits the batched form into the
+    # H-only kernel (pairs of different keys) and the 16-row kernel over each
+    # row block's same-key range; these sets put every read in one key group
+    # (no H K-mer at all, or the same largest H K-mer once) or give mostly
+    # distinct keys
+    rng = np.random.default_rng({"no_h": 81, "one_key": 82, "random": 83}[kind])
+    reads = []
+    for i in range(520):
+        L = int(rng.integers(120, 300))
+        if kind == "no_h":       # A and G only: every K-mer is below 0x8000
+            s = rng.choice(np.frombuffer(b"AG", np.uint8), L).tobytes()
+        elif kind == "one_key":  # CCCCCCCC (0xFFFF, the largest K-mer) once, elsewhere no C
+            s = bytearray(rng.choice(np.frombuffer(b"AGT", np.uint8), L).tobytes())
+            p = int(rng.integers(0, L - 8))
+            s[p:p + 8] = b"CCCCCCCC"
+            s = bytes(s)
+        else:
+            s = rng.choice(np.frombuffer(b"ACGT", np.uint8), L).tobytes()
+        reads.append(s)
+    # a few near-copies so that pairs pass the threshold
+    reads += [bytes(r[:-3]) + b"AAA" for r in reads[:60]]
+    reads = synth.preprocess_order(reads)
+    counts = [_check(engine, reads, 8, thr, mode) for thr in (0.75, 0.3)
+              for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
+    assert counts[0] == counts[1] == counts[2] > 0
