@@ -108,23 +108,58 @@ __device__ __forceinline__ int prep_bucket(uint32_t val, int K) {
 constexpr int kPrepThreads = 256;
 constexpr int kPrepPer = CRISPY_MAX_READ_LEN / kPrepThreads;   // positions per thread
 
+// Per-read K-mer counts in shared memory.  Two 16-bit counts per 32-bit
+// word (K <= 7, 32 KB at K = 7); at K = 8 five 12-bit counts per 64-bit word
+// (102 KB instead of 128 KB, so that two blocks share an SM).  A count never
+// exceeds a read's tuples (2041 < 4096), so no field overflows.
+struct PrepHist16 {
+    uint32_t* h;
+    static constexpr size_t bytes(uint32_t K4) { return (size_t)((K4 + 1) / 2) * 4; }
+    __device__ void clear_all(uint32_t K4) const {
+        for (int i = threadIdx.x; i < (int)((K4 + 1) / 2); i += blockDim.x) h[i] = 0;
+    }
+    __device__ uint32_t add(uint32_t v) const {   // old count
+        const uint32_t sh = (v & 1u) * 16u;
+        return (atomicAdd(&h[v >> 1], 1u << sh) >> sh) & 0xFFFFu;
+    }
+    __device__ uint32_t get(uint32_t v) const { return (h[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu; }
+    __device__ void clear(uint32_t v) const { h[v >> 1] = 0; }
+};
+struct PrepHist12 {
+    unsigned long long* h;
+    static constexpr size_t bytes(uint32_t K4) { return (size_t)((K4 + 4) / 5) * 8; }
+    __device__ void clear_all(uint32_t K4) const {
+        for (int i = threadIdx.x; i < (int)((K4 + 4) / 5); i += blockDim.x) h[i] = 0ull;
+    }
+    __device__ uint32_t add(uint32_t v) const {
+        const uint32_t w = v / 5u, sh = 12u * (v - 5u * w);
+        return (uint32_t)(atomicAdd(&h[w], 1ull << sh) >> sh) & 0xFFFu;
+    }
+    __device__ uint32_t get(uint32_t v) const {
+        const uint32_t w = v / 5u;
+        return (uint32_t)(h[w] >> (12u * (v - 5u * w))) & 0xFFFu;
+    }
+    __device__ void clear(uint32_t v) const { h[v / 5u] = 0ull; }
+};
+
+template <typename Hist>
 __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
     const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
     const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
     uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
     uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt, int32_t* __restrict__ nsec) {
-    extern __shared__ uint32_t hist[];
+    extern __shared__ __align__(16) unsigned long long hist_words[];
+    const Hist hist{reinterpret_cast<decltype(Hist::h)>(hist_words)};
     __shared__ int s_max, s_hpos;
     __shared__ uint32_t s_hmax;
     __shared__ int s_bcnt[64], s_bstart[64];
     const uint32_t K4 = 1u << (2 * K);
-    const int hwords = (int)((K4 + 1) / 2);
     // K = 8: two sections, H (K-mer >= 0x8000) then L, grouped by the 4-byte
     // bank of a 16-bit plane word; K <= 7: one section, grouped by the bank of
     // a 32-bit word index (value mod 32)
     const int nsections = K == 8 ? 2 : 1;
-    for (int i = threadIdx.x; i < hwords; i += blockDim.x) hist[i] = 0;
+    hist.clear_all(K4);
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_hpos = 0; }
         if (threadIdx.x < 64) s_bcnt[threadIdx.x] = 0;
@@ -142,9 +177,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
             rank[k] = -1;
             if (p < T) {
                 const uint32_t v = kmer_at(s, p, K);
-                const uint32_t sh = (v & 1u) * 16u;
-                const uint32_t old = atomicAdd(&hist[v >> 1], 1u << sh);
-                const uint32_t t = (old >> sh) & 0xFFFFu;
+                const uint32_t t = hist.add(v);
                 val[k] = t * K4 + v;
                 if ((int)t >= dense_levels) {
                     dst[ent_at(atomicAdd(&s_hpos, 1), lane)] = val[k];
@@ -190,7 +223,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
             const int p = threadIdx.x + k * kPrepThreads;
             if (p < T) {
                 const uint32_t v = val[k] & (K4 - 1u);
-                const int c = (int)((hist[v >> 1] >> ((v & 1u) * 16u)) & 0xFFFFu);
+                const int c = (int)hist.get(v);
                 mx = max(mx, c);
                 if (v >= 0x8000u) hm = max(hm, v);
             }
@@ -203,7 +236,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
             nhigh[r] = s_hpos;
             uint32_t info = 0;
             if (K == 8 && s_hmax >= 0x8000u) {
-                const uint32_t c = (hist[s_hmax >> 1] >> ((s_hmax & 1u) * 16u)) & 0xFFFFu;
+                const uint32_t c = hist.get(s_hmax);
                 info = (s_hmax << 16) | c;
             }
             hinfo[r] = info;
@@ -211,7 +244,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kPrepPer; ++k)
-            if (threadIdx.x + k * kPrepThreads < T) hist[(val[k] & (K4 - 1u)) >> 1] = 0;
+            if (threadIdx.x + k * kPrepThreads < T) hist.clear(val[k] & (K4 - 1u));
         __syncthreads();
     }
 }
@@ -1955,13 +1988,16 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     if (k == 8) CRISPY_TRY(kmer_order(ctx));
     const int64_t* loff = k == 8 ? j.offp.as<int64_t>() : j.off.as<int64_t>();
     CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 4) * 4, s));
-    const size_t hsmem = (size_t)(((1u << (2 * k)) + 1) / 2) * 4;
-    CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)hsmem));
-    const int grid = std::min(n, ctx->sm_count * (k >= 8 ? 1 : 8));
+    const uint32_t K4 = 1u << (2 * k);
+    auto prep = k == 8 ? kmer_prep_kernel<PrepHist12> : kmer_prep_kernel<PrepHist16>;
+    const size_t hsmem = k == 8 ? PrepHist12::bytes(K4) : PrepHist16::bytes(K4);
+    CRISPY_CK(ctx, cudaFuncSetAttribute(prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep, kPrepThreads, hsmem);
+    const int grid = std::min(n, ctx->sm_count * std::max(1, std::min(per_sm, 8)));
     int32_t* cntmax = j.cntmax.as<int32_t>();
     int32_t* nhigh = cntmax + n;
-    kmer_prep_kernel<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), loff,
+    prep<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), loff,
                                               j.t.as<int32_t>(), n, k, dense_levels_for(k),
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
