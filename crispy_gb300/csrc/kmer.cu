@@ -97,10 +97,10 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // bank of its 16-bit plane word.
 __device__ __forceinline__ int prep_bucket(uint32_t val, int K) {
     if (K == 8) {
-        // H: bank of a 32-bit plane word (K-mer - 0x8000); L: 4-byte bank
-        // of a 16-bit plane word
+        // the bank of the K-mer's 32-bit plane word (H: K-mer - 0x8000,
+        // L: K-mer), per section
         const uint32_t v = val & 0xFFFFu;
-        return v >= 0x8000u ? (int)(v & 31u) : 32 + (int)((v >> 1) & 31u);
+        return (v >= 0x8000u ? 0 : 32) + (int)(v & 31u);
     }
     return (int)(val & 31u);
 }
@@ -485,9 +485,8 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
 
 // K = 8: an H stream and an L stream per group; the H section of a read's
 // raw list follows its high-level entries, the L section follows the H
-// section.  Each stream indexes its own plane whose guard words start at
-// 32768: H: K-mer - 0x8000, 32-bit words (bank = word mod 32); L: K-mer,
-// 16-bit words (bank = word / 2 mod 32).
+// section.  Each stream indexes a plane of 32-bit words (bank = word mod
+// 32) whose guard words start at 32768: H: K-mer - 0x8000, L: K-mer.
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
     const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
@@ -507,7 +506,7 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
                          0x8000u, 32768u, 1u, tent + tstart[g]);
         __syncwarp();
         sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + nH, tgentL[g],
-                         ent + gstart[g], 0u, 32768u, 2u, tent + tstart[g] + (int64_t)32 * EtH);
+                         ent + gstart[g], 0u, 32768u, 1u, tent + tstart[g] + (int64_t)32 * EtH);
         __syncwarp();
     }
 }
@@ -549,8 +548,8 @@ struct TileArgs {
     // an order, pairs are kept whose lower read ID lies in [olo, ohi)
     const int32_t* perm;
     int olo, ohi;
-    // K = 8 batched split: per item the 64-read column groups [x, y) of the
-    // 16-row kernel, which then keeps only pairs with [same]; the per-read
+    // K = 8 batched split: per item the 32-read column groups [x, y) of the
+    // two-phase kernel, which then keeps only pairs with [same]; the per-read
     // H / L entry counts (H-only kernel)
     const int2* item_q;
     int same_only;
@@ -1159,27 +1158,35 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
 }
 
 // ---------------------------------------------------------------------------
-// K = 8 tile kernel.  The reference's merge for K = 8 gives
+// K = 8.  The reference's merge for K = 8 gives
 //     m = minsum(H) + [same] * minsum(L)
 // (H = K-mers >= 0x8000, L = the rest; kmerMain.cpp:275-278 against
-// kmerKernel.cu:37-45), so the two halves are counted apart.  A block owns 16
-// row reads; first occurrences live in two planes (H: K-mer - 0x8000, 32-bit
-// words of which the low 16 bits are used, so that the H stream's schedule
-// by 32-bit banks serves both K = 8 kernels; L: K-mer, 16-bit words; 32,768
-// words each plus guard words, 192 KB together) and repeated occurrences in
-// a shared hash.  Each lane owns two column
-// reads, one of each of two adjacent 32-read groups, and gathers one 16-bit
-// word per read and step into the low / high half of a 32-bit counter
-// input: 16 rows x 2 columns per LOP3.  An H phase over the groups' H
-// streams and an L phase over their L streams give the two bit-sliced sums;
-// m is formed bit-sliced with the [same] mask per (row, column).
+// kmerKernel.cu:37-45), so the two halves are counted apart.  [same] holds
+// when the two reads' H keys (largest H K-mer and its count, or none) agree.
+// Both K = 8 tile kernels own 32 row reads per block and hold one plane of
+// 32-bit words in shared memory: the word of a K-mer (H: K-mer - 0x8000, L:
+// K-mer; 32,768 words plus 32 guard words, 128 KB) has the bit of each row
+// read with a first occurrence of it; repeated occurrences sit in a shared
+// hash.  A lane owns one column read and gathers one word per step of the
+// column group's scheduled stream (H and L streams, both by 32-bit bank):
+// one LOP3 of the carry-save tree counts 32 rows.
+//   * kmer_tile8h_kernel (batched form): the pairs whose H keys differ, with
+//     the reads in H-key order all pairs outside the key groups: H only.
+//   * kmer_tile8_kernel: H and then L with the plane refilled in between,
+//     the H sums of up to kGroups8 column groups per warp kept in registers;
+//     the batched form runs it over each row group's same-key column range,
+//     the staged form over every pair of a stage.
 // ---------------------------------------------------------------------------
-constexpr int kRows8 = 16;
-constexpr int kTile8Threads = 1024;
-constexpr int kTile8Warps = kTile8Threads / 32;
-constexpr int kPlane8 = 32768 + 64;    // 16-bit L plane words: K-mers + guard words
-constexpr int kPlaneH = 32768 + 32;    // 32-bit H plane words: K-mers + guard words
-constexpr size_t kSmem8 = (size_t)kPlaneH * 4 + (size_t)kPlane8 * 2;
+constexpr int kRows8 = 32;
+constexpr int kPlaneH = 32768 + 32;    // 32-bit plane words: K-mers + guard words
+constexpr size_t kSmem8 = (size_t)kPlaneH * 4;
+constexpr int kTile8HThreads = 1024;   // 32 warps: the stream loads' latency is hidden by warps
+constexpr int kTile8HWarps = kTile8HThreads / 32;
+// two-phase kernel: 32 warps while two groups' H sums fit 64 registers
+// (counts of 9 bits and below), else 16 warps
+template <int B>
+constexpr int tile8_threads() { return B <= 9 ? 1024 : 512; }
+constexpr int kGroups8 = 2;            // column groups per warp and round (two-phase kernel)
 
 __device__ __noinline__ uint32_t hash_find8(const uint32_t* hkeys, const uint32_t* hmask,
                                             uint32_t key) {
@@ -1192,239 +1199,6 @@ __device__ __noinline__ uint32_t hash_find8(const uint32_t* hkeys, const uint32_
     }
     return 0u;
 }
-
-// 16 scheduled entries of each of two streams (columns in the low and high
-// half); an exhausted stream reads guard word 32768 (zero).  W: the plane's
-// word type (only the low 16 bits are set).
-template <int B, typename W>
-__device__ __forceinline__ uint32_t gather8_16(const W* __restrict__ plane, uint4 qa0, uint4 qa1,
-                                               uint4 qb0, uint4 qb1, Counter<B>& cnt) {
-    const uint32_t xa[8] = {qa0.x, qa0.y, qa0.z, qa0.w, qa1.x, qa1.y, qa1.z, qa1.w};
-    const uint32_t xb[8] = {qb0.x, qb0.y, qb0.z, qb0.w, qb1.x, qb1.y, qb1.z, qb1.w};
-    uint32_t w[16];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        w[2 * k] = (uint32_t)plane[xa[k] & 0xFFFFu] | ((uint32_t)plane[xb[k] & 0xFFFFu] << 16);
-        w[2 * k + 1] = (uint32_t)plane[xa[k] >> 16] | ((uint32_t)plane[xb[k] >> 16] << 16);
-    }
-    return cnt.add16(w);
-}
-
-template <int B, typename W>
-__device__ __forceinline__ void phase8(const W* __restrict__ plane, const uint4* epa, int ea,
-                                       const uint4* epb, int eb, uint32_t* X) {
-    const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
-    Counter<B> cnt;
-    cnt.clear();
-    const int E = max(ea, eb);
-    // the next batch's entries are in flight while the current one is reduced
-    uint4 a0 = 0 < ea ? __ldg(epa) : guard, a1 = 0 < ea ? __ldg(epa + 32) : guard;
-    uint4 b0 = 0 < eb ? __ldg(epb) : guard, b1 = 0 < eb ? __ldg(epb + 32) : guard;
-    for (int e = 0; e < E; e += 16) {
-        const int o = ((e + 16) >> 3) * 32;
-        const uint4 na0 = e + 16 < ea ? __ldg(epa + o) : guard, na1 = e + 16 < ea ? __ldg(epa + o + 32) : guard;
-        const uint4 nb0 = e + 16 < eb ? __ldg(epb + o) : guard, nb1 = e + 16 < eb ? __ldg(epb + o + 32) : guard;
-        cnt.add_sixteens1(gather8_16<B, W>(plane, a0, a1, b0, b1, cnt));
-        a0 = na0; a1 = na1; b0 = nb0; b1 = nb1;
-    }
-    cnt.planes(X);
-}
-
-template <int B>
-__global__ void __launch_bounds__(kTile8Threads, 1) kmer_tile8_kernel(TileArgs a) {
-    extern __shared__ __align__(16) uint32_t PH[];   // H plane (32-bit words), then L plane (16-bit)
-    __shared__ uint32_t hkeys[kHashSlots];
-    __shared__ uint32_t hmask[kHashSlots];
-    __shared__ int s_rowT[kRows8];
-    __shared__ uint32_t s_rowH[kRows8];
-    __shared__ int s_item[4];
-    __shared__ int s_tmin, s_any_high;
-    __shared__ uint32_t s_rows_ok;
-    const bool queued = a.items != nullptr;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned full = 0xffffffffu;
-    for (int it = 0;; ++it) {
-        if (threadIdx.x == 0) {
-            if (queued) {
-                const unsigned w = atomicAdd(a.queue_head, 1u);
-                s_item[3] = (int)w < a.nitems;
-                if (s_item[3]) {
-                    s_item[0] = a.items[w];
-                    s_item[1] = a.item_q ? a.item_q[w].x : 0;
-                    s_item[2] = a.item_q ? a.item_q[w].y : (a.n + 63) / 64;
-                }
-            } else {
-                s_item[0] = a.r_lo / kRows8 + blockIdx.x;
-                s_item[1] = a.c_lo / 64;
-                s_item[2] = (a.c_hi + 63) / 64;
-                s_item[3] = it == 0;
-            }
-        }
-        __syncthreads();
-        if (!s_item[3]) break;
-        const int rg = s_item[0], q0 = s_item[1], q1 = s_item[2];
-        __syncthreads();
-        const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
-        const int r0 = rg * kRows8;
-        if (warp == 0) {
-            const int r = r0 + lane;
-            const bool ok = lane < kRows8 && r >= rlo && r < rhi && !a.dense_group[r >> 5];
-            const int tr = ok ? a.tcount[r] : INT_MAX;
-            if (lane < kRows8) { s_rowT[lane] = tr; s_rowH[lane] = ok ? a.hinfo[r] : 0u; }
-            const unsigned okm = __ballot_sync(full, ok);
-            const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
-            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; }
-        }
-        uint4* P4 = reinterpret_cast<uint4*>(PH);
-        for (int i = threadIdx.x; i < (int)(kSmem8 / 16); i += kTile8Threads) P4[i] = make_uint4(0, 0, 0, 0);
-        for (int i = threadIdx.x; i < kHashSlots; i += kTile8Threads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
-        __syncthreads();
-        uint32_t* PL32 = PH + kPlaneH;
-        for (int b = warp; b < kRows8; b += kTile8Warps) {
-            if (!((s_rows_ok >> b) & 1u)) continue;
-            const int r = r0 + b;
-            const uint32_t* src = a.ent + a.gstart[r >> 5];
-            const int T = s_rowT[b];
-            for (int e = lane; e < T; e += 32) {
-                const uint32_t idx = src[ent_at(e, r & 31)];
-                if (idx < 65536u) {
-                    // first occurrence: its plane word
-                    if (idx >= 0x8000u) atomicOr(&PH[idx - 0x8000u], 1u << b);
-                    else atomicOr(&PL32[idx >> 1], (1u << b) << ((idx & 1u) * 16u));
-                } else {
-                    uint32_t h = hash_slot(idx);
-                    for (int probe = 0; probe < kHashSlots; ++probe) {
-                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
-                        if (old == kSentinel || old == idx) {
-                            atomicOr(&hmask[h], 1u << b);
-                            break;
-                        }
-                        h = (h + 1) & (kHashSlots - 1);
-                    }
-                    s_any_high = 1;
-                }
-            }
-        }
-        __syncthreads();
-        const bool any_high = s_any_high != 0;
-        const uint32_t rows_ok = s_rows_ok;
-        for (int q = max(q0, r0 / 64) + warp; q < q1; q += kTile8Warps) {
-            const int gA = 2 * q, gB = 2 * q + 1;
-            const bool hasB = gB < a.ngroups;
-            const int cA = 64 * q + lane, cB = cA + 32;
-            const bool okA = cA >= a.c_lo && cA < a.c_hi && cA < a.n;
-            const bool okB = cB >= a.c_lo && cB < a.c_hi && cB < a.n;
-            const uint32_t vA = okA ? (half_mask(cA - r0) & rows_ok & 0xFFFFu) : 0u;
-            const uint32_t vB = okB ? (half_mask(cB - r0) & rows_ok & 0xFFFFu) : 0u;
-            const uint32_t vmask = vA | (vB << 16);
-            if (!__any_sync(full, vmask)) continue;
-            const uint4* epAH = reinterpret_cast<const uint4*>(a.tent + a.tstart[gA]) + lane;
-            const uint4* epAL = reinterpret_cast<const uint4*>(a.tent + a.tstart[gA] + 32LL * a.tgent[gA]) + lane;
-            const uint4* epBH = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB]) + lane : epAH;
-            const uint4* epBL = hasB ? reinterpret_cast<const uint4*>(a.tent + a.tstart[gB] + 32LL * a.tgent[gB]) + lane : epAL;
-            // [same] per (row, column): the L sums count only where it holds
-            const uint32_t hA = okA ? a.hinfo[cA] : 0u, hB = okB ? a.hinfo[cB] : 0u;
-            uint32_t same = 0;
-#pragma unroll
-            for (int b = 0; b < kRows8; ++b) {
-                const uint32_t hr = s_rowH[b];
-                same |= (uint32_t)((hr == 0u && hA == 0u) || (hr != 0u && hr == hA)) << b;
-                same |= (uint32_t)((hr == 0u && hB == 0u) || (hr != 0u && hr == hB)) << (b + 16);
-            }
-            // same_only: the H-only kernel has taken the pairs without [same]
-            const uint32_t keep = a.same_only ? same : 0xffffffffu;
-            if (a.same_only && !__any_sync(full, same & vmask)) continue;
-            uint32_t XH[B], XL[B];
-            phase8<B, uint32_t>(PH, epAH, a.tgent[gA], epBH, hasB ? a.tgent[gB] : 0, XH);
-            // a warp none of whose pairs has [same] skips the L phase (reads
-            // ordered by their H key make most warps like that)
-            if (__any_sync(full, same & vmask)) {
-                phase8<B, uint16_t>(reinterpret_cast<const uint16_t*>(PH + kPlaneH), epAL, a.tgentL[gA], epBL,
-                                    hasB ? a.tgentL[gB] : 0, XL);
-            } else {
-#pragma unroll
-                for (int k = 0; k < B; ++k) XL[k] = 0u;
-            }
-            if (any_high) {
-                // repeated occurrences (rank >= 1) lead each read's level list
-                const int nhA = okA ? a.nhigh[cA] : 0, nhB = okB ? a.nhigh[cB] : 0;
-                const int maxh = (int)__reduce_max_sync(full, (unsigned)max(nhA, nhB));
-                const uint32_t* rpA = a.ent + a.gstart[gA];
-                const uint32_t* rpB = hasB ? a.ent + a.gstart[gB] : rpA;
-                for (int j = 0; j < maxh; ++j) {
-                    uint32_t hH = 0, hL = 0;
-                    if (j < nhA) {
-                        const uint32_t key = __ldg(rpA + ent_at(j, lane));
-                        const uint32_t w = hash_find8(hkeys, hmask, key);
-                        if ((key & 0xFFFFu) >= 0x8000u) hH |= w; else hL |= w;
-                    }
-                    if (j < nhB) {
-                        const uint32_t key = __ldg(rpB + ent_at(j, lane));
-                        const uint32_t w = hash_find8(hkeys, hmask, key) << 16;
-                        if ((key & 0xFFFFu) >= 0x8000u) hH |= w; else hL |= w;
-                    }
-                    Counter<B>::add_at(XH, hH, 0);
-                    Counter<B>::add_at(XL, hL, 0);
-                }
-            }
-            // X = XH + (XL & same), bit-sliced
-            uint32_t X[B];
-            uint32_t carry = 0;
-#pragma unroll
-            for (int k = 0; k < B; ++k) {
-                const uint32_t y = XL[k] & same;
-                X[k] = XH[k] ^ y ^ carry;
-                carry = (XH[k] & y) | (carry & (XH[k] ^ y));
-            }
-            // threshold: per half a lower bound of mmin, then exact per candidate
-            const int tcA = okA ? a.tcount[cA] : 0, tcB = okB ? a.tcount[cB] : 0;
-            const uint32_t loA = a.smin[min(s_tmin, tcA)], loB = a.smin[min(s_tmin, tcB)];
-            uint32_t cand = 0;
-            if (vmask && (loA < (1u << B) || loB < (1u << B))) {
-                const uint32_t okbits = (loA < (1u << B) ? 0xFFFFu : 0u) | (loB < (1u << B) ? 0xFFFF0000u : 0u);
-                uint32_t gt = 0, eq = 0xffffffffu;
-#pragma unroll
-                for (int k = B - 1; k >= 0; --k) {
-                    const uint32_t bit = (((loA >> k) & 1u) ? 0xFFFFu : 0u) | (((loB >> k) & 1u) ? 0xFFFF0000u : 0u);
-                    gt |= eq & X[k] & ~bit;
-                    eq &= ~(X[k] ^ bit);
-                }
-                cand = (gt | eq) & vmask & okbits & keep;
-            }
-            while (__any_sync(full, cand)) {
-                bool pass = false;
-                int r = 0, c = 0, m = 0, mn = 1;
-                if (cand) {
-                    const int bit = __ffs(cand) - 1;
-                    cand &= cand - 1;
-#pragma unroll
-                    for (int k = 0; k < B; ++k) m |= (int)((X[k] >> bit) & 1u) << k;
-                    r = r0 + (bit & 15);
-                    c = bit < 16 ? cA : cB;
-                    mn = min(s_rowT[bit & 15], bit < 16 ? tcA : tcB);
-                    pass = m >= (int)a.mmin[mn];
-                }
-                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// ---------------------------------------------------------------------------
-// K = 8 H-only tile kernel (batched form).  With the reads in their H-key
-// order, a pair has [same] only inside one key group, so m = minsum(H) for
-// every pair outside the groups.  This kernel takes exactly those pairs; the
-// 16-row kernel above takes each row block's same-key column range.  A
-// block owns 32 row reads: first H occurrences live in one plane of 32-bit
-// words (32,768 plus 32 guard words, 128 KB), repeated H occurrences in the
-// shared hash.  A lane owns one column read and gathers one 32-bit word per
-// step: 32 rows per LOP3 and one shared load per step.
-// ---------------------------------------------------------------------------
-constexpr int kRows8H = 32;
-constexpr size_t kSmem8H = (size_t)kPlaneH * 4;
-constexpr int kTile8HThreads = 1024;   // 32 warps: the stream loads' latency is hidden by warps
-constexpr int kTile8HWarps = kTile8HThreads / 32;
 
 // 16 scheduled entries of one stream: their plane words into the counter;
 // returns the weight-16 carry.
@@ -1441,7 +1215,7 @@ __device__ __forceinline__ uint32_t gather8h_c16(const uint32_t* __restrict__ pl
     return cnt.add16(w);
 }
 
-// A column's H stream (E steps, a multiple of 16) against the plane: two
+// A column's stream (E steps, a multiple of 16) against the plane: two
 // 16-entry batches per carry chain, the next pair's first batch in flight.
 // E is the column group's step count, the same for every lane, so the
 // second batch's branch does not diverge.
@@ -1465,15 +1239,156 @@ __device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, cons
     cnt.planes(X);
 }
 
+// Per-block row state of both K = 8 kernels.
+struct Rows8 {
+    int rowT[kRows8];            // tuple counts (INT_MAX for rows not taken)
+    uint32_t keyv[kRows8];       // the rows' distinct H keys ...
+    uint32_t keym[kRows8];       // ... and the rows holding each
+    int nkeys, tmin, rep;
+    uint32_t rows_ok;
+};
+
+// Warp 0: the row group's rows in [rlo, rhi), their tuple counts and keys.
+__device__ __forceinline__ void rows8_setup(const TileArgs& a, Rows8& rs, int rg, int rlo, int rhi) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int r = rg * kRows8 + lane;
+    const bool ok = r >= rlo && r < rhi && r < a.n && !a.dense_group[rg];
+    const int tr = ok ? a.tcount[r] : INT_MAX;
+    const uint32_t hr = ok ? a.hinfo[r] : 0u;
+    rs.rowT[lane] = tr;
+    const unsigned okm = __ballot_sync(full, ok);
+    const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
+    const unsigned rowsk = __match_any_sync(full, hr) & okm;
+    const bool leader = ok && lane == __ffs(rowsk) - 1;
+    const unsigned lm = __ballot_sync(full, leader);
+    if (leader) {
+        const int k = __popc(lm & ((1u << lane) - 1u));
+        rs.keyv[k] = hr;
+        rs.keym[k] = rowsk;
+    }
+    if (lane == 0) { rs.tmin = tm; rs.rows_ok = okm; rs.nkeys = __popc(lm); }
+}
+
+// The rows with the same H key as column key hc ([same] per row).
+__device__ __forceinline__ uint32_t same8(const Rows8& rs, int nkeys, uint32_t hc) {
+    uint32_t same = 0;
+    for (int k = 0; k < nkeys; ++k) same |= rs.keyv[k] == hc ? rs.keym[k] : 0u;
+    return same;
+}
+
+// All threads: zero the plane and the hash, then put the first occurrences
+// of the rows' kH-section K-mers into the plane and their repeated ones into
+// the hash (rs.rep set when there are any).  A read's level list holds its
+// repeated entries first, then the H section, then the L section.  Ends
+// with a barrier.
+template <bool kH>
+__device__ void fill8(const TileArgs& a, Rows8& rs, int rg, uint32_t* plane, uint32_t* hkeys,
+                      uint32_t* hmask, int threads) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = threads >> 5;
+    __syncthreads();   // the previous users of the plane and the hash are done
+    uint4* P4 = reinterpret_cast<uint4*>(plane);
+    for (int i = threadIdx.x; i < (int)(kSmem8 / 16); i += threads) P4[i] = make_uint4(0, 0, 0, 0);
+    for (int i = threadIdx.x; i < kHashSlots; i += threads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
+    if (threadIdx.x == 0) rs.rep = 0;
+    __syncthreads();
+    const uint32_t* src = a.ent + a.gstart[rg];
+    for (int b = warp; b < kRows8; b += warps) {
+        if (!((rs.rows_ok >> b) & 1u)) continue;
+        const int r = rg * kRows8 + b;
+        const int nh = a.nhigh[r], nH = a.nsec[2 * (int64_t)r];
+        // H: the repeated entries and the H section; L: the repeated entries
+        // and the L section (positions past the H section)
+        const int e_end = kH ? nh + nH : rs.rowT[b] - nH;
+        for (int i = lane; i < e_end; i += 32) {
+            const int e = kH || i < nh ? i : i + nH;
+            const uint32_t idx = src[ent_at(e, b)];
+            const bool hk = (idx & 0xFFFFu) >= 0x8000u;
+            if (hk != kH) continue;
+            if (idx < 65536u) {
+                atomicOr(&plane[kH ? idx - 0x8000u : idx], 1u << b);
+            } else {
+                uint32_t h = hash_slot(idx);
+                for (int probe = 0; probe < kHashSlots; ++probe) {
+                    const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
+                    if (old == kSentinel || old == idx) {
+                        atomicOr(&hmask[h], 1u << b);
+                        break;
+                    }
+                    h = (h + 1) & (kHashSlots - 1);
+                }
+                rs.rep = 1;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// One column's kH-section sums against the rows: the scheduled stream, then
+// its repeated entries looked up in the hash.  Whole warps call it.
+template <int B, bool kH>
+__device__ __forceinline__ void column8(const TileArgs& a, const uint32_t* plane, const uint32_t* hkeys,
+                                        const uint32_t* hmask, bool any_rep, int q, int c, bool okc,
+                                        uint32_t* X) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint16_t* st = a.tent + a.tstart[q] + (kH ? 0 : 32LL * a.tgent[q]);
+    phase8h<B>(plane, reinterpret_cast<const uint4*>(st) + lane, kH ? a.tgent[q] : a.tgentL[q], X);
+    if (any_rep) {
+        const int nh = okc ? a.nhigh[c] : 0;
+        const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
+        const uint32_t* rp = a.ent + a.gstart[q];
+        for (int j = 0; j < maxh; ++j) {
+            uint32_t w = 0;
+            if (j < nh) {
+                const uint32_t key = __ldg(rp + ent_at(j, lane));
+                if (((key & 0xFFFFu) >= 0x8000u) == kH) w = hash_find8(hkeys, hmask, key);
+            }
+            Counter<B>::add_at(X, w, 0);
+        }
+    }
+}
+
+// Threshold and emission of one column's 32 row pairs (vmask: the pairs to
+// consider): a lower bound of mmin first, then exact per candidate.
+template <int B>
+__device__ __forceinline__ void emit8(const TileArgs& a, const Rows8& rs, const uint32_t* X, uint32_t vmask,
+                                      int r0, int c, int tc) {
+    const uint32_t lo = a.smin[min(rs.tmin, tc)];
+    uint32_t cand = 0;
+    if (vmask && lo < (1u << B)) {
+        uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+        for (int k = B - 1; k >= 0; --k) {
+            const uint32_t bit = ((lo >> k) & 1u) ? 0xffffffffu : 0u;
+            gt |= eq & X[k] & ~bit;
+            eq &= ~(X[k] ^ bit);
+        }
+        cand = (gt | eq) & vmask;
+    }
+    while (__any_sync(0xffffffffu, cand)) {
+        bool pass = false;
+        int r = 0, m = 0, mn = 1;
+        if (cand) {
+            const int bit = __ffs(cand) - 1;
+            cand &= cand - 1;
+#pragma unroll
+            for (int k = 0; k < B; ++k) m |= (int)((X[k] >> bit) & 1u) << k;
+            r = r0 + bit;
+            mn = min(rs.rowT[bit], tc);
+            pass = m >= (int)a.mmin[mn];
+        }
+        emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
+    }
+}
+
 template <int B>
 __global__ void __launch_bounds__(kTile8HThreads, 1) kmer_tile8h_kernel(TileArgs a) {
-    extern __shared__ __align__(16) uint32_t PH[];
+    extern __shared__ __align__(16) uint32_t plane[];
     __shared__ uint32_t hkeys[kHashSlots];
     __shared__ uint32_t hmask[kHashSlots];
-    __shared__ int s_rowT[kRows8H];
-    __shared__ uint32_t s_keyv[kRows8H], s_keym[kRows8H];
-    __shared__ int s_item, s_tmin, s_any_high, s_nkeys;
-    __shared__ uint32_t s_rows_ok;
+    __shared__ Rows8 rs;
+    __shared__ int s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned full = 0xffffffffu;
     for (;;) {
@@ -1484,109 +1399,113 @@ __global__ void __launch_bounds__(kTile8HThreads, 1) kmer_tile8h_kernel(TileArgs
         __syncthreads();
         const int rg = s_item;
         if (rg < 0) break;
-        const int r0 = rg * kRows8H;
-        if (warp == 0) {
-            const int r = r0 + lane;
-            const bool ok = r < a.n && !a.dense_group[rg];
-            const int tr = ok ? a.tcount[r] : INT_MAX;
-            const uint32_t hr = ok ? a.hinfo[r] : 0u;
-            s_rowT[lane] = tr;
-            const unsigned okm = __ballot_sync(full, ok);
-            const int tm = (int)__reduce_min_sync(full, (unsigned)tr);
-            // the rows' distinct H keys, each with its row mask
-            const unsigned rowsk = __match_any_sync(full, hr) & okm;
-            const bool leader = ok && lane == __ffs(rowsk) - 1;
-            const unsigned lm = __ballot_sync(full, leader);
-            if (leader) {
-                const int k = __popc(lm & ((1u << lane) - 1u));
-                s_keyv[k] = hr;
-                s_keym[k] = rowsk;
-            }
-            if (lane == 0) { s_tmin = tm; s_rows_ok = okm; s_any_high = 0; s_nkeys = __popc(lm); }
-        }
-        uint4* P4 = reinterpret_cast<uint4*>(PH);
-        for (int i = threadIdx.x; i < (int)(kSmem8H / 16); i += kTile8HThreads) P4[i] = make_uint4(0, 0, 0, 0);
-        for (int i = threadIdx.x; i < kHashSlots; i += kTile8HThreads) { hkeys[i] = kSentinel; hmask[i] = 0u; }
-        __syncthreads();
-        const uint32_t* src = a.ent + a.gstart[rg];
-        for (int b = warp; b < kRows8H; b += kTile8HWarps) {
-            if (!((s_rows_ok >> b) & 1u)) continue;
-            const int r = r0 + b;
-            // high-level entries, then the H section of the read's list
-            const int eh = a.nhigh[r] + a.nsec[2 * (int64_t)r];
-            for (int e = lane; e < eh; e += 32) {
-                const uint32_t idx = src[ent_at(e, b)];
-                if (idx < 65536u) {
-                    if (idx >= 0x8000u) atomicOr(&PH[idx - 0x8000u], 1u << b);
-                } else if ((idx & 0xFFFFu) >= 0x8000u) {
-                    uint32_t h = hash_slot(idx);
-                    for (int probe = 0; probe < kHashSlots; ++probe) {
-                        const uint32_t old = atomicCAS(&hkeys[h], kSentinel, idx);
-                        if (old == kSentinel || old == idx) {
-                            atomicOr(&hmask[h], 1u << b);
-                            break;
-                        }
-                        h = (h + 1) & (kHashSlots - 1);
-                    }
-                    s_any_high = 1;
-                }
-            }
-        }
-        __syncthreads();
-        const bool any_high = s_any_high != 0;
-        const uint32_t rows_ok = s_rows_ok;
-        const int nkeys = s_nkeys;
+        const int r0 = rg * kRows8;
+        if (warp == 0) rows8_setup(a, rs, rg, 0, a.n);
+        fill8<true>(a, rs, rg, plane, hkeys, hmask, kTile8HThreads);
+        const bool any_rep = rs.rep != 0;
+        const uint32_t rows_ok = rs.rows_ok;
+        const int nkeys = rs.nkeys;
         for (int q = rg + warp; q < a.ngroups; q += kTile8HWarps) {
             const int c = 32 * q + lane;
             const bool okc = c < a.n;
-            const uint32_t hc = okc ? a.hinfo[c] : 0u;
-            uint32_t same = 0;
-            for (int k = 0; k < nkeys; ++k) same |= s_keyv[k] == hc ? s_keym[k] : 0u;
+            const uint32_t same = same8(rs, nkeys, okc ? a.hinfo[c] : 0u);
+            // pairs with [same] belong to the two-phase kernel
             const uint32_t vmask = okc ? (half_mask(c - r0) & rows_ok & ~same) : 0u;
             if (!__any_sync(full, vmask)) continue;
             uint32_t X[B];
-            phase8h<B>(PH, reinterpret_cast<const uint4*>(a.tent + a.tstart[q]) + lane, a.tgent[q], X);
-            if (any_high) {
-                // repeated H occurrences (rank >= 1) lead the column's list
-                const int nh = okc ? a.nhigh[c] : 0;
-                const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
-                const uint32_t* rp = a.ent + a.gstart[q];
-                for (int j = 0; j < maxh; ++j) {
-                    uint32_t w = 0;
-                    if (j < nh) {
-                        const uint32_t key = __ldg(rp + ent_at(j, lane));
-                        if ((key & 0xFFFFu) >= 0x8000u) w = hash_find8(hkeys, hmask, key);
-                    }
-                    Counter<B>::add_at(X, w, 0);
+            column8<B, true>(a, plane, hkeys, hmask, any_rep, q, c, okc, X);
+            emit8<B>(a, rs, X, vmask, r0, c, okc ? a.tcount[c] : 0);
+        }
+        __syncthreads();
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileArgs a) {
+    constexpr int kTile8Threads = tile8_threads<B>();
+    constexpr int kTile8Warps = kTile8Threads / 32;
+    extern __shared__ __align__(16) uint32_t plane[];
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots];
+    __shared__ Rows8 rs;
+    __shared__ int s_item[4];
+    const bool queued = a.items != nullptr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            if (queued) {
+                const unsigned w = atomicAdd(a.queue_head, 1u);
+                s_item[3] = (int)w < a.nitems;
+                if (s_item[3]) {
+                    s_item[0] = a.items[w];
+                    s_item[1] = a.item_q ? a.item_q[w].x : 0;
+                    s_item[2] = a.item_q ? a.item_q[w].y : a.ngroups;
                 }
+            } else {
+                s_item[0] = a.r_lo / kRows8 + blockIdx.x;
+                s_item[1] = a.c_lo / 32;
+                s_item[2] = (a.c_hi + 31) / 32;
+                s_item[3] = it == 0;
             }
-            // threshold: a lower bound of mmin per column, then exact per candidate
-            const int tc = okc ? a.tcount[c] : 0;
-            const uint32_t lo = a.smin[min(s_tmin, tc)];
-            uint32_t cand = 0;
-            if (vmask && lo < (1u << B)) {
-                uint32_t gt = 0, eq = 0xffffffffu;
+        }
+        __syncthreads();
+        if (!s_item[3]) break;
+        const int rg = s_item[0], q0 = s_item[1], q1 = s_item[2];
+        const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
+        const int r0 = rg * kRows8;
+        if (warp == 0) rows8_setup(a, rs, rg, rlo, rhi);
+        __syncthreads();
+        const uint32_t rows_ok = rs.rows_ok;
+        const int nkeys = rs.nkeys;
+        // rounds of kTile8Warps x kGroups8 column groups: H sums, then the
+        // plane refilled with L, then L sums where [same] holds, and emission
+        for (int base = max(q0, rg); base < q1; base += kTile8Warps * kGroups8) {
+            fill8<true>(a, rs, rg, plane, hkeys, hmask, kTile8Threads);
+            const bool rep_h = rs.rep != 0;
+            uint32_t XH[kGroups8][B], same[kGroups8], vm[kGroups8];
+            bool any_same = false;
 #pragma unroll
-                for (int k = B - 1; k >= 0; --k) {
-                    const uint32_t bit = ((lo >> k) & 1u) ? 0xffffffffu : 0u;
-                    gt |= eq & X[k] & ~bit;
-                    eq &= ~(X[k] ^ bit);
-                }
-                cand = (gt | eq) & vmask;
+            for (int g = 0; g < kGroups8; ++g) {
+                const int q = base + warp * kGroups8 + g;
+                const int c = 32 * q + lane;
+                const bool okc = q < q1 && c >= a.c_lo && c < a.c_hi && c < a.n;
+                same[g] = same8(rs, nkeys, okc ? a.hinfo[c] : 0u);
+                // same_only: the H-only kernel has taken the pairs without [same]
+                vm[g] = okc ? (half_mask(c - r0) & rows_ok & (a.same_only ? same[g] : 0xffffffffu)) : 0u;
+#pragma unroll
+                for (int k = 0; k < B; ++k) XH[g][k] = 0u;
+                if (__any_sync(full, vm[g])) column8<B, true>(a, plane, hkeys, hmask, rep_h, q, c, okc, XH[g]);
+                any_same |= (same[g] & vm[g]) != 0u;
             }
-            while (__any_sync(full, cand)) {
-                bool pass = false;
-                int r = 0, m = 0, mn = 1;
-                if (cand) {
-                    const int bit = __ffs(cand) - 1;
-                    cand &= cand - 1;
+            // the L phase only where some pair of the block has [same]
+            const bool blk_same = __syncthreads_or(any_same) != 0;
+            bool rep_l = false;
+            if (blk_same) {
+                fill8<false>(a, rs, rg, plane, hkeys, hmask, kTile8Threads);
+                rep_l = rs.rep != 0;
+            }
 #pragma unroll
-                    for (int k = 0; k < B; ++k) m |= (int)((X[k] >> bit) & 1u) << k;
-                    r = r0 + bit;
-                    mn = min(s_rowT[bit], tc);
-                    pass = m >= (int)a.mmin[mn];
+            for (int g = 0; g < kGroups8; ++g) {
+                if (!__any_sync(full, vm[g])) continue;
+                const int q = base + warp * kGroups8 + g;
+                const int c = 32 * q + lane;
+                const bool okc = q < q1 && c >= a.c_lo && c < a.c_hi && c < a.n;
+                uint32_t XL[B];
+#pragma unroll
+                for (int k = 0; k < B; ++k) XL[k] = 0u;
+                if (blk_same && __any_sync(full, same[g] & vm[g]))
+                    column8<B, false>(a, plane, hkeys, hmask, rep_l, q, c, okc, XL);
+                // X = XH + (XL & same), bit-sliced
+                uint32_t X[B];
+                uint32_t carry = 0;
+#pragma unroll
+                for (int k = 0; k < B; ++k) {
+                    const uint32_t y = XL[k] & same[g];
+                    X[k] = XH[g][k] ^ y ^ carry;
+                    carry = (XH[g][k] & y) | (carry & (XH[g][k] ^ y));
                 }
-                emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
+                emit8<B>(a, rs, X, vm[g], r0, c, okc ? a.tcount[c] : 0);
             }
         }
         __syncthreads();
@@ -1737,11 +1656,11 @@ int bits_for(uint64_t v) {
 
 // Dense level planes kept in shared memory for K (0: dense kernel only).
 // Row reads per tile block: 128-bit plane words for K <= 6, 64-bit for
-// K = 7 (one 16,384-word level fills the budget), 16-bit for K = 8.
+// K = 7 (one 16,384-word level fills the budget), 32-bit for K = 8.
 int tile_rows_for(int K) { return K == 8 ? kRows8 : K == 7 ? kTileRows : kRows128; }
 
 int dense_levels_for(int K) {
-    if (K >= 8) return 1;   // first occurrences in the two 16-bit planes of the K = 8 kernel
+    if (K >= 8) return 1;   // first occurrences in the 32-bit plane of the K = 8 kernels
     const int per_level = (1 << (2 * K)) * (tile_rows_for(K) / 8);   // bytes of one level's words
     return std::max(1, std::min(4, kPlaneBudget / per_level));
 }
@@ -2099,17 +2018,14 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     // the dense kernel (flags per 32-read group); K = 8 sends every group there.
     const int levels = dense_levels_for(K);
     const int rows_blk = tile_rows_for(K);   // row reads per tile block
-    // the hash of a K = 8 block holds the high-level entries of up to 32 rows
-    // (H-only kernel), so K = 8 decides per 32-read group
-    const int hash_blk = K == 8 ? kRows8H : rows_blk;
-    const int nrg = (n + hash_blk - 1) / hash_blk;
+    const int nrg = (n + rows_blk - 1) / rows_blk;
     std::vector<uint8_t> dense(j.ngroups, 0);
     bool any_dense = false;
     for (int rg = 0; rg < nrg; ++rg) {
         int64_t high = 0;
-        for (int r = rg * hash_blk; r < std::min(n, rg * hash_blk + hash_blk); ++r) high += j.h_cntmax[n + r];
+        for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); ++r) high += j.h_cntmax[n + r];
         if (levels == 0 || high > kHashMaxKeys) {
-            for (int r = rg * hash_blk; r < std::min(n, rg * hash_blk + hash_blk); r += 32) dense[r >> 5] = 1;
+            for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32) dense[r >> 5] = 1;
             any_dense = true;
         }
     }
@@ -2120,17 +2036,17 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     const uint32_t K4 = 1u << (2 * K);
     const int B = std::max(8, bits_for((uint64_t)j.max_t));
     TileFn tile = K == 8 ? tile8_fn_for(B) : rows_blk == kRows128 ? tile128_fn_for(B) : tile_fn_for(B);
-    const int tile_threads = K == 8 ? kTile8Threads : kTileThreads;
-    const size_t tsmem = !fast ? 0 : K == 8 ? kSmem8     // H and L planes + guards
+    const int tile_threads = K == 8 ? (B <= 9 ? tile8_threads<9>() : tile8_threads<10>()) : kTileThreads;
+    const size_t tsmem = !fast ? 0 : K == 8 ? kSmem8     // one plane + guards
                                              : ((size_t)levels * K4 + 32) * (rows_blk / 8);   // planes + guards
     const size_t dsmem = (size_t)((K4 + 1) / 2) * 4;
     if (fast) CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
-    // K = 8 batched: the H-only kernel over all row groups plus the 16-row
-    // kernel over each row block's same-key column range (the H keys must be
+    // K = 8 batched: the H-only kernel over all row groups plus the two-phase
+    // kernel over each row group's same-key column range (the H keys must be
     // in order along the positions, as the read order makes them)
     const bool split8 = fast && K == 8 && mode == CRISPY_MODE_BATCHED && j.hkeys_ordered;
     TileFn tile_h = split8 ? tile8h_fn_for(B) : nullptr;
-    if (split8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8H));
+    if (split8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
     // K = 8 jobs hold their reads in the read order built at rebuild: the
@@ -2220,21 +2136,21 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         } else {
             // Batched: persistent launches over work queues of row groups
             // (each with all its columns), longest first.  K = 8 split: the
-            // H-only kernel over the 32-row groups, then the 16-row kernel
-            // over each 16-row block's same-key column range.
+            // H-only kernel over the 32-row groups, then the two-phase kernel
+            // over each row group's same-key column range.
             std::vector<int> items, items_s;
             std::vector<int2> q_s;
             if (split8) {
                 for (int g = 0; g < j.ngroups; ++g)
                     if (!dense[g]) items.push_back(g);
-                for (int rb = 0; rb * kRows8 < n; ++rb) {
-                    const int r0 = rb * kRows8, r1 = std::min(n, r0 + kRows8);
-                    if (dense[r0 >> 5]) continue;
+                for (int g = 0; g < j.ngroups; ++g) {
+                    const int r0 = g * kRows8, r1 = std::min(n, r0 + kRows8);
+                    if (dense[g]) continue;
                     // columns of the keys of rows r0 .. r1-1: one range, the keys being in order
-                    const int q0 = std::max(r0 / 64, j.h_run_lo[r0] / 64);
-                    const int q1 = (j.h_run_hi[r1 - 1] + 63) / 64;
+                    const int q0 = std::max(g, j.h_run_lo[r0] / 32);
+                    const int q1 = (j.h_run_hi[r1 - 1] + 31) / 32;
                     if (q1 > q0) {
-                        items_s.push_back(rb);
+                        items_s.push_back(g);
                         q_s.push_back(make_int2(q0, q1));
                     }
                 }
@@ -2260,7 +2176,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 }
                 CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 8, s));
                 const TileFn main_fn = split8 ? tile_h : tile;
-                const size_t main_smem = split8 ? kSmem8H : tsmem;
+                const size_t main_smem = split8 ? kSmem8 : tsmem;
                 TileArgs t2 = ta;
                 t2.r_lo = 0; t2.r_hi = n; t2.c_lo = 0; t2.c_hi = n;
                 t2.items = d_items; t2.nitems = (int)nh; t2.queue_head = head;

@@ -80,7 +80,8 @@ def test_kmer_short_reads_no_tuples(engine):
 def test_kmer_long_reads(engine):
     reads = _reads(150, 21, root=2100, dist="uniform", a=1500, b=2048, cents=6)
     _check(engine, reads, 6, 0.5, cg.MODE_BATCHED)
-    _check(engine, reads, 8, 0.7, cg.MODE_BATCHED)
+    # K = 8 counts of 11 bits: the two-phase kernel's 16-warp form
+    assert _check(engine, reads, 8, 0.7, cg.MODE_BATCHED) == _check(engine, reads, 8, 0.7, cg.MODE_STAGED)
 
 
 def test_kmer_uneven_lengths(engine):
