@@ -105,3 +105,33 @@ def test_failed_job_is_isolated():
         assert e.value.code in (cg.E_UNSUPPORTED, cg.E_INPUT)
         assert srv.wait(ok) == cg.JOB_DONE
         assert srv.result(ok)[0] > 0
+
+
+def test_mixed_k_jobs(engine):
+    # k = 8 jobs hold their reads in their own read order on their slot's
+    # context; served alone, mixed with k = 6 jobs, and through the Engine,
+    # they give the same chunks
+    def job8(n, seed):
+        reads = synth.make_read_set(synth.ReadSetSpec(n, max(4, n // 50), 260, "normal", 250, 30, 8, seed))
+        return synth.pack_reads(reads)
+    jobs = [(_job(1500, 901), 6, 10), (job8(2500, 902), 8, 5), (_job(900, 903), 6, 10),
+            (job8(1200, 904), 8, 5), (job8(4000, 905), 8, 10)]
+    alone = []
+    with cg.Server(0, 0, 1) as srv:
+        for (buf, offs, lens), k, band in jobs:
+            jid = srv.submit(buf, offs, lens, k=k, band=band)
+            assert srv.wait(jid) == cg.JOB_DONE
+            alone.append(srv.result(jid))
+    with cg.Server(0, 0, 3) as srv:
+        ids = [srv.submit(buf, offs, lens, k=k, band=band) for (buf, offs, lens), k, band in jobs]
+        for jid, want in zip(ids, alone):
+            assert srv.wait(jid) == cg.JOB_DONE
+            _same(srv.result(jid), want)
+    (buf, offs, lens), k, band = jobs[1]
+    n = len(lens)
+    engine.kmer_prepare(buf, offs, lens, k)
+    kp = engine.kmer_run(cg.default_threshold(n, -1.0, 0), cg.MODE_BATCHED, False)
+    engine.gen_prepare_from_kmer()
+    chunks = engine.gen_run_from_kmer(band, cg.default_threshold(n, -1.0, 1), cg.MODE_BATCHED)
+    _same((kp, chunks), alone[1])
+    assert kp > 0 and sum(len(c[2]) for c in chunks) > 0
