@@ -155,3 +155,14 @@ def test_kmer_k8_key_groups(engine, kind):
     counts = [_check(engine, reads, 8, thr, mode) for thr in (0.75, 0.3)
               for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
     assert counts[0] == counts[1] == counts[2] > 0
+
+
+@pytest.mark.parametrize("n", [10, 37, 99, 150])
+def test_kmer_k8_small_sets(engine, n):
+    # stage tiles (arrayDim 4 and 32) narrower than the K = 8 kernels' 32-row
+    # blocks, partial row and column groups, every form
+    reads = _reads(n + n // 10 + 5, 300 + n, k=8)[:n]
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    counts = [_check(engine, reads, 8, thr, mode) for thr in (t, 0.75)
+              for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
+    assert counts[0] == counts[1] == counts[2] and counts[3] == counts[4] == counts[5]
