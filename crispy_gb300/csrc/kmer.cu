@@ -2044,7 +2044,11 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     // K = 8 batched: the H-only kernel over all row groups plus the two-phase
     // kernel over each row group's same-key column range (the H keys must be
     // in order along the positions, as the read order makes them)
-    const bool split8 = fast && K == 8 && mode == CRISPY_MODE_BATCHED && j.hkeys_ordered;
+    // (CRISPY_KMER_K8_SPLIT=0 selects the one-kernel form, the same
+    // survivors: the two-phase kernel over every column)
+    const char* split_env = std::getenv("CRISPY_KMER_K8_SPLIT");
+    const bool split8 = fast && K == 8 && mode == CRISPY_MODE_BATCHED && j.hkeys_ordered &&
+                        !(split_env && std::strcmp(split_env, "0") == 0);
     TileFn tile_h = split8 ? tile8h_fn_for(B) : nullptr;
     if (split8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));

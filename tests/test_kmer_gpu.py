@@ -166,3 +166,14 @@ def test_kmer_k8_small_sets(engine, n):
     counts = [_check(engine, reads, 8, thr, mode) for thr in (t, 0.75)
               for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
     assert counts[0] == counts[1] == counts[2] and counts[3] == counts[4] == counts[5]
+
+
+def test_kmer_k8_one_kernel_form(engine, monkeypatch):
+    # the batched K = 8 form without the split (the two-phase kernel over
+    # every column, as when the H keys are not in order) gives the same
+    # survivors as the split form and the oracle
+    reads = _reads(700, 812, root=520, dist="uniform", a=200, b=480, cents=25, k=8)
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    split = _check(engine, reads, 8, t, cg.MODE_BATCHED)
+    monkeypatch.setenv("CRISPY_KMER_K8_SPLIT", "0")
+    assert _check(engine, reads, 8, t, cg.MODE_BATCHED) == split
