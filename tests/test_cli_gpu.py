@@ -157,3 +157,11 @@ def test_crispydist_reads_parsed_differently(tmp_path):
     src = str(tmp_path / "src_Clean")
     open(src, "w").write("".join(lines))
     _fused_vs_two(tmp_path, src, 6, 10, "batched")
+
+
+@pytest.mark.parametrize("mode", ["batched", "staged"])
+def test_crispydist_k8_matches_two_programs(tmp_path, mode):
+    # k = 8: kmerDist's read order stays inside the process; genDist takes the
+    # survivors by read ID, as from the .kpair file
+    src = os.path.join(GOLD, "syn600", "syn600_Clean")
+    _fused_vs_two(tmp_path, src, 8, 5, mode)
