@@ -75,6 +75,10 @@ def test_kmer_heavy_multiplicity(engine):
 def test_kmer_short_reads_no_tuples(engine):
     reads = synth.preprocess_order([b"ACGTA", b"ACGTC", b"GGGGGG", b"ACGTACGTAA"] + _reads(40, 11))
     _check(engine, reads, 6, 1.0, cg.MODE_BATCHED)
+    # K = 8: reads of 7 (no tuple, H key "none") and 8 (one tuple) nt
+    reads8 = synth.preprocess_order([b"ACGTACG", b"CCCCCCC", b"TTTTTTTT", b"ACGTACGTA"] + _reads(40, 12, k=8))
+    for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN):
+        _check(engine, reads8, 8, 1.0, mode)
 
 
 def test_kmer_long_reads(engine):
