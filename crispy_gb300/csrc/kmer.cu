@@ -533,7 +533,8 @@ struct TileArgs {
     int64_t cap;
     // plain: one rectangle of rows x cols (one reference stage)
     int r_lo, r_hi, c_lo, c_hi;
-    // batched: work queue over 64-row groups (all their columns)
+    // batched: work queue over row groups (all their columns, or the
+    // column range of item_q)
     const int* items;
     int nitems;
     unsigned int* queue_head;
@@ -2014,8 +2015,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     CRISPY_CK(ctx, cudaMemcpyAsync(j.mmin.ptr, mmin.data(), mmin.size() * 2, cudaMemcpyHostToDevice, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(j.smin.ptr, smin.data(), smin.size() * 2, cudaMemcpyHostToDevice, s));
 
-    // Rows of 64-row groups whose high-level entries exceed the hash go to
-    // the dense kernel (flags per 32-read group); K = 8 sends every group there.
+    // Rows of tile row groups whose high-level entries exceed the hash go to
+    // the dense kernel (flags per 32-read group).
     const int levels = dense_levels_for(K);
     const int rows_blk = tile_rows_for(K);   // row reads per tile block
     const int nrg = (n + rows_blk - 1) / rows_blk;
