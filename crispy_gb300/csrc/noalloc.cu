@@ -16,12 +16,13 @@
 // caller.  Each call clears the part that must start at zero (the
 // error word) before its kernel runs.
 //
-// The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress, with that device current; make that first call
-// before any stream capture.
+// Every call looks up the array's device address with cudaGetSymbolAddress,
+// with the caller's device current (the lookup allocates nothing).  The
+// address is not cached: after a cudaDeviceReset, or under a context other
+// than the device's primary one, a cached address could point outside the
+// current context.  The call is synchronous (it waits for its kernel to
+// report bad inputs), so it cannot run inside a stream capture.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "internal.h"
 
@@ -49,12 +50,24 @@ struct Best {
     unsigned l;
 };
 
+// Error bits in the error word: 1 = a pair index outside [0, n), 2 = a band
+// wider than the rows the host sized, 4 = a read longer than max_len.  A
+// rejected pair gets dist NaN and score / ml / al -1.
+__device__ __forceinline__ void reject(int* err_word, int bit, int64_t p, float* dist, int32_t* score,
+                                       int32_t* ml, int32_t* al) {
+    atomicOr(err_word, bit);
+    dist[p] = __int_as_float(0x7fc00000);
+    if (score) score[p] = -1;
+    if (ml) ml[p] = -1;
+    if (al) al[p] = -1;
+}
+
 // The wide-band recurrence of gen.cu (rows over read2 = pair[1], columns over
 // read1 = pair[0], band coordinates x = j - i + kb + 1), reading the ASCII
 // reads directly so that no packed copy has to be allocated.
 __global__ void __launch_bounds__(32) noalloc_wide_kernel(
     int* scratch, int row_stride, const char* __restrict__ seq, const int64_t* __restrict__ off,
-    const int32_t* __restrict__ len, int n, const int2* __restrict__ pairs, int64_t npairs,
+    const int32_t* __restrict__ len, int n, int max_len, const int2* __restrict__ pairs, int64_t npairs,
     int band, float* __restrict__ dist, int32_t* __restrict__ score, int32_t* __restrict__ ml,
     int32_t* __restrict__ al) {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,15 +77,17 @@ __global__ void __launch_bounds__(32) noalloc_wide_kernel(
     for (int64_t p = tid; p < npairs; p += nthreads) {
         const int2 pr = pairs[p];
         if (pr.x < 0 || pr.x >= n || pr.y < 0 || pr.y >= n) {
-            atomicOr(&scratch[kErrorWord], 1);
-            dist[p] = __int_as_float(0x7fc00000);
+            reject(&scratch[kErrorWord], 1, p, dist, score, ml, al);
             continue;
         }
         const int l1 = len[pr.x], l2 = len[pr.y];
+        if (l1 > max_len || l2 > max_len || l1 < 0 || l2 < 0) {
+            reject(&scratch[kErrorWord], 4, p, dist, score, ml, al);
+            continue;
+        }
         const int kb = band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
-        if (2 * kb + 3 > rs) {   // wider than the host's bound: the inputs lied
-            atomicOr(&scratch[kErrorWord], 2);
-            dist[p] = __int_as_float(0x7fc00000);
+        if (2 * kb + 3 > rs) {   // cannot happen once the lengths are checked; kept as a guard
+            reject(&scratch[kErrorWord], 2, p, dist, score, ml, al);
             continue;
         }
         const int width = 2 * kb + 3;
@@ -122,9 +137,6 @@ __global__ void __launch_bounds__(32) noalloc_wide_kernel(
     }
 }
 
-std::mutex g_mu;
-int* g_addr[64] = {};   // device address of g_noalloc_scratch per device
-
 }  // namespace
 
 extern "C" int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offsets,
@@ -146,23 +158,12 @@ extern "C" int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offs
         return crispy::fail(nullptr, CRISPY_E_UNSUPPORTED,
                             "gen_align_noalloc: band half-width %d needs more than the %zu-byte scratch",
                             kb_max, kScratchBytes);
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 64)
-        return crispy::fail(nullptr, CRISPY_E_DEVICE, "gen_align_noalloc: no current device");
-    int* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> g(g_mu);
-        if (!g_addr[dev]) {
-            void* ptr = nullptr;
-            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess)
-                return crispy::fail(nullptr, CRISPY_E_DEVICE, "cudaGetSymbolAddress: %s",
-                                    cudaGetErrorString(e));
-            g_addr[dev] = static_cast<int*>(ptr);
-        }
-        scratch = g_addr[dev];
-    }
+    // the array's address in the current context, looked up on every call
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return crispy::fail(nullptr, CRISPY_E_DEVICE, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    int* scratch = static_cast<int*>(ptr);
     if (npairs == 0) return CRISPY_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if ((e = cudaMemsetAsync(scratch + kErrorWord, 0, sizeof(int), s)) != cudaSuccess)
@@ -171,7 +172,7 @@ extern "C" int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offs
     // `fit`, so every thread's rows lie inside the array, below the error word
     const int64_t threads = std::min<int64_t>(fit, ((npairs + 31) / 32) * 32);
     noalloc_wide_kernel<<<(unsigned)(threads / 32), 32, 0, s>>>(
-        scratch, rs, d_seq, d_offsets, d_lengths, n, reinterpret_cast<const int2*>(d_pairs), npairs,
+        scratch, rs, d_seq, d_offsets, d_lengths, n, max_len, reinterpret_cast<const int2*>(d_pairs), npairs,
         band, d_dist, d_score, d_ml, d_al);
     if ((e = cudaGetLastError()) != cudaSuccess)
         return crispy::fail(nullptr, CRISPY_E_DEVICE, "gen_align_noalloc launch: %s", cudaGetErrorString(e));
@@ -181,6 +182,7 @@ extern "C" int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offs
         return crispy::fail(nullptr, CRISPY_E_DEVICE, "gen_align_noalloc: %s", cudaGetErrorString(e));
     if (flag)
         return crispy::fail(nullptr, CRISPY_E_INPUT,
-                            "gen_align_noalloc: a pair index is outside [0, n) or a read is longer than max_len");
+                            "gen_align_noalloc: %s", (flag & 1) ? "a pair index is outside [0, n)"
+                                                     : "a read is longer than max_len");
     return CRISPY_OK;
 }

@@ -184,12 +184,14 @@ int crispy_gen_align(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs,
  * NULL).  The DP rows live in a fixed 8 MiB array inside the library that
  * every GPU loading it holds until exit; nothing is allocated.  All calls
  * share that array: calls that overlap on the GPU race and must be
- * serialised by the caller.  The first call on a device resolves the
- * array's address (with that device current); make it before any stream
- * capture.  Returns CRISPY_E_UNSUPPORTED when max_len exceeds 2048 or the
- * band needs more scratch than the array holds, CRISPY_E_INPUT when a pair
- * index is outside [0, n) or a read is longer than max_len (the call waits
- * for its kernel to report this). */
+ * serialised by the caller.  Every call looks up the array's address in
+ * the current device's context (a lookup, not an allocation).  The call is
+ * synchronous: it waits for its kernel, which reports bad inputs, so it
+ * cannot be made inside a stream capture.  Returns CRISPY_E_UNSUPPORTED
+ * when max_len exceeds 2048 or the band needs more scratch than the array
+ * holds, CRISPY_E_INPUT when a pair index is outside [0, n) or a read of a
+ * pair is longer than max_len; such a pair gets dist NaN and score, ml and
+ * al -1, and every other pair its result. */
 int crispy_gen_align_noalloc(const char* d_seq, const int64_t* d_offsets,
                              const int32_t* d_lengths, int n, int max_len,
                              const int32_t* d_pairs, int64_t npairs, int band,

@@ -60,3 +60,26 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("port", "reference")
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm runs oracle/ code only: after a run, the process has
+    not mapped libcrispy_gb300.so, and its config equals the GPU arm's."""
+    code = (
+        "import sys, json, argparse; sys.path.insert(0, %r); import bench\n"
+        "a = argparse.Namespace(workload='small_1k', cpu_sample_reads=200, warmup=0, steps=1)\n"
+        "line = bench.run_reference(a, None, 1, 0)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'loaded': 'libcrispy_gb300' in maps, 'config': line['config']}))\n" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["loaded"] is False
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    n = d["config"]["n_reads"]
+    want = bench._config("small_1k", n, 6, 10, oracle.default_threshold(n, -1.0, 0),
+                         oracle.default_threshold(n, -1.0, 1), 1)
+    assert d["config"] == want
