@@ -178,7 +178,7 @@ def _cpu_sample(reads, k, band, m, workdir):
     cores = os.cpu_count() or 1
     n = len(sub)
     # the full workload's thresholds (the subset keeps its read lengths)
-    tk = oracle.default_threshold(len(reads), -1.0, 0)
+    tk = oracle.default_threshold(len(reads), -1.0, 2)
     tg = oracle.default_threshold(len(reads), -1.0, 1)
     t0 = time.perf_counter()
     subprocess.run([oracle.CLI_PATH, "kmer", "-i", fa, "-k", str(k), "-t", repr(tk), "-n", str(cores)],
@@ -700,7 +700,7 @@ def run_reference(args, dist, ws, rank):
     _, k, band = WORKLOADS[args.workload]
     n = len(reads)
     m = min(args.cpu_sample_reads, n)
-    thr_k = oracle.default_threshold(n, -1.0, 0)
+    thr_k = oracle.default_threshold(n, -1.0, 2)
     thr_g = oracle.default_threshold(n, -1.0, 1)
     rates = []
     with tempfile.TemporaryDirectory() as td:

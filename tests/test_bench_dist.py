@@ -80,6 +80,6 @@ def test_reference_arm_loads_no_product_library():
     import bench
     import oracle
     n = d["config"]["n_reads"]
-    want = bench._config("small_1k", n, 6, 10, oracle.default_threshold(n, -1.0, 0),
+    want = bench._config("small_1k", n, 6, 10, oracle.default_threshold(n, -1.0, 2),
                          oracle.default_threshold(n, -1.0, 1), 1)
     assert d["config"] == want

@@ -68,7 +68,7 @@ def test_full_config_vs_oracle(engine, workload, modes):
     k, band = 6, 10
     thr_k = cg.default_threshold(n, -1.0, 0)
     thr_g = cg.default_threshold(n, -1.0, 1)
-    assert thr_k == oracle.default_threshold(n, -1.0, 0)
+    assert thr_k == oracle.default_threshold(n, -1.0, 2)
     assert thr_g == oracle.default_threshold(n, -1.0, 1)
     want_p, want_d = oracle.kmer_all(buf, offs, lens, k, thr_k)
     assert len(want_p) > 0
