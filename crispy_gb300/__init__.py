@@ -119,6 +119,7 @@ PROTOTYPES = {
     "crispy_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "crispy_set_timing": (C.c_int, [_P, C.c_int]),
     "crispy_probe_int32": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "crispy_probe_lds128": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "crispy_tune_report": (C.c_int, [C.c_char_p, C.c_size_t]),
     "crispy_ctx_set_mem_cap": (C.c_int, [_P, C.c_size_t]),
     "crispy_ctx_mem_in_use": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
@@ -330,6 +331,12 @@ class Engine:
         g = C.c_double()
         self._check(self.lib.crispy_probe_int32(self.h, C.byref(g)))
         return g.value
+
+    def probe_lds128_wavefronts(self) -> float:
+        """Conflict-free 128-bit shared-load throughput, L1 wavefronts/s."""
+        w = C.c_double()
+        self._check(self.lib.crispy_probe_lds128(self.h, C.byref(w)))
+        return w.value
 
     def kmer_run(self, thr: float, mode: int = MODE_BATCHED, dists: bool = True) -> int:
         n = C.c_int64()

@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
-CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "serve.cu", "noalloc.cu", "pre.cu"]
+CU_SOURCES = ["ctx.cu", "sort.cu", "kmer.cu", "gen.cu", "gen16.cu", "serve.cu", "noalloc.cu", "pre.cu"]
 CXX_SOURCES = ["fasta.cpp", "pre_io.cpp", "clust.cpp"]
 CLI = {"kmerDist": "cli_kmer.cpp", "genDist": "cli_gen.cpp", "crispyDist": "cli_pipe.cpp",
        "preprocess": "cli_pre.cpp", "crispyRun": "cli_run.cpp", "aveclust": "cli_clust.cpp",

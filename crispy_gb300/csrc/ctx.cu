@@ -36,6 +36,31 @@ __global__ void __launch_bounds__(256) int32_probe_kernel(uint32_t seed, uint32_
     for (int c = 0; c < 8; ++c) acc ^= x[c] ^ y[c];
     if (acc == 0x9e3779b9u) *sink = acc;   // keeps the chains live
 }
+
+// Shared-memory gather probe: every warp issues conflict-free 128-bit shared
+// loads (a quarter-warp reads 128 contiguous bytes: one L1 wavefront), eight
+// independent chains per thread whose next index depends on the loaded
+// value, so nothing is hoisted.  One warp-wide load = 4 wavefronts.
+constexpr int kLdsIters = 2048;
+constexpr int kLdsWords = 1024;   // uint4 words: 16 KB
+__global__ void __launch_bounds__(256) lds128_probe_kernel(uint32_t seed, uint32_t* sink) {
+    __shared__ uint4 buf[kLdsWords];
+    for (int i = threadIdx.x; i < kLdsWords; i += blockDim.x) buf[i] = make_uint4(0, 0, 0, 0);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    uint32_t idx[8], acc = seed;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) idx[c] = (uint32_t)(c * 128 + (threadIdx.x >> 5) * 32);
+    for (int i = 0; i < kLdsIters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const uint4 v = buf[(idx[c] + lane) & (kLdsWords - 1)];
+            idx[c] += v.x + 32u;   // v.x is 0: the next 32 words
+            acc ^= v.y ^ v.z ^ v.w;
+        }
+    }
+    if (acc == 0x9e3779b9u) *sink = acc;   // keeps the loads live
+}
 }  // namespace
 
 namespace crispy {
@@ -334,6 +359,39 @@ int crispy_probe_int32(crispy_ctx* ctx, double* gops) {
     if (e != cudaSuccess) return cuda_fail(ctx, e, "int32 probe", __FILE__, __LINE__);
     const double ops = (double)blocks * 256 * kProbeIters * 16;
     *gops = ops / (best * 1e-3) / 1e9;
+    return CRISPY_OK;
+}
+
+int crispy_probe_lds128(crispy_ctx* ctx, double* wavefronts_per_s) {
+    if (!ctx || !wavefronts_per_s) return CRISPY_E_INPUT;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    uint32_t* sink = nullptr;
+    CRISPY_CK(ctx, cudaMalloc(&sink, 4));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lds128_probe_kernel, 256, 0);
+    const int blocks = ctx->sm_count * per_sm * 4;
+    lds128_probe_kernel<<<blocks, 256, 0, s>>>(1u, sink);   // warm-up
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a, s);
+        lds128_probe_kernel<<<blocks, 256, 0, s>>>(2u + rep, sink);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaError_t e = cudaGetLastError();
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "lds128 probe", __FILE__, __LINE__);
+    const double warp_loads = (double)blocks * (256 / 32) * kLdsIters * 8;
+    *wavefronts_per_s = warp_loads * 4 / (best * 1e-3);
     return CRISPY_OK;
 }
 

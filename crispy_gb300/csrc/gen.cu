@@ -38,6 +38,7 @@
 #include <string>
 #include <tuple>
 
+#include "gen_args.h"
 #include "internal.h"
 
 namespace crispy {
@@ -49,25 +50,6 @@ constexpr int kGO = -10, kGE = -1, kMatch = 5, kMismatch = -4;  // genMain.h:32-
 constexpr int kGenThreads = 256;
 constexpr int kGenWarps = kGenThreads / 32;
 constexpr int kSmWords = 132;           // 128 words of 16 symbols + refill padding
-
-struct GenArgs {
-    const uint32_t* packed;
-    const int64_t* woff;
-    const int32_t* len;
-    const int2* pairs;
-    const uint32_t* order;   // optional permutation (length buckets)
-    int64_t count;
-    int band;
-    float* dist;
-    int32_t* score;
-    int32_t* ml;
-    int32_t* al;
-    unsigned int* queue;     // optional work counter (persistent launch)
-    // All 1.  Adds written as multiply-adds by these run on the FMA pipe;
-    // distinct multipliers keep the compiler from factoring a common
-    // product back into ALU adds.
-    int one[6];
-};
 
 __device__ __forceinline__ int kband_of(int l1, int l2, int band) {
     return band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
@@ -578,12 +560,16 @@ constexpr int kBinSlots[] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256
 constexpr int kNumBins = sizeof(kBinSlots) / sizeof(kBinSlots[0]);
 __constant__ int c_bin_slots[kNumBins] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256};
 
-// Per-pair classification for the launch plan, on the device: band-slot
-// bin (wide last), a sort key (bin, then longer pairs first), band cells,
-// the widest band, per-bin counts and the widest bin of each load window.
-// stats: [0] cells, [1] max kBand, [2 + b] pairs of order-bin b (1..13),
-// [16 + w] widest order-bin of window w.
-constexpr int kStatBins = 2, kStatWindows = 16;
+// Per-pair classification for the launch plan, on the device.  Order-bin
+// ob: band-slot bin b (1..12) for a pair the 16-bit kernel takes (L1 + L2
+// <= kGen16MaxSum), kNumBins + b for a longer pair (32-bit kernels), and
+// 2 * kNumBins for the wide-band kernel (last).  Sort key: order-bin, then
+// longer pairs first.  stats: [0] cells, [1] max kBand, [kStatBins + ob]
+// pairs of order-bin ob, [kStatWindows + 2w] widest band-slot bin of load
+// window w (kNumBins = wide), [kStatWindows + 2w + 1] 1 when the window
+// holds a pair beyond the 16-bit range.
+constexpr int kStatBins = 2, kStatWindows = 32;
+constexpr int kWideOrderBin = 2 * kNumBins;
 __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t count,
                                     const int32_t* __restrict__ len, int band, int nbins,
                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
@@ -592,7 +578,7 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
     const int lane = threadIdx.x & 31;
     const bool ok = p < count;
     unsigned long long cells = 0;
-    int kb = 0, ob = -1;
+    int kb = 0, ob = -1, wb = -1, lng = 0;
     if (ok) {
         const int2 pr = pairs[p];
         const int l1 = len[pr.x], l2 = len[pr.y];
@@ -600,7 +586,9 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
         int bin = 0;
         for (int b = 1; b < nbins; ++b)
             if (c_bin_slots[b] >= kb + 1) { bin = b; break; }
-        ob = bin == 0 ? nbins : bin;   // wide pairs sort last
+        lng = l1 + l2 > kGen16MaxSum ? 1 : 0;
+        wb = bin == 0 ? nbins : bin;
+        ob = bin == 0 ? 2 * nbins : bin + lng * nbins;   // wide pairs sort last
         if (keys) {
             keys[p] = ((uint32_t)ob << 13) | (uint32_t)(8191 - (l1 + l2));
             vals[p] = (uint32_t)p;
@@ -619,13 +607,16 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
     if (ok && lane == __ffs(same_bin) - 1) atomicAdd(&stats[kStatBins + ob], (unsigned long long)__popc(same_bin));
     const int64_t win = ok ? p / CRISPY_GEN_WINDOW : -1;
     const unsigned same_win = __match_any_sync(0xffffffffu, (unsigned long long)win);
-    const int obw = __reduce_max_sync(same_win, ob);   // max over the lanes of this window
-    if (ok && lane == __ffs(same_win) - 1)
-        atomicMax(&stats[kStatWindows + win], (unsigned long long)obw);
+    const int wbw = __reduce_max_sync(same_win, wb);   // max over the lanes of this window
+    const int lw = __reduce_max_sync(same_win, lng);
+    if (ok && lane == __ffs(same_win) - 1) {
+        atomicMax(&stats[kStatWindows + 2 * win], (unsigned long long)wbw);
+        if (lw) atomicMax(&stats[kStatWindows + 2 * win + 1], 1ull);
+    }
 }
-// untuned shape per bin (the plain form always uses it)
+// untuned 32-bit shape per bin (the plain form always uses it)
 constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 14, 5, 15, 6, 16, 7, 11, 12, 13};
-static_assert(kStatBins + kNumBins < kStatWindows, "per-bin counters overlap the window slots");
+static_assert(kStatBins + kWideOrderBin < kStatWindows, "per-bin counters overlap the window slots");
 
 using WarpFn = void (*)(GenArgs);
 WarpFn shape_fn(int shape) {
@@ -658,7 +649,7 @@ WarpFn shape_fn(int shape) {
 // same bits, so tuning only picks speed.
 // ---------------------------------------------------------------------------
 struct TuneKey {
-    int band, bin, len_bucket, sms;   // len_bucket reserved (0)
+    int band, bin, len_bucket, sms;   // bin = order-bin (above kNumBins: pairs beyond the 16-bit range)
     bool operator<(const TuneKey& o) const {
         return std::tie(band, bin, len_bucket, sms) < std::tie(o.band, o.bin, o.len_bucket, o.sms);
     }
@@ -676,7 +667,37 @@ bool autotune_enabled() {
     return !(e && e[0] == '0');
 }
 
+// Shape indices: 0..kNumShapes-1 the 32-bit kernel (kShapes), kNumShapes + i
+// the 16-bit kernel's shape i (gen16.cu).
+int num_shapes_all() { return kNumShapes + gen16_num_shapes(); }
+bool is16(int shape) { return shape >= kNumShapes; }
+int shape_slots(int shape) {
+    if (is16(shape)) {
+        const Shape16 h = gen16_shape(shape - kNumShapes);
+        return 2 * h.g * h.r;
+    }
+    return kShapes[shape].g * kShapes[shape].c;
+}
+// untuned 16-bit shape per bin (index into gen16's shapes), -1 = none
+constexpr int kDefault16[kNumBins] = {-1, 0, 1, 2, 4, 5, 7, 8, 9, 10, 11, 12, 13};
+int default_shape(int order_bin) {
+    if (order_bin >= 1 && order_bin < kNumBins && kDefault16[order_bin] >= 0)
+        return kNumShapes + kDefault16[order_bin];
+    return kDefaultShape[order_bin > kNumBins ? order_bin - kNumBins : order_bin];
+}
+
+// CRISPY_GEN_SHAPE=<index> makes the batched form run every bin the shape
+// covers in that shape (tests reach each shape this way); unset or out of
+// range: the autotuned shape.
+int forced_shape() {
+    const char* e = std::getenv("CRISPY_GEN_SHAPE");
+    if (!e || !*e) return -1;
+    const int v = std::atoi(e);
+    return v >= 0 && v < num_shapes_all() ? v : -1;
+}
+
 int launch_shape(crispy_ctx* ctx, cudaStream_t s, int shape, GenArgs a, bool timed) {
+    if (is16(shape)) return gen16_launch(ctx, s, shape - kNumShapes, a, timed);
     WarpFn fn = shape_fn(shape);
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGenThreads, 0);
@@ -698,7 +719,7 @@ __global__ void gather_stride_kernel(const uint32_t* __restrict__ src, int64_t n
 
 int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs& a,
                const uint32_t* d_order, int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf) {
-    const int dflt = kDefaultShape[bin];
+    const int dflt = default_shape(bin);
     if (!autotune_enabled() || n_items < 4096) return dflt;
     const TuneKey key{band, bin, 0, ctx->sm_count};
     {
@@ -718,11 +739,12 @@ int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs
     cudaEventCreate(&e1);
     int best = dflt;
     float best_ms = 1e30f, dflt_ms = 0;
-    const int need = kBinSlots[bin];
+    const int need = kBinSlots[bin < kNumBins ? bin : bin - kNumBins];
     int qslot = 0;
-    for (int sh = 0; sh < kNumShapes; ++sh) {
-        const int slots = kShapes[sh].g * kShapes[sh].c;
+    for (int sh = 0; sh < num_shapes_all(); ++sh) {
+        const int slots = shape_slots(sh);
         if (slots < need || slots > 2 * need) continue;
+        if (is16(sh) && bin >= kNumBins) continue;   // pairs beyond the 16-bit range
         float ms = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
             GenArgs t = a;
@@ -764,9 +786,9 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     GenJob& g = ctx->gen;
     if (count <= 0) return CRISPY_OK;
     const int64_t nwin = (count + CRISPY_GEN_WINDOW - 1) / CRISPY_GEN_WINDOW;
-    const int nstats = kStatWindows + (int)nwin;
+    const int nstats = kStatWindows + 2 * (int)nwin;
     const bool sorted = mode == CRISPY_MODE_BATCHED;
-    CRISPY_TRY(ensure(ctx, g.cstats, (size_t)(nstats + kNumBins) * 8));
+    CRISPY_TRY(ensure(ctx, g.cstats, (size_t)nstats * 8));
     if (sorted) {
         CRISPY_TRY(ensure(ctx, g.ckeys, (size_t)count * 4));
         CRISPY_TRY(ensure(ctx, g.ckeys_alt, (size_t)count * 4));
@@ -784,7 +806,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         if (sorted) {
             uint32_t* sk = nullptr;
             CRISPY_TRY(sort_u32_payload(ctx, s, g.ckeys.as<uint32_t>(), g.ckeys_alt.as<uint32_t>(),
-                                        g.cvals.as<uint32_t>(), g.cvals_alt.as<uint32_t>(), count, 17, &sk,
+                                        g.cvals.as<uint32_t>(), g.cvals_alt.as<uint32_t>(), count, 18, &sk,
                                         &d_order, g.scan));
         }
         CRISPY_CK(ctx, cudaGetLastError());
@@ -797,7 +819,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
             (uint64_t)(uintptr_t)g.ckeys_alt.ptr, (uint64_t)(uintptr_t)g.cvals.ptr,
             (uint64_t)(uintptr_t)g.cvals_alt.ptr, (uint64_t)(uintptr_t)g.scan.ptr});
         CRISPY_TRY(graph_run(ctx, s, key, classify));
-        // where the 3-pass (17-bit) sort leaves the payload: the alternate
+        // where the 3-pass (18-bit) sort leaves the payload: the alternate
         // buffer, or the input when there is nothing to sort
         d_order = count > 1 ? g.cvals_alt.as<uint32_t>() : g.cvals.as<uint32_t>();
     } else {
@@ -844,11 +866,12 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
             a.score = d_score ? d_score + w0 : nullptr;
             a.ml = d_ml ? d_ml + w0 : nullptr;
             a.al = d_al ? d_al + w0 : nullptr;
-            const int ob = (int)st[kStatWindows + w];   // widest order-bin (kNumBins = wide)
-            if (mode == CRISPY_MODE_PLAIN || ob >= kNumBins) {
+            const int wb = (int)st[kStatWindows + 2 * w];   // widest band-slot bin (kNumBins = wide)
+            const bool lng = st[kStatWindows + 2 * w + 1] != 0;
+            if (mode == CRISPY_MODE_PLAIN || wb >= kNumBins) {
                 CRISPY_TRY(launch_wide(a, nullptr, n_items));
             } else {
-                CRISPY_TRY(launch_shape(ctx, s, kDefaultShape[ob], a, true));
+                CRISPY_TRY(launch_shape(ctx, s, default_shape(lng ? wb + kNumBins : wb), a, true));
                 ctx->stats.gen_launches++;
             }
         }
@@ -857,21 +880,25 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     }
     // BATCHED: bins in ascending width, wide last
     int64_t at = 0;
-    for (int ob = 1; ob <= kNumBins; ++ob) {
+    for (int ob = 1; ob <= kWideOrderBin; ++ob) {
         const int64_t n_items = (int64_t)st[kStatBins + ob];
         if (n_items == 0) continue;
         const uint32_t* ord = d_order + at;
         at += n_items;
-        if (ob == kNumBins) {
+        if (ob == kWideOrderBin) {
             CRISPY_TRY(launch_wide(base, ord, n_items));
             continue;
         }
         GenArgs a = base;
         a.order = ord;
         a.count = n_items;
-        const int shape = pick_shape(ctx, s, band, ob, a, ord, n_items, g.tune_sample, g.tune_queue);
+        int shape = pick_shape(ctx, s, band, ob, a, ord, n_items, g.tune_sample, g.tune_queue);
+        const int forced = forced_shape();
+        if (forced >= 0 && shape_slots(forced) >= kBinSlots[ob < kNumBins ? ob : ob - kNumBins] &&
+            !(is16(forced) && ob >= kNumBins))
+            shape = forced;
         CRISPY_TRY(ensure(ctx, g.queue, 64 * 4));
-        a.queue = g.queue.as<unsigned int>() + ob;
+        a.queue = g.queue.as<unsigned int>() + ob;   // one counter per order-bin (< 64)
         CRISPY_CK(ctx, cudaMemsetAsync(a.queue, 0, 4, s));
         CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
         ctx->stats.gen_launches++;
@@ -1294,15 +1321,23 @@ int crispy_tune_report(char* buf, size_t len) {
         std::lock_guard<std::mutex> g(g_tune_mu);
         bool first = true;
         for (auto& kv : g_tuned) {
-            char item[256];
-            const Shape sh = kShapes[kv.second.shape];
+            char item[320];
+            const int shp = kv.second.shape;
+            int lanes, slots_lane, per_block;
+            if (is16(shp)) {
+                const Shape16 h = gen16_shape(shp - kNumShapes);
+                lanes = h.g; slots_lane = 2 * h.r; per_block = gen16_pairs_per_block(shp - kNumShapes);
+            } else {
+                lanes = kShapes[shp].g; slots_lane = kShapes[shp].c; per_block = kGenWarps * (32 / lanes);
+            }
+            const int b = kv.first.bin;
             snprintf(item, sizeof item,
                      "%s{\"stage\": \"gen\", \"band\": %d, \"band_slots\": %d, \"len_bucket\": %d, "
-                     "\"sms\": %d, \"lanes_per_pair\": %d, \"slots_per_lane\": %d, "
+                     "\"sms\": %d, \"kernel\": \"%s\", \"lanes_per_pair\": %d, \"slots_per_lane\": %d, "
                      "\"pairs_per_block\": %d, \"sample\": %lld, \"ms\": %.4f, \"default_ms\": %.4f}",
-                     first ? "" : ", ", kv.first.band, kBinSlots[kv.first.bin], kv.first.len_bucket,
-                     kv.first.sms, sh.g, sh.c, kGenWarps * (32 / sh.g), (long long)kv.second.sample,
-                     kv.second.ms_best, kv.second.ms_default);
+                     first ? "" : ", ", kv.first.band, kBinSlots[b < kNumBins ? b : b - kNumBins],
+                     b < kNumBins ? 0 : 1, kv.first.sms, is16(shp) ? "gen16_kernel" : "gen_warp_kernel", lanes,
+                     slots_lane, per_block, (long long)kv.second.sample, kv.second.ms_best, kv.second.ms_default);
             out += item;
             first = false;
         }

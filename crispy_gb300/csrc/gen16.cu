@@ -1,0 +1,475 @@
+// gen16.cu -- genDist's banded Needleman-Wunsch with two cells per 32-bit
+// register: the DP the batched and staged runs take for every pair with
+// L1 + L2 <= kGen16MaxSum (3600) that fits a register band.
+//
+// Reference semantics are those of gen.cu (genCPU.cpp:290-466 restated by
+// genKernel.cu:372-780): rows i over read2 = pair[1], columns j over read1 =
+// pair[0], band |i - j| <= kBand = (L1 + L2) / (2 * band), boundary cells
+// M = 0, up / left candidates penalised by the neighbour's own choice
+// (GO = -10 after a diagonal, GE = -1 after the same gap, 0 after the other
+// gap; genMain.h:32-35), ties diag > up > left, the last maximum of the last
+// row and of the last column, (float)ML / (float)AL.
+//
+// Keys.  A cell on anti-diagonal s = i + j holds K = 4*M + t + 4*s + kBase,
+// t its choice's tag: 3 diagonal, 1 up, 0 left.  A cell's three candidates
+// carry distinct tags, so one unsigned three-way maximum of their keys gives
+// the maximum and the reference's tie order at once: one __vimax3_u16x2 per
+// two cells.  The winner's tag bits b0 = t & 1, b1 = t >> 1 give the two
+// gap candidates it sends to the next anti-diagonal, already keyed:
+//   up:    K + 5 (1 - b0) - 38 b1   = 4 (M + pen_up)   + 1 + 4 (s+1) + kBase
+//   left:  K + 3 b0 - 42 b1         = 4 (M + pen_left) + 0 + 4 (s+1) + kBase
+// (pen_up = -10 / -1 / 0 and pen_left = -10 / 0 / -1 after a diagonal / up /
+// left choice), and the diagonal candidate two steps later is
+// (K | 3) + 28 - 36 * mismatch.  Every cell the recurrence reaches has
+// -4 min(i,j) <= M <= 5 min(i,j) (the diagonal candidate has no state and a
+// gap never gains), so 4M + 4s lies in [-4s, 14s]: with kBase = 4 * 3632 +
+// 128 every key of a pair with L1 + L2 <= 3600 -- and of the up to 32 steps
+// a sweep runs past a pair's end -- lies in [128, 65507].  Cells outside the
+// band, before the matrix or of a finished pair hold the key 8, below every
+// candidate of an in-band cell.  No 16-bit half ever wraps, so plain 32-bit
+// adds and multiply-adds act on both halves at once.
+//
+// Path counters.  AL = (i + j) - A and ML = (i + j) - 2A + (B - 4096), with
+// A = diagonal moves and B = 4096 + mismatches - (i0 + j0), (i0, j0) the
+// boundary cell the path leaves (A = 0, B = 4096 - s there): a diagonal move
+// adds 1 to A and the mismatch to B, a gap adds nothing.  Both are kept
+// doubled (bit 0 clear) in 16-bit halves, so the masks b0 * 0xFFFF and
+// 2 b1 * 0x7FFF (one multiply each) select the winner's counters with two
+// bitwise muxes per array.
+//
+// Layout.  G lanes per pair, R registers per lane: register r of lane l
+// holds slot l*R + r in its low half and slot G*R + l*R + r in its high
+// half.  Slot q hosts diagonal 2q - kBand + P at step parity P; its up /
+// left neighbours are slots q + 1 / q - 1 of the previous step, i.e.
+// registers r + 1 / r - 1 of the same lane, so only the lane's edge
+// register crosses lanes (one shuffle per step for keys, A and B).
+// Symbols: 2 bits each, first symbol in the low bits, in shared memory; per
+// block of 16 steps each slot's 8 mismatch flags per parity come from two
+// 16-symbol windows.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
+
+#include "gen_args.h"
+#include "internal.h"
+
+namespace crispy {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int kSmWords = 132;        // 128 words of 16 symbols + refill padding
+constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
+constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
+constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
+constexpr uint32_t kLo = 0x00010001u;   // 1 in each half
+constexpr uint32_t kOut = 8u;           // key of a cell outside the band / matrix
+constexpr uint32_t kOut2 = kOut * kLo;
+constexpr int kMisOff = 4096;           // offset of the B counter
+constexpr int kRefNegInf = -1000000;    // genCPU.cpp:350 initial last-row/column maximum
+static_assert(18 * (kGen16MaxSum + kSlack) + 131 < 65536, "16-bit keys would wrap");
+static_assert(kBase % 4 == 0, "the score is read back as (K - 4s - kBase) / 4");
+
+constexpr int kClean = 0, kTrack = 1, kFull = 2;
+
+__device__ __forceinline__ int kband16(int l1, int l2, int band) {
+    return band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
+}
+
+// Runtime multipliers (all derived from GenArgs::one, whose values the
+// compiler cannot see): products by them stay multiply-adds on the FMA pipe
+// instead of turning into shift / add sequences on the ALU.
+struct Mul {
+    uint32_t one, two, n36, m5, n19, m3, n21, mffff, m7fff, neg1;
+};
+
+__device__ __forceinline__ Mul make_mul(const int* o) {
+    Mul m;
+    m.one = (uint32_t)o[0];
+    m.two = 2u * (uint32_t)o[1];
+    m.n36 = (uint32_t)(-36) * (uint32_t)o[2];
+    m.m5 = 5u * (uint32_t)o[3];
+    m.n19 = (uint32_t)(-19) * (uint32_t)o[4];
+    m.m3 = 3u * (uint32_t)o[5];
+    m.n21 = (uint32_t)(-21) * (uint32_t)o[0];
+    m.mffff = 0xFFFFu * (uint32_t)o[1];
+    m.m7fff = 0x7FFFu * (uint32_t)o[2];
+    m.neg1 = (uint32_t)(-1) * (uint32_t)o[3];
+    return m;
+}
+
+template <int R>
+struct St {
+    uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
+    uint32_t U[R], F[R]; // up / left candidates the last step sent
+    uint32_t A[2][R];    // doubled diagonal-move counters by parity
+    uint32_t B[2][R];    // doubled mismatch counters by parity
+    uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
+    uint32_t CP[2][R];   // per half: 0xFFFF in band, kOut outside
+};
+
+struct Pair16 {
+    int kb, l1, l2, shift;   // shift = kb & 1: odd bands run one step late
+};
+
+struct Best16 {
+    int m;
+    uint32_t ab;   // (doubled A << 16) | doubled B of the cell
+    int at;
+};
+
+// 16 symbols starting at read position pos, first symbol in bits 0-1 (pos
+// may be negative: zeros shift in; past the read: zeros).
+__device__ __forceinline__ uint32_t window16(const uint32_t* sm, int pos) {
+    if (pos >= 16 * (kSmWords - 2)) return 0u;
+    if (pos >= 0) {
+        const int k = pos >> 4;
+        return __funnelshift_r(sm[k], sm[k + 1], (pos & 15) * 2);
+    }
+    if (pos > -16) return sm[0] << (-pos * 2);
+    return 0u;
+}
+
+// Mismatch flags of the block.  Parity-0 cells k = 0..7 of slot q compare
+// read1[j0 - 1 + k] with read2[i0 - 1 + k], parity-1 cells read1[j0 - 1 + k]
+// with read2[i0 + k], (i0, j0) the slot's parity-0 cell at the block start.
+// A flag sits at bit 2k of its half.  A finished pair's caps close.
+template <int G, int R>
+__device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
+                                            int s0, const Pair16& pc, bool finished) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        uint32_t f0[2], f1[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = (h * G + gl) * R + r;
+            const int d0 = 2 * q - pc.kb;
+            const int i0 = (s0 + d0) >> 1, j0 = (s0 - d0) >> 1;   // s0 + d0 is even
+            const uint32_t w1 = window16(sm1, j0 - 1);
+            const uint32_t w2 = window16(sm2, i0 - 1);
+            const uint32_t x0 = w1 ^ w2, x1 = w1 ^ (w2 >> 2);
+            f0[h] = (x0 | (x0 >> 1)) & 0x55555555u;
+            f1[h] = (x1 | (x1 >> 1)) & 0x55555555u;
+        }
+        st.MW[0][r] = __byte_perm(f0[0], f0[1], 0x5410);
+        st.MW[1][r] = __byte_perm(f1[0], f1[1], 0x5410);
+        if (finished) { st.CP[0][r] = kOut2; st.CP[1][r] = kOut2; }
+    }
+}
+
+// Border blocks: a cell with s < |d| lies before the matrix (i < 0 or
+// j < 0); s == |d| is a boundary cell (i == 0: row 0, sends its left
+// candidate unpenalised, tag up; j == 0: column 0, tag left) with M = 0,
+// A = 0 and B = 4096 - s.
+__device__ __forceinline__ uint32_t border_key(uint32_t kh, int d, int s) {
+    const int ad = d < 0 ? -d : d;
+    if (s < ad) return kOut;
+    if (s == ad) return (uint32_t)((d < 0 ? 1 : 0) + 4 * s + kBase);
+    return kh;
+}
+
+template <int G, int R, int P>
+__device__ __forceinline__ void border_fix(uint32_t& K, uint32_t& A, uint32_t& B, int r, int gl, int s,
+                                           const Pair16& pc, bool keys) {
+    const int dl = 2 * (gl * R + r) - pc.kb + P;
+    const int dh = 2 * ((G + gl) * R + r) - pc.kb + P;
+    if (keys) {
+        K = border_key(K & 0xFFFFu, dl, s) | (border_key(K >> 16, dh, s) << 16);
+        return;
+    }
+    const uint32_t b0 = (uint32_t)(2 * (kMisOff - s));
+    if (s <= (dl < 0 ? -dl : dl)) { A &= 0xFFFF0000u; B = (B & 0xFFFF0000u) | b0; }
+    if (s <= (dh < 0 ? -dh : dh)) { A &= 0x0000FFFFu; B = (B & 0x0000FFFFu) | (b0 << 16); }
+}
+
+// The cell of slot q (held by this lane) at the current parity: key half and
+// packed counters.
+template <int G, int R, int P>
+__device__ __forceinline__ void take(const St<R>& st, int q, int gl, uint32_t& key, uint32_t& ab) {
+    const int rl = q - gl * R;
+    const bool hi = (unsigned)rl >= (unsigned)R;
+    const int rr = hi ? q - (G + gl) * R : rl;
+    uint32_t kk = 0, aa = 0, bb = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (r == rr) { kk = st.K[P][r]; aa = st.A[P][r]; bb = st.B[P][r]; }
+    if (hi) { kk >>= 16; aa >>= 16; bb >>= 16; }
+    key = kk & 0xFFFFu;
+    ab = ((aa & 0xFFFFu) << 16) | (bb & 0xFFFFu);
+}
+
+__device__ __forceinline__ bool mine(int q, int gl, int G, int R) {
+    return (unsigned)(q - gl * R) < (unsigned)R || (unsigned)(q - (G + gl) * R) < (unsigned)R;
+}
+
+// Last row (i = l2, tracked as `col`, ordered by j) and last column (j = l1,
+// `row`, ordered by i): each holds at most one cell per step; the lane that
+// holds it keeps the last maximum (>=), genCPU.cpp:442-464.
+template <int G, int R, int P>
+__device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pair16& pc, Best16& col,
+                                        Best16& row) {
+    const int dr = 2 * pc.l2 - s, jr = s - pc.l2;
+    const int qr = (dr + pc.kb - P) >> 1;
+    const int dc = s - 2 * pc.l1, ic = s - pc.l1;
+    const int qc = (dc + pc.kb - P) >> 1;
+    const bool hr = jr >= 1 && jr <= pc.l1 && dr >= -pc.kb && dr <= pc.kb && mine(qr, gl, G, R);
+    const bool hc = ic >= 1 && ic <= pc.l2 && dc >= -pc.kb && dc <= pc.kb && mine(qc, gl, G, R);
+    if (hr) {
+        uint32_t key, ab;
+        take<G, R, P>(st, qr, gl, key, ab);
+        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        if (m >= col.m) { col.m = m; col.ab = ab; col.at = jr; }
+    }
+    if (hc) {
+        uint32_t key, ab;
+        take<G, R, P>(st, qc, gl, key, ab);
+        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        if (m >= row.m) { row.m = m; row.ab = ab; row.at = ic; }
+    }
+}
+
+// One anti-diagonal step at parity P for the lane's 2R cells.
+template <int G, int R, int P, int kMode>
+__device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& pc, const Mul& mu,
+                                       Best16& col, Best16& row) {
+    constexpr int Q = P ^ 1;
+    uint32_t nK, nA, nB;
+    if (P == 0) {
+        // left of register 0 = register R-1 of the previous lane; lane 0's
+        // high half takes the last lane's low half, its low half nothing
+        const int src = (gl + G - 1) & (G - 1);
+        nK = __shfl_sync(0xffffffffu, st.F[R - 1], src, G);
+        nA = __shfl_sync(0xffffffffu, st.A[Q][R - 1], src, G);
+        nB = __shfl_sync(0xffffffffu, st.B[Q][R - 1], src, G);
+        if (gl == 0) { nK = (nK << 16) | kOut; nA <<= 16; nB <<= 16; }
+    } else {
+        // up of register R-1 = register 0 of the next lane; the last lane's
+        // low half takes lane 0's high half, its high half nothing
+        const int src = (gl + 1) & (G - 1);
+        nK = __shfl_sync(0xffffffffu, st.U[0], src, G);
+        nA = __shfl_sync(0xffffffffu, st.A[Q][0], src, G);
+        nB = __shfl_sync(0xffffffffu, st.B[Q][0], src, G);
+        if (gl == G - 1) { nK = (nK >> 16) | (kOut << 16); nA >>= 16; nB >>= 16; }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        // parity 0 reads register r-1 (runs downwards), parity 1 register
+        // r+1 (runs upwards), so a neighbour is read before it is rewritten
+        const int r = P == 0 ? R - 1 - k : k;
+        uint32_t upK, lfK, upA, lfA, upB, lfB;
+        if (P == 0) {
+            upK = st.U[r]; upA = st.A[Q][r]; upB = st.B[Q][r];
+            lfK = r > 0 ? st.F[r - 1] : nK;
+            lfA = r > 0 ? st.A[Q][r - 1] : nA;
+            lfB = r > 0 ? st.B[Q][r - 1] : nB;
+        } else {
+            lfK = st.F[r]; lfA = st.A[Q][r]; lfB = st.B[Q][r];
+            upK = r < R - 1 ? st.U[r + 1] : nK;
+            upA = r < R - 1 ? st.A[Q][r + 1] : nA;
+            upB = r < R - 1 ? st.B[Q][r + 1] : nB;
+        }
+        const uint32_t mm = st.MW[P][r] & kLo;
+        st.MW[P][r] >>= 2;
+        const uint32_t od = (st.K[P][r] | 0x00030003u) * mu.one + 0x001C001Cu;
+        const uint32_t kd = mm * mu.n36 + od;
+        uint32_t K = __vimax3_u16x2(kd, upK, lfK);
+        uint32_t A, B;
+        if (kMode == kFull) border_fix<G, R, P>(K, A, B, r, gl, s, pc, true);
+        K = __vminu2(K, st.CP[P][r]);
+        const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
+        const uint32_t xn1 = x1 * mu.neg1 + kLo;
+        st.U[r] = x2 * mu.n19 + (xn1 * mu.m5 + K);
+        st.F[r] = x2 * mu.n21 + (x1 * mu.m3 + K);
+        const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
+        const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
+        const uint32_t bd = mm * mu.two + st.B[P][r];
+        const uint32_t at = (upA & m0) | (lfA & ~m0);
+        const uint32_t bt = (upB & m0) | (lfB & ~m0);
+        A = (ad & m1) | (at & ~m1);
+        B = (bd & m1) | (bt & ~m1);
+        if (kMode == kFull) border_fix<G, R, P>(K, A, B, r, gl, s, pc, false);
+        st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
+    }
+    if (kMode != kClean) track16<G, R, P>(st, gl, s, pc, col, row);
+}
+
+template <int G, int R, int kMode>
+__device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu, Best16& col,
+                                        Best16& row) {
+#pragma unroll 1
+    for (int t = 0; t < kSteps; t += 2) {
+        step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, col, row);
+        step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, col, row);
+    }
+}
+
+// Largest m over a G-lane sub-group, ties to the largest index `at`.
+template <int G>
+__device__ __forceinline__ Best16 group_best16(Best16 b, int lane) {
+    const long long mine = (long long)b.m * 4294967296LL + (long long)(unsigned)(b.at + 1);
+    long long key = mine;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const long long other = __shfl_xor_sync(0xffffffffu, key, o);
+        key = other > key ? other : key;
+    }
+    const unsigned group = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const unsigned who = __ballot_sync(0xffffffffu, mine == key) & group;
+    Best16 r;
+    r.m = (int)(key >> 32);
+    r.at = (int)(unsigned)(key & 0xffffffffu) - 1;
+    r.ab = __shfl_sync(0xffffffffu, b.ab, __ffs(who) - 1);
+    return r;
+}
+
+template <int G, int R>
+__global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs a) {
+    constexpr int kPerWarp = 32 / G;
+    __shared__ uint32_t smem[kWarps][kPerWarp][2][kSmWords];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / G, gl = lane % G;
+    uint32_t* sm1 = smem[warp][sub][0];
+    uint32_t* sm2 = smem[warp][sub][1];
+    const Mul mu = make_mul(a.one);
+    int64_t base = a.queue ? -1 : ((int64_t)blockIdx.x * kWarps + warp) * kPerWarp;
+    const int64_t stride = (int64_t)gridDim.x * kWarps * kPerWarp;
+    for (;;) {
+        if (a.queue) {
+            unsigned w = 0;
+            if (lane == 0) w = atomicAdd(a.queue, (unsigned)kPerWarp);
+            base = __shfl_sync(0xffffffffu, w, 0);
+        }
+        if (base >= a.count) break;
+        const int64_t item = base + sub;
+        const bool valid = item < a.count;
+        int64_t p = -1;
+        Pair16 pc{0, 0, 0, 0};
+        int2 pr = make_int2(0, 0);
+        if (valid) {
+            p = a.order ? (int64_t)a.order[item] : item;
+            pr = a.pairs[p];
+            pc.l1 = a.len[pr.x];
+            pc.l2 = a.len[pr.y];
+            pc.kb = kband16(pc.l1, pc.l2, a.band);
+        }
+        pc.shift = pc.kb & 1;
+        const int nw1 = (pc.l1 + 15) >> 4, nw2 = (pc.l2 + 15) >> 4;
+        const uint32_t* g1 = a.packed + (valid ? a.woff[pr.x] : 0);
+        const uint32_t* g2 = a.packed + (valid ? a.woff[pr.y] : 0);
+        // first symbol to the low bits: the bit reversal also swaps the two
+        // bits of each symbol, which a mismatch test (xor, then or of the
+        // pair) does not see
+        for (int k = gl; k < kSmWords; k += G) {
+            sm1[k] = k < nw1 ? __brev(g1[k]) : 0u;
+            sm2[k] = k < nw2 ? __brev(g2[k]) : 0u;
+        }
+        __syncwarp();
+        St<R> st;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
+            st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
+            st.MW[0][r] = 0; st.MW[1][r] = 0;
+            uint32_t c0 = 0, c1 = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int q = (h * G + gl) * R + r;
+                // parity 0 hosts diagonal 2q - kb, parity 1 diagonal 2q - kb + 1
+                c0 |= (valid && q <= pc.kb ? 0xFFFFu : kOut) << (16 * h);
+                c1 |= (valid && q + 1 <= pc.kb ? 0xFFFFu : kOut) << (16 * h);
+            }
+            st.CP[0][r] = c0; st.CP[1][r] = c1;
+        }
+        Best16 col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
+        // the sweep ends at the last in-band cell of the last row or column
+        int s_end = -1;
+        if (valid) {
+            if (max(1, pc.l2 - pc.kb) <= min(pc.l1, pc.l2 + pc.kb)) s_end = pc.l2 + min(pc.l1, pc.l2 + pc.kb);
+            if (max(1, pc.l1 - pc.kb) <= min(pc.l2, pc.l1 + pc.kb))
+                s_end = max(s_end, pc.l1 + min(pc.l2, pc.l1 + pc.kb));
+        }
+        const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(0, s_end + pc.shift));
+        const int clean_hi = 2 * min(pc.l1, pc.l2) - pc.kb - 1;
+        for (int t0 = 0; t0 <= t_end; t0 += kSteps) {
+            const int s0 = t0 - pc.shift;
+            const bool finished = s0 > s_end;
+            block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
+            const bool started = s0 >= pc.kb + 2;
+            const bool clean = finished || (started && s0 + kSteps - 1 < clean_hi);
+            if (__all_sync(0xffffffffu, clean))
+                block16<G, R, kClean>(st, gl, s0, pc, mu, col, row);
+            else if (__all_sync(0xffffffffu, started || finished))
+                block16<G, R, kTrack>(st, gl, s0, pc, mu, col, row);
+            else
+                block16<G, R, kFull>(st, gl, s0, pc, mu, col, row);
+        }
+        col = group_best16<G>(col, lane);
+        row = group_best16<G>(row, lane);
+        if (gl == 0 && valid) {
+            const bool use_col = col.m > row.m;   // genKernel.cu:765-768
+            const Best16& b = use_col ? col : row;
+            int mlv = 0, alv = 0;
+            if (b.at >= 0) {
+                const int ij = use_col ? pc.l2 + b.at : b.at + pc.l1;
+                const int A = (int)(b.ab >> 17);
+                const int Bm = (int)((b.ab & 0xFFFFu) >> 1) - kMisOff;
+                alv = ij - A;
+                mlv = ij - 2 * A + Bm;
+            }
+            a.dist[p] = __fdiv_rn((float)mlv, (float)alv);
+            if (a.score) a.score[p] = b.m;
+            if (a.ml) a.ml[p] = mlv;
+            if (a.al) a.al[p] = alv;
+        }
+        __syncwarp();
+        if (!a.queue) base += stride;
+    }
+}
+
+constexpr Shape16 kShapes16[] = {{4, 1}, {4, 2}, {4, 4}, {8, 2}, {4, 5}, {4, 6}, {8, 3},
+                                 {4, 7}, {8, 4}, {8, 5}, {8, 6}, {16, 4}, {16, 6}, {32, 4}};
+constexpr int kNumShapes16 = sizeof(kShapes16) / sizeof(kShapes16[0]);
+
+using Fn16 = void (*)(GenArgs);
+Fn16 fn16(int i) {
+    switch (i) {
+        case 0: return gen16_kernel<4, 1>;
+        case 1: return gen16_kernel<4, 2>;
+        case 2: return gen16_kernel<4, 4>;
+        case 3: return gen16_kernel<8, 2>;
+        case 4: return gen16_kernel<4, 5>;
+        case 5: return gen16_kernel<4, 6>;
+        case 6: return gen16_kernel<8, 3>;
+        case 7: return gen16_kernel<4, 7>;
+        case 8: return gen16_kernel<8, 4>;
+        case 9: return gen16_kernel<8, 5>;
+        case 10: return gen16_kernel<8, 6>;
+        case 11: return gen16_kernel<16, 4>;
+        case 12: return gen16_kernel<16, 6>;
+        default: return gen16_kernel<32, 4>;
+    }
+}
+
+}  // namespace
+
+int gen16_num_shapes() { return kNumShapes16; }
+Shape16 gen16_shape(int i) { return kShapes16[i]; }
+int gen16_pairs_per_block(int i) { return kWarps * (32 / kShapes16[i].g); }
+
+int gen16_launch(crispy_ctx* ctx, cudaStream_t s, int shape, const GenArgs& a, bool timed) {
+    Fn16 fn = fn16(shape);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0);
+    const int64_t per_block = gen16_pairs_per_block(shape);
+    const int blocks = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
+                                              (a.count + per_block - 1) / per_block);
+    if (timed) ev_begin(ctx, ctx->ev_gen, s);
+    fn<<<std::max(blocks, 1), kThreads, 0, s>>>(a);
+    if (timed) ev_end(ctx, ctx->ev_gen, s);
+    count_launch(ctx);
+    return CRISPY_OK;
+}
+
+}  // namespace crispy

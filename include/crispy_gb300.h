@@ -343,6 +343,12 @@ int crispy_tune_report(char* buf, size_t len);
  * are integer-bound.  No reference counterpart (measurement utility). */
 int crispy_probe_int32(crispy_ctx* ctx, double* gops);
 
+/* Measured shared-memory gather throughput of this GPU in L1 wavefronts per
+ * second (conflict-free 128-bit loads, one wavefront = one quarter-warp's 128
+ * bytes): the roofline denominator of the k-mer tile kernels, whose bound is
+ * the L1 data pipe.  No reference counterpart (measurement utility). */
+int crispy_probe_lds128(crispy_ctx* ctx, double* wavefronts_per_s);
+
 /* ---- memory cap of one context (device bytes); 0 = unlimited.  An
  *      allocation that would exceed it fails with CRISPY_E_OOM, exactly as
  *      an exhausted device would.  The server gives every slot a share of
