@@ -43,9 +43,15 @@
 // left neighbours are slots q + 1 / q - 1 of the previous step, i.e.
 // registers r + 1 / r - 1 of the same lane, so only the lane's edge
 // register crosses lanes (one shuffle per step for keys, A and B).
-// Symbols: 2 bits each, first symbol in the low bits, in shared memory; per
-// block of 16 steps each slot's 8 mismatch flags per parity come from two
-// 16-symbol windows.
+// Symbols: 2 bits each, first symbol in the low bits, in shared memory
+// behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
+// windows out of four 32-symbol windows (consecutive slots of a lane read
+// windows one symbol apart) and folds them into 8 mismatch flags per slot
+// and parity.
+// Border: a slot hosts one diagonal d per parity, so it enters the matrix
+// once, at s = |d|, as a boundary cell (row 0 or column 0).  Every slot's cap
+// starts closed (key 8); the two boundary cells of a step (d = s and d = -s)
+// get their boundary values and open their slot's cap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,7 +66,8 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-constexpr int kSmWords = 132;        // 128 words of 16 symbols + refill padding
+constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
+constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
 constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
 constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
 constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
@@ -72,7 +79,7 @@ constexpr int kRefNegInf = -1000000;    // genCPU.cpp:350 initial last-row/colum
 static_assert(18 * (kGen16MaxSum + kSlack) + 131 < 65536, "16-bit keys would wrap");
 static_assert(kBase % 4 == 0, "the score is read back as (K - 4s - kBase) / 4");
 
-constexpr int kClean = 0, kTrack = 1, kFull = 2;
+constexpr int kClean = 0, kTrack = 1, kStart = 2;
 
 __device__ __forceinline__ int kband16(int l1, int l2, int band) {
     return band >= 2 ? (l1 + l2) / (2 * band) : max(l1, l2);
@@ -120,68 +127,85 @@ struct Best16 {
     int at;
 };
 
-// 16 symbols starting at read position pos, first symbol in bits 0-1 (pos
-// may be negative: zeros shift in; past the read: zeros).
-__device__ __forceinline__ uint32_t window16(const uint32_t* sm, int pos) {
-    if (pos >= 16 * (kSmWords - 2)) return 0u;
-    if (pos >= 0) {
-        const int k = pos >> 4;
-        return __funnelshift_r(sm[k], sm[k + 1], (pos & 15) * 2);
-    }
-    if (pos > -16) return sm[0] << (-pos * 2);
-    return 0u;
+// 32 symbols starting at read position pos as (lo, hi) words, first symbol
+// in bits 0-1 of lo (before the read and past it: zeros).  sm points at the
+// pad, so word w of the read is sm[kPadWords + w].
+__device__ __forceinline__ void window32(const uint32_t* sm, int pos, uint32_t& lo, uint32_t& hi) {
+    const int w = min(max(pos >> 4, -kPadWords), 128) + kPadWords;
+    const int sh = (pos & 15) * 2;
+    const uint32_t a = sm[w], b = sm[w + 1], c = sm[w + 2];
+    lo = __funnelshift_r(a, b, sh);
+    hi = __funnelshift_r(b, c, sh);
 }
 
 // Mismatch flags of the block.  Parity-0 cells k = 0..7 of slot q compare
 // read1[j0 - 1 + k] with read2[i0 - 1 + k], parity-1 cells read1[j0 - 1 + k]
-// with read2[i0 + k], (i0, j0) the slot's parity-0 cell at the block start.
-// A flag sits at bit 2k of its half.  A finished pair's caps close.
+// with read2[i0 + k], (i0, j0) = ((s0 + d0) / 2, (s0 - d0) / 2) the slot's
+// parity-0 cell at the block start, d0 = 2q - kb.  The lane's R slots of a
+// half are consecutive, q = qb + r: read1 windows start at J - r, read2
+// windows at I + r, all inside one 32-symbol window per read.  A flag sits
+// at bit 2k of its half.  A finished pair's caps close.
 template <int G, int R>
 __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
                                             int s0, const Pair16& pc, bool finished) {
+    uint32_t f0[2][R], f1[2][R];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int qb = (h * G + gl) * R;
+        const int d0 = 2 * qb - pc.kb;
+        const int I = ((s0 + d0) >> 1) - 1, J = ((s0 - d0) >> 1) - 1;   // s0 + d0 is even
+        uint32_t a_lo, a_hi, b_lo, b_hi;
+        window32(sm1, J - (R - 1), a_lo, a_hi);   // read1 from J - (R-1): slot r at offset R-1-r
+        window32(sm2, I, b_lo, b_hi);             // read2 from I: slot r at offset r
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t w1 = __funnelshift_r(a_lo, a_hi, 2 * (R - 1 - r));
+            const uint32_t w2 = __funnelshift_r(b_lo, b_hi, 2 * r);
+            const uint32_t w2n = __funnelshift_r(b_lo, b_hi, 2 * r + 2);   // read2 one symbol on
+            const uint32_t x0 = w1 ^ w2, x1 = w1 ^ w2n;
+            f0[h][r] = (x0 | (x0 >> 1)) & 0x55555555u;
+            f1[h][r] = (x1 | (x1 >> 1)) & 0x55555555u;
+        }
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        uint32_t f0[2], f1[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int q = (h * G + gl) * R + r;
-            const int d0 = 2 * q - pc.kb;
-            const int i0 = (s0 + d0) >> 1, j0 = (s0 - d0) >> 1;   // s0 + d0 is even
-            const uint32_t w1 = window16(sm1, j0 - 1);
-            const uint32_t w2 = window16(sm2, i0 - 1);
-            const uint32_t x0 = w1 ^ w2, x1 = w1 ^ (w2 >> 2);
-            f0[h] = (x0 | (x0 >> 1)) & 0x55555555u;
-            f1[h] = (x1 | (x1 >> 1)) & 0x55555555u;
-        }
-        st.MW[0][r] = __byte_perm(f0[0], f0[1], 0x5410);
-        st.MW[1][r] = __byte_perm(f1[0], f1[1], 0x5410);
+        st.MW[0][r] = __byte_perm(f0[0][r], f0[1][r], 0x5410);
+        st.MW[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x5410);
         if (finished) { st.CP[0][r] = kOut2; st.CP[1][r] = kOut2; }
     }
 }
 
-// Border blocks: a cell with s < |d| lies before the matrix (i < 0 or
-// j < 0); s == |d| is a boundary cell (i == 0: row 0, sends its left
-// candidate unpenalised, tag up; j == 0: column 0, tag left) with M = 0,
-// A = 0 and B = 4096 - s.
-__device__ __forceinline__ uint32_t border_key(uint32_t kh, int d, int s) {
-    const int ad = d < 0 ? -d : d;
-    if (s < ad) return kOut;
-    if (s == ad) return (uint32_t)((d < 0 ? 1 : 0) + 4 * s + kBase);
-    return kh;
+// Boundary events of a step: slot q = (d + kb - P) / 2 for d = s (column
+// 0, j = 0, tag left) and d = -s (row 0, i = 0, tag up), when it lies in
+// the band and in this lane: register *r (-1: none) and half *h.
+template <int G, int R, int P>
+__device__ __forceinline__ void boundary_slot(int d, const Pair16& pc, int gl, int* r, int* h) {
+    *r = -1;
+    *h = 0;
+    if (pc.l1 <= 0 || d < -pc.kb || d > pc.kb) return;   // no pair, or outside the band
+    const int q = (d + pc.kb - P) >> 1;
+    const int rl = q - gl * R, rh = q - (G + gl) * R;
+    if ((unsigned)rl < (unsigned)R) { *r = rl; *h = 0; }
+    else if ((unsigned)rh < (unsigned)R) { *r = rh; *h = 1; }
 }
 
-template <int G, int R, int P>
-__device__ __forceinline__ void border_fix(uint32_t& K, uint32_t& A, uint32_t& B, int r, int gl, int s,
-                                           const Pair16& pc, bool keys) {
-    const int dl = 2 * (gl * R + r) - pc.kb + P;
-    const int dh = 2 * ((G + gl) * R + r) - pc.kb + P;
-    if (keys) {
-        K = border_key(K & 0xFFFFu, dl, s) | (border_key(K >> 16, dh, s) << 16);
-        return;
-    }
+// Sets one half to a boundary cell at step s (M = 0, A = 0, B = 4096 - s,
+// doubled) and opens its cap.
+__device__ __forceinline__ void boundary_set(uint32_t& K, uint32_t& A, uint32_t& B, uint32_t& CP, int h,
+                                             int s, uint32_t tag) {
+    const uint32_t key = tag + (uint32_t)(4 * s + kBase);
     const uint32_t b0 = (uint32_t)(2 * (kMisOff - s));
-    if (s <= (dl < 0 ? -dl : dl)) { A &= 0xFFFF0000u; B = (B & 0xFFFF0000u) | b0; }
-    if (s <= (dh < 0 ? -dh : dh)) { A &= 0x0000FFFFu; B = (B & 0x0000FFFFu) | (b0 << 16); }
+    if (h == 0) {
+        K = (K & 0xFFFF0000u) | key;
+        A &= 0xFFFF0000u;
+        B = (B & 0xFFFF0000u) | b0;
+        CP |= 0x0000FFFFu;
+    } else {
+        K = (K & 0x0000FFFFu) | (key << 16);
+        A &= 0x0000FFFFu;
+        B = (B & 0x0000FFFFu) | (b0 << 16);
+        CP |= 0xFFFF0000u;
+    }
 }
 
 // The cell of slot q (held by this lane) at the current parity: key half and
@@ -230,28 +254,32 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
     }
 }
 
-// One anti-diagonal step at parity P for the lane's 2R cells.
+// One anti-diagonal step at parity P for the lane's 2R cells.  sel0 / sel1
+// are the lane's byte selectors for the edge register's neighbour: identity,
+// or (lane 0 at parity 0) its low half moved up over an empty slot, or (the
+// last lane at parity 1) its high half moved down under an empty slot.
 template <int G, int R, int P, int kMode>
 __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& pc, const Mul& mu,
-                                       Best16& col, Best16& row) {
+                                       uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
     constexpr int Q = P ^ 1;
     uint32_t nK, nA, nB;
     if (P == 0) {
-        // left of register 0 = register R-1 of the previous lane; lane 0's
-        // high half takes the last lane's low half, its low half nothing
+        // left of register 0 = register R-1 of the previous lane
         const int src = (gl + G - 1) & (G - 1);
-        nK = __shfl_sync(0xffffffffu, st.F[R - 1], src, G);
-        nA = __shfl_sync(0xffffffffu, st.A[Q][R - 1], src, G);
-        nB = __shfl_sync(0xffffffffu, st.B[Q][R - 1], src, G);
-        if (gl == 0) { nK = (nK << 16) | kOut; nA <<= 16; nB <<= 16; }
+        nK = __byte_perm(__shfl_sync(0xffffffffu, st.F[R - 1], src, G), kOut2, sel0);
+        nA = __byte_perm(__shfl_sync(0xffffffffu, st.A[Q][R - 1], src, G), 0u, sel0);
+        nB = __byte_perm(__shfl_sync(0xffffffffu, st.B[Q][R - 1], src, G), 0u, sel0);
     } else {
-        // up of register R-1 = register 0 of the next lane; the last lane's
-        // low half takes lane 0's high half, its high half nothing
+        // up of register R-1 = register 0 of the next lane
         const int src = (gl + 1) & (G - 1);
-        nK = __shfl_sync(0xffffffffu, st.U[0], src, G);
-        nA = __shfl_sync(0xffffffffu, st.A[Q][0], src, G);
-        nB = __shfl_sync(0xffffffffu, st.B[Q][0], src, G);
-        if (gl == G - 1) { nK = (nK >> 16) | (kOut << 16); nA >>= 16; nB >>= 16; }
+        nK = __byte_perm(__shfl_sync(0xffffffffu, st.U[0], src, G), kOut2, sel1);
+        nA = __byte_perm(__shfl_sync(0xffffffffu, st.A[Q][0], src, G), 0u, sel1);
+        nB = __byte_perm(__shfl_sync(0xffffffffu, st.B[Q][0], src, G), 0u, sel1);
+    }
+    int ra = -1, ha = 0, rb = -1, hb = 0;
+    if (kMode == kStart && s >= 0) {
+        boundary_slot<G, R, P>(s, pc, gl, &ra, &ha);            // column 0
+        if (s > 0) boundary_slot<G, R, P>(-s, pc, gl, &rb, &hb);   // row 0
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -271,37 +299,46 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             upB = r < R - 1 ? st.B[Q][r + 1] : nB;
         }
         const uint32_t mm = st.MW[P][r] & kLo;
-        st.MW[P][r] >>= 2;
+        st.MW[P][r] = __umulhi(st.MW[P][r], 0x40000000u);   // >> 2 on the multiplier
         const uint32_t od = (st.K[P][r] | 0x00030003u) * mu.one + 0x001C001Cu;
         const uint32_t kd = mm * mu.n36 + od;
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
-        uint32_t A, B;
-        if (kMode == kFull) border_fix<G, R, P>(K, A, B, r, gl, s, pc, true);
         K = __vminu2(K, st.CP[P][r]);
+        const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
+        const uint32_t bd = mm * mu.two + st.B[P][r];
+        uint32_t A, B;
+        if (kMode == kStart && (r == ra || r == rb)) {
+            // a boundary cell: its own values, not the recurrence's
+            const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
+            const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
+            A = (ad & m1) | (((upA & m0) | (lfA & ~m0)) & ~m1);
+            B = (bd & m1) | (((upB & m0) | (lfB & ~m0)) & ~m1);
+            if (r == ra) boundary_set(K, A, B, st.CP[P][r], ha, s, 0u);
+            if (r == rb) boundary_set(K, A, B, st.CP[P][r], hb, s, 1u);
+        }
         const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
         const uint32_t xn1 = x1 * mu.neg1 + kLo;
         st.U[r] = x2 * mu.n19 + (xn1 * mu.m5 + K);
         st.F[r] = x2 * mu.n21 + (x1 * mu.m3 + K);
-        const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
-        const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
-        const uint32_t bd = mm * mu.two + st.B[P][r];
-        const uint32_t at = (upA & m0) | (lfA & ~m0);
-        const uint32_t bt = (upB & m0) | (lfB & ~m0);
-        A = (ad & m1) | (at & ~m1);
-        B = (bd & m1) | (bt & ~m1);
-        if (kMode == kFull) border_fix<G, R, P>(K, A, B, r, gl, s, pc, false);
+        if (!(kMode == kStart && (r == ra || r == rb))) {
+            const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
+            const uint32_t at = (upA & m0) | (lfA & ~m0);
+            const uint32_t bt = (upB & m0) | (lfB & ~m0);
+            A = (ad & m1) | (at & ~m1);
+            B = (bd & m1) | (bt & ~m1);
+        }
         st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
     }
     if (kMode != kClean) track16<G, R, P>(st, gl, s, pc, col, row);
 }
 
 template <int G, int R, int kMode>
-__device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu, Best16& col,
-                                        Best16& row) {
+__device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu,
+                                        uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
 #pragma unroll 1
     for (int t = 0; t < kSteps; t += 2) {
-        step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, col, row);
-        step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, col, row);
+        step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, sel0, sel1, col, row);
+        step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, sel0, sel1, col, row);
     }
 }
 
@@ -325,7 +362,7 @@ __device__ __forceinline__ Best16 group_best16(Best16 b, int lane) {
 }
 
 template <int G, int R>
-__global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs a) {
+__global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16_kernel(GenArgs a) {
     constexpr int kPerWarp = 32 / G;
     __shared__ uint32_t smem[kWarps][kPerWarp][2][kSmWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -333,6 +370,8 @@ __global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs
     uint32_t* sm1 = smem[warp][sub][0];
     uint32_t* sm2 = smem[warp][sub][1];
     const Mul mu = make_mul(a.one);
+    const uint32_t sel0 = gl == 0 ? 0x1054u : 0x3210u;       // parity 0: lane 0's low half moves up
+    const uint32_t sel1 = gl == G - 1 ? 0x7632u : 0x3210u;   // parity 1: last lane's high half moves down
     int64_t base = a.queue ? -1 : ((int64_t)blockIdx.x * kWarps + warp) * kPerWarp;
     const int64_t stride = (int64_t)gridDim.x * kWarps * kPerWarp;
     for (;;) {
@@ -362,8 +401,9 @@ __global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs
         // bits of each symbol, which a mismatch test (xor, then or of the
         // pair) does not see
         for (int k = gl; k < kSmWords; k += G) {
-            sm1[k] = k < nw1 ? __brev(g1[k]) : 0u;
-            sm2[k] = k < nw2 ? __brev(g2[k]) : 0u;
+            const int w = k - kPadWords;
+            sm1[k] = w >= 0 && w < nw1 ? __brev(g1[w]) : 0u;
+            sm2[k] = w >= 0 && w < nw2 ? __brev(g2[w]) : 0u;
         }
         __syncwarp();
         St<R> st;
@@ -372,15 +412,8 @@ __global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs
             st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
             st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
-            uint32_t c0 = 0, c1 = 0;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int q = (h * G + gl) * R + r;
-                // parity 0 hosts diagonal 2q - kb, parity 1 diagonal 2q - kb + 1
-                c0 |= (valid && q <= pc.kb ? 0xFFFFu : kOut) << (16 * h);
-                c1 |= (valid && q + 1 <= pc.kb ? 0xFFFFu : kOut) << (16 * h);
-            }
-            st.CP[0][r] = c0; st.CP[1][r] = c1;
+            // every cap starts closed; a slot's boundary cell opens it
+            st.CP[0][r] = kOut2; st.CP[1][r] = kOut2;
         }
         Best16 col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
         // the sweep ends at the last in-band cell of the last row or column
@@ -396,14 +429,14 @@ __global__ void __launch_bounds__(kThreads, R <= 4 ? 6 : 4) gen16_kernel(GenArgs
             const int s0 = t0 - pc.shift;
             const bool finished = s0 > s_end;
             block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
-            const bool started = s0 >= pc.kb + 2;
+            const bool started = s0 > pc.kb;   // every boundary cell is behind (s = |d| <= kb)
             const bool clean = finished || (started && s0 + kSteps - 1 < clean_hi);
             if (__all_sync(0xffffffffu, clean))
-                block16<G, R, kClean>(st, gl, s0, pc, mu, col, row);
+                block16<G, R, kClean>(st, gl, s0, pc, mu, sel0, sel1, col, row);
             else if (__all_sync(0xffffffffu, started || finished))
-                block16<G, R, kTrack>(st, gl, s0, pc, mu, col, row);
+                block16<G, R, kTrack>(st, gl, s0, pc, mu, sel0, sel1, col, row);
             else
-                block16<G, R, kFull>(st, gl, s0, pc, mu, col, row);
+                block16<G, R, kStart>(st, gl, s0, pc, mu, sel0, sel1, col, row);
         }
         col = group_best16<G>(col, lane);
         row = group_best16<G>(row, lane);
