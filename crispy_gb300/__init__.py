@@ -131,6 +131,9 @@ PROTOTYPES = {
     "crispy_server_wait": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_int)]),
     "crispy_server_result": (C.c_int, [_P, C.c_uint64, SINK, _P, _i64p, _i64p]),
     "crispy_server_cancel": (C.c_int, [_P, C.c_uint64]),
+    "crispy_server_job_memory": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                                           C.POINTER(C.c_int)]),
+    "crispy_server_job_bytes": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
     "crispy_server_stats": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), _i64p, _i64p]),
     "crispy_server_stats_reset": (C.c_int, [_P]),
     "crispy_server_last_error": (C.c_char_p, [_P]),
@@ -487,6 +490,14 @@ class Server:
         self._check(self.lib.crispy_server_result(self.h, job, f, None, C.byref(kp), C.byref(gp)))
         return kp.value, chunks
 
+    def job_memory(self, job: int) -> dict:
+        """Memory of the run that served a finished job (call before result())."""
+        r = C.c_size_t()
+        nd = C.c_size_t()
+        cs = C.c_int()
+        self._check(self.lib.crispy_server_job_memory(self.h, job, C.byref(r), C.byref(nd), C.byref(cs)))
+        return {"reserved": r.value, "needed": nd.value, "cohort_size": cs.value}
+
     def cancel(self, job: int):
         self._check(self.lib.crispy_server_cancel(self.h, job))
 
@@ -501,6 +512,16 @@ class Server:
 
     def reset_stats(self):
         self._check(self.lib.crispy_server_stats_reset(self.h))
+
+
+def server_job_bytes(lens, k: int = 6) -> int:
+    """Device bytes the server's admission reserves for a job with these read lengths."""
+    lens = np.ascontiguousarray(lens, dtype=np.int32)
+    b = C.c_size_t()
+    rc = load_library().crispy_server_job_bytes(_ptr(lens), len(lens), k, C.byref(b))
+    if rc != OK:
+        raise CrispyError(rc, "server_job_bytes")
+    return b.value
 
 
 def compute_kmer_dist(fasta: str, k: int = 6, thr: float = -1.0, dists: bool = False,

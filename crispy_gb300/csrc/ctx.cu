@@ -86,6 +86,10 @@ int cuda_fail(crispy_ctx* ctx, cudaError_t e, const char* what, const char* file
 }
 
 int ensure(crispy_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (ctx) {
+        if (b.epoch != ctx->run_epoch) { b.epoch = ctx->run_epoch; b.need = 0; }
+        if (bytes > b.need) { ctx->run_need += bytes - b.need; b.need = bytes; }
+    }
     if (bytes <= b.bytes && b.ptr) return CRISPY_OK;
     release(ctx, b);
     size_t want = bytes < 256 ? 256 : bytes;

@@ -498,13 +498,16 @@ __global__ void gen_keys_kernel(const float* __restrict__ dist, const uint32_t* 
     vals[i] = p;
 }
 
+// pair_base: the job's first position in a cohort's read set (0 otherwise),
+// so that output pairs hold the job's own read indices.
 __global__ void gen_gather_kernel(const int2* __restrict__ pairs, const uint32_t* __restrict__ keys,
                                   const uint32_t* __restrict__ vals, int64_t count,
-                                  uint2* __restrict__ out_pairs, float* __restrict__ out_dists) {
+                                  uint2* __restrict__ out_pairs, float* __restrict__ out_dists,
+                                  int pair_base = 0) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const int2 pr = pairs[vals[i]];
-    out_pairs[i] = make_uint2((uint32_t)pr.x, (uint32_t)pr.y);
+    out_pairs[i] = make_uint2((uint32_t)(pr.x - pair_base), (uint32_t)(pr.y - pair_base));
     out_dists[i] = __uint_as_float(keys[i]);
 }
 
@@ -923,17 +926,20 @@ int gen_check_pairs(crispy_ctx* ctx, const int32_t* pairs, int64_t npairs) {
 }
 
 // Threshold, windows, chunking, stable sort; delivers chunks to the sink.
+// d_dist: the pairs' distances (default: the context's distance buffer);
+// pair_base is subtracted from the output pairs (a cohort job's base).
 int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npairs, float thr,
-               crispy_sink sink, void* user, int64_t* nsurv, bool use_graph) {
+               crispy_sink sink, void* user, int64_t* nsurv, bool use_graph, const float* d_dist = nullptr,
+               int pair_base = 0) {
     GenJob& g = ctx->gen;
+    const float* dist = d_dist ? d_dist : g.dist.as<float>();
     *nsurv = 0;
     if (npairs == 0) return CRISPY_OK;
     CRISPY_TRY(ensure(ctx, g.flags, (size_t)npairs));
     CRISPY_TRY(ensure(ctx, g.surv_idx, (size_t)npairs * 4));
     const int64_t ntiles = (npairs + kScanTile - 1) / kScanTile;
     CRISPY_TRY(ensure(ctx, g.blocksum, (size_t)ntiles * 4));
-    gen_flag_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, s>>>(g.dist.as<float>(), npairs, thr,
-                                                                   g.flags.as<uint8_t>());
+    gen_flag_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, s>>>(dist, npairs, thr, g.flags.as<uint8_t>());
     count_launch(ctx);
     int64_t total = 0;
     CRISPY_TRY(compact_flags(ctx, s, g.flags.as<uint8_t>(), npairs, g.surv_idx.as<uint32_t>(),
@@ -970,7 +976,7 @@ int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npa
         const int64_t b = chunks[ci].first, c = chunks[ci].second;
         const unsigned blocks = (unsigned)((c + 255) / 256);
         auto chunk_work = [&]() -> int {
-            gen_keys_kernel<<<blocks, 256, 0, s>>>(g.dist.as<float>(), g.surv_idx.as<uint32_t>(), b, c,
+            gen_keys_kernel<<<blocks, 256, 0, s>>>(dist, g.surv_idx.as<uint32_t>(), b, c,
                                                   g.keys.as<uint32_t>(), g.vals.as<uint32_t>());
             count_launch(ctx);
             uint32_t *sk = nullptr, *sv = nullptr;
@@ -979,7 +985,7 @@ int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npa
                                         g.vals.as<uint32_t>(), g.vals_alt.as<uint32_t>(), c, 32, &sk,
                                         &sv, g.scan));
             gen_gather_kernel<<<blocks, 256, 0, s>>>(d_pairs, sk, sv, c, g.out_pairs.as<uint2>(),
-                                                    g.out_dists.as<float>());
+                                                    g.out_dists.as<float>(), pair_base);
             count_launch(ctx);
             CRISPY_CK(ctx, cudaGetLastError());
             return CRISPY_OK;
@@ -987,7 +993,7 @@ int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npa
         if (use_graph) {
             CRISPY_TRY(ensure(ctx, g.scan, sort_tmp_bytes(c)));
             const std::string key = "gchunk," + key_of({(uint64_t)b, (uint64_t)c, (uint64_t)(uintptr_t)d_pairs,
-                (uint64_t)(uintptr_t)g.dist.ptr, (uint64_t)(uintptr_t)g.surv_idx.ptr, (uint64_t)(uintptr_t)g.keys.ptr,
+                (uint64_t)(uintptr_t)dist, (uint64_t)(uintptr_t)g.surv_idx.ptr, (uint64_t)(uintptr_t)g.keys.ptr,
                 (uint64_t)(uintptr_t)g.keys_alt.ptr, (uint64_t)(uintptr_t)g.vals.ptr, (uint64_t)(uintptr_t)g.vals_alt.ptr,
                 (uint64_t)(uintptr_t)g.scan.ptr, (uint64_t)(uintptr_t)g.out_pairs.ptr, (uint64_t)(uintptr_t)g.out_dists.ptr});
             CRISPY_TRY(graph_run(ctx, s, key, chunk_work));
@@ -1390,3 +1396,47 @@ int crispy_gen_run_from_kmer(crispy_ctx* ctx, int band, float thr, int mode, cri
 }
 
 }  // extern "C"
+
+namespace crispy {
+
+// genDist over a cohort after kmer_run_cohort (server cross-job batching):
+// every job's survivors go through one classification and one set of
+// persistent bin launches (the jobs share every launch); then each job's
+// slice is thresholded, chunked and sorted on its own, with its own
+// threshold, and its chunks (in its own read indices) go to its sink.
+int gen_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, const std::vector<int64_t>& counts,
+                   int band, std::vector<int64_t>& gen_counts) {
+    GenJob& g = ctx->gen;
+    KmerJob& k = ctx->kmer;
+    if (!g.ready || !k.ready) return fail(ctx, CRISPY_E_STATE, "gen cohort needs kmer_run_cohort and gen_prepare");
+    if (counts.size() != jobs.size()) return fail(ctx, CRISPY_E_STATE, "gen cohort: %zu counts for %zu jobs",
+                                                  counts.size(), jobs.size());
+    int64_t total = 0;
+    for (int64_t c : counts) total += c;
+    if (total != k.nsurv || k.spilled) return fail(ctx, CRISPY_E_STATE, "gen cohort: survivor counts do not match");
+    if (band <= 0) band = 2;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    ctx->stats = crispy_stats{};
+    ctx->ev_gen.used = 0;
+    gen_counts.assign(jobs.size(), 0);
+    if (total > 0) {
+        CRISPY_TRY(ensure(ctx, g.dist, (size_t)total * 4));
+        CRISPY_TRY(gen_dispatch_impl(ctx, s, k.pairs.as<int2>(), total, band, CRISPY_MODE_BATCHED,
+                                     g.dist.as<float>(), nullptr, nullptr, nullptr));
+    }
+    int64_t off = 0;
+    for (size_t c = 0; c < jobs.size(); ++c) {
+        int64_t ns = 0;
+        if (counts[c] > 0)
+            CRISPY_TRY(gen_finish(ctx, s, k.pairs.as<int2>() + off, counts[c], jobs[c].thr, jobs[c].sink,
+                                  jobs[c].user, &ns, false, g.dist.as<float>() + off, jobs[c].base));
+        gen_counts[c] = ns;
+        off += counts[c];
+    }
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    ctx->stats.gen_kernel_ms = ev_sum_ms(ctx->ev_gen);
+    return CRISPY_OK;
+}
+
+}  // namespace crispy

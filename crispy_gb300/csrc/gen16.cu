@@ -44,10 +44,10 @@
 // registers r + 1 / r - 1 of the same lane, so only the lane's edge
 // register crosses lanes (one shuffle per step for keys, A and B).
 // Symbols: 2 bits each, first symbol in the low bits, in shared memory
-// behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
+// behind a zero pad; per block of 32 (R > 5: 16) steps a lane cuts its slots' 16-symbol
 // windows out of four 32-symbol windows (consecutive slots of a lane read
-// windows one symbol apart) and folds them into 8 mismatch flags per slot
-// and parity.
+// windows one symbol apart) and folds them into 16 (8) mismatch flags per
+// slot and parity.
 // Border: a slot hosts one diagonal d per parity, so it enters the matrix
 // once, at s = |d|, as a boundary cell (row 0 or column 0).  Every slot's cap
 // starts closed (key 8); the two boundary cells of a step (d = s and d = -s)
@@ -68,7 +68,11 @@ constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
 constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
-constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
+constexpr int kSteps = 16;           // steps per flag word: 8 cells per slot and parity
+// Blocks of 32 steps (two flag words per slot and parity) where the
+// registers allow, 16 steps above R = 5.
+template <int R>
+constexpr int block_steps() { return R <= 5 ? 32 : 16; }
 constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
 constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
 constexpr uint32_t kLo = 0x00010001u;   // 1 in each half
@@ -114,11 +118,15 @@ struct St {
     uint32_t A[2][R];    // doubled diagonal-move counters by parity
     uint32_t B[2][R];    // doubled mismatch counters by parity
     uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
+    uint32_t MW2[2][R];  // the next 8 steps' flags (32-step blocks)
     uint32_t CP[2][R];   // per half: 0xFFFF in band, kOut outside
 };
 
 struct Pair16 {
     int kb, l1, l2, shift;   // shift = kb & 1: odd bands run one step late
+    // steps at which this lane may hold a last-row / last-column cell: four
+    // windows of 2R steps (last row, then last column; low and high slots)
+    int tw[4];
 };
 
 struct Best16 {
@@ -144,7 +152,8 @@ __device__ __forceinline__ void window32(const uint32_t* sm, int pos, uint32_t& 
 // parity-0 cell at the block start, d0 = 2q - kb.  The lane's R slots of a
 // half are consecutive, q = qb + r: read1 windows start at J - r, read2
 // windows at I + r, all inside one 32-symbol window per read.  A flag sits
-// at bit 2k of its half.  A finished pair's caps close.
+// at bit 2k of its half (cells 8..15 of a 32-step block in MW2).  A
+// finished pair's caps close.
 template <int G, int R>
 __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
                                             int s0, const Pair16& pc, bool finished) {
@@ -171,6 +180,10 @@ __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, cons
     for (int r = 0; r < R; ++r) {
         st.MW[0][r] = __byte_perm(f0[0][r], f0[1][r], 0x5410);
         st.MW[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x5410);
+        if (block_steps<R>() == 32) {   // flags of cells 8..15
+            st.MW2[0][r] = __byte_perm(f0[0][r], f0[1][r], 0x7632);
+            st.MW2[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x7632);
+        }
         if (finished) { st.CP[0][r] = kOut2; st.CP[1][r] = kOut2; }
     }
 }
@@ -329,14 +342,22 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         }
         st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
     }
-    if (kMode != kClean) track16<G, R, P>(st, gl, s, pc, col, row);
+    if (kMode != kClean) {
+        const bool near = (unsigned)(s - pc.tw[0]) < 2u * R || (unsigned)(s - pc.tw[1]) < 2u * R ||
+                          (unsigned)(s - pc.tw[2]) < 2u * R || (unsigned)(s - pc.tw[3]) < 2u * R;
+        if (near) track16<G, R, P>(st, gl, s, pc, col, row);
+    }
 }
 
 template <int G, int R, int kMode>
 __device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu,
                                         uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
 #pragma unroll 1
-    for (int t = 0; t < kSteps; t += 2) {
+    for (int t = 0; t < block_steps<R>(); t += 2) {
+        if (block_steps<R>() == 32 && t == kSteps) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) { st.MW[0][r] = st.MW2[0][r]; st.MW[1][r] = st.MW2[1][r]; }
+        }
         step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, sel0, sel1, col, row);
         step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, sel0, sel1, col, row);
     }
@@ -384,7 +405,7 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         const int64_t item = base + sub;
         const bool valid = item < a.count;
         int64_t p = -1;
-        Pair16 pc{0, 0, 0, 0};
+        Pair16 pc{0, 0, 0, 0, {INT_MIN / 2, INT_MIN / 2, INT_MIN / 2, INT_MIN / 2}};
         int2 pr = make_int2(0, 0);
         if (valid) {
             p = a.order ? (int64_t)a.order[item] : item;
@@ -394,6 +415,16 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
             pc.kb = kband16(pc.l1, pc.l2, a.band);
         }
         pc.shift = pc.kb & 1;
+        if (valid) {
+            // last row i = l2: slot (2 l2 - s + kb - P) / 2 falls in [qa, qa + R) for
+            // s in [2 l2 + kb - 2 qa - 2R + 1, 2 l2 + kb - 2 qa]; last column j = l1:
+            // slot (s - 2 l1 + kb - P) / 2 for s in [2 l1 - kb + 2 qa, 2 l1 - kb + 2 qa + 2R - 1]
+            const int qlo = gl * R, qhi = (G + gl) * R;
+            pc.tw[0] = 2 * pc.l2 + pc.kb - 2 * qlo - 2 * R + 1;
+            pc.tw[1] = 2 * pc.l2 + pc.kb - 2 * qhi - 2 * R + 1;
+            pc.tw[2] = 2 * pc.l1 - pc.kb + 2 * qlo;
+            pc.tw[3] = 2 * pc.l1 - pc.kb + 2 * qhi;
+        }
         const int nw1 = (pc.l1 + 15) >> 4, nw2 = (pc.l2 + 15) >> 4;
         const uint32_t* g1 = a.packed + (valid ? a.woff[pr.x] : 0);
         const uint32_t* g2 = a.packed + (valid ? a.woff[pr.y] : 0);
@@ -411,7 +442,7 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         for (int r = 0; r < R; ++r) {
             st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
             st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
-            st.MW[0][r] = 0; st.MW[1][r] = 0;
+            st.MW[0][r] = 0; st.MW[1][r] = 0; st.MW2[0][r] = 0; st.MW2[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
             st.CP[0][r] = kOut2; st.CP[1][r] = kOut2;
         }
@@ -425,12 +456,13 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         }
         const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(0, s_end + pc.shift));
         const int clean_hi = 2 * min(pc.l1, pc.l2) - pc.kb - 1;
-        for (int t0 = 0; t0 <= t_end; t0 += kSteps) {
+        constexpr int kBlock = block_steps<R>();
+        for (int t0 = 0; t0 <= t_end; t0 += kBlock) {
             const int s0 = t0 - pc.shift;
             const bool finished = s0 > s_end;
             block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
             const bool started = s0 > pc.kb;   // every boundary cell is behind (s = |d| <= kb)
-            const bool clean = finished || (started && s0 + kSteps - 1 < clean_hi);
+            const bool clean = finished || (started && s0 + kBlock - 1 < clean_hi);
             if (__all_sync(0xffffffffu, clean))
                 block16<G, R, kClean>(st, gl, s0, pc, mu, sel0, sel1, col, row);
             else if (__all_sync(0xffffffffu, started || finished))

@@ -15,10 +15,14 @@
 
 namespace crispy {
 
-// Grow-only device allocation owned by a context.
+// Grow-only device allocation owned by a context.  need / epoch track the
+// largest size requested during the context's current run (see
+// crispy_ctx::run_need).
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
+    size_t need = 0;
+    uint64_t epoch = 0;
     template <class T> T* as() const { return static_cast<T*>(ptr); }
 };
 
@@ -120,6 +124,11 @@ struct crispy_ctx {
     bool use_graphs = true;
     size_t mem_cap = 0;      // 0 = unlimited
     size_t mem_in_use = 0;   // bytes held by DevBuf allocations
+    // device bytes the current run has asked for (each buffer's largest
+    // request since the run began, summed): the run's own peak, whatever
+    // larger buffers earlier runs left behind.  A new run bumps run_epoch.
+    uint64_t run_epoch = 1;
+    size_t run_need = 0;
     cudaEvent_t t_begin = nullptr, t_end = nullptr;
 };
 
@@ -180,6 +189,19 @@ int scan_stage_fasta(const char* path, int flavour, FastaBuffer& buf, std::vecto
 // writeToFile gives record i, newline excluded (pre_io.cpp).
 int32_t raw_records(const crispy_raw* r);
 int64_t raw_header_line(const crispy_raw* r, int32_t i);
+
+// One job of a cohort run (server cross-job batching): its reads sit at
+// positions [base, base + n) of the cohort's read set; thr is its k-mer
+// (kmer_run_cohort) or genetic (gen_run_cohort) cut threshold.
+struct CohortJob {
+    int base = 0, n = 0;
+    float thr = 0.0f;
+    crispy_sink sink = nullptr;   // genDist chunks of this job (gen_run_cohort)
+    void* user = nullptr;
+};
+int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::vector<int64_t>& counts);
+int gen_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, const std::vector<int64_t>& counts,
+                   int band, std::vector<int64_t>& gen_counts);
 
 // radix sort / scan helpers (sort.cu)
 size_t sort_tmp_bytes(int64_t n);   // scratch a sort of n items needs

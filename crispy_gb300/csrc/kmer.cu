@@ -555,7 +555,31 @@ struct TileArgs {
     const int2* item_q;
     int same_only;
     const int32_t* nsec;
+    // Cohort (several jobs' reads back to back, each starting at a multiple
+    // of 128 positions; 128-row kernel, batched form): per item its job and
+    // its end column group; per job (base, n, A, stage_dim) and its
+    // threshold tables at mmin / smin + tbl[job]; survivors carry the job
+    // in key bits 44 and up and count per job in job_counter.
+    const int* item_job;
+    const int* item_cend;
+    const int4* cjob;
+    const int* ctbl;
+    unsigned long long* job_counter;
 };
+
+// Parameters of the job a survivor belongs to (the whole run, or one job of
+// a cohort): local positions are (r - base, c - base).
+struct EmitJob {
+    const uint16_t* mmin;
+    const uint16_t* smin;
+    int n, A, sd, base;
+    uint64_t tag;
+    unsigned long long* jcount;
+};
+
+__device__ __forceinline__ EmitJob emit_job_of(const TileArgs& a) {
+    return EmitJob{a.mmin, a.smin, a.n, a.A, a.stage_dim, 0, 0ull, nullptr};
+}
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b) {
     const uint32_t u = l ^ a;
@@ -579,7 +603,8 @@ __device__ __forceinline__ uint64_t stage_key(int r, int c, int n, int A, int sd
 // lies in [olo, ohi) are kept (the stage rows of one pass).
 __device__ __forceinline__ void emit(unsigned long long* counter, uint64_t* keys, uint32_t* vals,
                                      int64_t cap, int n, int A, int sd, const int32_t* perm,
-                                     int olo, int ohi, bool pass, int r, int c, int m, int mn) {
+                                     int olo, int ohi, bool pass, int r, int c, int m, int mn,
+                                     int base_pos = 0, uint64_t tag = 0, unsigned long long* jcount = nullptr) {
     if (perm != nullptr && pass) {
         const int pr = __ldg(perm + r), pc = __ldg(perm + c);
         r = min(pr, pc);
@@ -591,12 +616,15 @@ __device__ __forceinline__ void emit(unsigned long long* counter, uint64_t* keys
     const int lane = threadIdx.x & 31;
     unsigned long long base = 0;
     const int leader = __ffs(pm) - 1;
-    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(pm));
+    if (lane == leader) {
+        base = atomicAdd(counter, (unsigned long long)__popc(pm));
+        if (jcount) atomicAdd(jcount, (unsigned long long)__popc(pm));
+    }
     base = __shfl_sync(0xffffffffu, base, leader);
     if (pass) {
         const unsigned long long idx = base + __popc(pm & ((1u << lane) - 1u));
         if (idx < (unsigned long long)cap) {
-            keys[idx] = stage_key(r, c, n, A, sd);
+            keys[idx] = tag | stage_key(r - base_pos, c - base_pos, n, A, sd);
             // kmerKernel.cu:47: 1.0f - (float)matches / min(T1, T2), IEEE
             const float d = __fsub_rn(1.0f, __fdiv_rn((float)m, (float)mn));
             vals[idx] = __float_as_uint(d);
@@ -737,9 +765,10 @@ __device__ __forceinline__ void gather16(const char* __restrict__ Pb, uint4 q0, 
 // compare against a lower bound of mmin over the lane's pairs, then the
 // exact test per candidate.
 template <int B>
-__device__ __forceinline__ void finish_half(const TileArgs& a, const uint32_t* X, uint32_t vmask,
-                                            int rbase, int t_min, const int* rowT, int c, int tc) {
-    const uint32_t lo = a.smin[min(t_min, tc)];
+__device__ __forceinline__ void finish_half(const TileArgs& a, const EmitJob& ej, const uint32_t* X,
+                                            uint32_t vmask, int rbase, int t_min, const int* rowT, int c,
+                                            int tc) {
+    const uint32_t lo = ej.smin[min(t_min, tc)];
     uint32_t cand = 0;
     if (vmask && lo < (1u << B)) {
         uint32_t gt = 0, eq = 0xffffffffu;
@@ -761,9 +790,10 @@ __device__ __forceinline__ void finish_half(const TileArgs& a, const uint32_t* X
             for (int k = 0; k < B; ++k) m |= (int)((X[k] >> b) & 1u) << k;
             r = rbase + b;
             mn = min(rowT[b], tc);
-            pass = m >= (int)a.mmin[mn];
+            pass = m >= (int)ej.mmin[mn];
         }
-        emit(a.counter, a.keys, a.vals, a.cap, a.n, a.A, a.stage_dim, a.perm, a.olo, a.ohi, pass, r, c, m, mn);
+        emit(a.counter, a.keys, a.vals, a.cap, ej.n, ej.A, ej.sd, a.perm, a.olo, a.ohi, pass, r, c, m, mn,
+             ej.base, ej.tag, ej.jcount);
     }
 }
 
@@ -839,8 +869,9 @@ __device__ void tile_columns(const TileArgs& a, const uint2* __restrict__ P,
             }
         }
         const int tc = col_ok ? a.tcount[c] : 0;
-        finish_half<B>(a, X0, vm0, r0, tmin0, s_rowT, c, tc);
-        finish_half<B>(a, X1, vm1, r0 + 32, tmin1, s_rowT + 32, c, tc);
+        const EmitJob ej = emit_job_of(a);
+        finish_half<B>(a, ej, X0, vm0, r0, tmin0, s_rowT, c, tc);
+        finish_half<B>(a, ej, X1, vm1, r0 + 32, tmin1, s_rowT + 32, c, tc);
     }
 }
 
@@ -864,7 +895,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile_kernel(TileArgs a) 
                 if (s_item[3]) {
                     s_item[0] = a.items[w];
                     s_item[1] = 0;
-                    s_item[2] = (a.n + 31) / 32;
+                    s_item[2] = a.item_cend ? a.item_cend[w] : (a.n + 31) / 32;
+                    s_item[4] = a.item_job ? a.item_job[w] : -1;
                 }
             } else {
                 s_item[0] = a.r_lo / kTileRows + blockIdx.x;
@@ -876,6 +908,16 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile_kernel(TileArgs a) 
         __syncthreads();
         if (!s_item[3]) break;
         const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
+        EmitJob ej = emit_job_of(a);
+        if (queued && s_item[4] >= 0) {
+            const int jb = s_item[4];
+            const int4 cj = a.cjob[jb];
+            ej.mmin = a.mmin + a.ctbl[jb];
+            ej.smin = a.smin + a.ctbl[jb];
+            ej.base = cj.x; ej.n = cj.y; ej.A = cj.z; ej.sd = cj.w;
+            ej.tag = (uint64_t)jb << 44;
+            ej.jcount = a.job_counter + jb;
+        }
         __syncthreads();   // every thread has read s_item
         const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
         // ---- row group set-up: rows of dense 32-read groups are left to
@@ -994,7 +1036,7 @@ __device__ __noinline__ uint4 hash_find4(const uint32_t* hkeys, const uint4* hma
 }
 
 template <int B>
-__device__ void tile_columns128(const TileArgs& a, const uint4* __restrict__ P,
+__device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint4* __restrict__ P,
                                 const uint32_t* hkeys, const uint4* hmask, bool any_high, int rg,
                                 const uint32_t* s_rows_ok, const int* s_tmin, const int* s_rowT,
                                 int cg0, int cg1) {
@@ -1060,7 +1102,7 @@ __device__ void tile_columns128(const TileArgs& a, const uint4* __restrict__ P,
         const int tc = col_ok ? a.tcount[c] : 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            finish_half<B>(a, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
+            finish_half<B>(a, ej, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
     }
 }
 
@@ -1071,7 +1113,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
     __shared__ uint32_t hkeys[kHashSlots];
     __shared__ uint4 hmask[kHashSlots];
     __shared__ int s_rowT[kRows128];
-    __shared__ int s_item[4];
+    __shared__ int s_item[5];
     __shared__ int s_tmin[4], s_any_high;
     __shared__ uint32_t s_rows_ok[4];
     const bool queued = a.items != nullptr;
@@ -1084,7 +1126,8 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
                 if (s_item[3]) {
                     s_item[0] = a.items[w];
                     s_item[1] = 0;
-                    s_item[2] = (a.n + 31) / 32;
+                    s_item[2] = a.item_cend ? a.item_cend[w] : (a.n + 31) / 32;
+                    s_item[4] = a.item_job ? a.item_job[w] : -1;
                 }
             } else {
                 // one row group per x block; the stage's column groups are
@@ -1100,6 +1143,16 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
         __syncthreads();
         if (!s_item[3]) break;
         const int rg = s_item[0], cg0 = s_item[1], cg1 = s_item[2];
+        EmitJob ej = emit_job_of(a);
+        if (queued && s_item[4] >= 0) {
+            const int jb = s_item[4];
+            const int4 cj = a.cjob[jb];
+            ej.mmin = a.mmin + a.ctbl[jb];
+            ej.smin = a.smin + a.ctbl[jb];
+            ej.base = cj.x; ej.n = cj.y; ej.A = cj.z; ej.sd = cj.w;
+            ej.tag = (uint64_t)jb << 44;
+            ej.jcount = a.job_counter + jb;
+        }
         __syncthreads();   // every thread has read s_item
         const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
         // ---- row group set-up: rows of dense 32-read groups are left to
@@ -1152,7 +1205,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
             }
         }
         __syncthreads();
-        tile_columns128<B>(a, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
+        tile_columns128<B>(a, ej, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
                            max(cg0, 4 * rg), cg1);
         __syncthreads();
     }
@@ -1609,6 +1662,21 @@ __global__ void kmer_decode_kernel(const uint64_t* __restrict__ keys,
     const uint64_t k = keys[i];
     const uint64_t rc = k % ((uint64_t)n * (uint64_t)n);
     pairs[i] = make_int2((int)(rc / (uint64_t)n), (int)(rc % (uint64_t)n));
+    if (dists) dists[i] = __uint_as_float(vals[i]);
+}
+
+// Cohort survivors after the sort: job in key bits 44 and up, then the
+// job's own stage key; pairs come out at cohort positions (base added).
+__global__ void kmer_decode_cohort_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                          int64_t count, const int4* __restrict__ cjob,
+                                          int2* __restrict__ pairs, float* __restrict__ dists) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint64_t k = keys[i];
+    const int4 cj = cjob[(int)(k >> 44)];
+    const uint64_t n = (uint64_t)cj.y;
+    const uint64_t rc = (k & ((1ull << 44) - 1)) % (n * n);
+    pairs[i] = make_int2(cj.x + (int)(rc / n), cj.x + (int)(rc % n));
     if (dists) dists[i] = __uint_as_float(vals[i]);
 }
 
@@ -2404,3 +2472,180 @@ int crispy_kmer_stream(crispy_ctx* ctx, crispy_sink sink, void* user) {
 }
 
 }  // extern "C"
+
+namespace crispy {
+
+// A cohort of k-mer jobs in one batched run (the server's cross-job
+// batching): the reads prepared on ctx are the jobs' reads back to back,
+// job c at positions [base, base + n) with base a multiple of 128.  One
+// persistent 128-row tile launch takes every job's row groups from one work
+// queue, each row group only over its own job's columns and with its job's
+// threshold tables; the survivors of all jobs are sorted at once (job
+// first, then each job's stage order) and decoded to cohort positions.
+// On return counts[c] holds job c's survivors, contiguous in job order in
+// the context's pair list.  CRISPY_E_UNSUPPORTED when the cohort needs a
+// path the cohort form does not take (K > 6, rows for the dense kernel,
+// more survivors than the device share): the caller then runs the jobs
+// one by one.
+int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::vector<int64_t>& counts) {
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer cohort before kmer_prepare");
+    const int n = j.n, K = j.k;
+    const int nj = (int)jobs.size();
+    if (K > 6 || nj < 1 || nj > 1024) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: K %d, %d jobs", K, nj);
+    const int levels = dense_levels_for(K);
+    if (levels <= 0) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: no shared-memory planes for K %d", K);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    ctx->stats = crispy_stats{};
+    ctx->ev_kmer.used = 0;
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_begin, s));
+    // per job: tile size, threshold tables (one block of max_t + 1 entries each)
+    std::vector<int4> cj(nj);
+    std::vector<int> tbl(nj);
+    std::vector<uint16_t> mmin_all, smin_all;
+    int key_hi = 0;
+    for (int c = 0; c < nj; ++c) {
+        const CohortJob& q = jobs[c];
+        const int A = crispy_array_dim(q.n);
+        if (A <= 0 || q.base % kRows128 != 0 || q.base + q.n > n || q.n > 65536)
+            return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: job %d (n %d at %d) unsupported", c, q.n, q.base);
+        const int sd = (q.n + A - 1) / A;
+        cj[c] = make_int4(q.base, q.n, A, sd);
+        std::vector<uint16_t> mm, sm;
+        build_mmin(q.thr, j.max_t, mm, sm);
+        tbl[c] = (int)mmin_all.size();
+        mmin_all.insert(mmin_all.end(), mm.begin(), mm.end());
+        smin_all.insert(smin_all.end(), sm.begin(), sm.end());
+        key_hi = std::max(key_hi, bits_for((uint64_t)sd * (sd + 1) / 2 * (uint64_t)q.n * (uint64_t)q.n));
+    }
+    if (key_hi > 44) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: stage keys of %d bits", key_hi);
+    // row groups of each job, each over its own job's column groups; rows of
+    // 32-read groups with too many high-level entries would need the dense
+    // kernel, which the cohort form does not run
+    std::vector<int> items, item_job, item_cend;
+    std::vector<std::pair<int64_t, int>> order;
+    for (int c = 0; c < nj; ++c) {
+        const int b = jobs[c].base, e = b + jobs[c].n;
+        for (int rg = b / kRows128; rg * kRows128 < e; ++rg) {
+            int64_t high = 0;
+            for (int r = rg * kRows128; r < std::min(e, rg * kRows128 + kRows128); ++r) high += j.h_cntmax[n + r];
+            if (high > kHashMaxKeys) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: row group %d needs the dense kernel", rg);
+            const int cend = (e + 31) / 32;
+            order.push_back({-(int64_t)(cend - 4 * rg), (int)items.size()});
+            items.push_back(rg);
+            item_job.push_back(c);
+            item_cend.push_back(cend);
+        }
+    }
+    // most columns first
+    std::sort(order.begin(), order.end());
+    std::vector<int> it2(items.size()), ij2(items.size()), ic2(items.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+        it2[i] = items[order[i].second];
+        ij2[i] = item_job[order[i].second];
+        ic2[i] = item_cend[order[i].second];
+    }
+    const size_t ni = it2.size();
+    const size_t tb = mmin_all.size();
+    // one device block: items | jobs | cends | cjob | tbl | job counters | head | tables
+    const size_t off_job = ni * 4, off_cend = off_job + ni * 4, off_cj = (off_cend + ni * 4 + 15) / 16 * 16;
+    const size_t off_tbl = off_cj + (size_t)nj * 16, off_cnt = (off_tbl + (size_t)nj * 4 + 7) / 8 * 8;
+    const size_t off_head = off_cnt + (size_t)(nj + 1) * 8, off_mm = off_head + 16;
+    const size_t off_sm = off_mm + tb * 2, off_dense = off_sm + tb * 2;
+    const size_t total_bytes = off_dense + (size_t)j.ngroups + 16;   // dense flags: all zero
+    CRISPY_TRY(ensure(ctx, j.work, total_bytes + 16));
+    std::vector<char> blob(total_bytes, 0);
+    std::memcpy(blob.data(), it2.data(), ni * 4);
+    std::memcpy(blob.data() + off_job, ij2.data(), ni * 4);
+    std::memcpy(blob.data() + off_cend, ic2.data(), ni * 4);
+    std::memcpy(blob.data() + off_cj, cj.data(), (size_t)nj * 16);
+    std::memcpy(blob.data() + off_tbl, tbl.data(), (size_t)nj * 4);
+    std::memcpy(blob.data() + off_mm, mmin_all.data(), tb * 2);
+    std::memcpy(blob.data() + off_sm, smin_all.data(), tb * 2);
+    char* d = j.work.as<char>();
+    CRISPY_CK(ctx, cudaMemcpyAsync(d, blob.data(), total_bytes, cudaMemcpyHostToDevice, s));
+    // survivors: the same capacity rule as a single run over all positions
+    const int64_t cap = std::min(kmer_device_pair_cap(), std::max<int64_t>(1 << 20, 16LL * n));
+    CRISPY_TRY(ensure(ctx, j.keys, (size_t)cap * 8));
+    CRISPY_TRY(ensure(ctx, j.keys_alt, (size_t)cap * 8));
+    CRISPY_TRY(ensure(ctx, j.vals, (size_t)cap * 4));
+    CRISPY_TRY(ensure(ctx, j.vals_alt, (size_t)cap * 4));
+    CRISPY_TRY(ensure(ctx, j.counter, 64));
+    CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
+    const uint32_t K4 = 1u << (2 * K);
+    const int B = std::max(8, bits_for((uint64_t)j.max_t));
+    TileFn tile = tile128_fn_for(B);
+    const size_t tsmem = ((size_t)levels * K4 + 32) * (kRows128 / 8);
+    CRISPY_CK(ctx, cudaFuncSetAttribute(tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+    TileArgs ta{};
+    ta.ent = j.ent.as<uint32_t>(); ta.gstart = j.gstart.as<int64_t>(); ta.gent = j.gent.as<int32_t>();
+    ta.tent = j.tent.as<uint16_t>(); ta.tstart = j.tstart.as<int64_t>(); ta.tgent = j.tgent.as<int32_t>();
+    ta.k65536 = 65536u; ta.k8 = 8u;
+    ta.hinfo = j.hinfo.as<uint32_t>(); ta.ngroups = j.ngroups;
+    ta.nhigh = j.cntmax.as<int32_t>() + n;
+    ta.tcount = j.t.as<int32_t>();
+    ta.dense_group = reinterpret_cast<const uint8_t*>(d + off_dense);   // no dense group (checked above)
+    ta.mmin = reinterpret_cast<const uint16_t*>(d + off_mm);
+    ta.smin = reinterpret_cast<const uint16_t*>(d + off_sm);
+    ta.n = n; ta.K4 = K4; ta.levels = levels; ta.A = crispy_array_dim(n); ta.stage_dim = 1;
+    ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
+    ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
+    ta.perm = nullptr; ta.olo = 0; ta.ohi = n;
+    ta.r_lo = 0; ta.r_hi = n; ta.c_lo = 0; ta.c_hi = n;
+    ta.items = reinterpret_cast<const int*>(d); ta.nitems = (int)ni;
+    ta.queue_head = reinterpret_cast<unsigned int*>(d + off_head);
+    ta.item_job = reinterpret_cast<const int*>(d + off_job);
+    ta.item_cend = reinterpret_cast<const int*>(d + off_cend);
+    ta.cjob = reinterpret_cast<const int4*>(d + off_cj);
+    ta.ctbl = reinterpret_cast<const int*>(d + off_tbl);
+    ta.job_counter = reinterpret_cast<unsigned long long*>(d + off_cnt);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile, kTileThreads, tsmem);
+    const int grid = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count, (int64_t)ni);
+    if (ni > 0) {
+        ev_begin(ctx, ctx->ev_kmer, s);
+        tile<<<grid, kTileThreads, tsmem, s>>>(ta);
+        ev_end(ctx, ctx->ev_kmer, s);
+        count_launch(ctx);
+        ctx->stats.kmer_launches += 1;
+    }
+    CRISPY_CK(ctx, cudaGetLastError());
+    unsigned long long total = 0;
+    std::vector<unsigned long long> jc(nj);
+    CRISPY_CK(ctx, cudaMemcpyAsync(&total, j.counter.ptr, 8, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(jc.data(), d + off_cnt, (size_t)nj * 8, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    if ((int64_t)total > cap) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: %llu survivors beyond the device share", total);
+    j.nsurv = (int64_t)total;
+    CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));
+    CRISPY_TRY(ensure(ctx, j.dists, (size_t)std::max<int64_t>(j.nsurv, 1) * 4));
+    CRISPY_TRY(ensure(ctx, j.sort_tmp, sort_tmp_bytes(j.nsurv)));
+    uint64_t* sk = nullptr;
+    uint32_t* sv = nullptr;
+    CRISPY_TRY(sort_u64_payload(ctx, s, j.keys.as<uint64_t>(), j.keys_alt.as<uint64_t>(), j.vals.as<uint32_t>(),
+                                j.vals_alt.as<uint32_t>(), j.nsurv, 44 + bits_for((uint64_t)nj), true, &sk, &sv,
+                                j.sort_tmp));
+    if (j.nsurv > 0) {
+        kmer_decode_cohort_kernel<<<(unsigned)((j.nsurv + 255) / 256), 256, 0, s>>>(
+            sk, sv, j.nsurv, ta.cjob, j.pairs.as<int2>(), j.dists.as<float>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+    }
+    j.spilled = false;
+    j.have_dists = true;
+    counts.assign(jc.begin(), jc.end());
+    CRISPY_CK(ctx, cudaEventRecord(ctx->t_end, s));
+    CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->t_begin, ctx->t_end);
+    ctx->stats.total_ms = tot;
+    ctx->stats.kmer_kernel_ms = ev_sum_ms(ctx->ev_kmer);
+    int64_t pairs = 0;
+    for (const CohortJob& q : jobs) pairs += (int64_t)q.n * (q.n - 1) / 2;
+    ctx->stats.kmer_pairs = pairs;
+    ctx->stats.kmer_survivors = j.nsurv;
+    return CRISPY_OK;
+}
+
+}  // namespace crispy

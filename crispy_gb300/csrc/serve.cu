@@ -6,16 +6,26 @@
 // slot.  Jobs queue in arrival order.  A worker that is free takes the
 // oldest queued job whose memory estimate fits the budget still unclaimed,
 // so a large job at the head does not stall small ones behind it; a job
-// larger than the whole budget fails at submit with CRISPY_E_OOM.  Each job
-// runs prepare -> kmer_run -> gen_prepare -> gen_run_from_kmer on its slot
-// with all intermediates in HBM, so jobs on different slots overlap on the
-// device; results are copied to host memory at completion.  Slots share no
-// device state, which is what keeps a job's result identical alone and in
-// a mix.
+// larger than the whole budget fails at submit with CRISPY_E_OOM.
+//
+// Small jobs share the kernels: with the oldest fitting job the worker
+// takes every other queued job of the same K and band that is small enough
+// and fits the budget (a cohort, up to kCohortReads reads in all).  The
+// cohort's reads go up as one read set, each job at a 128-aligned base; one
+// persistent k-mer tile launch takes all their row groups from one queue,
+// each over its own job's columns with its own threshold, and one set of
+// genDist bin launches aligns all their survivors; each job is then cut,
+// chunked and sorted on its own (kmer_run_cohort, gen_run_cohort).  A job
+// alone runs prepare -> kmer_run -> gen_prepare -> gen_run_from_kmer.
+// Everything stays in HBM until the chunks come back; jobs on different
+// slots overlap on the device.  A job's result is the same alone, in a
+// cohort and in a mix: per-pair work never depends on other jobs, and its
+// thresholds, stage order and chunks are its own.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -27,6 +37,17 @@
 namespace {
 
 using clock_type = std::chrono::steady_clock;
+
+// Cohort limits: members of at most kCohortJobReads reads (larger jobs run
+// alone), at most kCohortReads reads and kCohortJobs jobs per cohort.
+constexpr int kCohortJobReads = 16384;
+constexpr int kCohortReads = 65536;
+constexpr int kCohortJobs = 64;
+
+bool cohorts_enabled() {
+    const char* e = std::getenv("CRISPY_SERVE_COHORT");
+    return !(e && e[0] == '0');
+}
 
 struct Job {
     uint64_t id = 0;
@@ -44,6 +65,10 @@ struct Job {
     std::vector<int> chunk_id;
     std::vector<std::vector<uint32_t>> chunk_pairs;
     std::vector<std::vector<float>> chunk_dists;
+    // memory of the run that served the job (alone or in a cohort): bytes
+    // reserved at admission for all its jobs, bytes the run asked for
+    size_t run_reserved = 0, run_needed = 0;
+    int cohort_size = 1;
 };
 
 // Device bytes a job needs at its peak (generous; the server only uses it
@@ -103,6 +128,101 @@ struct crispy_server {
         return nullptr;
     }
 
+    bool cohort_member(const Job* j) const {
+        return cohorts_enabled() && j->k >= 2 && j->k <= 6 && j->n >= 10 && j->n <= kCohortJobReads;
+    }
+
+    // With `first` taken: the other queued jobs that can share its run.
+    std::vector<Job*> take_cohort(Job* first) {   // caller holds mu
+        std::vector<Job*> c{first};
+        if (!cohort_member(first)) return c;
+        auto aligned = [](int n) { return (n + 127) / 128 * 128; };
+        int reads = aligned(first->n);
+        size_t mem = first->mem;
+        for (auto it = queue.begin(); it != queue.end() && (int)c.size() < kCohortJobs;) {
+            Job* j = *it;
+            if (cohort_member(j) && j->k == first->k && j->band == first->band &&
+                reads + aligned(j->n) <= kCohortReads && claimed + mem + j->mem <= budget) {
+                c.push_back(j);
+                reads += aligned(j->n);
+                mem += j->mem;
+                it = queue.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        return c;
+    }
+
+    // Several jobs in one run: reads back to back at 128-aligned bases, with
+    // reads of K - 1 symbols (no k-mer, no pair) filling the gaps.
+    int run_cohort(crispy_ctx* c, const std::vector<Job*>& js) {
+        const int k = js[0]->k;
+        std::vector<crispy::CohortJob> kj(js.size()), gj(js.size());
+        std::string bases;
+        std::vector<int64_t> off;
+        std::vector<int32_t> len;
+        const std::string pad((size_t)(k - 1), 'A');
+        for (size_t q = 0; q < js.size(); ++q) {
+            const Job* j = js[q];
+            kj[q].base = (int)len.size();
+            kj[q].n = j->n;
+            kj[q].thr = crispy_default_threshold(j->n, j->kthr, 0);
+            gj[q] = kj[q];
+            gj[q].thr = crispy_default_threshold(j->n, j->gthr, 1);
+            gj[q].sink = sink_to_job;
+            gj[q].user = js[q];
+            for (int i = 0; i < j->n; ++i) {
+                off.push_back((int64_t)bases.size());
+                len.push_back(j->len[i]);
+                bases.append(j->bases, (size_t)j->off[i], (size_t)j->len[i]);
+            }
+            while (len.size() % 128 != 0) {
+                off.push_back((int64_t)bases.size());
+                len.push_back(k - 1);
+                bases += pad;
+            }
+        }
+        int rc = crispy_kmer_prepare(c, bases.data(), off.data(), len.data(), (int)len.size(), k);
+        std::vector<int64_t> kc, gc;
+        if (rc == CRISPY_OK) rc = crispy::kmer_run_cohort(c, kj, kc);
+        if (rc == CRISPY_OK) rc = crispy_gen_prepare_from_kmer(c);
+        if (rc == CRISPY_OK) rc = crispy::gen_run_cohort(c, gj, kc, js[0]->band, gc);
+        if (rc == CRISPY_OK)
+            for (size_t q = 0; q < js.size(); ++q) js[q]->kmer_pairs = kc[q];
+        return rc;
+    }
+
+    // Runs one job or a cohort on slot context c; fills each job's status.
+    void run_jobs(crispy_ctx* c, const std::vector<Job*>& js) {
+        c->run_epoch++;
+        c->run_need = 0;
+        size_t reserved = 0;
+        for (Job* j : js) reserved += j->mem;
+        bool done = false;
+        if (js.size() > 1) {
+            const int rc = run_cohort(c, js);
+            if (rc == CRISPY_OK) {
+                for (Job* j : js) j->status = CRISPY_OK;
+                done = true;
+            } else {
+                // the cohort form declined (or failed): every job alone, from scratch
+                for (Job* j : js) {
+                    j->chunk_id.clear(); j->chunk_pairs.clear(); j->chunk_dists.clear();
+                    j->gen_pairs = 0; j->kmer_pairs = 0;
+                }
+            }
+        }
+        if (!done)
+            for (Job* j : js) run_job(c, j);
+        const size_t need = c->run_need;
+        for (Job* j : js) {
+            j->run_reserved = reserved;
+            j->run_needed = need;
+            j->cohort_size = done ? (int)js.size() : 1;
+        }
+    }
+
     void run_job(crispy_ctx* c, Job* j) {
         int rc = crispy_kmer_prepare(c, j->bases.data(), j->off.data(), j->len.data(), j->n, j->k);
         const float kt = crispy_default_threshold(j->n, j->kthr, 0);
@@ -123,22 +243,30 @@ struct crispy_server {
             Job* j = nullptr;
             work_cv.wait(lk, [&] { return stopping || (j = take_fitting()) != nullptr; });
             if (!j) return;   // stopping
-            claimed += j->mem;
-            j->state = CRISPY_JOB_RUNNING;
+            const std::vector<Job*> js = take_cohort(j);
+            size_t mem = 0;
+            for (Job* x : js) {
+                mem += x->mem;
+                x->state = CRISPY_JOB_RUNNING;
+            }
+            claimed += mem;
             lk.unlock();
-            run_job(c, j);
+            run_jobs(c, js);
             // give memory back when this slot holds more than its share
             size_t in_use = 0;
             crispy_ctx_mem_in_use(c, &in_use);
             if (in_use > budget / ctx.size()) crispy_ctx_trim(c);
             lk.lock();
-            claimed -= j->mem;
-            j->t_done = clock_type::now();
-            j->state = j->status == CRISPY_OK ? CRISPY_JOB_DONE : CRISPY_JOB_FAILED;
-            if (j->status == CRISPY_OK) {
-                latencies_ms.push_back(
-                    std::chrono::duration<double, std::milli>(j->t_done - j->t_submit).count());
-                pairs_done += (int64_t)j->n * (j->n - 1) / 2;
+            claimed -= mem;
+            const auto now = clock_type::now();
+            for (Job* x : js) {
+                x->t_done = now;
+                x->state = x->status == CRISPY_OK ? CRISPY_JOB_DONE : CRISPY_JOB_FAILED;
+                if (x->status == CRISPY_OK) {
+                    latencies_ms.push_back(
+                        std::chrono::duration<double, std::milli>(x->t_done - x->t_submit).count());
+                    pairs_done += (int64_t)x->n * (x->n - 1) / 2;
+                }
             }
             done_cv.notify_all();
             work_cv.notify_all();
@@ -284,6 +412,39 @@ int crispy_server_result(crispy_server* s, uint64_t id, crispy_sink sink, void* 
     }
     delete j;
     return rc;
+}
+
+int crispy_server_job_memory(crispy_server* s, uint64_t id, size_t* reserved, size_t* needed,
+                             int* cohort_size) {
+    if (!s) return CRISPY_E_INPUT;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) {
+        s->err = "unknown job id";
+        return CRISPY_E_INPUT;
+    }
+    const Job* j = it->second;
+    if (j->state != CRISPY_JOB_DONE) {
+        s->err = "job not finished";
+        return CRISPY_E_STATE;
+    }
+    if (reserved) *reserved = j->run_reserved;
+    if (needed) *needed = j->run_needed;
+    if (cohort_size) *cohort_size = j->cohort_size;
+    return CRISPY_OK;
+}
+
+int crispy_server_job_bytes(const int32_t* lengths, int n, int k, size_t* bytes) {
+    if (!lengths || n <= 0 || !bytes) return CRISPY_E_INPUT;
+    Job j;
+    j.n = n;
+    j.k = k;
+    j.len.assign(lengths, lengths + n);
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) total += std::max(0, lengths[i]);
+    j.bases.assign((size_t)total, 'A');
+    *bytes = estimate_bytes(j);
+    return CRISPY_OK;
 }
 
 int crispy_server_cancel(crispy_server* s, uint64_t id) {

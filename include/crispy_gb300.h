@@ -369,6 +369,11 @@ int crispy_ctx_trim(crispy_ctx* ctx);
  * admitted as slots and memory free up and their kernels overlap on the
  * device.  Each job runs kmerDist -> genDist with every intermediate
  * resident in HBM, and its result is the same chunk list a lone run gives.
+ * Small jobs of the same K and band that are queued together run as one
+ * cohort: one persistent k-mer launch over all their row groups (each over
+ * its own columns, with its own threshold) and one set of genDist launches
+ * over all their survivors, then per-job thresholds, chunks and sorts
+ * (CRISPY_SERVE_COHORT=0 runs every job alone).
  * Submit, wait, result and cancel are thread-safe. */
 #define CRISPY_JOB_QUEUED    0
 #define CRISPY_JOB_RUNNING   1
@@ -396,6 +401,15 @@ int crispy_server_result(crispy_server* srv, uint64_t job_id, crispy_sink sink,
                          void* user, int64_t* kmer_pairs, int64_t* gen_pairs);
 /* Cancels a queued job (a running one finishes). */
 int crispy_server_cancel(crispy_server* srv, uint64_t job_id);
+/* Memory of the run that served a finished job (before its result is
+ * taken): *reserved = device bytes the admission reserved for all the jobs
+ * of that run (the job alone, or its cohort), *needed = device bytes the
+ * run asked for at its peak, *cohort_size = jobs that shared the run. */
+int crispy_server_job_memory(crispy_server* srv, uint64_t job_id, size_t* reserved,
+                             size_t* needed, int* cohort_size);
+/* The device bytes the server's admission reserves for a job of n reads of
+ * these lengths at K = k (no device work). */
+int crispy_server_job_bytes(const int32_t* lengths, int n, int k, size_t* bytes);
 /* Submit-to-finish latency percentiles (ms) over finished jobs, finished
  * job count and pairs processed (sum of n(n-1)/2). */
 int crispy_server_stats(crispy_server* srv, double* p50_ms, double* p99_ms,

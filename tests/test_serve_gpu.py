@@ -135,3 +135,48 @@ def test_mixed_k_jobs(engine):
     chunks = engine.gen_run_from_kmer(band, cg.default_threshold(n, -1.0, 1), cg.MODE_BATCHED)
     _same((kp, chunks), alone[1])
     assert kp > 0 and sum(len(c[2]) for c in chunks) > 0
+
+
+def _engine_run(eng, buf, offs, lens, k=6, band=10):
+    n = len(lens)
+    eng.kmer_prepare(buf, offs, lens, k)
+    kp = eng.kmer_run(cg.default_threshold(n, -1.0, 0), cg.MODE_BATCHED, False)
+    eng.gen_prepare_from_kmer()
+    return kp, eng.gen_run_from_kmer(band, cg.default_threshold(n, -1.0, 1), cg.MODE_BATCHED)
+
+
+def test_cohort_jobs_bit_exact_and_within_reservation():
+    """Jobs queued behind a running one share one run (a cohort: one k-mer
+    launch over all their row groups, one set of genDist launches over all
+    their survivors); each job's result equals a lone Engine run, and every
+    run asks for no more device memory than admission reserved for it."""
+    sizes = (3000, 500, 1200, 64, 2048, 777, 5000, 129, 16, 4096)
+    jobs = [_job(n, 900 + i) for i, n in enumerate(sizes)]
+    jobs.append(_job(1500, 77, dist="uniform", a=300, b=500, root=520))
+    with cg.Engine(0) as eng:
+        want = [_engine_run(eng, *j) for j in jobs]
+    with cg.Server(0, 0, 1) as srv:
+        ids = [srv.submit(*j) for j in jobs]   # all but the first queue behind it
+        cohort = []
+        for i, jid in enumerate(ids):
+            assert srv.wait(jid) == cg.JOB_DONE
+            mem = srv.job_memory(jid)
+            assert 0 < mem["needed"] <= mem["reserved"], (i, mem)
+            cohort.append(mem["cohort_size"])
+            _same(srv.result(jid), want[i])
+    assert max(cohort) > 1, "no cohort formed"
+
+
+def test_admission_estimate_bounds_each_run():
+    """A job alone: the device bytes its run asks for stay within the
+    estimate the server admits it with (crispy_server_job_bytes)."""
+    with cg.Server(0, 0, 1) as srv:
+        for n, seed in ((500, 1), (6000, 2), (20000, 3), (48000, 4)):
+            buf, offs, lens = _job(n, 4000 + seed)
+            jid = srv.submit(buf, offs, lens)
+            assert srv.wait(jid) == cg.JOB_DONE
+            mem = srv.job_memory(jid)
+            assert mem["cohort_size"] == 1
+            assert mem["reserved"] == cg.server_job_bytes(lens, 6)
+            assert 0 < mem["needed"] <= mem["reserved"], (n, mem)
+            srv.result(jid)
