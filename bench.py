@@ -453,6 +453,8 @@ def run_ours(args, dist, ws, rank, local):
     line["autotune"] = tune
     if not args.no_serve:
         line["serve"] = serve_bench(args, local)
+    if rank == 0 and not args.no_configs:
+        line["configs"] = config_bench(args, local)
     if rank == 0 and not args.no_pre:
         line["preprocess"] = preprocess_bench(args, local)
         line["aveclust"] = clust_bench(args, local, chunks, n)
@@ -469,6 +471,72 @@ def run_ours(args, dist, ws, rank, local):
                                         "run's rate is the sample's"}
     eng.close()
     return line
+
+
+def config_bench(args, local: int) -> dict:
+    """The other benchmark read sets, timed beside the headline one:
+    plain_20k (20,000 reads, k = 6, band 10) in the batched, staged and plain
+    forms, and the stress set (496,820 reads, k = 8, band 5) in the batched
+    and staged forms (its plain form takes about a minute per step).  Per
+    form: CUDA-event step time over a few steps (L2 flushed before each) and
+    the all-pairs rate; the forms' outputs are compared bit for bit."""
+    import torch
+
+    import crispy_gb300 as cg
+
+    out = {}
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    names = {cg.MODE_BATCHED: "batched", cg.MODE_STAGED: "staged", cg.MODE_PLAIN: "plain"}
+    for name, forms in (("plain_20k", (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)),
+                        ("stress_500k", (cg.MODE_BATCHED, cg.MODE_STAGED))):
+        _, k, band = WORKLOADS[name]
+        reads = synth.make_read_set(name)
+        buf, offs, lens = synth.pack_reads(reads)
+        n = len(lens)
+        n_pairs = n * (n - 1) // 2
+        thr_k = cg.default_threshold(n, -1.0, 0)
+        thr_g = cg.default_threshold(n, -1.0, 1)
+        res = {"n_reads": n, "k": k, "band": band}
+        outputs = {}
+        with cg.Engine(local, timing=True) as eng:
+            stream = torch.cuda.Stream()
+            eng.set_stream(stream.cuda_stream)
+            eng.kmer_prepare(buf, offs, lens, k)
+            eng.gen_prepare_from_kmer()
+            for mode in forms:
+                steps, warm = (3, 2) if mode == cg.MODE_BATCHED else (2, 1) if mode == cg.MODE_STAGED else (1, 0)
+                times, last = [], None
+                for it in range(warm + steps):
+                    with torch.cuda.stream(stream):
+                        flush.zero_()
+                        a = torch.cuda.Event(enable_timing=True)
+                        b = torch.cuda.Event(enable_timing=True)
+                        a.record(stream)
+                    eng.kmer_rebuild()
+                    kp = eng.kmer_run(thr_k, mode, False)
+                    chunks = eng.gen_run_from_kmer(band, thr_g, mode)
+                    with torch.cuda.stream(stream):
+                        b.record(stream)
+                    b.synchronize()
+                    if it >= warm:
+                        times.append(a.elapsed_time(b))
+                    last = (kp, chunks)
+                ms = float(np.mean(times))
+                res[names[mode]] = {"ms_per_step": ms, "value": n_pairs / (ms / 1e3), "steps": steps}
+                outputs[names[mode]] = last
+        b_kp, b_ch = outputs["batched"]
+        res["kmer_survivors"] = b_kp
+        res["gen_survivors"] = int(sum(len(c[2]) for c in b_ch))
+        for label, (kp, ch) in outputs.items():
+            if label == "batched":
+                continue
+            res[f"{label}_identical_to_batched"] = bool(
+                kp == b_kp and len(ch) == len(b_ch) and
+                all(np.array_equal(x[1], y[1]) and np.array_equal(x[2].view(np.uint32), y[2].view(np.uint32))
+                    for x, y in zip(ch, b_ch)))
+            res[f"batched_over_{label}"] = res[label]["ms_per_step"] / res["batched"]["ms_per_step"]
+        out[name] = res
+    return out
 
 
 def preprocess_bench(args, local: int) -> dict:
@@ -543,7 +611,9 @@ def clust_bench(args, local: int, chunks, n: int) -> dict:
         t0 = time.perf_counter()
         st = cg.aveclust(ch, n, os.path.join(td, "wl"))
         out[args.workload] = {"reads": n, "edges": int(sum(len(c[1]) for c in ch)),
-                              "merges": int(st["merges"]), "ms": (time.perf_counter() - t0) * 1e3}
+                              "merges": int(st["merges"]), "ms": (time.perf_counter() - t0) * 1e3,
+                              "phases_ms": {"edges": st["ms_edges"], "update_min": st["ms_update"],
+                                            "merges": st["ms_merges"], "levels_and_output": st["ms_output"]}}
         reads = synth.make_read_set("plain_20k")
         buf, offs, lens = synth.pack_reads(reads)
         m = len(lens)
@@ -757,7 +827,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-pre", action="store_true")
-    ap.add_argument("--serve-jobs", type=int, default=60)
+    ap.add_argument("--no-configs", action="store_true", help="skip the plain_20k / stress_500k lines")
+    ap.add_argument("--serve-jobs", type=int, default=240)
     ap.add_argument("--serve-slots", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

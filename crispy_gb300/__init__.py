@@ -59,7 +59,9 @@ _i64p = C.POINTER(C.c_int64)
 
 class ClustStats(C.Structure):
     _fields_ = [("pairs_read", C.c_int64), ("merges", C.c_int64), ("roots", C.c_int32),
-                ("singletons", C.c_int32), ("end_level", C.c_float), ("report", C.c_char * 2048)]
+                ("singletons", C.c_int32), ("end_level", C.c_float), ("report", C.c_char * 2048),
+                ("ms_edges", C.c_double), ("ms_update", C.c_double), ("ms_merges", C.c_double),
+                ("ms_output", C.c_double)]
 
 
 class PreOpts(C.Structure):
@@ -573,7 +575,9 @@ def aveclust(chunks, num_reads: int, out_base: str, end_level: float = -1.0,
     if rc != OK:
         raise CrispyError(rc, lib.crispy_last_error(None).decode())
     return {"pairs_read": st.pairs_read, "merges": st.merges, "roots": st.roots,
-            "singletons": st.singletons, "end_level": st.end_level, "report": st.report.decode()}
+            "singletons": st.singletons, "end_level": st.end_level, "report": st.report.decode(),
+            "ms_edges": st.ms_edges, "ms_update": st.ms_update, "ms_merges": st.ms_merges,
+            "ms_output": st.ms_output}
 
 
 def sparsecut(in_base: str, num_reads: int, cutoffs) -> dict:

@@ -31,6 +31,7 @@
 // (aveclust.cpp:244-305), an order this code cannot and does not copy: it
 // visits roots by ascending node ID.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -555,7 +556,13 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
     unsigned long long max_edges = (unsigned long long)num_reads;
     int64_t read_pairs = 0;
     char line[96];
+    using tclock = std::chrono::steady_clock;
+    auto ms_since = [](tclock::time_point t) {
+        return std::chrono::duration<double, std::milli>(tclock::now() - t).count();
+    };
+    double ms_edges = 0, ms_update = 0, ms_merges = 0;
     while (!C.all_loaded) {
+        const auto t_edges = tclock::now();
         if (C.total_edges < max_edges) {
             while (C.total_edges <= max_edges && !heads.empty()) {
                 std::pop_heap(heads.begin(), heads.end(), HeadAfter());
@@ -579,7 +586,11 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
             if ((double)max_edges > kUpperEdges) C.end_level = C.lambda;
         }
         if (heads.empty()) C.all_loaded = true;
+        ms_edges += ms_since(t_edges);
+        const auto t_update = tclock::now();
         C.update_all_min();
+        ms_update += ms_since(t_update);
+        const auto t_merges = tclock::now();
         float min_in = C.inexact.min();
         int mi = C.exact.argmin();
         float min_ex = C.exact[mi];
@@ -593,8 +604,10 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
             mi = C.exact.argmin();
             min_ex = C.exact[mi];
         }
+        ms_merges += ms_since(t_merges);
     }
     if (fo) { std::fclose(fo); std::fclose(fo1); }
+    const auto t_output = tclock::now();
 
     // roots and singletons (aveclust.cpp:944-955), then printClusters at
     // the levels the reference's float loop visits
@@ -626,6 +639,10 @@ extern "C" int crispy_aveclust(const uint32_t* const* pairs, const float* const*
         stats->singletons = (int32_t)orphans.size();
         stats->end_level = C.end_level;
         std::snprintf(stats->report, sizeof stats->report, "%s", report.c_str());
+        stats->ms_edges = ms_edges;
+        stats->ms_update = ms_update;
+        stats->ms_merges = ms_merges;
+        stats->ms_output = ms_since(t_output);
     }
     return CRISPY_OK;
 }

@@ -44,10 +44,10 @@
 // registers r + 1 / r - 1 of the same lane, so only the lane's edge
 // register crosses lanes (one shuffle per step for keys, A and B).
 // Symbols: 2 bits each, first symbol in the low bits, in shared memory
-// behind a zero pad; per block of 32 (R > 5: 16) steps a lane cuts its slots' 16-symbol
+// behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
 // windows out of four 32-symbol windows (consecutive slots of a lane read
-// windows one symbol apart) and folds them into 16 (8) mismatch flags per
-// slot and parity.
+// windows one symbol apart) and folds them into 8 mismatch flags per slot
+// and parity.
 // Border: a slot hosts one diagonal d per parity, so it enters the matrix
 // once, at s = |d|, as a boundary cell (row 0 or column 0).  Every slot's cap
 // starts closed (key 8); the two boundary cells of a step (d = s and d = -s)
@@ -68,11 +68,7 @@ constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
 constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
-constexpr int kSteps = 16;           // steps per flag word: 8 cells per slot and parity
-// Blocks of 32 steps (two flag words per slot and parity) where the
-// registers allow, 16 steps above R = 5.
-template <int R>
-constexpr int block_steps() { return R <= 5 ? 32 : 16; }
+constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
 constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
 constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
 constexpr uint32_t kLo = 0x00010001u;   // 1 in each half
@@ -113,12 +109,11 @@ __device__ __forceinline__ Mul make_mul(const int* o) {
 
 template <int R>
 struct St {
-    uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
+    uint32_t K[2][R];    // by step parity: (K | 3) + 28, the base of the diagonal candidate two steps on
     uint32_t U[R], F[R]; // up / left candidates the last step sent
     uint32_t A[2][R];    // doubled diagonal-move counters by parity
     uint32_t B[2][R];    // doubled mismatch counters by parity
     uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
-    uint32_t MW2[2][R];  // the next 8 steps' flags (32-step blocks)
     uint32_t CP[2][R];   // per half: 0xFFFF in band, kOut outside
 };
 
@@ -152,8 +147,7 @@ __device__ __forceinline__ void window32(const uint32_t* sm, int pos, uint32_t& 
 // parity-0 cell at the block start, d0 = 2q - kb.  The lane's R slots of a
 // half are consecutive, q = qb + r: read1 windows start at J - r, read2
 // windows at I + r, all inside one 32-symbol window per read.  A flag sits
-// at bit 2k of its half (cells 8..15 of a 32-step block in MW2).  A
-// finished pair's caps close.
+// at bit 2k of its half.  A finished pair's caps close.
 template <int G, int R>
 __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
                                             int s0, const Pair16& pc, bool finished) {
@@ -180,10 +174,6 @@ __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, cons
     for (int r = 0; r < R; ++r) {
         st.MW[0][r] = __byte_perm(f0[0][r], f0[1][r], 0x5410);
         st.MW[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x5410);
-        if (block_steps<R>() == 32) {   // flags of cells 8..15
-            st.MW2[0][r] = __byte_perm(f0[0][r], f0[1][r], 0x7632);
-            st.MW2[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x7632);
-        }
         if (finished) { st.CP[0][r] = kOut2; st.CP[1][r] = kOut2; }
     }
 }
@@ -256,13 +246,13 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
     if (hr) {
         uint32_t key, ab;
         take<G, R, P>(st, qr, gl, key, ab);
-        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        const int m = ((int)(key & ~3u) - 28 - 4 * s - kBase) >> 2;   // key = (K | 3) + 28
         if (m >= col.m) { col.m = m; col.ab = ab; col.at = jr; }
     }
     if (hc) {
         uint32_t key, ab;
         take<G, R, P>(st, qc, gl, key, ab);
-        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        const int m = ((int)(key & ~3u) - 28 - 4 * s - kBase) >> 2;   // key = (K | 3) + 28
         if (m >= row.m) { row.m = m; row.ab = ab; row.at = ic; }
     }
 }
@@ -313,8 +303,7 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         }
         const uint32_t mm = st.MW[P][r] & kLo;
         st.MW[P][r] = __umulhi(st.MW[P][r], 0x40000000u);   // >> 2 on the multiplier
-        const uint32_t od = (st.K[P][r] | 0x00030003u) * mu.one + 0x001C001Cu;
-        const uint32_t kd = mm * mu.n36 + od;
+        const uint32_t kd = mm * mu.n36 + st.K[P][r];   // K[P] holds (K | 3) + 28
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
         const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
@@ -340,7 +329,10 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             A = (ad & m1) | (at & ~m1);
             B = (bd & m1) | (bt & ~m1);
         }
-        st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
+        // the diagonal candidate's base two steps on, (K | 3) + 28 = K - t + 31,
+        // on the multiplier pipe
+        st.K[P][r] = x2 * mu.neg1 + (x1 * mu.neg1 + (K * mu.one + 0x001F001Fu));
+        st.A[P][r] = A; st.B[P][r] = B;
     }
     if (kMode != kClean) {
         const bool near = (unsigned)(s - pc.tw[0]) < 2u * R || (unsigned)(s - pc.tw[1]) < 2u * R ||
@@ -353,11 +345,7 @@ template <int G, int R, int kMode>
 __device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu,
                                         uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
 #pragma unroll 1
-    for (int t = 0; t < block_steps<R>(); t += 2) {
-        if (block_steps<R>() == 32 && t == kSteps) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) { st.MW[0][r] = st.MW2[0][r]; st.MW[1][r] = st.MW2[1][r]; }
-        }
+    for (int t = 0; t < kSteps; t += 2) {
         step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, sel0, sel1, col, row);
         step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, sel0, sel1, col, row);
     }
@@ -440,9 +428,10 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         St<R> st;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
+            // K[] holds (K | 3) + 28, here that of a closed cell (key 8)
+            st.K[0][r] = (kOut + 31) * kLo; st.K[1][r] = (kOut + 31) * kLo; st.U[r] = kOut2; st.F[r] = kOut2;
             st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
-            st.MW[0][r] = 0; st.MW[1][r] = 0; st.MW2[0][r] = 0; st.MW2[1][r] = 0;
+            st.MW[0][r] = 0; st.MW[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
             st.CP[0][r] = kOut2; st.CP[1][r] = kOut2;
         }
@@ -456,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         }
         const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(0, s_end + pc.shift));
         const int clean_hi = 2 * min(pc.l1, pc.l2) - pc.kb - 1;
-        constexpr int kBlock = block_steps<R>();
+        constexpr int kBlock = kSteps;
         for (int t0 = 0; t0 <= t_end; t0 += kBlock) {
             const int s0 = t0 - pc.shift;
             const bool finished = s0 > s_end;

@@ -280,6 +280,10 @@ typedef struct crispy_clust_stats {
     int32_t singletons;   /* reads never merged */
     float end_level;      /* the final endLevel (lambda once the edge cap was hit) */
     char report[2048];    /* printClusters' "Dist: ... numOTUs ..." lines */
+    /* aveclust only: host time (ms) in its phases -- taking edges from the
+     * chunks and absorbing them into link maps, the per-round minimum
+     * updates, the merges, cluster levels and file output */
+    double ms_edges, ms_update, ms_merges, ms_output;
 } crispy_clust_stats;
 
 /* Sparse average-linkage clustering (aveclust's main loop,
