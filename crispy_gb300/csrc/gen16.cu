@@ -109,7 +109,7 @@ __device__ __forceinline__ Mul make_mul(const int* o) {
 
 template <int R>
 struct St {
-    uint32_t K[2][R];    // by step parity: (K | 3) + 28, the base of the diagonal candidate two steps on
+    uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
     uint32_t U[R], F[R]; // up / left candidates the last step sent
     uint32_t A[2][R];    // doubled diagonal-move counters by parity
     uint32_t B[2][R];    // doubled mismatch counters by parity
@@ -246,13 +246,13 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
     if (hr) {
         uint32_t key, ab;
         take<G, R, P>(st, qr, gl, key, ab);
-        const int m = ((int)(key & ~3u) - 28 - 4 * s - kBase) >> 2;   // key = (K | 3) + 28
+        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
         if (m >= col.m) { col.m = m; col.ab = ab; col.at = jr; }
     }
     if (hc) {
         uint32_t key, ab;
         take<G, R, P>(st, qc, gl, key, ab);
-        const int m = ((int)(key & ~3u) - 28 - 4 * s - kBase) >> 2;   // key = (K | 3) + 28
+        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
         if (m >= row.m) { row.m = m; row.ab = ab; row.at = ic; }
     }
 }
@@ -303,7 +303,8 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         }
         const uint32_t mm = st.MW[P][r] & kLo;
         st.MW[P][r] = __umulhi(st.MW[P][r], 0x40000000u);   // >> 2 on the multiplier
-        const uint32_t kd = mm * mu.n36 + st.K[P][r];   // K[P] holds (K | 3) + 28
+        const uint32_t od = (st.K[P][r] | 0x00030003u) * mu.one + 0x001C001Cu;
+        const uint32_t kd = mm * mu.n36 + od;
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
         const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
@@ -329,10 +330,7 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             A = (ad & m1) | (at & ~m1);
             B = (bd & m1) | (bt & ~m1);
         }
-        // the diagonal candidate's base two steps on, (K | 3) + 28 = K - t + 31,
-        // on the multiplier pipe
-        st.K[P][r] = x2 * mu.neg1 + (x1 * mu.neg1 + (K * mu.one + 0x001F001Fu));
-        st.A[P][r] = A; st.B[P][r] = B;
+        st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
     }
     if (kMode != kClean) {
         const bool near = (unsigned)(s - pc.tw[0]) < 2u * R || (unsigned)(s - pc.tw[1]) < 2u * R ||
@@ -428,8 +426,7 @@ __global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16
         St<R> st;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            // K[] holds (K | 3) + 28, here that of a closed cell (key 8)
-            st.K[0][r] = (kOut + 31) * kLo; st.K[1][r] = (kOut + 31) * kLo; st.U[r] = kOut2; st.F[r] = kOut2;
+            st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
             st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
