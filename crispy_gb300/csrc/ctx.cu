@@ -246,6 +246,8 @@ int crispy_ctx_create(int device, crispy_ctx** out) {
         return fail(nullptr, CRISPY_E_DEVICE, "stream: %s", cudaGetErrorString(e));
     }
     for (auto& s : ctx->side) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
+    for (auto& e : ctx->join_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     ctx->stream = ctx->own_stream;
     cudaEventCreate(&ctx->t_begin);
     cudaEventCreate(&ctx->t_end);
@@ -309,6 +311,8 @@ int crispy_ctx_destroy(crispy_ctx* ctx) {
     }
     cudaEventDestroy(ctx->t_begin);
     cudaEventDestroy(ctx->t_end);
+    cudaEventDestroy(ctx->fork_ev);
+    for (auto e : ctx->join_ev) cudaEventDestroy(e);
     for (auto& s : ctx->side) cudaStreamDestroy(s);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;

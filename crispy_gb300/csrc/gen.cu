@@ -562,15 +562,20 @@ constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 constexpr int kBinSlots[] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256};
 constexpr int kNumBins = sizeof(kBinSlots) / sizeof(kBinSlots[0]);
 __constant__ int c_bin_slots[kNumBins] = {0, 8, 16, 32, 40, 48, 56, 64, 80, 96, 128, 192, 256};
+// the sort key holds the order-bin (up to 2 * kNumBins) in 5 bits
+static_assert(2 * kNumBins < 32, "order-bins overflow the 18-bit sort key");
 
 // Per-pair classification for the launch plan, on the device.  Order-bin
 // ob: band-slot bin b (1..12) for a pair the 16-bit kernel takes (L1 + L2
 // <= kGen16MaxSum), kNumBins + b for a longer pair (32-bit kernels), and
 // 2 * kNumBins for the wide-band kernel (last).  Sort key: order-bin, then
-// longer pairs first.  stats: [0] cells, [1] max kBand, [kStatBins + ob]
-// pairs of order-bin ob, [kStatWindows + 2w] widest band-slot bin of load
-// window w (kNumBins = wide), [kStatWindows + 2w + 1] 1 when the window
-// holds a pair beyond the 16-bit range.
+// longer sweeps first (the anti-diagonal of the pair's last in-band cell of
+// the last row or column, where the register kernels stop), so that the
+// pairs of a warp, which runs until its longest sweep ends, end together.
+// stats: [0] cells, [1] max kBand, [kStatBins + ob] pairs of order-bin ob,
+// [kStatWindows + 2w] widest band-slot bin of load window w (kNumBins =
+// wide), [kStatWindows + 2w + 1] 1 when the window holds a pair beyond the
+// 16-bit range.
 constexpr int kStatBins = 2, kStatWindows = 32;
 constexpr int kWideOrderBin = 2 * kNumBins;
 __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t count,
@@ -593,7 +598,10 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
         wb = bin == 0 ? nbins : bin;
         ob = bin == 0 ? 2 * nbins : bin + lng * nbins;   // wide pairs sort last
         if (keys) {
-            keys[p] = ((uint32_t)ob << 13) | (uint32_t)(8191 - (l1 + l2));
+            int se = 0;
+            if (max(1, l2 - kb) <= min(l1, l2 + kb)) se = l2 + min(l1, l2 + kb);
+            if (max(1, l1 - kb) <= min(l2, l1 + kb)) se = max(se, l1 + min(l2, l1 + kb));
+            keys[p] = ((uint32_t)ob << 13) | (uint32_t)(8191 - min(se + (kb & 1), 8191));
             vals[p] = (uint32_t)p;
         }
         cells = (unsigned long long)band_cells_of(l1, l2, band);
@@ -842,7 +850,8 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     base.pairs = d_pairs;
     base.band = band;
     base.dist = d_dist; base.score = d_score; base.ml = d_ml; base.al = d_al;
-    auto launch_wide = [&](const GenArgs& ga, const uint32_t* order, int64_t n_items) -> int {
+    auto launch_wide = [&](const GenArgs& ga, const uint32_t* order, int64_t n_items, cudaStream_t ls,
+                           bool timed) -> int {
         const int rs = 2 * kbmax + 3;
         const int threads = 128;
         const int64_t want_threads = std::min<int64_t>(n_items, (int64_t)ctx->sm_count * 4 * threads);
@@ -851,9 +860,9 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         WideArgs w{};
         w.g = ga; w.g.order = order; w.g.count = n_items;
         w.scratch = g.buckets.as<int>(); w.row_stride = rs;
-        ev_begin(ctx, ctx->ev_gen, s);
-        gen_wide_kernel<<<blocks, threads, 0, s>>>(w);
-        ev_end(ctx, ctx->ev_gen, s);
+        if (timed) ev_begin(ctx, ctx->ev_gen, ls);
+        gen_wide_kernel<<<blocks, threads, 0, ls>>>(w);
+        if (timed) ev_end(ctx, ctx->ev_gen, ls);
         count_launch(ctx);
         ctx->stats.gen_launches++;
         return CRISPY_OK;
@@ -872,7 +881,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
             const int wb = (int)st[kStatWindows + 2 * w];   // widest band-slot bin (kNumBins = wide)
             const bool lng = st[kStatWindows + 2 * w + 1] != 0;
             if (mode == CRISPY_MODE_PLAIN || wb >= kNumBins) {
-                CRISPY_TRY(launch_wide(a, nullptr, n_items));
+                CRISPY_TRY(launch_wide(a, nullptr, n_items, s, true));
             } else {
                 CRISPY_TRY(launch_shape(ctx, s, default_shape(lng ? wb + kNumBins : wb), a, true));
                 ctx->stats.gen_launches++;
@@ -881,31 +890,64 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         CRISPY_CK(ctx, cudaGetLastError());
         return CRISPY_OK;
     }
-    // BATCHED: bins in ascending width, wide last
+    // BATCHED: bins in ascending width, wide last.  Every bin's shape is
+    // picked first (the autotuner times its samples alone on s); then the
+    // bins' persistent launches alternate between two side streams, so that
+    // a bin's tail (its last, shortest pairs on a few SMs) overlaps the next
+    // bin's start.  One event pair on s brackets them all.
+    struct BinRun {
+        int ob;
+        int64_t at, n;
+        int shape;
+    };
+    std::vector<BinRun> runs;
     int64_t at = 0;
     for (int ob = 1; ob <= kWideOrderBin; ++ob) {
         const int64_t n_items = (int64_t)st[kStatBins + ob];
         if (n_items == 0) continue;
-        const uint32_t* ord = d_order + at;
+        BinRun r{ob, at, n_items, -1};
         at += n_items;
-        if (ob == kWideOrderBin) {
-            CRISPY_TRY(launch_wide(base, ord, n_items));
+        if (ob != kWideOrderBin) {
+            GenArgs a = base;
+            a.order = d_order + r.at;
+            a.count = n_items;
+            r.shape = pick_shape(ctx, s, band, ob, a, a.order, n_items, g.tune_sample, g.tune_queue);
+            const int forced = forced_shape();
+            if (forced >= 0 && shape_slots(forced) >= kBinSlots[ob < kNumBins ? ob : ob - kNumBins] &&
+                !(is16(forced) && ob >= kNumBins))
+                r.shape = forced;
+        }
+        runs.push_back(r);
+    }
+    CRISPY_TRY(ensure(ctx, g.queue, 64 * 4));
+    CRISPY_CK(ctx, cudaMemsetAsync(g.queue.ptr, 0, 64 * 4, s));   // one counter per order-bin (< 64)
+    const bool fork = runs.size() > 1;
+    ev_begin(ctx, ctx->ev_gen, s);
+    if (fork) {
+        CRISPY_CK(ctx, cudaEventRecord(ctx->fork_ev, s));
+        for (int k = 0; k < 2; ++k) CRISPY_CK(ctx, cudaStreamWaitEvent(ctx->side[k], ctx->fork_ev, 0));
+    }
+    for (size_t i = 0; i < runs.size(); ++i) {
+        const BinRun& r = runs[i];
+        cudaStream_t ls = fork ? ctx->side[i & 1] : s;
+        if (r.ob == kWideOrderBin) {
+            CRISPY_TRY(launch_wide(base, d_order + r.at, r.n, ls, false));
             continue;
         }
         GenArgs a = base;
-        a.order = ord;
-        a.count = n_items;
-        int shape = pick_shape(ctx, s, band, ob, a, ord, n_items, g.tune_sample, g.tune_queue);
-        const int forced = forced_shape();
-        if (forced >= 0 && shape_slots(forced) >= kBinSlots[ob < kNumBins ? ob : ob - kNumBins] &&
-            !(is16(forced) && ob >= kNumBins))
-            shape = forced;
-        CRISPY_TRY(ensure(ctx, g.queue, 64 * 4));
-        a.queue = g.queue.as<unsigned int>() + ob;   // one counter per order-bin (< 64)
-        CRISPY_CK(ctx, cudaMemsetAsync(a.queue, 0, 4, s));
-        CRISPY_TRY(launch_shape(ctx, s, shape, a, true));
+        a.order = d_order + r.at;
+        a.count = r.n;
+        a.queue = g.queue.as<unsigned int>() + r.ob;
+        CRISPY_TRY(launch_shape(ctx, ls, r.shape, a, false));
         ctx->stats.gen_launches++;
     }
+    if (fork) {
+        for (int k = 0; k < 2; ++k) {
+            CRISPY_CK(ctx, cudaEventRecord(ctx->join_ev[k], ctx->side[k]));
+            CRISPY_CK(ctx, cudaStreamWaitEvent(s, ctx->join_ev[k], 0));
+        }
+    }
+    ev_end(ctx, ctx->ev_gen, s);
     CRISPY_CK(ctx, cudaGetLastError());
     return CRISPY_OK;
 }

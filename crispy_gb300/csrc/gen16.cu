@@ -66,6 +66,11 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
+// Blocks per SM for the register budget, counted in warps per SM
+// sub-partition (16K registers each): 3 warps give a lane up to 168
+// registers, 4 up to 128.
+template <int R>
+constexpr int min_blocks16() { return R <= 3 ? 6 : (R == 4 ? 5 : 3); }
 constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
 constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
 constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
@@ -302,8 +307,8 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             upB = r < R - 1 ? st.B[Q][r + 1] : nB;
         }
         const uint32_t mm = st.MW[P][r] & kLo;
-        st.MW[P][r] = __umulhi(st.MW[P][r], 0x40000000u);   // >> 2 on the multiplier
-        const uint32_t od = (st.K[P][r] | 0x00030003u) * mu.one + 0x001C001Cu;
+        st.MW[P][r] >>= 2;
+        const uint32_t od = (st.K[P][r] | 0x00030003u) + 0x001C001Cu;
         const uint32_t kd = mm * mu.n36 + od;
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
@@ -369,8 +374,9 @@ __device__ __forceinline__ Best16 group_best16(Best16 b, int lane) {
 }
 
 template <int G, int R>
-__global__ void __launch_bounds__(kThreads, R <= 3 ? 6 : (R == 4 ? 5 : 4)) gen16_kernel(GenArgs a) {
+__global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenArgs a) {
     constexpr int kPerWarp = 32 / G;
+    static_assert(R <= 16, "a lane's slot windows must fit one 32-symbol window per read");
     __shared__ uint32_t smem[kWarps][kPerWarp][2][kSmWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / G, gl = lane % G;

@@ -113,6 +113,7 @@ struct crispy_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     cudaStream_t side[8] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[2] = {};   // fork / join of side-stream launches
     bool timing = false;
     std::string err;
     crispy_stats stats{};

@@ -8,9 +8,10 @@
 // so a large job at the head does not stall small ones behind it; a job
 // larger than the whole budget fails at submit with CRISPY_E_OOM.
 //
-// Small jobs share the kernels: with the oldest fitting job the worker
-// takes every other queued job of the same K and band that is small enough
-// and fits the budget (a cohort, up to kCohortReads reads in all).  The
+// Small jobs share the kernels: when the queue holds a backlog (at least as
+// many jobs as slots), with the oldest fitting job the worker takes every
+// other queued job of the same K and band that is small enough and fits the
+// budget (a cohort, up to kCohortReads reads in all).  The
 // cohort's reads go up as one read set, each job at a 128-aligned base; one
 // persistent k-mer tile launch takes all their row groups from one queue,
 // each over its own job's columns with its own threshold, and one set of
@@ -41,7 +42,7 @@ using clock_type = std::chrono::steady_clock;
 // Cohort limits: members of at most kCohortJobReads reads (larger jobs run
 // alone), at most kCohortReads reads and kCohortJobs jobs per cohort.
 constexpr int kCohortJobReads = 16384;
-constexpr int kCohortReads = 65536;
+constexpr int kCohortReads = 32768;
 constexpr int kCohortJobs = 64;
 
 bool cohorts_enabled() {
@@ -133,9 +134,12 @@ struct crispy_server {
     }
 
     // With `first` taken: the other queued jobs that can share its run.
+    // A cohort forms only under a backlog -- at least as many jobs still
+    // queued as there are slots, so that every slot has work anyway -- since
+    // a job that could start alone on an idle slot finishes sooner alone.
     std::vector<Job*> take_cohort(Job* first) {   // caller holds mu
         std::vector<Job*> c{first};
-        if (!cohort_member(first)) return c;
+        if (!cohort_member(first) || queue.size() < ctx.size()) return c;
         auto aligned = [](int n) { return (n + 127) / 128 * 128; };
         int reads = aligned(first->n);
         size_t mem = first->mem;
