@@ -274,7 +274,8 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
                       &g.ml, &g.al, &g.flags, &g.scan, &g.blocksum, &g.surv_idx, &g.keys,
                       &g.keys_alt, &g.vals, &g.vals_alt, &g.out_pairs, &g.out_dists, &g.order,
                       &g.buckets, &g.queue, &g.err, &g.tune_sample, &g.tune_queue, &g.cstats,
-                      &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt, &g.acc_pairs, &g.acc_dists})
+                      &g.ckeys, &g.ckeys_alt, &g.cvals, &g.cvals_alt, &g.acc_pairs, &g.acc_dists,
+                      &g.dirs})
         release(ctx, *b);
     PreJob& pj = ctx->pre;
     for (DevBuf* b : {&pj.seq, &pj.off, &pj.len, &pj.freq, &pj.woff, &pj.pad, &pj.alive, &pj.idx,

@@ -573,11 +573,13 @@ static_assert(2 * kNumBins < 32, "order-bins overflow the 18-bit sort key");
 // the last row or column, where the register kernels stop), so that the
 // pairs of a warp, which runs until its longest sweep ends, end together.
 // stats: [0] cells, [1] max kBand, [kStatBins + ob] pairs of order-bin ob,
-// [kStatWindows + 2w] widest band-slot bin of load window w (kNumBins =
-// wide), [kStatWindows + 2w + 1] 1 when the window holds a pair beyond the
-// 16-bit range.
+// [kStatMaxSum16] the largest L1 + L2 of a pair the 16-bit kernel takes
+// (it sizes that kernel's tag storage), [kStatWindows + 2w] widest band-slot
+// bin of load window w (kNumBins = wide), [kStatWindows + 2w + 1] 1 when
+// the window holds a pair beyond the 16-bit range.
 constexpr int kStatBins = 2, kStatWindows = 32;
 constexpr int kWideOrderBin = 2 * kNumBins;
+constexpr int kStatMaxSum16 = kStatBins + kWideOrderBin + 1;
 __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t count,
                                     const int32_t* __restrict__ len, int band, int nbins,
                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
@@ -587,6 +589,7 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
     const bool ok = p < count;
     unsigned long long cells = 0;
     int kb = 0, ob = -1, wb = -1, lng = 0;
+    int sum_reg = 0;   // L1 + L2 of a pair for the register kernels' 16-bit form
     if (ok) {
         const int2 pr = pairs[p];
         const int l1 = len[pr.x], l2 = len[pr.y];
@@ -595,6 +598,7 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
         for (int b = 1; b < nbins; ++b)
             if (c_bin_slots[b] >= kb + 1) { bin = b; break; }
         lng = l1 + l2 > kGen16MaxSum ? 1 : 0;
+        if (bin != 0 && !lng) sum_reg = l1 + l2;
         wb = bin == 0 ? nbins : bin;
         ob = bin == 0 ? 2 * nbins : bin + lng * nbins;   // wide pairs sort last
         if (keys) {
@@ -610,9 +614,11 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
     // every pair, so per-pair atomics would serialise
     cells = __reduce_add_sync(0xffffffffu, (unsigned)cells) + 0ull;   // cells < 2^32 per warp
     const unsigned kbw = __reduce_max_sync(0xffffffffu, (unsigned)kb);
+    const unsigned sum16 = __reduce_max_sync(0xffffffffu, (unsigned)sum_reg);
     if (lane == 0) {
         if (cells) atomicAdd(&stats[0], cells);
         atomicMax(&stats[1], (unsigned long long)kbw);
+        if (sum16) atomicMax(&stats[kStatMaxSum16], (unsigned long long)sum16);
     }
     const unsigned same_bin = __match_any_sync(0xffffffffu, ob);
     if (ok && lane == __ffs(same_bin) - 1) atomicAdd(&stats[kStatBins + ob], (unsigned long long)__popc(same_bin));
@@ -627,7 +633,7 @@ __global__ void gen_classify_kernel(const int2* __restrict__ pairs, int64_t coun
 }
 // untuned 32-bit shape per bin (the plain form always uses it)
 constexpr int kDefaultShape[kNumBins] = {-1, 0, 3, 4, 14, 5, 15, 6, 16, 7, 11, 12, 13};
-static_assert(kStatBins + kWideOrderBin < kStatWindows, "per-bin counters overlap the window slots");
+static_assert(kStatMaxSum16 < kStatWindows, "per-bin counters overlap the window slots");
 
 using WarpFn = void (*)(GenArgs);
 WarpFn shape_fn(int shape) {
@@ -728,15 +734,21 @@ __global__ void gather_stride_kernel(const uint32_t* __restrict__ src, int64_t n
     if (i < want) dst[i] = src[i * n / want];
 }
 
+// Status; the shape in *out.
 int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs& a,
-               const uint32_t* d_order, int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf) {
+               const uint32_t* d_order, int64_t n_items, DevBuf& sample_buf, DevBuf& queue_buf,
+               DevBuf& dirs_buf, int* out) {
     const int dflt = default_shape(bin);
-    if (!autotune_enabled() || n_items < 4096) return dflt;
+    *out = dflt;
+    if (!autotune_enabled() || n_items < 4096) return CRISPY_OK;
     const TuneKey key{band, bin, 0, ctx->sm_count};
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tuned.find(key);
-        if (it != g_tuned.end()) return it->second.shape;
+        if (it != g_tuned.end()) {
+            *out = it->second.shape;
+            return CRISPY_OK;
+        }
     }
     // strided sample of the bin (keeps its length spread), taken on the device
     const int64_t want = std::min<int64_t>(n_items, 24576);
@@ -745,26 +757,40 @@ int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs
     gather_stride_kernel<<<(unsigned)((want + 255) / 256), 256, 0, s>>>(d_order, n_items, want,
                                                                       sample_buf.as<uint32_t>());
     count_launch(ctx);
+    const int need = kBinSlots[bin < kNumBins ? bin : bin - kNumBins];
+    auto candidate = [&](int sh) {
+        const int slots = shape_slots(sh);
+        return slots >= need && slots <= 2 * need && !(is16(sh) && bin >= kNumBins);
+    };
+    int64_t dir_words = 0;   // tag storage of the 16-bit candidates
+    for (int sh = 0; sh < num_shapes_all(); ++sh)
+        if (candidate(sh) && is16(sh))
+            dir_words = std::max(dir_words, gen16_dir_words(ctx, sh - kNumShapes, want, a.dir_blocks));
+    if (dir_words) CRISPY_TRY(ensure(ctx, dirs_buf, (size_t)dir_words * 4));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     int best = dflt;
     float best_ms = 1e30f, dflt_ms = 0;
-    const int need = kBinSlots[bin < kNumBins ? bin : bin - kNumBins];
     int qslot = 0;
     for (int sh = 0; sh < num_shapes_all(); ++sh) {
-        const int slots = shape_slots(sh);
-        if (slots < need || slots > 2 * need) continue;
-        if (is16(sh) && bin >= kNumBins) continue;   // pairs beyond the 16-bit range
+        if (!candidate(sh)) continue;
         float ms = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
             GenArgs t = a;
             t.order = sample_buf.as<uint32_t>();
             t.count = want;
+            t.dirs = dirs_buf.as<uint32_t>();
+            t.dirs_words = dir_words;
             t.queue = queue_buf.as<unsigned int>() + (qslot++ % 64);
             CRISPY_CK(ctx, cudaMemsetAsync(t.queue, 0, 4, s));
             cudaEventRecord(e0, s);
-            launch_shape(ctx, s, sh, t, false);
+            const int rc = launch_shape(ctx, s, sh, t, false);
+            if (rc != CRISPY_OK) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return rc;
+            }
             cudaEventRecord(e1, s);
             cudaEventSynchronize(e1);
             float m = 0;
@@ -779,7 +805,8 @@ int pick_shape(crispy_ctx* ctx, cudaStream_t s, int band, int bin, const GenArgs
     CRISPY_CK(ctx, cudaGetLastError());
     std::lock_guard<std::mutex> g(g_tune_mu);
     g_tuned[key] = TuneEntry{best, best_ms, dflt_ms, want};
-    return best;
+    *out = best;
+    return CRISPY_OK;
 }
 
 }  // namespace
@@ -850,6 +877,7 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     base.pairs = d_pairs;
     base.band = band;
     base.dist = d_dist; base.score = d_score; base.ml = d_ml; base.al = d_al;
+    base.dir_blocks = gen16_dir_blocks((int)st[kStatMaxSum16]);
     auto launch_wide = [&](const GenArgs& ga, const uint32_t* order, int64_t n_items, cudaStream_t ls,
                            bool timed) -> int {
         const int rs = 2 * kbmax + 3;
@@ -868,6 +896,21 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         return CRISPY_OK;
     };
     if (mode == CRISPY_MODE_PLAIN || mode == CRISPY_MODE_STAGED) {
+        // tag storage for the windows the 16-bit kernel takes (one at a time)
+        int64_t dir_words = 0;
+        for (int64_t w = 0; mode == CRISPY_MODE_STAGED && w < nwin; ++w) {
+            const int wb = (int)st[kStatWindows + 2 * w];
+            const int sh = wb >= kNumBins ? -1 : default_shape(st[kStatWindows + 2 * w + 1] ? wb + kNumBins : wb);
+            if (sh >= 0 && is16(sh))
+                dir_words = std::max(dir_words, gen16_dir_words(ctx, sh - kNumShapes,
+                                                                std::min<int64_t>(CRISPY_GEN_WINDOW, count - w * CRISPY_GEN_WINDOW),
+                                                                base.dir_blocks));
+        }
+        if (dir_words) {
+            CRISPY_TRY(ensure(ctx, g.dirs, (size_t)dir_words * 4));
+            base.dirs = g.dirs.as<uint32_t>();
+            base.dirs_words = dir_words;
+        }
         for (int64_t w = 0; w < nwin; ++w) {
             const int64_t w0 = w * CRISPY_GEN_WINDOW;
             const int64_t n_items = std::min<int64_t>(CRISPY_GEN_WINDOW, count - w0);
@@ -911,7 +954,8 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
             GenArgs a = base;
             a.order = d_order + r.at;
             a.count = n_items;
-            r.shape = pick_shape(ctx, s, band, ob, a, a.order, n_items, g.tune_sample, g.tune_queue);
+            CRISPY_TRY(pick_shape(ctx, s, band, ob, a, a.order, n_items, g.tune_sample, g.tune_queue, g.dirs,
+                                  &r.shape));
             const int forced = forced_shape();
             if (forced >= 0 && shape_slots(forced) >= kBinSlots[ob < kNumBins ? ob : ob - kNumBins] &&
                 !(is16(forced) && ob >= kNumBins))
@@ -922,6 +966,12 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
     CRISPY_TRY(ensure(ctx, g.queue, 64 * 4));
     CRISPY_CK(ctx, cudaMemsetAsync(g.queue.ptr, 0, 64 * 4, s));   // one counter per order-bin (< 64)
     const bool fork = runs.size() > 1;
+    // tag storage of the 16-bit launches: one half per side stream
+    int64_t dir_words = 0;
+    for (const BinRun& r : runs)
+        if (r.shape >= 0 && is16(r.shape))
+            dir_words = std::max(dir_words, gen16_dir_words(ctx, r.shape - kNumShapes, r.n, base.dir_blocks));
+    if (dir_words) CRISPY_TRY(ensure(ctx, g.dirs, (size_t)dir_words * 4 * (fork ? 2 : 1)));
     ev_begin(ctx, ctx->ev_gen, s);
     if (fork) {
         CRISPY_CK(ctx, cudaEventRecord(ctx->fork_ev, s));
@@ -938,6 +988,10 @@ int gen_dispatch_impl(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int6
         a.order = d_order + r.at;
         a.count = r.n;
         a.queue = g.queue.as<unsigned int>() + r.ob;
+        if (dir_words) {
+            a.dirs = g.dirs.as<uint32_t>() + (fork ? (int64_t)(i & 1) * dir_words : 0);
+            a.dirs_words = dir_words;
+        }
         CRISPY_TRY(launch_shape(ctx, ls, r.shape, a, false));
         ctx->stats.gen_launches++;
     }

@@ -29,20 +29,28 @@
 // candidate of an in-band cell.  No 16-bit half ever wraps, so plain 32-bit
 // adds and multiply-adds act on both halves at once.
 //
-// Path counters.  AL = (i + j) - A and ML = (i + j) - 2A + (B - 4096), with
-// A = diagonal moves and B = 4096 + mismatches - (i0 + j0), (i0, j0) the
-// boundary cell the path leaves (A = 0, B = 4096 - s there): a diagonal move
-// adds 1 to A and the mismatch to B, a gap adds nothing.  Both are kept
-// doubled (bit 0 clear) in 16-bit halves, so the masks b0 * 0xFFFF and
-// 2 b1 * 0x7FFF (one multiply each) select the winner's counters with two
-// bitwise muxes per array.
+// ML and AL by a path walk.  Every cell's tag t (its choice) goes into a
+// per-register word, 2 bits per cell and step, stored every 8 steps to the
+// pair's region of `dirs`.  After the sweep the pair's lanes walk the path
+// back from the chosen last-row / last-column cell E to the boundary cell
+// (i0, j0) it leaves, following the tags (the reference's tie-broken
+// choices), and count A = diagonal moves and the gap penalties Gp (each gap
+// move's penalty from the tag of the cell it leaves; a boundary cell's tag
+// gives 0).  The score identity M(E) = 5 (A - mism) - 4 mism + Gp gives the
+// mismatches, and AL = (iE + jE) - A, ML = (iE + jE) - 2A + mism - (i0 + j0)
+// (genCPU.cpp:426-440: a diagonal adds 1 - hit to ML, a gap 1; AL counts
+// every move from the boundary cell's own AL = i0 + j0).
 //
 // Layout.  G lanes per pair, R registers per lane: register r of lane l
 // holds slot l*R + r in its low half and slot G*R + l*R + r in its high
 // half.  Slot q hosts diagonal 2q - kBand + P at step parity P; its up /
 // left neighbours are slots q + 1 / q - 1 of the previous step, i.e.
 // registers r + 1 / r - 1 of the same lane, so only the lane's edge
-// register crosses lanes (one shuffle per step for keys, A and B).
+// register crosses lanes (one shuffle of keys per step).
+// Tags: step tau = s + (kBand & 1) (odd bands run one step late) lies in
+// sub-block sb = tau / 8; register r of lane l keeps that sub-block's tags
+// in word (sb * G + l) * R + r of the pair's region, the step's tag at bits
+// 2 (7 - tau % 8) of the half.
 // Symbols: 2 bits each, first symbol in the low bits, in shared memory
 // behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
 // windows out of four 32-symbol windows (consecutive slots of a lane read
@@ -73,13 +81,14 @@ template <int R>
 constexpr int min_blocks16() { return R <= 3 ? 6 : (R == 4 ? 5 : 3); }
 constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
 constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
+constexpr int kPairWords = 2 * kSmWords + 4;    // both reads of a pair, 4 words apart in banks
+static_assert(kPairWords % 32 == 4 && kSmWords % 4 == 0, "shared layout");
 constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
 constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
 constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
 constexpr uint32_t kLo = 0x00010001u;   // 1 in each half
 constexpr uint32_t kOut = 8u;           // key of a cell outside the band / matrix
 constexpr uint32_t kOut2 = kOut * kLo;
-constexpr int kMisOff = 4096;           // offset of the B counter
 constexpr int kRefNegInf = -1000000;    // genCPU.cpp:350 initial last-row/column maximum
 static_assert(18 * (kGen16MaxSum + kSlack) + 131 < 65536, "16-bit keys would wrap");
 static_assert(kBase % 4 == 0, "the score is read back as (K - 4s - kBase) / 4");
@@ -94,20 +103,18 @@ __device__ __forceinline__ int kband16(int l1, int l2, int band) {
 // compiler cannot see): products by them stay multiply-adds on the FMA pipe
 // instead of turning into shift / add sequences on the ALU.
 struct Mul {
-    uint32_t one, two, n36, m5, n19, m3, n21, mffff, m7fff, neg1;
+    uint32_t one, four, n36, m5, n19, m3, n21, neg1;
 };
 
 __device__ __forceinline__ Mul make_mul(const int* o) {
     Mul m;
     m.one = (uint32_t)o[0];
-    m.two = 2u * (uint32_t)o[1];
+    m.four = 4u * (uint32_t)o[1];
     m.n36 = (uint32_t)(-36) * (uint32_t)o[2];
     m.m5 = 5u * (uint32_t)o[3];
     m.n19 = (uint32_t)(-19) * (uint32_t)o[4];
     m.m3 = 3u * (uint32_t)o[5];
     m.n21 = (uint32_t)(-21) * (uint32_t)o[0];
-    m.mffff = 0xFFFFu * (uint32_t)o[1];
-    m.m7fff = 0x7FFFu * (uint32_t)o[2];
     m.neg1 = (uint32_t)(-1) * (uint32_t)o[3];
     return m;
 }
@@ -116,8 +123,7 @@ template <int R>
 struct St {
     uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
     uint32_t U[R], F[R]; // up / left candidates the last step sent
-    uint32_t A[2][R];    // doubled diagonal-move counters by parity
-    uint32_t B[2][R];    // doubled mismatch counters by parity
+    uint32_t D[R];       // tags of the current 8 steps, 2 bits per cell, first step highest
     uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
     uint32_t CP[2][R];   // per half: 0xFFFF in band, kOut outside
 };
@@ -131,7 +137,6 @@ struct Pair16 {
 
 struct Best16 {
     int m;
-    uint32_t ab;   // (doubled A << 16) | doubled B of the cell
     int at;
 };
 
@@ -197,39 +202,30 @@ __device__ __forceinline__ void boundary_slot(int d, const Pair16& pc, int gl, i
     else if ((unsigned)rh < (unsigned)R) { *r = rh; *h = 1; }
 }
 
-// Sets one half to a boundary cell at step s (M = 0, A = 0, B = 4096 - s,
-// doubled) and opens its cap.
-__device__ __forceinline__ void boundary_set(uint32_t& K, uint32_t& A, uint32_t& B, uint32_t& CP, int h,
-                                             int s, uint32_t tag) {
+// Sets one half to a boundary cell at step s (M = 0) and opens its cap.
+__device__ __forceinline__ void boundary_set(uint32_t& K, uint32_t& CP, int h, int s, uint32_t tag) {
     const uint32_t key = tag + (uint32_t)(4 * s + kBase);
-    const uint32_t b0 = (uint32_t)(2 * (kMisOff - s));
     if (h == 0) {
         K = (K & 0xFFFF0000u) | key;
-        A &= 0xFFFF0000u;
-        B = (B & 0xFFFF0000u) | b0;
         CP |= 0x0000FFFFu;
     } else {
         K = (K & 0x0000FFFFu) | (key << 16);
-        A &= 0x0000FFFFu;
-        B = (B & 0x0000FFFFu) | (b0 << 16);
         CP |= 0xFFFF0000u;
     }
 }
 
-// The cell of slot q (held by this lane) at the current parity: key half and
-// packed counters.
+// The key of slot q (held by this lane) at the current parity.
 template <int G, int R, int P>
-__device__ __forceinline__ void take(const St<R>& st, int q, int gl, uint32_t& key, uint32_t& ab) {
+__device__ __forceinline__ uint32_t take(const St<R>& st, int q, int gl) {
     const int rl = q - gl * R;
     const bool hi = (unsigned)rl >= (unsigned)R;
     const int rr = hi ? q - (G + gl) * R : rl;
-    uint32_t kk = 0, aa = 0, bb = 0;
+    uint32_t kk = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r)
-        if (r == rr) { kk = st.K[P][r]; aa = st.A[P][r]; bb = st.B[P][r]; }
-    if (hi) { kk >>= 16; aa >>= 16; bb >>= 16; }
-    key = kk & 0xFFFFu;
-    ab = ((aa & 0xFFFFu) << 16) | (bb & 0xFFFFu);
+        if (r == rr) kk = st.K[P][r];
+    if (hi) kk >>= 16;
+    return kk & 0xFFFFu;
 }
 
 __device__ __forceinline__ bool mine(int q, int gl, int G, int R) {
@@ -249,16 +245,14 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
     const bool hr = jr >= 1 && jr <= pc.l1 && dr >= -pc.kb && dr <= pc.kb && mine(qr, gl, G, R);
     const bool hc = ic >= 1 && ic <= pc.l2 && dc >= -pc.kb && dc <= pc.kb && mine(qc, gl, G, R);
     if (hr) {
-        uint32_t key, ab;
-        take<G, R, P>(st, qr, gl, key, ab);
+        const uint32_t key = take<G, R, P>(st, qr, gl);
         const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
-        if (m >= col.m) { col.m = m; col.ab = ab; col.at = jr; }
+        if (m >= col.m) { col.m = m; col.at = jr; }
     }
     if (hc) {
-        uint32_t key, ab;
-        take<G, R, P>(st, qc, gl, key, ab);
+        const uint32_t key = take<G, R, P>(st, qc, gl);
         const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
-        if (m >= row.m) { row.m = m; row.ab = ab; row.at = ic; }
+        if (m >= row.m) { row.m = m; row.at = ic; }
     }
 }
 
@@ -269,20 +263,15 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
 template <int G, int R, int P, int kMode>
 __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& pc, const Mul& mu,
                                        uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
-    constexpr int Q = P ^ 1;
-    uint32_t nK, nA, nB;
+    uint32_t nK;
     if (P == 0) {
         // left of register 0 = register R-1 of the previous lane
         const int src = (gl + G - 1) & (G - 1);
         nK = __byte_perm(__shfl_sync(0xffffffffu, st.F[R - 1], src, G), kOut2, sel0);
-        nA = __byte_perm(__shfl_sync(0xffffffffu, st.A[Q][R - 1], src, G), 0u, sel0);
-        nB = __byte_perm(__shfl_sync(0xffffffffu, st.B[Q][R - 1], src, G), 0u, sel0);
     } else {
         // up of register R-1 = register 0 of the next lane
         const int src = (gl + 1) & (G - 1);
         nK = __byte_perm(__shfl_sync(0xffffffffu, st.U[0], src, G), kOut2, sel1);
-        nA = __byte_perm(__shfl_sync(0xffffffffu, st.A[Q][0], src, G), 0u, sel1);
-        nB = __byte_perm(__shfl_sync(0xffffffffu, st.B[Q][0], src, G), 0u, sel1);
     }
     int ra = -1, ha = 0, rb = -1, hb = 0;
     if (kMode == kStart && s >= 0) {
@@ -294,17 +283,13 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         // parity 0 reads register r-1 (runs downwards), parity 1 register
         // r+1 (runs upwards), so a neighbour is read before it is rewritten
         const int r = P == 0 ? R - 1 - k : k;
-        uint32_t upK, lfK, upA, lfA, upB, lfB;
+        uint32_t upK, lfK;
         if (P == 0) {
-            upK = st.U[r]; upA = st.A[Q][r]; upB = st.B[Q][r];
+            upK = st.U[r];
             lfK = r > 0 ? st.F[r - 1] : nK;
-            lfA = r > 0 ? st.A[Q][r - 1] : nA;
-            lfB = r > 0 ? st.B[Q][r - 1] : nB;
         } else {
-            lfK = st.F[r]; lfA = st.A[Q][r]; lfB = st.B[Q][r];
+            lfK = st.F[r];
             upK = r < R - 1 ? st.U[r + 1] : nK;
-            upA = r < R - 1 ? st.A[Q][r + 1] : nA;
-            upB = r < R - 1 ? st.B[Q][r + 1] : nB;
         }
         const uint32_t mm = st.MW[P][r] & kLo;
         st.MW[P][r] >>= 2;
@@ -312,30 +297,17 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         const uint32_t kd = mm * mu.n36 + od;
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
-        const uint32_t ad = st.A[P][r] * mu.one + 2u * kLo;
-        const uint32_t bd = mm * mu.two + st.B[P][r];
-        uint32_t A, B;
         if (kMode == kStart && (r == ra || r == rb)) {
-            // a boundary cell: its own values, not the recurrence's
-            const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
-            const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
-            A = (ad & m1) | (((upA & m0) | (lfA & ~m0)) & ~m1);
-            B = (bd & m1) | (((upB & m0) | (lfB & ~m0)) & ~m1);
-            if (r == ra) boundary_set(K, A, B, st.CP[P][r], ha, s, 0u);
-            if (r == rb) boundary_set(K, A, B, st.CP[P][r], hb, s, 1u);
+            // a boundary cell: its own key, not the recurrence's
+            if (r == ra) boundary_set(K, st.CP[P][r], ha, s, 0u);
+            if (r == rb) boundary_set(K, st.CP[P][r], hb, s, 1u);
         }
         const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
         const uint32_t xn1 = x1 * mu.neg1 + kLo;
         st.U[r] = x2 * mu.n19 + (xn1 * mu.m5 + K);
         st.F[r] = x2 * mu.n21 + (x1 * mu.m3 + K);
-        if (!(kMode == kStart && (r == ra || r == rb))) {
-            const uint32_t m0 = x1 * mu.mffff, m1 = x2 * mu.m7fff;
-            const uint32_t at = (upA & m0) | (lfA & ~m0);
-            const uint32_t bt = (upB & m0) | (lfB & ~m0);
-            A = (ad & m1) | (at & ~m1);
-            B = (bd & m1) | (bt & ~m1);
-        }
-        st.K[P][r] = K; st.A[P][r] = A; st.B[P][r] = B;
+        st.D[r] = x2 * mu.one + (st.D[r] * mu.four + x1);   // tag t = b0 + 2 b1
+        st.K[P][r] = K;
     }
     if (kMode != kClean) {
         const bool near = (unsigned)(s - pc.tw[0]) < 2u * R || (unsigned)(s - pc.tw[1]) < 2u * R ||
@@ -344,49 +316,126 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
     }
 }
 
+// A block of 16 steps: two halves of 8, after each of which the lane's tag
+// words go to `dst` (sub-block h at dst + h * G * R; nullptr: not stored).
 template <int G, int R, int kMode>
 __device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu,
-                                        uint32_t sel0, uint32_t sel1, Best16& col, Best16& row) {
+                                        uint32_t sel0, uint32_t sel1, Best16& col, Best16& row,
+                                        uint32_t* dst) {
 #pragma unroll 1
-    for (int t = 0; t < kSteps; t += 2) {
-        step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, sel0, sel1, col, row);
-        step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, sel0, sel1, col, row);
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+        for (int t = 0; t < 8; t += 2) {
+            step16<G, R, 0, kMode>(st, gl, s0 + 8 * h + t, pc, mu, sel0, sel1, col, row);
+            step16<G, R, 1, kMode>(st, gl, s0 + 8 * h + t + 1, pc, mu, sel0, sel1, col, row);
+        }
+        if (dst) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[h * G * R + r] = st.D[r];
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) st.D[r] = 0;
     }
 }
 
 // Largest m over a G-lane sub-group, ties to the largest index `at`.
 template <int G>
-__device__ __forceinline__ Best16 group_best16(Best16 b, int lane) {
-    const long long mine = (long long)b.m * 4294967296LL + (long long)(unsigned)(b.at + 1);
-    long long key = mine;
+__device__ __forceinline__ Best16 group_best16(Best16 b) {
+    long long key = (long long)b.m * 4294967296LL + (long long)(unsigned)(b.at + 1);
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
         const long long other = __shfl_xor_sync(0xffffffffu, key, o);
         key = other > key ? other : key;
     }
-    const unsigned group = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-    const unsigned who = __ballot_sync(0xffffffffu, mine == key) & group;
     Best16 r;
     r.m = (int)(key >> 32);
     r.at = (int)(unsigned)(key & 0xffffffffu) - 1;
-    r.ab = __shfl_sync(0xffffffffu, b.ab, __ffs(who) - 1);
     return r;
+}
+
+// Penalty of a gap move (g: 1 up, 0 left) out of a cell with tag t:
+// GO after a diagonal, GE after the same gap, 0 after the other gap
+// (genCPU.cpp:404-414; a boundary cell's tag gives 0).
+__device__ __forceinline__ int gap_pen(int g, int t) { return t == 3 ? -10 : (t == g ? -1 : 0); }
+
+// Walks the path back from cell (i, j) to the boundary over the tags the
+// sweep stored in `region`, staging up to kDepth sub-blocks at a time in
+// `stage` (the G lanes of the pair load them together; every lane walks).
+// Returns the diagonal moves in *na, the gap penalties in *gp; (i, j) ends
+// at the boundary cell.
+template <int G, int R>
+__device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, const Pair16& pc, int gl,
+                                       bool walking, int& i, int& j, int* na, int* gp) {
+    constexpr int kGR = G * R;
+    constexpr int kDepth = (2 * kSmWords) / kGR < 8 ? (2 * kSmWords) / kGR : 8;
+    static_assert(kDepth >= 1 && kGR % 4 == 0, "tag staging");
+    int lo = INT_MAX;   // first staged sub-block
+    int a = 0, g = 0, gprev = -1;
+    while (__any_sync(0xffffffffu, walking)) {
+        if (walking && i > 0 && j > 0) {
+            const int sb = (i + j + pc.shift) >> 3;
+            if (sb < lo) {
+                lo = max(0, sb - kDepth + 1);
+                const int n4 = (sb + 1 - lo) * (kGR / 4);
+                const uint4* src = reinterpret_cast<const uint4*>(region + (int64_t)lo * kGR);
+                uint4* dst = reinterpret_cast<uint4*>(stage);
+                for (int k = gl; k < n4; k += G) dst[k] = src[k];
+            }
+        }
+        __syncwarp();
+        while (walking) {
+            if (i == 0 || j == 0) {
+                if (gprev >= 0) g += gap_pen(gprev, j == 0 ? 0 : 1);   // column 0: tag left, row 0: up
+                walking = false;
+                break;
+            }
+            const int tau = i + j + pc.shift;
+            const int sb = tau >> 3;
+            if (sb < lo) break;   // stage the sub-blocks below
+            const int q = (i - j + pc.kb - (tau & 1)) >> 1;
+            const int hi = q >= kGR ? 1 : 0;
+            const int qq = min(max(q - hi * kGR, 0), kGR - 1);
+            // the half's tags of steps tau % 8, tau % 8 - 1, ... from bit 0 up
+            const uint32_t x = ((stage[(sb - lo) * kGR + qq] >> (16 * hi)) & 0xFFFFu) >> (2 * (7 - (tau & 7)));
+            const int t = (int)(x & 3u);
+            if (gprev >= 0) g += gap_pen(gprev, t);
+            if (t == 3) {
+                // a diagonal move keeps the slot and goes two steps back: the
+                // run of diagonal tags at steps tau, tau - 2, ... in this word
+                const uint32_t y = ~x & 0x3333u;
+                const int k = min(y ? (__ffs(y) - 1) >> 2 : 4, min(i, j));
+                a += k; i -= k; j -= k; gprev = -1;
+            } else if (t == 1) {
+                --j; gprev = 1;
+            } else {
+                --i; gprev = 0;
+            }
+        }
+        __syncwarp();
+    }
+    *na = a;
+    *gp = g;
 }
 
 template <int G, int R>
 __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenArgs a) {
     constexpr int kPerWarp = 32 / G;
     static_assert(R <= 16, "a lane's slot windows must fit one 32-symbol window per read");
-    __shared__ uint32_t smem[kWarps][kPerWarp][2][kSmWords];
+    // per pair: read1, read2; a stride of 4 words over 32 banks puts the
+    // pairs of a warp, which read the same offsets, in different banks
+    __shared__ __align__(16) uint32_t smem[kWarps][kPerWarp][kPairWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / G, gl = lane % G;
-    uint32_t* sm1 = smem[warp][sub][0];
-    uint32_t* sm2 = smem[warp][sub][1];
+    uint32_t* sm1 = smem[warp][sub];
+    uint32_t* sm2 = sm1 + kSmWords;
     const Mul mu = make_mul(a.one);
     const uint32_t sel0 = gl == 0 ? 0x1054u : 0x3210u;       // parity 0: lane 0's low half moves up
     const uint32_t sel1 = gl == G - 1 ? 0x7632u : 0x3210u;   // parity 1: last lane's high half moves down
     int64_t base = a.queue ? -1 : ((int64_t)blockIdx.x * kWarps + warp) * kPerWarp;
     const int64_t stride = (int64_t)gridDim.x * kWarps * kPerWarp;
+    // this sub-group's tag region: [sub-block][lane][register] words
+    const int64_t region_words = (int64_t)a.dir_blocks * 2 * G * R;
+    uint32_t* region = a.dirs + (((int64_t)blockIdx.x * kWarps + warp) * kPerWarp + sub) * region_words;
     for (;;) {
         if (a.queue) {
             unsigned w = 0;
@@ -433,12 +482,12 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
-            st.A[0][r] = 0; st.A[1][r] = 0; st.B[0][r] = 0; st.B[1][r] = 0;
+            st.D[r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
             st.CP[0][r] = kOut2; st.CP[1][r] = kOut2;
         }
-        Best16 col{kRefNegInf, 0u, -1}, row{kRefNegInf, 0u, -1};
+        Best16 col{kRefNegInf, -1}, row{kRefNegInf, -1};
         // the sweep ends at the last in-band cell of the last row or column
         int s_end = -1;
         if (valid) {
@@ -447,33 +496,44 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
                 s_end = max(s_end, pc.l1 + min(pc.l2, pc.l1 + pc.kb));
         }
         const int t_end = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(0, s_end + pc.shift));
+        // the region holds dir_blocks blocks (sized on the host for the
+        // launch's longest pair); a sweep that would not fit stores nothing
+        // and reports ML = AL = -1
+        const bool fits = (t_end >> 4) < a.dir_blocks;
         const int clean_hi = 2 * min(pc.l1, pc.l2) - pc.kb - 1;
         constexpr int kBlock = kSteps;
         for (int t0 = 0; t0 <= t_end; t0 += kBlock) {
             const int s0 = t0 - pc.shift;
             const bool finished = s0 > s_end;
             block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
+            uint32_t* dst = fits && !finished ? region + ((int64_t)(t0 >> 4) * 2 * G + gl) * R : nullptr;
             const bool started = s0 > pc.kb;   // every boundary cell is behind (s = |d| <= kb)
             const bool clean = finished || (started && s0 + kBlock - 1 < clean_hi);
             if (__all_sync(0xffffffffu, clean))
-                block16<G, R, kClean>(st, gl, s0, pc, mu, sel0, sel1, col, row);
+                block16<G, R, kClean>(st, gl, s0, pc, mu, sel0, sel1, col, row, dst);
             else if (__all_sync(0xffffffffu, started || finished))
-                block16<G, R, kTrack>(st, gl, s0, pc, mu, sel0, sel1, col, row);
+                block16<G, R, kTrack>(st, gl, s0, pc, mu, sel0, sel1, col, row, dst);
             else
-                block16<G, R, kStart>(st, gl, s0, pc, mu, sel0, sel1, col, row);
+                block16<G, R, kStart>(st, gl, s0, pc, mu, sel0, sel1, col, row, dst);
         }
-        col = group_best16<G>(col, lane);
-        row = group_best16<G>(row, lane);
+        col = group_best16<G>(col);
+        row = group_best16<G>(row);
+        const bool use_col = col.m > row.m;   // genKernel.cu:765-768
+        const Best16 b = use_col ? col : row;
+        // end cell E: last row (l2, at) or last column (at, l1)
+        int wi = use_col ? pc.l2 : b.at, wj = use_col ? b.at : pc.l1;
+        int na = 0, gp = 0;
+        __syncwarp();   // the sub-group's tag stores before its loads; the sequences are dead
+        walk16<G, R>(region, sm1, pc, gl, fits && valid && b.at >= 0, wi, wj, &na, &gp);
         if (gl == 0 && valid) {
-            const bool use_col = col.m > row.m;   // genKernel.cu:765-768
-            const Best16& b = use_col ? col : row;
             int mlv = 0, alv = 0;
-            if (b.at >= 0) {
+            if (!fits) {
+                mlv = alv = -1;
+            } else if (b.at >= 0) {
                 const int ij = use_col ? pc.l2 + b.at : b.at + pc.l1;
-                const int A = (int)(b.ab >> 17);
-                const int Bm = (int)((b.ab & 0xFFFFu) >> 1) - kMisOff;
-                alv = ij - A;
-                mlv = ij - 2 * A + Bm;
+                const int mism = (5 * na + gp - b.m) / 9;   // M(E) = 5 na - 9 mism + gp
+                alv = ij - na;
+                mlv = ij - 2 * na + mism - (wi + wj);
             }
             a.dist[p] = __fdiv_rn((float)mlv, (float)alv);
             if (a.score) a.score[p] = b.m;
@@ -488,6 +548,12 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
 constexpr Shape16 kShapes16[] = {{4, 1}, {4, 2}, {4, 4}, {8, 2}, {4, 5}, {4, 6}, {8, 3},
                                  {4, 7}, {8, 4}, {8, 5}, {8, 6}, {16, 4}, {16, 6}, {32, 4}};
 constexpr int kNumShapes16 = sizeof(kShapes16) / sizeof(kShapes16[0]);
+constexpr bool shapes_within_max_r() {
+    for (const Shape16& h : kShapes16)
+        if (h.r > kGen16MaxR) return false;
+    return true;
+}
+static_assert(shapes_within_max_r(), "kGen16MaxR bounds every shape's registers");
 
 using Fn16 = void (*)(GenArgs);
 Fn16 fn16(int i) {
@@ -515,15 +581,45 @@ int gen16_num_shapes() { return kNumShapes16; }
 Shape16 gen16_shape(int i) { return kShapes16[i]; }
 int gen16_pairs_per_block(int i) { return kWarps * (32 / kShapes16[i].g); }
 
-int gen16_launch(crispy_ctx* ctx, cudaStream_t s, int shape, const GenArgs& a, bool timed) {
-    Fn16 fn = fn16(shape);
+namespace {
+int gen16_grid(crispy_ctx* ctx, int shape, int64_t count) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn16(shape), kThreads, 0);
     const int64_t per_block = gen16_pairs_per_block(shape);
-    const int blocks = (int)std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
-                                              (a.count + per_block - 1) / per_block);
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(1, per_sm) * ctx->sm_count,
+                                                       (count + per_block - 1) / per_block));
+}
+}  // namespace
+
+int64_t gen16_lane_regs_per_sm() {
+    static const int64_t v = [] {
+        int64_t best = 0;
+        for (int i = 0; i < kNumShapes16; ++i) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn16(i), kThreads, 0) != cudaSuccess) {
+                cudaGetLastError();
+                per_sm = 2048 / kThreads;
+            }
+            best = std::max<int64_t>(best, (int64_t)per_sm * kThreads * kShapes16[i].r);
+        }
+        return best;
+    }();
+    return v;
+}
+
+int64_t gen16_dir_words(crispy_ctx* ctx, int shape, int64_t count, int dir_blocks) {
+    const Shape16 h = kShapes16[shape];
+    // one region per pair slot of the grid: blocks x threads / G pairs
+    return (int64_t)gen16_grid(ctx, shape, count) * kThreads / h.g * dir_blocks * 2 * h.g * h.r;
+}
+
+int gen16_launch(crispy_ctx* ctx, cudaStream_t s, int shape, const GenArgs& a, bool timed) {
+    const int blocks = gen16_grid(ctx, shape, a.count);
+    if (!a.dirs || a.dir_blocks < 1 || a.dirs_words < gen16_dir_words(ctx, shape, a.count, a.dir_blocks))
+        return fail(ctx, CRISPY_E_STATE, "gen16: tag storage of %lld words for %lld pairs is too small",
+                    (long long)a.dirs_words, (long long)a.count);
     if (timed) ev_begin(ctx, ctx->ev_gen, s);
-    fn<<<std::max(blocks, 1), kThreads, 0, s>>>(a);
+    fn16(shape)<<<blocks, kThreads, 0, s>>>(a);
     if (timed) ev_end(ctx, ctx->ev_gen, s);
     count_launch(ctx);
     return CRISPY_OK;

@@ -23,6 +23,12 @@ struct GenArgs {
     int32_t* ml;
     int32_t* al;
     unsigned int* queue;     // optional work counter (persistent launch)
+    // 16-bit kernel only: every cell's choice, 2 bits, for the path walk
+    // (gen16_dir_words words: one region per pair the grid holds at a
+    // time, dir_blocks 16-step blocks long)
+    uint32_t* dirs;
+    int64_t dirs_words;
+    int dir_blocks;
     // All 1.  Adds written as multiply-adds by these run on the FMA pipe;
     // distinct multipliers keep the compiler from factoring a common
     // product back into ALU adds.
@@ -43,6 +49,15 @@ int gen16_num_shapes();
 Shape16 gen16_shape(int i);
 // Pairs per block of a shape (all its warps).
 int gen16_pairs_per_block(int i);
+// Registers per lane of the widest shape (bounds the tag storage).
+constexpr int kGen16MaxR = 7;
+// 16-step blocks a pair's sweep runs at most, for pairs with L1 + L2 <= max_sum.
+inline int gen16_dir_blocks(int max_sum) { return (max_sum + 1) / 16 + 1; }
+// Words of choice storage a launch of shape i over `count` pairs needs.
+int64_t gen16_dir_words(crispy_ctx* ctx, int shape, int64_t count, int dir_blocks);
+// Largest resident threads x registers per lane of one SM over the shapes:
+// a launch holds at most this many tag words per SM and sub-block.
+int64_t gen16_lane_regs_per_sm();
 // Launch shape i over a.count pairs: persistent grid sized by occupancy.
 int gen16_launch(crispy_ctx* ctx, cudaStream_t s, int shape, const GenArgs& a, bool timed);
 

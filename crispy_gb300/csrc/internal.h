@@ -78,6 +78,7 @@ struct GenJob {
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
         vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue,
         cstats, ckeys, ckeys_alt, cvals, cvals_alt, acc_pairs, acc_dists;
+    DevBuf dirs;   // the 16-bit DP's cell tags (two halves: one per concurrent bin launch)
     HostBuf h_pairs, h_dists;
 };
 

@@ -33,6 +33,7 @@
 #include <thread>
 #include <unordered_map>
 
+#include "gen_args.h"
 #include "internal.h"
 
 namespace {
@@ -57,7 +58,9 @@ struct Job {
     std::vector<int32_t> len;
     int n = 0, k = 6, band = 10;
     float kthr = -1, gthr = -1;
-    size_t mem = 0;
+    int maxlen = 0;
+    size_t mem_base = 0;   // estimate without the genDist cell tags
+    size_t mem = 0;        // estimate of a lone run
     int state = CRISPY_JOB_QUEUED;
     int status = CRISPY_OK;
     std::string err;
@@ -72,16 +75,12 @@ struct Job {
     int cohort_size = 1;
 };
 
-// Device bytes a job needs at its peak (generous; the server only uses it
-// for admission).
-size_t estimate_bytes(const Job& j) {
+// Device bytes a job needs at its peak apart from the genDist cell tags
+// (generous; the server only uses it for admission).
+size_t estimate_base_bytes(const Job& j) {
     size_t reads = j.bases.size() + (size_t)j.n * 16;
     int64_t t = 0;
-    int maxlen = 0;
-    for (int i = 0; i < j.n; ++i) {
-        t += std::max(0, j.len[i] - j.k + 1);
-        maxlen = std::max(maxlen, j.len[i]);
-    }
+    for (int i = 0; i < j.n; ++i) t += std::max(0, j.len[i] - j.k + 1);
     // level entries + the scheduled tile stream (spare steps per group) +
     // per-read bank counts
     const size_t groups = (size_t)(j.n + 31) / 32;
@@ -89,6 +88,50 @@ size_t estimate_bytes(const Job& j) {
     const size_t survivors = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 24;
     const size_t gen = (size_t)std::max<int64_t>(1 << 20, 16LL * j.n) * 48 + reads;
     return 2 * reads + entries + survivors + gen + (8u << 20);
+}
+
+// Bytes of the 16-bit DP's cell tags a run over n reads of at most maxlen
+// symbols may ask for: two launches in flight, each holding one word per
+// resident lane, register and sub-block (two per 16-step block, for pairs
+// of L1 + L2 <= min(2 maxlen, kGen16MaxSum)), and never more lanes than
+// 32 per possible pair plus a block.  It depends on the run, not the job:
+// a cohort counts it once.
+size_t tag_bytes(int maxlen, int64_t n, int sms) {
+    const int64_t pairs = n * (n - 1) / 2;
+    const int64_t lane_regs = std::min<int64_t>((int64_t)sms * crispy::gen16_lane_regs_per_sm(),
+                                                (32 * pairs + 128) * crispy::kGen16MaxR);
+    const int64_t blocks = crispy::gen16_dir_blocks(std::min(2 * maxlen, crispy::kGen16MaxSum));
+    return (size_t)(2 * lane_regs * 2 * blocks * 4);
+}
+
+// Estimate of one run over the jobs js (a lone job or a cohort).
+size_t run_bytes(const std::vector<Job*>& js, int sms) {
+    size_t base = 0;
+    int maxlen = 0;
+    int64_t n = 0;
+    for (const Job* j : js) {
+        base += j->mem_base;
+        maxlen = std::max(maxlen, j->maxlen);
+        n += j->n;
+    }
+    return base + tag_bytes(maxlen, n, sms);
+}
+
+void set_estimate(Job& j, int sms) {
+    j.maxlen = 0;
+    for (int i = 0; i < j.n; ++i) j.maxlen = std::max(j.maxlen, j.len[i]);
+    j.mem_base = estimate_base_bytes(j);
+    j.mem = j.mem_base + tag_bytes(j.maxlen, j.n, sms);
+}
+
+// SMs of a device for the estimates (a GB300's 152 when it cannot be read).
+int device_sms(int device) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    return sms;
 }
 
 int sink_to_job(void* user, int chunk, const void* pairs, const float* dists, int64_t count) {
@@ -105,6 +148,7 @@ int sink_to_job(void* user, int chunk, const void* pairs, const float* dists, in
 
 struct crispy_server {
     int device = 0;
+    int sms = 152;   // the device's SMs, for the estimates
     size_t budget = 0, claimed = 0;
     std::vector<crispy_ctx*> ctx;
     std::vector<std::thread> workers;
@@ -142,14 +186,17 @@ struct crispy_server {
         if (!cohort_member(first) || queue.size() < ctx.size()) return c;
         auto aligned = [](int n) { return (n + 127) / 128 * 128; };
         int reads = aligned(first->n);
-        size_t mem = first->mem;
         for (auto it = queue.begin(); it != queue.end() && (int)c.size() < kCohortJobs;) {
             Job* j = *it;
-            if (cohort_member(j) && j->k == first->k && j->band == first->band &&
-                reads + aligned(j->n) <= kCohortReads && claimed + mem + j->mem <= budget) {
+            bool take = cohort_member(j) && j->k == first->k && j->band == first->band &&
+                        reads + aligned(j->n) <= kCohortReads;
+            if (take) {
                 c.push_back(j);
+                take = claimed + run_bytes(c, sms) <= budget;
+                if (!take) c.pop_back();
+            }
+            if (take) {
                 reads += aligned(j->n);
-                mem += j->mem;
                 it = queue.erase(it);
             } else {
                 ++it;
@@ -201,8 +248,7 @@ struct crispy_server {
     void run_jobs(crispy_ctx* c, const std::vector<Job*>& js) {
         c->run_epoch++;
         c->run_need = 0;
-        size_t reserved = 0;
-        for (Job* j : js) reserved += j->mem;
+        const size_t reserved = run_bytes(js, sms);
         bool done = false;
         if (js.size() > 1) {
             const int rc = run_cohort(c, js);
@@ -248,11 +294,8 @@ struct crispy_server {
             work_cv.wait(lk, [&] { return stopping || (j = take_fitting()) != nullptr; });
             if (!j) return;   // stopping
             const std::vector<Job*> js = take_cohort(j);
-            size_t mem = 0;
-            for (Job* x : js) {
-                mem += x->mem;
-                x->state = CRISPY_JOB_RUNNING;
-            }
+            const size_t mem = run_bytes(js, sms);
+            for (Job* x : js) x->state = CRISPY_JOB_RUNNING;
             claimed += mem;
             lk.unlock();
             run_jobs(c, js);
@@ -286,6 +329,7 @@ int crispy_server_create(int device, size_t hbm_budget_bytes, int slots, crispy_
     *out = nullptr;
     auto* s = new crispy_server();
     s->device = device;
+    s->sms = device_sms(device);
     if (hbm_budget_bytes == 0) {
         size_t free_b = 0, total = 0;
         cudaSetDevice(device);
@@ -342,7 +386,7 @@ int crispy_server_submit(crispy_server* s, const char* seqbuf, const int64_t* of
     j->band = band <= 0 ? 2 : band;
     j->kthr = kmer_thr;
     j->gthr = gen_thr;
-    j->mem = estimate_bytes(*j);
+    set_estimate(*j, s->sms);
     j->t_submit = clock_type::now();
     std::lock_guard<std::mutex> g(s->mu);
     if (j->mem > s->budget) {
@@ -447,7 +491,10 @@ int crispy_server_job_bytes(const int32_t* lengths, int n, int k, size_t* bytes)
     int64_t total = 0;
     for (int i = 0; i < n; ++i) total += std::max(0, lengths[i]);
     j.bases.assign((size_t)total, 'A');
-    *bytes = estimate_bytes(j);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    set_estimate(j, device_sms(dev));
+    *bytes = j.mem;
     return CRISPY_OK;
 }
 
