@@ -30,8 +30,8 @@
 // adds and multiply-adds act on both halves at once.
 //
 // ML and AL by a path walk.  Every cell's tag t (its choice) goes into a
-// per-register word, 2 bits per cell and step, stored every 8 steps to the
-// pair's region of `dirs`.  After the sweep the pair's lanes walk the path
+// per-register word per parity, 2 bits per cell, stored every 16 steps to
+// the pair's region of `dirs`.  After the sweep the pair's lanes walk the path
 // back from the chosen last-row / last-column cell E to the boundary cell
 // (i0, j0) it leaves, following the tags (the reference's tie-broken
 // choices), and count A = diagonal moves and the gap penalties Gp (each gap
@@ -48,9 +48,10 @@
 // registers r + 1 / r - 1 of the same lane, so only the lane's edge
 // register crosses lanes (one shuffle of keys per step).
 // Tags: step tau = s + (kBand & 1) (odd bands run one step late) lies in
-// sub-block sb = tau / 8; register r of lane l keeps that sub-block's tags
-// in word (sb * G + l) * R + r of the pair's region, the step's tag at bits
-// 2 (7 - tau % 8) of the half.
+// block b = tau / 16 at parity P = tau % 2; register r of lane l keeps the
+// block's tags of parity P in word ((2b + P) * G + l) * R + r of the pair's
+// region, the step's tag at bits 2 (7 - (tau % 16) / 2) of the half, so a
+// diagonal (same slot, same parity) runs through consecutive fields.
 // Symbols: 2 bits each, first symbol in the low bits, in shared memory
 // behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
 // windows out of four 32-symbol windows (consecutive slots of a lane read
@@ -123,7 +124,7 @@ template <int R>
 struct St {
     uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
     uint32_t U[R], F[R]; // up / left candidates the last step sent
-    uint32_t D[R];       // tags of the current 8 steps, 2 bits per cell, first step highest
+    uint32_t D[2][R];    // tags of the block by parity, 2 bits per cell, first step highest
     uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
     uint32_t CP[2][R];   // per half: 0xFFFF in band, kOut outside
 };
@@ -306,7 +307,7 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         const uint32_t xn1 = x1 * mu.neg1 + kLo;
         st.U[r] = x2 * mu.n19 + (xn1 * mu.m5 + K);
         st.F[r] = x2 * mu.n21 + (x1 * mu.m3 + K);
-        st.D[r] = x2 * mu.one + (st.D[r] * mu.four + x1);   // tag t = b0 + 2 b1
+        st.D[P][r] = x2 * mu.one + (st.D[P][r] * mu.four + x1);   // tag t = b0 + 2 b1
         st.K[P][r] = K;
     }
     if (kMode != kClean) {
@@ -316,25 +317,28 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
     }
 }
 
-// A block of 16 steps: two halves of 8, after each of which the lane's tag
-// words go to `dst` (sub-block h at dst + h * G * R; nullptr: not stored).
+// A block of 16 steps, after which the lane's tag words go to `dst`
+// (parity P at dst + P * G * R; nullptr: not stored).
 template <int G, int R, int kMode>
 __device__ __forceinline__ void block16(St<R>& st, int gl, int s0, const Pair16& pc, const Mul& mu,
                                         uint32_t sel0, uint32_t sel1, Best16& col, Best16& row,
                                         uint32_t* dst) {
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-#pragma unroll 1
-        for (int t = 0; t < 8; t += 2) {
-            step16<G, R, 0, kMode>(st, gl, s0 + 8 * h + t, pc, mu, sel0, sel1, col, row);
-            step16<G, R, 1, kMode>(st, gl, s0 + 8 * h + t + 1, pc, mu, sel0, sel1, col, row);
-        }
-        if (dst) {
+    for (int t = 0; t < kSteps; t += 2) {
+        step16<G, R, 0, kMode>(st, gl, s0 + t, pc, mu, sel0, sel1, col, row);
+        step16<G, R, 1, kMode>(st, gl, s0 + t + 1, pc, mu, sel0, sel1, col, row);
+    }
+    if (dst) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) dst[h * G * R + r] = st.D[r];
+        for (int r = 0; r < R; ++r) {
+            dst[r] = st.D[0][r];
+            dst[G * R + r] = st.D[1][r];
         }
+    }
 #pragma unroll
-        for (int r = 0; r < R; ++r) st.D[r] = 0;
+    for (int r = 0; r < R; ++r) {
+        st.D[0][r] = 0;
+        st.D[1][r] = 0;
     }
 }
 
@@ -359,7 +363,7 @@ __device__ __forceinline__ Best16 group_best16(Best16 b) {
 __device__ __forceinline__ int gap_pen(int g, int t) { return t == 3 ? -10 : (t == g ? -1 : 0); }
 
 // Walks the path back from cell (i, j) to the boundary over the tags the
-// sweep stored in `region`, staging up to kDepth sub-blocks at a time in
+// sweep stored in `region`, staging up to kDepth 16-step blocks at a time in
 // `stage` (the G lanes of the pair load them together; every lane walks).
 // Returns the diagonal moves in *na, the gap penalties in *gp; (i, j) ends
 // at the boundary cell.
@@ -367,17 +371,18 @@ template <int G, int R>
 __device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, const Pair16& pc, int gl,
                                        bool walking, int& i, int& j, int* na, int* gp) {
     constexpr int kGR = G * R;
-    constexpr int kDepth = (2 * kSmWords) / kGR < 8 ? (2 * kSmWords) / kGR : 8;
+    constexpr int kBlockWords = 2 * kGR;   // a block: parity 0, parity 1
+    constexpr int kDepth = (2 * kSmWords) / kBlockWords < 4 ? (2 * kSmWords) / kBlockWords : 4;
     static_assert(kDepth >= 1 && kGR % 4 == 0, "tag staging");
-    int lo = INT_MAX;   // first staged sub-block
+    int lo = INT_MAX;   // first staged block
     int a = 0, g = 0, gprev = -1;
     while (__any_sync(0xffffffffu, walking)) {
         if (walking && i > 0 && j > 0) {
-            const int sb = (i + j + pc.shift) >> 3;
-            if (sb < lo) {
-                lo = max(0, sb - kDepth + 1);
-                const int n4 = (sb + 1 - lo) * (kGR / 4);
-                const uint4* src = reinterpret_cast<const uint4*>(region + (int64_t)lo * kGR);
+            const int blk = (i + j + pc.shift) >> 4;
+            if (blk < lo) {
+                lo = max(0, blk - kDepth + 1);
+                const int n4 = (blk + 1 - lo) * (kBlockWords / 4);
+                const uint4* src = reinterpret_cast<const uint4*>(region + (int64_t)lo * kBlockWords);
                 uint4* dst = reinterpret_cast<uint4*>(stage);
                 for (int k = gl; k < n4; k += G) dst[k] = src[k];
             }
@@ -390,20 +395,22 @@ __device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, 
                 break;
             }
             const int tau = i + j + pc.shift;
-            const int sb = tau >> 3;
-            if (sb < lo) break;   // stage the sub-blocks below
-            const int q = (i - j + pc.kb - (tau & 1)) >> 1;
+            const int blk = tau >> 4;
+            if (blk < lo) break;   // stage the blocks below
+            const int par = tau & 1;
+            const int q = (i - j + pc.kb - par) >> 1;
             const int hi = q >= kGR ? 1 : 0;
-            const int qq = min(max(q - hi * kGR, 0), kGR - 1);
-            // the half's tags of steps tau % 8, tau % 8 - 1, ... from bit 0 up
-            const uint32_t x = ((stage[(sb - lo) * kGR + qq] >> (16 * hi)) & 0xFFFFu) >> (2 * (7 - (tau & 7)));
+            const int qq = min(max(q - hi * kGR, 0), kGR - 1);   // in range for every in-band cell
+            // the half's tags of this parity at steps tau, tau - 2, ... from bit 0 up
+            const uint32_t w = stage[(blk - lo) * kBlockWords + par * kGR + qq];
+            const uint32_t x = ((w >> (16 * hi)) & 0xFFFFu) >> (2 * (7 - ((tau & 15) >> 1)));
             const int t = (int)(x & 3u);
             if (gprev >= 0) g += gap_pen(gprev, t);
             if (t == 3) {
-                // a diagonal move keeps the slot and goes two steps back: the
-                // run of diagonal tags at steps tau, tau - 2, ... in this word
-                const uint32_t y = ~x & 0x3333u;
-                const int k = min(y ? (__ffs(y) - 1) >> 2 : 4, min(i, j));
+                // a diagonal move keeps the slot and the parity: the run of
+                // diagonal tags at steps tau, tau - 2, ... in this word
+                const uint32_t z = ~(x & (x >> 1)) & 0x5555u;
+                const int k = min(z ? (__ffs(z) - 1) >> 1 : 8, min(i, j));
                 a += k; i -= k; j -= k; gprev = -1;
             } else if (t == 1) {
                 --j; gprev = 1;
@@ -482,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
-            st.D[r] = 0;
+            st.D[0][r] = 0; st.D[1][r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
             st.CP[0][r] = kOut2; st.CP[1][r] = kOut2;
