@@ -14,13 +14,14 @@
 // t its choice's tag: 3 diagonal, 1 up, 0 left.  A cell's three candidates
 // carry distinct tags, so one unsigned three-way maximum of their keys gives
 // the maximum and the reference's tie order at once: one __vimax3_u16x2 per
-// two cells.  The winner's tag bits b0 = t & 1, b1 = t >> 1 give the two
-// gap candidates it sends to the next anti-diagonal, already keyed:
-//   up:    K + 5 (1 - b0) - 38 b1   = 4 (M + pen_up)   + 1 + 4 (s+1) + kBase
-//   left:  K + 3 b0 - 42 b1         = 4 (M + pen_left) + 0 + 4 (s+1) + kBase
+// two cells.  The winner's tag t and x2 = t & 2 give the two gap candidates
+// it sends to the next anti-diagonal, already keyed, by multiply-adds:
+//   up:    K + 5 - 5 t - 14 x2   = 4 (M + pen_up)   + 1 + 4 (s+1) + kBase
+//   left:  K + 3 t - 24 x2       = 4 (M + pen_left) + 0 + 4 (s+1) + kBase
 // (pen_up = -10 / -1 / 0 and pen_left = -10 / 0 / -1 after a diagonal / up /
 // left choice), and the diagonal candidate two steps later is
-// (K | 3) + 28 - 36 * mismatch.  Every cell the recurrence reaches has
+// (K | 3) + 28 - 36 * mismatch; the cell stores its base K - t + 31 =
+// (K | 3) + 28 in place of K (one three-input add).  Every cell the recurrence reaches has
 // -4 min(i,j) <= M <= 5 min(i,j) (the diagonal candidate has no state and a
 // gap never gains), so 4M + 4s lies in [-4s, 14s]: with kBase = 4 * 3632 +
 // 128 every key of a pair with L1 + L2 <= 3600 -- and of the up to 32 steps
@@ -104,7 +105,7 @@ __device__ __forceinline__ int kband16(int l1, int l2, int band) {
 // compiler cannot see): products by them stay multiply-adds on the FMA pipe
 // instead of turning into shift / add sequences on the ALU.
 struct Mul {
-    uint32_t one, four, n36, m5, n19, m3, n21, neg1;
+    uint32_t one, four, n36, n5, n14, m3, n24, c5;
 };
 
 __device__ __forceinline__ Mul make_mul(const int* o) {
@@ -112,17 +113,17 @@ __device__ __forceinline__ Mul make_mul(const int* o) {
     m.one = (uint32_t)o[0];
     m.four = 4u * (uint32_t)o[1];
     m.n36 = (uint32_t)(-36) * (uint32_t)o[2];
-    m.m5 = 5u * (uint32_t)o[3];
-    m.n19 = (uint32_t)(-19) * (uint32_t)o[4];
+    m.n5 = (uint32_t)(-5) * (uint32_t)o[3];
+    m.n14 = (uint32_t)(-14) * (uint32_t)o[4];
     m.m3 = 3u * (uint32_t)o[5];
-    m.n21 = (uint32_t)(-21) * (uint32_t)o[0];
-    m.neg1 = (uint32_t)(-1) * (uint32_t)o[3];
+    m.n24 = (uint32_t)(-24) * (uint32_t)o[0];
+    m.c5 = 5u * kLo * (uint32_t)o[1];
     return m;
 }
 
 template <int R>
 struct St {
-    uint32_t K[2][R];    // keys by step parity (the diagonal source two steps on)
+    uint32_t K[2][R];    // diagonal bases (K | 3) + 28 by step parity, for two steps on
     uint32_t U[R], F[R]; // up / left candidates the last step sent
     uint32_t D[2][R];    // tags of the block by parity, 2 bits per cell, first step highest
     uint32_t MW[2][R];   // mismatch flags of the block by parity, 2 bits per step
@@ -247,12 +248,12 @@ __device__ __forceinline__ void track16(const St<R>& st, int gl, int s, const Pa
     const bool hc = ic >= 1 && ic <= pc.l2 && dc >= -pc.kb && dc <= pc.kb && mine(qc, gl, G, R);
     if (hr) {
         const uint32_t key = take<G, R, P>(st, qr, gl);
-        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        const int m = ((int)key - 31 - 4 * s - kBase) >> 2;
         if (m >= col.m) { col.m = m; col.at = jr; }
     }
     if (hc) {
         const uint32_t key = take<G, R, P>(st, qc, gl);
-        const int m = ((int)(key & ~3u) - 4 * s - kBase) >> 2;
+        const int m = ((int)key - 31 - 4 * s - kBase) >> 2;
         if (m >= row.m) { row.m = m; row.at = ic; }
     }
 }
@@ -294,8 +295,7 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
         }
         const uint32_t mm = st.MW[P][r] & kLo;
         st.MW[P][r] >>= 2;
-        const uint32_t od = (st.K[P][r] | 0x00030003u) + 0x001C001Cu;
-        const uint32_t kd = mm * mu.n36 + od;
+        const uint32_t kd = mm * mu.n36 + st.K[P][r];
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
         if (kMode == kStart && (r == ra || r == rb)) {
@@ -303,12 +303,11 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             if (r == ra) boundary_set(K, st.CP[P][r], ha, s, 0u);
             if (r == rb) boundary_set(K, st.CP[P][r], hb, s, 1u);
         }
-        const uint32_t x1 = K & kLo, x2 = K & (2u * kLo);
-        const uint32_t xn1 = x1 * mu.neg1 + kLo;
-        st.U[r] = x2 * mu.n19 + (xn1 * mu.m5 + K);
-        st.F[r] = x2 * mu.n21 + (x1 * mu.m3 + K);
-        st.D[P][r] = x2 * mu.one + (st.D[P][r] * mu.four + x1);   // tag t = b0 + 2 b1
-        st.K[P][r] = K;
+        const uint32_t t = K & (3u * kLo), x2 = K & (2u * kLo);
+        st.U[r] = x2 * mu.n14 + (t * mu.n5 + (K * mu.one + mu.c5));
+        st.F[r] = x2 * mu.n24 + (t * mu.m3 + K);
+        st.D[P][r] = st.D[P][r] * mu.four + t;
+        st.K[P][r] = K - t + 31u * kLo;
     }
     if (kMode != kClean) {
         const bool near = (unsigned)(s - pc.tw[0]) < 2u * R || (unsigned)(s - pc.tw[1]) < 2u * R ||
@@ -488,7 +487,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
         St<R> st;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            st.K[0][r] = kOut2; st.K[1][r] = kOut2; st.U[r] = kOut2; st.F[r] = kOut2;
+            st.K[0][r] = 39u * kLo; st.K[1][r] = 39u * kLo; st.U[r] = kOut2; st.F[r] = kOut2;
             st.D[0][r] = 0; st.D[1][r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
             // every cap starts closed; a slot's boundary cell opens it
