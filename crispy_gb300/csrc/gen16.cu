@@ -487,6 +487,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
         St<R> st;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
+            // a closed cell (key 8) has the diagonal base (8 | 3) + 28 = 39
             st.K[0][r] = 39u * kLo; st.K[1][r] = 39u * kLo; st.U[r] = kOut2; st.F[r] = kOut2;
             st.D[0][r] = 0; st.D[1][r] = 0;
             st.MW[0][r] = 0; st.MW[1][r] = 0;
