@@ -53,11 +53,11 @@
 // block's tags of parity P in word ((2b + P) * G + l) * R + r of the pair's
 // region, the step's tag at bits 2 (7 - (tau % 16) / 2) of the half, so a
 // diagonal (same slot, same parity) runs through consecutive fields.
-// Symbols: 2 bits each, first symbol in the low bits, in shared memory
-// behind a zero pad; per block of 16 steps a lane cuts its slots' 16-symbol
+// Symbols: two bit planes per read in shared memory, 32 symbols per word,
+// behind a zero pad; every 32 steps a lane cuts its slots' 17-symbol
 // windows out of four 32-symbol windows (consecutive slots of a lane read
-// windows one symbol apart) and folds them into 8 mismatch flags per slot
-// and parity.
+// windows one symbol apart) and folds them into 16 one-bit mismatch flags
+// per slot and parity.
 // Border: a slot hosts one diagonal d per parity, so it enters the matrix
 // once, at s = |d|, as a boundary cell (row 0 or column 0).  Every slot's cap
 // starts closed (key 8); the two boundary cells of a step (d = s and d = -s)
@@ -81,11 +81,16 @@ constexpr int kWarps = kThreads / 32;
 // registers, 4 up to 128.
 template <int R>
 constexpr int min_blocks16() { return R <= 3 ? 6 : (R == 4 ? 5 : 3); }
-constexpr int kPadWords = 12;        // zero words before a read: positions down to -192
-constexpr int kSmWords = kPadWords + 128 + 4;   // pad, 2048 symbols, zero tail
+// A read in shared memory: two bit planes (bit 0 and bit 1 of each symbol's
+// code), 32 symbols per word, each behind kPlanePad zero words (positions
+// down to -192) and before 2 zero tail words.
+constexpr int kPlanePad = 6;
+constexpr int kPlaneWords = kPlanePad + 64 + 2;
+constexpr int kSmWords = 2 * kPlaneWords;
 constexpr int kPairWords = 2 * kSmWords + 4;    // both reads of a pair, 4 words apart in banks
 static_assert(kPairWords % 32 == 4 && kSmWords % 4 == 0, "shared layout");
 constexpr int kSteps = 16;           // steps per block: 8 cells per slot and parity
+constexpr int kSetupSteps = 32;      // steps per window set-up: 16 cells per slot and parity
 constexpr int kSlack = 32;           // steps a sweep may run past a pair's end
 constexpr int kBase = 4 * (kGen16MaxSum + kSlack) + 128;
 constexpr uint32_t kLo = 0x00010001u;   // 1 in each half
@@ -142,24 +147,23 @@ struct Best16 {
     int at;
 };
 
-// 32 symbols starting at read position pos as (lo, hi) words, first symbol
-// in bits 0-1 of lo (before the read and past it: zeros).  sm points at the
-// pad, so word w of the read is sm[kPadWords + w].
-__device__ __forceinline__ void window32(const uint32_t* sm, int pos, uint32_t& lo, uint32_t& hi) {
-    const int w = min(max(pos >> 4, -kPadWords), 128) + kPadWords;
-    const int sh = (pos & 15) * 2;
-    const uint32_t a = sm[w], b = sm[w + 1], c = sm[w + 2];
-    lo = __funnelshift_r(a, b, sh);
-    hi = __funnelshift_r(b, c, sh);
+// 32 symbols starting at read position pos as their two bit planes (first
+// symbol in bit 0; before the read and past it: zeros).
+__device__ __forceinline__ void window32(const uint32_t* sm, int pos, uint32_t& p0, uint32_t& p1) {
+    const int w = min(max(pos >> 5, -kPlanePad), 64) + kPlanePad;
+    const int sh = pos & 31;
+    p0 = __funnelshift_r(sm[w], sm[w + 1], sh);
+    p1 = __funnelshift_r(sm[kPlaneWords + w], sm[kPlaneWords + w + 1], sh);
 }
 
-// Mismatch flags of the block.  Parity-0 cells k = 0..7 of slot q compare
+// Mismatch flags of 32 steps.  Parity-0 cells k = 0..15 of slot q compare
 // read1[j0 - 1 + k] with read2[i0 - 1 + k], parity-1 cells read1[j0 - 1 + k]
 // with read2[i0 + k], (i0, j0) = ((s0 + d0) / 2, (s0 - d0) / 2) the slot's
-// parity-0 cell at the block start, d0 = 2q - kb.  The lane's R slots of a
-// half are consecutive, q = qb + r: read1 windows start at J - r, read2
-// windows at I + r, all inside one 32-symbol window per read.  A flag sits
-// at bit 2k of its half.  A finished pair's caps close.
+// parity-0 cell at the set-up, d0 = 2q - kb.  The lane's R slots of a half
+// are consecutive, q = qb + r: read1 windows start at J - r, read2 windows
+// at I + r, all inside one 32-symbol window per read.  A flag sits at bit k
+// of its half (a mismatch: either plane differs).  A finished pair's caps
+// close.
 template <int G, int R>
 __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, const uint32_t* sm2, int gl,
                                             int s0, const Pair16& pc, bool finished) {
@@ -169,17 +173,14 @@ __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, cons
         const int qb = (h * G + gl) * R;
         const int d0 = 2 * qb - pc.kb;
         const int I = ((s0 + d0) >> 1) - 1, J = ((s0 - d0) >> 1) - 1;   // s0 + d0 is even
-        uint32_t a_lo, a_hi, b_lo, b_hi;
-        window32(sm1, J - (R - 1), a_lo, a_hi);   // read1 from J - (R-1): slot r at offset R-1-r
-        window32(sm2, I, b_lo, b_hi);             // read2 from I: slot r at offset r
+        uint32_t a0, a1, b0, b1;
+        window32(sm1, J - (R - 1), a0, a1);   // read1 from J - (R-1): slot r at offset R-1-r
+        window32(sm2, I, b0, b1);             // read2 from I: slot r at offset r
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const uint32_t w1 = __funnelshift_r(a_lo, a_hi, 2 * (R - 1 - r));
-            const uint32_t w2 = __funnelshift_r(b_lo, b_hi, 2 * r);
-            const uint32_t w2n = __funnelshift_r(b_lo, b_hi, 2 * r + 2);   // read2 one symbol on
-            const uint32_t x0 = w1 ^ w2, x1 = w1 ^ w2n;
-            f0[h][r] = (x0 | (x0 >> 1)) & 0x55555555u;
-            f1[h][r] = (x1 | (x1 >> 1)) & 0x55555555u;
+            const uint32_t u0 = a0 >> (R - 1 - r), u1 = a1 >> (R - 1 - r);
+            f0[h][r] = (u0 ^ (b0 >> r)) | (u1 ^ (b1 >> r));
+            f1[h][r] = (u0 ^ (b0 >> (r + 1))) | (u1 ^ (b1 >> (r + 1)));   // read2 one symbol on
         }
     }
 #pragma unroll
@@ -188,6 +189,27 @@ __device__ __forceinline__ void block_setup(St<R>& st, const uint32_t* sm1, cons
         st.MW[1][r] = __byte_perm(f1[0][r], f1[1][r], 0x5410);
         if (finished) { st.CP[0][r] = kOut2; st.CP[1][r] = kOut2; }
     }
+}
+
+// Even bits of x to its low half, odd bits to its high half, in order.
+__device__ __forceinline__ uint32_t unzip_bits(uint32_t x) {
+    uint32_t t;
+    t = (x ^ (x >> 1)) & 0x22222222u; x ^= t ^ (t << 1);
+    t = (x ^ (x >> 2)) & 0x0C0C0C0Cu; x ^= t ^ (t << 2);
+    t = (x ^ (x >> 4)) & 0x00F000F0u; x ^= t ^ (t << 4);
+    t = (x ^ (x >> 8)) & 0x0000FF00u; x ^= t ^ (t << 8);
+    return x;
+}
+
+// Plane word k of a read (symbols 32 (k - kPlanePad) ..) from its packed
+// words (16 symbols each, first symbol in the top bits): the bit reversal
+// puts symbol q's code bits at 2q + 1 (bit 0) and 2q (bit 1).
+__device__ __forceinline__ void plane_word(const uint32_t* g, int nw, int k, uint32_t& p0, uint32_t& p1) {
+    const int w = 2 * (k - kPlanePad);
+    const uint32_t x0 = w >= 0 && w < nw ? unzip_bits(__brev(g[w])) : 0u;
+    const uint32_t x1 = w + 1 >= 0 && w + 1 < nw ? unzip_bits(__brev(g[w + 1])) : 0u;
+    p0 = __byte_perm(x0, x1, 0x7632);   // code bit 0 of symbols 0..31
+    p1 = __byte_perm(x0, x1, 0x5410);   // code bit 1
 }
 
 // Boundary events of a step: slot q = (d + kb - P) / 2 for d = s (column
@@ -294,7 +316,7 @@ __device__ __forceinline__ void step16(St<R>& st, int gl, int s, const Pair16& p
             upK = r < R - 1 ? st.U[r + 1] : nK;
         }
         const uint32_t mm = st.MW[P][r] & kLo;
-        st.MW[P][r] >>= 2;
+        st.MW[P][r] >>= 1;
         const uint32_t kd = mm * mu.n36 + st.K[P][r];
         uint32_t K = __vimax3_u16x2(kd, upK, lfK);
         K = __vminu2(K, st.CP[P][r]);
@@ -475,13 +497,9 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
         const int nw1 = (pc.l1 + 15) >> 4, nw2 = (pc.l2 + 15) >> 4;
         const uint32_t* g1 = a.packed + (valid ? a.woff[pr.x] : 0);
         const uint32_t* g2 = a.packed + (valid ? a.woff[pr.y] : 0);
-        // first symbol to the low bits: the bit reversal also swaps the two
-        // bits of each symbol, which a mismatch test (xor, then or of the
-        // pair) does not see
-        for (int k = gl; k < kSmWords; k += G) {
-            const int w = k - kPadWords;
-            sm1[k] = w >= 0 && w < nw1 ? __brev(g1[w]) : 0u;
-            sm2[k] = w >= 0 && w < nw2 ? __brev(g2[w]) : 0u;
+        for (int k = gl; k < kPlaneWords; k += G) {
+            plane_word(g1, nw1, k, sm1[k], sm1[kPlaneWords + k]);
+            plane_word(g2, nw2, k, sm2[k], sm2[kPlaneWords + k]);
         }
         __syncwarp();
         St<R> st;
@@ -512,7 +530,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks16<R>()) gen16_kernel(GenA
         for (int t0 = 0; t0 <= t_end; t0 += kBlock) {
             const int s0 = t0 - pc.shift;
             const bool finished = s0 > s_end;
-            block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
+            if ((t0 & (kSetupSteps - 1)) == 0) block_setup<G, R>(st, sm1, sm2, gl, s0, pc, finished);
             uint32_t* dst = fits && !finished ? region + ((int64_t)(t0 >> 4) * 2 * G + gl) * R : nullptr;
             const bool started = s0 > pc.kb;   // every boundary cell is behind (s = |d| <= kb)
             const bool clean = finished || (started && s0 + kBlock - 1 < clean_hi);
