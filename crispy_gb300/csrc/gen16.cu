@@ -383,32 +383,71 @@ __device__ __forceinline__ Best16 group_best16(Best16 b) {
 // (genCPU.cpp:404-414; a boundary cell's tag gives 0).
 __device__ __forceinline__ int gap_pen(int g, int t) { return t == 3 ? -10 : (t == g ? -1 : 0); }
 
+// Asynchronous 16-byte global-to-shared copies (cp.async), grouped.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Walks the path back from cell (i, j) to the boundary over the tags the
-// sweep stored in `region`, staging up to kDepth 16-step blocks at a time in
-// `stage` (the G lanes of the pair load them together; every lane walks).
-// Returns the diagonal moves in *na, the gap penalties in *gp; (i, j) ends
-// at the boundary cell.
+// sweep stored in `region`, a window of kDepth 16-step blocks at a time in
+// `stage` (the G lanes of the pair copy it together; every lane walks).
+// The path leaves a window [lo, top] exactly at block lo - 1 (a move goes
+// back at most one block), so the windows come in a fixed order: with
+// room for two, the next one is copied (cp.async) while the current one is
+// walked.  Returns the diagonal moves in *na, the gap penalties in *gp;
+// (i, j) ends at the boundary cell.
 template <int G, int R>
 __device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, const Pair16& pc, int gl,
                                        bool walking, int& i, int& j, int* na, int* gp) {
     constexpr int kGR = G * R;
     constexpr int kBlockWords = 2 * kGR;   // a block: parity 0, parity 1
-    constexpr int kDepth = (2 * kSmWords) / kBlockWords < 4 ? (2 * kSmWords) / kBlockWords : 4;
+    constexpr int kBlock4 = kBlockWords / 4;
+    constexpr bool kDouble = kSmWords / kBlockWords >= 1;   // two windows of at least a block
+    constexpr int kRoom = kDouble ? kSmWords / kBlockWords : (2 * kSmWords) / kBlockWords;
+    constexpr int kDepth = kRoom < 8 ? kRoom : 8;
+    constexpr int kBuf4 = kSmWords / 4;   // uint4 per buffer (double-buffered)
     static_assert(kDepth >= 1 && kGR % 4 == 0, "tag staging");
-    int lo = INT_MAX;   // first staged block
+    const uint4* region4 = reinterpret_cast<const uint4*>(region);
+    uint4* stage4 = reinterpret_cast<uint4*>(stage);
+    auto below = [](int top) { return top < 0 ? -1 : max(0, top - kDepth + 1) - 1; };
+    // window [max(0, top - kDepth + 1), top] into buffer b, one copy group
+    // (empty for top < 0)
+    auto issue = [&](int top, int b) {
+        if (top >= 0) {
+            const int lo = max(0, top - kDepth + 1);
+            const int n4 = (top + 1 - lo) * kBlock4;
+            const uint4* src = region4 + (int64_t)lo * kBlock4;
+            uint4* dst = stage4 + b * kBuf4;
+            for (int k = gl; k < n4; k += G) cp_async16(dst + k, src + k);
+        }
+        cp_async_commit();
+    };
+    int wtop = walking && i > 0 && j > 0 ? (i + j + pc.shift) >> 4 : -1;   // window walked next
+    int ntop = below(wtop);                                                   // the one after it
+    int cur = 0, lo = INT_MAX;
+    if (kDouble) {
+        issue(wtop, 0);
+        issue(ntop, 1);
+    }
     int a = 0, g = 0, gprev = -1;
     while (__any_sync(0xffffffffu, walking)) {
-        if (walking && i > 0 && j > 0) {
-            const int blk = (i + j + pc.shift) >> 4;
-            if (blk < lo) {
-                lo = max(0, blk - kDepth + 1);
-                const int n4 = (blk + 1 - lo) * (kBlockWords / 4);
-                const uint4* src = reinterpret_cast<const uint4*>(region + (int64_t)lo * kBlockWords);
-                uint4* dst = reinterpret_cast<uint4*>(stage);
-                for (int k = gl; k < n4; k += G) dst[k] = src[k];
+        const bool need = walking && i > 0 && j > 0;
+        if (need) {
+            lo = max(0, wtop - kDepth + 1);
+            if (kDouble) {
+                cp_async_wait<1>();   // the current window (the next may be in flight)
+            } else {
+                const int n4 = (wtop + 1 - lo) * kBlock4;
+                const uint4* src = region4 + (int64_t)lo * kBlock4;
+                for (int k = gl; k < n4; k += G) stage4[k] = src[k];
             }
         }
         __syncwarp();
+        const uint32_t* buf = stage + (kDouble ? cur * kSmWords : 0);
         while (walking) {
             if (i == 0 || j == 0) {
                 if (gprev >= 0) g += gap_pen(gprev, j == 0 ? 0 : 1);   // column 0: tag left, row 0: up
@@ -417,13 +456,13 @@ __device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, 
             }
             const int tau = i + j + pc.shift;
             const int blk = tau >> 4;
-            if (blk < lo) break;   // stage the blocks below
+            if (blk < lo) break;   // the next window
             const int par = tau & 1;
             const int q = (i - j + pc.kb - par) >> 1;
             const int hi = q >= kGR ? 1 : 0;
             const int qq = min(max(q - hi * kGR, 0), kGR - 1);   // in range for every in-band cell
             // the half's tags of this parity at steps tau, tau - 2, ... from bit 0 up
-            const uint32_t w = stage[(blk - lo) * kBlockWords + par * kGR + qq];
+            const uint32_t w = buf[(blk - lo) * kBlockWords + par * kGR + qq];
             const uint32_t x = ((w >> (16 * hi)) & 0xFFFFu) >> (2 * (7 - ((tau & 15) >> 1)));
             const int t = (int)(x & 3u);
             if (gprev >= 0) g += gap_pen(gprev, t);
@@ -440,7 +479,17 @@ __device__ __forceinline__ void walk16(const uint32_t* region, uint32_t* stage, 
             }
         }
         __syncwarp();
+        if (need) {
+            // the window is walked: its buffer takes the window after the next
+            const int t2 = below(ntop);
+            if (kDouble) issue(t2, cur);
+            cur ^= 1;
+            wtop = ntop;
+            ntop = t2;
+        }
     }
+    if (kDouble) cp_async_wait<0>();   // no copy may land in the next pair's sequences
+    __syncwarp();
     *na = a;
     *gp = g;
 }
