@@ -47,7 +47,9 @@ class Stats(C.Structure):
                 ("kmer_survivors", C.c_int64), ("gen_pairs", C.c_int64),
                 ("gen_cells", C.c_int64), ("gen_survivors", C.c_int64),
                 ("kernels_launched", C.c_int64), ("graph_launches", C.c_int64),
-                ("kmer_spilled", C.c_int64)]
+                ("kmer_spilled", C.c_int64), ("kmer_bound_entries", C.c_int64),
+                ("kmer_full_entries", C.c_int64), ("kmer_full_columns", C.c_int64),
+                ("kmer_rounds", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -47,7 +47,11 @@ struct KmerJob {
     std::vector<int32_t> h_tgent;    // tile stream: steps per lane in each group
     int64_t ntent = 0;
     DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
-    DevBuf tgentL, nsec;             // K = 8: L-stream steps per group; per-read H/L counts
+    DevBuf tgentL, nsec;             // second-stream steps per group; per-read section counts
+    // K <= 6: the split of every read's dense level entries into two
+    // sections (a hash of the plane word below split / 256: section 0), 0:
+    // one section; the tile kernel bounds each pair after section 0
+    int split = 0;
     std::vector<int32_t> h_nsec;
     // K = 8 read order: per-read arrays above (t, cntmax, hinfo, entries)
     // are by position in it; perm maps position -> read ID, offp holds the

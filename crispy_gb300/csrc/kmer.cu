@@ -60,6 +60,7 @@ constexpr int kHashBits = 11;
 constexpr int kHashSlots = 1 << kHashBits;   // high-level entries of one row group
 constexpr int kHashMaxKeys = kHashSlots / 2; // load factor <= 1/2 keeps probes short
 constexpr int kPlaneBudget = 128 * 1024;     // dense level planes per block
+constexpr int kSplitDefault = 112;           // section 0 of the split streams: 112/256 of the entries
 
 __device__ __forceinline__ uint32_t sym2(uint8_t c) {
     // A=0 G=1 T=2 C=3, everything else 0 (kmerMain.cpp:137-152)
@@ -92,17 +93,26 @@ __device__ __forceinline__ int64_t ent_at(int e, int lane) {
 // lane+1, ... mod 32), with the per-bank counts written to bcnt.  The tile kernel does not read this order directly: the
 // schedule kernel below turns it into a bank-conflict-avoiding stream.
 // ---------------------------------------------------------------------------
+// Section of a dense level entry (its plane word index) when a read's
+// dense entries are split in two (K <= 6): a multiplicative hash of the word
+// index above its bank bits, so that every bank splits in the same ratio;
+// section 0 iff the hash's top byte is below split.
+__device__ __forceinline__ int split_section(uint32_t val, uint32_t split) {
+    return ((val >> 3) * 0x9E3779B1u) >> 24 < split ? 0 : 1;
+}
+
 // Raw-list bucket of a dense level entry: K <= 7, the bank of its 32-bit
-// word index; K = 8, the section (H = K-mer >= 0x8000 first) and the 4-byte
-// bank of its 16-bit plane word.
-__device__ __forceinline__ int prep_bucket(uint32_t val, int K) {
+// word index (with a split, behind its section: 0..31 or 32..63); K = 8,
+// the section (H = K-mer >= 0x8000 first) and the 4-byte bank of its 16-bit
+// plane word.
+__device__ __forceinline__ int prep_bucket(uint32_t val, int K, uint32_t split) {
     if (K == 8) {
         // the bank of the K-mer's 32-bit plane word (H: K-mer - 0x8000,
         // L: K-mer), per section
         const uint32_t v = val & 0xFFFFu;
         return (v >= 0x8000u ? 0 : 32) + (int)(v & 31u);
     }
-    return (int)(val & 31u);
+    return (split ? 32 * split_section(val, split) : 0) + (int)(val & 31u);
 }
 
 constexpr int kPrepThreads = 256;
@@ -148,7 +158,8 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
     const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
     uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
-    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt, int32_t* __restrict__ nsec) {
+    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt, int32_t* __restrict__ nsec,
+    uint32_t split) {
     extern __shared__ __align__(16) unsigned long long hist_words[];
     const Hist hist{reinterpret_cast<decltype(Hist::h)>(hist_words)};
     __shared__ int s_max, s_hpos;
@@ -156,9 +167,9 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
     __shared__ int s_bcnt[64], s_bstart[64];
     const uint32_t K4 = 1u << (2 * K);
     // K = 8: two sections, H (K-mer >= 0x8000) then L, grouped by the 4-byte
-    // bank of a 16-bit plane word; K <= 7: one section, grouped by the bank of
-    // a 32-bit word index (value mod 32)
-    const int nsections = K == 8 ? 2 : 1;
+    // bank of a 16-bit plane word; K <= 7: one section (two with a split),
+    // grouped by the bank of a 32-bit word index (value mod 32)
+    const int nsections = K == 8 || split ? 2 : 1;
     hist.clear_all(K4);
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         if (threadIdx.x == 0) { s_max = 0; s_hmax = 0; s_hpos = 0; }
@@ -182,7 +193,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
                 if ((int)t >= dense_levels) {
                     dst[ent_at(atomicAdd(&s_hpos, 1), lane)] = val[k];
                 } else {
-                    rank[k] = atomicAdd(&s_bcnt[prep_bucket(val[k], K)], 1);
+                    rank[k] = atomicAdd(&s_bcnt[prep_bucket(val[k], K, split)], 1);
                 }
             }
         }
@@ -213,7 +224,7 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kPrepPer; ++k)
-            if (rank[k] >= 0) dst[ent_at(s_bstart[prep_bucket(val[k], K)] + rank[k], lane)] = val[k];
+            if (rank[k] >= 0) dst[ent_at(s_bstart[prep_bucket(val[k], K, split)] + rank[k], lane)] = val[k];
         __syncthreads();
         int mx = 0;
         uint32_t hm = 0;
@@ -483,6 +494,44 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_kernel(
     }
 }
 
+// K <= 6 with a split: two streams per group over the same 128-bit plane
+// words, section 0 then section 1, each scheduled on its own.  A group's
+// steps per stream (the largest section of its reads, rounded up to 16) are
+// set here on the device: tgent = section 0, tgentL = section 1, and the
+// section-1 stream starts right after section 0's, so the two read as one
+// stream of tgent + tgentL steps.  tstart leaves room for 2 * gent steps,
+// which bounds the sum (each section holds at most a read's tuples).
+__global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
+    const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
+    const int64_t* __restrict__ tstart, const int32_t* __restrict__ nhigh,
+    const int32_t* __restrict__ nsec, const uint16_t* __restrict__ bcnt, int n, int ngroups,
+    uint32_t guard_word, int32_t* __restrict__ tgent, int32_t* __restrict__ tgentL,
+    uint16_t* __restrict__ tent) {
+    __shared__ SchedSmem sm;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
+        const int r = g * 32 + lane;
+        const bool active = r < n;
+        const int rr = active ? r : 0;
+        const int nh = active ? nhigh[r] : 0;
+        const int n0 = active ? nsec[(int64_t)rr * 2] : 0;
+        const int n1 = active ? nsec[(int64_t)rr * 2 + 1] : 0;
+        const int E0 = ((int)__reduce_max_sync(full, (unsigned)n0) + 15) / 16 * 16;
+        const int E1 = ((int)__reduce_max_sync(full, (unsigned)n1) + 15) / 16 * 16;
+        if (lane == 0) {
+            tgent[g] = E0;
+            tgentL[g] = E1;
+        }
+        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, E0, ent + gstart[g], 0u,
+                        guard_word, 1u, tent + tstart[g]);
+        __syncwarp();
+        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + n0, E1, ent + gstart[g],
+                        0u, guard_word, 1u, tent + tstart[g] + (int64_t)32 * E0);
+        __syncwarp();
+    }
+}
+
 // K = 8: an H stream and an L stream per group; the H section of a read's
 // raw list follows its high-level entries, the L section follows the H
 // section.  Each stream indexes a plane of 32-bit words (bank = word mod
@@ -555,6 +604,14 @@ struct TileArgs {
     const int2* item_q;
     int same_only;
     const int32_t* nsec;
+    // K <= 6: split nonzero when the streams hold two sections (tgent steps
+    // of section 0, then tgentL of section 1); bound nonzero when the tile
+    // kernel bounds each pair after section 0 (the batched form), qfire the
+    // lanes holding a column that start a full-pass round; gstat (may be
+    // null) sums the entries of bound and full passes, the full-pass
+    // columns and the rounds
+    int split, bound, qfire;
+    unsigned long long* gstat;
     // Cohort (several jobs' reads back to back, each starting at a multiple
     // of 128 positions; 128-row kernel, batched form): per item its job and
     // its end column group; per job (base, n, A, stage_dim) and its
@@ -1035,61 +1092,223 @@ __device__ __noinline__ uint4 hash_find4(const uint32_t* hkeys, const uint4* hma
     return make_uint4(0u, 0u, 0u, 0u);
 }
 
+// Bound pass (K <= 6 with a split).  A read's dense level entries are split
+// in two sections by a hash of the plane word, each scheduled as its own
+// stream.  The first pass over a column group counts section 0 only, m0.
+// Every entry of row read a outside section 0 may still match, so
+//     m <= m0 + (Ta - a0),   a0 = a's section-0 entries,
+// and with Tb >= Ta the pair can pass only if m0 >= R_a = mmin[Ta] - Ta + a0,
+// a per-row constant held as bit planes in shared memory.  A lane (column)
+// with no row left alive is done; the others are pushed on the lane's own
+// stack of column groups and later counted in full (both sections, the
+// hash pass, the exact test).  A full-pass round takes one queued column
+// group per lane, so each lane keeps its place in its group's bank
+// schedule; lanes with nothing queued read guard words.  Columns shorter
+// than a row of the quarter (never with reads in length order) stay alive.
+constexpr int kQDepth = 8;    // column groups a lane may hold
+constexpr int kQFire = 28;    // a full-pass round runs once this many lanes hold one
+constexpr int kRPlanes = 12;  // bit planes of the per-row bound (counts < 4096)
+
+// Guard-word indices of one quad of steps for lanes without entries: step
+// k reads guard word (k + lane) mod 8, the bucket the schedule gives the
+// lane there.
+__device__ __forceinline__ uint4 guard_quad(uint32_t g0, int lane) {
+    uint32_t v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = g0 + (uint32_t)((k + lane) & 7);
+    return make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16), v[6] | (v[7] << 16));
+}
+
+// Counts of one column against the 128 row reads over steps [0, El) of its
+// stream (lanes beyond El read guard words up to the warp's Emax): 32
+// entries per iteration as two 16-entry batches, each gathered as two
+// halves of 8 (register budget); the next batch is in flight.
+template <int B, bool kLane>
+__device__ __forceinline__ void accumulate128(const char* __restrict__ Pb, const uint4* __restrict__ ep,
+                                              int El, int Emax, uint4 gq, uint32_t k65536, uint32_t k16,
+                                              Counter<B>* cnt) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cnt[q].clear();
+    // kLane: steps per lane (full-pass rounds); otherwise every lane runs Emax
+    auto ld = [&](int step) { return !kLane || step < El ? __ldg(ep + (step >> 3) * 32) : gq; };
+    uint4 a0, a1;
+    if (Emax > 0) { a0 = ld(0); a1 = ld(8); }
+    for (int e = 0; e < Emax; e += 32) {
+        const bool two = e + 16 < Emax;
+        uint4 b0, b1;
+        if (two) {
+            b0 = ld(e + 16);
+            b1 = ld(e + 24);
+        }
+        uint32_t ca[4];
+        gather16_128<B>(Pb, a0, a1, k65536, k16, cnt, ca);
+        if (e + 32 < Emax) {
+            a0 = ld(e + 32);
+            a1 = ld(e + 40);
+        }
+        if (two) {
+            uint32_t cb[4];
+            gather16_128<B>(Pb, b0, b1, k65536, k16, cnt, cb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cnt[q].add_sixteens2(ca[q], cb[q]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cnt[q].add_sixteens1(ca[q]);
+        }
+    }
+}
+
+// Row bounds of a 128-row block for the bound pass.
+struct RowBound {
+    const uint32_t* thr;    // [4][kRPlanes] bit planes of R_a per quarter
+    const uint32_t* live;   // [4] rows that can pass at all
+    const int* tmax;        // [4] largest row tuple count per quarter
+};
+
+// Stacks of the bound pass: s_q [warp][depth][lane] column groups, s_qn
+// [warp][lane] their sizes, s_qoff [warp][lane] the first position of a
+// warp's stack in its lane's pooled list (the warps' stacks in warp order).
+struct Stacks {
+    uint16_t* q;
+    uint8_t* qn;
+    uint8_t* qoff;
+};
+
+// Two phases.  First the warp's column groups [cg0, cg1), a bound pass
+// each (every pass in full without a bound), with full-pass rounds whenever
+// enough lanes hold a column or a stack is full.  Then (bound pass only) the
+// stacks' remains of every warp are pooled: round i takes the i-th column
+// of each lane's pooled list, so the last rounds of a row group run with
+// full lanes.  Every thread of the block calls this (the pool phase starts
+// with a block barrier).
 template <int B>
 __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint4* __restrict__ P,
                                 const uint32_t* hkeys, const uint4* hmask, bool any_high, int rg,
                                 const uint32_t* s_rows_ok, const int* s_tmin, const int* s_rowT,
-                                int cg0, int cg1) {
+                                const RowBound rb, const Stacks sk, int cg0, int cg1) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rg * kRows128;
     const char* __restrict__ Pb = reinterpret_cast<const char*>(P);
-    for (int cg = cg0 + warp; cg < cg1; cg += kTileWarps) {
-        const int c = cg * 32 + lane;
-        const bool col_ok = c >= a.c_lo && c < a.c_hi && c < a.n;
+    const bool bound = a.bound != 0;
+    const uint4 gq = guard_quad((uint32_t)a.levels * a.K4, lane);
+    uint16_t* s_q = sk.q + warp * (kQDepth * 32);
+    int cg = cg0 + warp;   // this warp's next column group for a first pass
+    int qn = 0;            // column groups on this lane's stack
+    // pool: this warp's next round, the lane's pooled columns, the rounds
+    int pi = warp, pc = 0, pmax = 0;
+    // entries gathered by live lanes: bound passes, full passes; full-pass
+    // columns and rounds
+    uint32_t st_bound = 0, st_full = 0, st_cols = 0, st_rounds = 0;
+    for (int pool = 0; pool < (bound ? 2 : 1); ++pool) {
+    if (pool) {
+        sk.qn[warp * 32 + lane] = (uint8_t)qn;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int run = 0;
+            for (int w = 0; w < kTileWarps; ++w) {
+                sk.qoff[w * 32 + threadIdx.x] = (uint8_t)run;
+                run += sk.qn[w * 32 + threadIdx.x];
+            }
+        }
+        __syncthreads();
+        pc = sk.qoff[(kTileWarps - 1) * 32 + lane] + sk.qn[(kTileWarps - 1) * 32 + lane];
+        pmax = (int)__reduce_max_sync(full, (unsigned)pc);
+    }
+    for (;;) {
+        bool round;
+        if (pool) {
+            if (pi >= pmax) break;
+            round = true;
+        } else {
+            // a full-pass round when enough lanes hold a column or a stack is full
+            const unsigned held = __ballot_sync(full, qn > 0);
+            round = held != 0u && (__popc(held) >= a.qfire || __any_sync(full, qn == kQDepth));
+            if (!round && cg >= cg1) break;
+        }
+        int ccg = 0;
+        bool active = true;
+        if (pool) {
+            active = pi < pc;
+            if (active) {
+                int w = 0;
+                while (w + 1 < kTileWarps && (int)sk.qoff[(w + 1) * 32 + lane] <= pi) ++w;
+                ccg = sk.q[w * (kQDepth * 32) + (pi - (int)sk.qoff[w * 32 + lane]) * 32 + lane];
+            }
+            pi += kTileWarps;
+        } else if (round) {
+            active = qn > 0;
+            if (active) {
+                --qn;
+                ccg = s_q[qn * 32 + lane];
+            }
+        } else {
+            ccg = cg;
+            cg += kTileWarps;
+        }
+        const int c = ccg * 32 + lane;
+        const bool col_ok = active && c >= a.c_lo && c < a.c_hi && c < a.n;
         uint32_t vm[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) vm[q] = col_ok ? half_mask(c - r0 - 32 * q) & s_rows_ok[q] : 0u;
-        if (!__any_sync(0xffffffffu, vm[0] | vm[1] | vm[2] | vm[3])) continue;
-        const int E = a.tgent[cg];
-        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[cg]) + lane;
+        const bool any_vm = (vm[0] | vm[1] | vm[2] | vm[3]) != 0u;
+        if (!__any_sync(full, any_vm)) continue;
+        // bound pass: section 0 of the group; full pass: every step of the
+        // lane's group (both sections with a split)
+        int El = a.tgent[ccg];
+        if (a.split && (round || !bound)) El += a.tgentL[ccg];
+        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[ccg]) + lane;
         Counter<B> cnt[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) cnt[q].clear();
-        // 32 entries per iteration as two 16-entry batches, each gathered as
-        // two halves of 8 (register budget); the next batch is in flight
-        uint4 a0, a1;
-        if (E > 0) { a0 = __ldg(ep); a1 = __ldg(ep + 32); }
-        for (int e = 0; e < E; e += 32) {
-            const bool two = e + 16 < E;
-            uint4 b0, b1;
-            if (two) {
-                b0 = __ldg(ep + ((e + 16) >> 3) * 32);
-                b1 = __ldg(ep + ((e + 16) >> 3) * 32 + 32);
-            }
-            uint32_t ca[4];
-            gather16_128<B>(Pb, a0, a1, a.k65536, a.k8 * 2u, cnt, ca);
-            if (e + 32 < E) {
-                a0 = __ldg(ep + ((e + 32) >> 3) * 32);
-                a1 = __ldg(ep + ((e + 32) >> 3) * 32 + 32);
-            }
-            if (two) {
-                uint32_t cb[4];
-                gather16_128<B>(Pb, b0, b1, a.k65536, a.k8 * 2u, cnt, cb);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) cnt[q].add_sixteens2(ca[q], cb[q]);
+        if (round) {
+            if (!any_vm) El = 0;
+            const int Emax = (int)__reduce_max_sync(full, (unsigned)El);
+            accumulate128<B, true>(Pb, ep, El, Emax, gq, a.k65536, a.k8 * 2u, cnt);
+        } else {
+            accumulate128<B, false>(Pb, ep, El, El, gq, a.k65536, a.k8 * 2u, cnt);
+        }
+        if (a.gstat && any_vm) {
+            const int2 ns = *reinterpret_cast<const int2*>(a.nsec + 2 * (int64_t)c);
+            if (round) {
+                st_full += (uint32_t)(ns.x + ns.y);
+                ++st_cols;
             } else {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) cnt[q].add_sixteens1(ca[q]);
+                st_bound += (uint32_t)ns.x;
             }
         }
+        if (round && lane == 0) ++st_rounds;
         uint32_t X[4][B];
 #pragma unroll
         for (int q = 0; q < 4; ++q) cnt[q].planes(X[q]);
+        const int tc = col_ok ? a.tcount[c] : 0;
+        if (bound && !round) {
+            bool alive = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (!vm[q]) continue;
+                if (tc < rb.tmax[q]) {
+                    alive = true;
+                    continue;
+                }
+                uint32_t gt = 0, eq = full;
+#pragma unroll
+                for (int k = B - 1; k >= 0; --k) {
+                    const uint32_t rk = rb.thr[q * kRPlanes + k];
+                    gt |= eq & X[q][k] & ~rk;
+                    eq &= ~(X[q][k] ^ rk);
+                }
+                if ((gt | eq) & vm[q] & rb.live[q]) alive = true;
+            }
+            if (alive) {
+                s_q[qn * 32 + lane] = (uint16_t)ccg;
+                ++qn;
+            }
+            continue;
+        }
         // rank >= levels: the hash (the entries lead each read's level list)
         if (any_high) {
             const int nh = col_ok ? a.nhigh[c] : 0;
-            const int maxh = (int)__reduce_max_sync(0xffffffffu, (unsigned)nh);
-            const uint32_t* __restrict__ rp = a.ent + a.gstart[cg];
+            const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
+            const uint32_t* __restrict__ rp = a.ent + a.gstart[ccg];
             for (int j = 0; j < maxh; ++j) {
                 const uint4 w = j < nh ? hash_find4(hkeys, hmask, __ldg(rp + ent_at(j, lane)))
                                        : make_uint4(0u, 0u, 0u, 0u);
@@ -1099,10 +1318,20 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
                 Counter<B>::add_at(X[3], w.w, 0);
             }
         }
-        const int tc = col_ok ? a.tcount[c] : 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
             finish_half<B>(a, ej, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
+    }
+    }
+    if (a.gstat) {
+        const uint32_t b = __reduce_add_sync(full, st_bound), f = __reduce_add_sync(full, st_full);
+        const uint32_t k = __reduce_add_sync(full, st_cols);
+        if (lane == 0) {
+            atomicAdd(a.gstat + 0, (unsigned long long)b);
+            atomicAdd(a.gstat + 1, (unsigned long long)f);
+            atomicAdd(a.gstat + 2, (unsigned long long)k);
+            atomicAdd(a.gstat + 3, (unsigned long long)st_rounds);
+        }
     }
 }
 
@@ -1116,6 +1345,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
     __shared__ int s_item[5];
     __shared__ int s_tmin[4], s_any_high;
     __shared__ uint32_t s_rows_ok[4];
+    // bound pass: per-row bounds and each warp's stacks of column groups
+    __shared__ uint32_t s_rthr[4 * kRPlanes], s_rlive[4];
+    __shared__ int s_tmax[4];
+    __shared__ uint16_t s_q[kTileWarps * kQDepth * 32];
+    __shared__ uint8_t s_qn[kTileWarps * 32], s_qoff[kTileWarps * 32];
     const bool queued = a.items != nullptr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int it = 0;; ++it) {
@@ -1166,6 +1400,22 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
             const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
             if (lane == 0) { s_tmin[warp] = tm; s_rows_ok[warp] = okm; }
             if (warp == 0 && lane == 0) s_any_high = 0;
+            if (a.bound) {
+                // R = mmin[T] - (T - a0), at least 0; rows without a passing
+                // count (mmin = 0xFFFF) are not live
+                const int a0 = ok ? a.nsec[2 * (int64_t)r] : 0;
+                const int mm = ok ? (int)ej.mmin[tr] : 0xFFFF;
+                const bool live = ok && mm != 0xFFFF;
+                const int R = live ? max(0, mm - (tr - a0)) : 0;
+#pragma unroll
+                for (int k = 0; k < kRPlanes; ++k) {
+                    const unsigned pl = __ballot_sync(0xffffffffu, (R >> k) & 1);
+                    if (lane == 0) s_rthr[warp * kRPlanes + k] = pl;
+                }
+                const unsigned lv = __ballot_sync(0xffffffffu, live);
+                const int tmx = (int)__reduce_max_sync(0xffffffffu, ok ? (unsigned)tr : 0u);
+                if (lane == 0) { s_rlive[warp] = lv; s_tmax[warp] = tmx; }
+            }
         }
         const int words = a.levels * (int)a.K4;   // + 32 zero guard words after the planes
         for (int i = threadIdx.x; i < words + 32; i += kTileThreads) P[i] = make_uint4(0, 0, 0, 0);
@@ -1205,8 +1455,10 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
             }
         }
         __syncthreads();
+        const RowBound rb{s_rthr, s_rlive, s_tmax};
+        const Stacks sk{s_q, s_qn, s_qoff};
         tile_columns128<B>(a, ej, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
-                           max(cg0, 4 * rg), cg1);
+                           rb, sk, max(cg0, 4 * rg), cg1);
         __syncthreads();
     }
 }
@@ -1717,6 +1969,14 @@ void build_mmin(float thr, int max_t, std::vector<uint16_t>& mmin, std::vector<u
     }
 }
 
+// Lanes holding a queued column that start a full-pass round of the bound
+// pass (CRISPY_KMER_QFIRE, 1..32).
+int kmer_qfire() {
+    int v = kQFire;
+    if (const char* e = std::getenv("CRISPY_KMER_QFIRE")) v = std::atoi(e);
+    return std::max(1, std::min(32, v));
+}
+
 int bits_for(uint64_t v) {
     int b = 0;
     while (b < 64 && (v >> b) != 0) ++b;
@@ -1814,7 +2074,9 @@ int kmer_groups(crispy_ctx* ctx, const int32_t* t) {
         // the conflicts left
         const int spare = tile_rows_for(j.k) == kRows128 || mt < 128 ? 0 : kSchedSpare;
         j.h_tgent[g] = (mt + spare + 15) / 16 * 16;
-        j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * j.h_tgent[g];
+        // split streams: the schedule kernel sets both sections' steps; room
+        // for two sections of gent steps each
+        j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * (j.split ? 2 * j.h_gent[g] : j.h_tgent[g]);
     }
     j.nent = j.h_gstart[j.ngroups];
     j.ntent = j.h_tstart[j.ngroups];
@@ -1856,6 +2118,13 @@ int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
         j.max_t = std::max(j.max_t, j.h_t[r]);
     }
     j.ngroups = (n + 31) / 32;
+    j.split = 0;
+    if (tile_rows_for(k) == kRows128) {
+        // CRISPY_KMER_SPLIT: section 0's share of the dense entries in 1/256
+        // (0: one section, no bound pass)
+        j.split = kSplitDefault;
+        if (const char* e = std::getenv("CRISPY_KMER_SPLIT")) j.split = std::max(0, std::min(255, std::atoi(e)));
+    }
     CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
     CRISPY_TRY(ensure(ctx, j.gstart, (size_t)(j.ngroups + 1) * 8));
@@ -1865,6 +2134,10 @@ int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
     CRISPY_TRY(ensure(ctx, j.bcnt, (size_t)n * 128));
     CRISPY_TRY(ensure(ctx, j.tstart, (size_t)(j.ngroups + 1) * 8));
     CRISPY_TRY(ensure(ctx, j.tgent, (size_t)j.ngroups * 4));
+    if (j.split) {
+        CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
+        CRISPY_TRY(ensure(ctx, j.nsec, (size_t)n * 8));
+    }
     if (k != 8) return kmer_groups(ctx, j.h_t.data());
     CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
     CRISPY_TRY(ensure(ctx, j.nsec, (size_t)n * 8));
@@ -1990,7 +2263,8 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
                                               j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
                                               j.ent.as<uint32_t>(), cntmax, nhigh,
                                               j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>(),
-                                              k == 8 ? j.nsec.as<int32_t>() : nullptr);
+                                              k == 8 || j.split ? j.nsec.as<int32_t>() : nullptr,
+                                              (uint32_t)j.split);
     count_launch(ctx);
     CRISPY_CK(ctx, cudaGetLastError());
     const int levels = dense_levels_for(k);
@@ -2041,6 +2315,14 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
             j.tgentL.as<int32_t>(), nhigh, j.nsec.as<int32_t>(), j.bcnt.as<uint16_t>(), n, j.ngroups,
             j.tent.as<uint16_t>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+    } else if (levels > 0 && j.split) {
+        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        kmer_sched_split_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
+            j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), nhigh, j.nsec.as<int32_t>(),
+            j.bcnt.as<uint16_t>(), n, j.ngroups, (uint32_t)levels * (1u << (2 * k)), j.tgent.as<int32_t>(),
+            j.tgentL.as<int32_t>(), j.tent.as<uint16_t>());
         count_launch(ctx);
         CRISPY_CK(ctx, cudaGetLastError());
     } else if (levels > 0) {
@@ -2151,7 +2433,11 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
         ta.counter = j.counter.as<unsigned long long>(); ta.keys = j.keys.as<uint64_t>();
         ta.vals = j.vals.as<uint32_t>(); ta.cap = cap;
         ta.perm = perm; ta.olo = olo; ta.ohi = ohi;
-        ta.nsec = K == 8 ? j.nsec.as<int32_t>() : nullptr;
+        ta.nsec = K == 8 || j.split ? j.nsec.as<int32_t>() : nullptr;
+        ta.split = j.split;
+        ta.bound = 0;
+        ta.qfire = kmer_qfire();
+        ta.gstat = nullptr;
         DenseArgs da{};
         da.perm = perm; da.olo = olo; da.ohi = ohi;
         da.seq = j.seq.as<uint8_t>(); da.off = loff; da.ent = ta.ent; da.gstart = ta.gstart;
@@ -2253,6 +2539,10 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 TileArgs t2 = ta;
                 t2.r_lo = 0; t2.r_hi = n; t2.c_lo = 0; t2.c_hi = n;
                 t2.items = d_items; t2.nitems = (int)nh; t2.queue_head = head;
+                // the bound pass needs the columns of whole row groups (the
+                // staged form's blocks hold too few to fill the lanes' stacks)
+                t2.bound = j.split != 0;
+                t2.gstat = j.split ? j.counter.as<unsigned long long>() + 1 : nullptr;
                 TileArgs t3 = t2;
                 t3.items = d_items_s; t3.nitems = (int)ns; t3.queue_head = head + 1;
                 t3.item_q = d_q; t3.same_only = 1;
@@ -2276,7 +2566,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr, (uint64_t)(uintptr_t)j.nsec.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap, (uint64_t)split8,
                     (uint64_t)nh, (uint64_t)ns, (uint64_t)grid, (uint64_t)grid_s, (uint64_t)any_dense, (uint64_t)A,
-                    (uint64_t)rlo, (uint64_t)rhi});
+                    (uint64_t)rlo, (uint64_t)rhi, (uint64_t)j.split, (uint64_t)t2.bound, (uint64_t)t2.qfire});
                 ev_begin(ctx, ctx->ev_kmer, s);
                 CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
@@ -2306,10 +2596,14 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             }
         }
         CRISPY_CK(ctx, cudaGetLastError());
-        unsigned long long total = 0;
-        CRISPY_CK(ctx, cudaMemcpyAsync(&total, j.counter.ptr, 8, cudaMemcpyDeviceToHost, s));
+        unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+        CRISPY_CK(ctx, cudaMemcpyAsync(cnt, j.counter.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
         CRISPY_CK(ctx, cudaStreamSynchronize(s));
-        *total_out = (int64_t)total;
+        *total_out = (int64_t)cnt[0];
+        ctx->stats.kmer_bound_entries += (int64_t)cnt[1];
+        ctx->stats.kmer_full_entries += (int64_t)cnt[2];
+        ctx->stats.kmer_full_columns += (int64_t)cnt[3];
+        ctx->stats.kmer_rounds += (int64_t)cnt[4];
         return CRISPY_OK;
     };
     // stable order: (stage, row, col)
@@ -2585,6 +2879,12 @@ int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::ve
     ta.hinfo = j.hinfo.as<uint32_t>(); ta.ngroups = j.ngroups;
     ta.nhigh = j.cntmax.as<int32_t>() + n;
     ta.tcount = j.t.as<int32_t>();
+    ta.tgentL = j.tgentL.as<int32_t>();
+    ta.nsec = j.split ? j.nsec.as<int32_t>() : nullptr;
+    ta.split = j.split;
+    ta.bound = j.split != 0;
+    ta.qfire = kmer_qfire();
+    ta.gstat = j.split ? j.counter.as<unsigned long long>() + 1 : nullptr;
     ta.dense_group = reinterpret_cast<const uint8_t*>(d + off_dense);   // no dense group (checked above)
     ta.mmin = reinterpret_cast<const uint16_t*>(d + off_mm);
     ta.smin = reinterpret_cast<const uint16_t*>(d + off_sm);
@@ -2611,11 +2911,16 @@ int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::ve
         ctx->stats.kmer_launches += 1;
     }
     CRISPY_CK(ctx, cudaGetLastError());
-    unsigned long long total = 0;
+    unsigned long long cnt[5] = {0, 0, 0, 0, 0};
     std::vector<unsigned long long> jc(nj);
-    CRISPY_CK(ctx, cudaMemcpyAsync(&total, j.counter.ptr, 8, cudaMemcpyDeviceToHost, s));
+    CRISPY_CK(ctx, cudaMemcpyAsync(cnt, j.counter.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaMemcpyAsync(jc.data(), d + off_cnt, (size_t)nj * 8, cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    const unsigned long long total = cnt[0];
+    ctx->stats.kmer_bound_entries = (int64_t)cnt[1];
+    ctx->stats.kmer_full_entries = (int64_t)cnt[2];
+    ctx->stats.kmer_full_columns = (int64_t)cnt[3];
+    ctx->stats.kmer_rounds = (int64_t)cnt[4];
     if ((int64_t)total > cap) return fail(ctx, CRISPY_E_UNSUPPORTED, "cohort: %llu survivors beyond the device share", total);
     j.nsurv = (int64_t)total;
     CRISPY_TRY(ensure(ctx, j.pairs, (size_t)std::max<int64_t>(j.nsurv, 1) * 8));

@@ -331,6 +331,13 @@ typedef struct crispy_stats {
     int64_t graph_launches;    /* CUDA graph replays among them (batched form) */
     int64_t kmer_spilled;      /* 1 when the last kmer run's survivors outgrew the device
                                   share and were gathered in pinned host memory */
+    /* bound pass of the batched 128-row tile kernel (K <= 6): level entries
+     * gathered by bound passes (section 0) and by full passes, the (row
+     * group, column) items counted in full and the full-pass rounds */
+    int64_t kmer_bound_entries;
+    int64_t kmer_full_entries;
+    int64_t kmer_full_columns;
+    int64_t kmer_rounds;
 } crispy_stats;
 int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */
