@@ -1545,6 +1545,17 @@ __device__ __forceinline__ void phase8h(const uint32_t* __restrict__ plane, cons
     cnt.planes(X);
 }
 
+// Count bound of the pairs without [same], whose m = minsum(H) <= min(|H_a|,
+// |H_b|): such a pair passes only if m >= mmin[min(Ta, Tb)], i.e. only if
+// the shorter read r (ties: either) has |H_r| >= mmin[T_r].  A read with
+// that property is H-heavy; a pair of two reads that are not can be skipped
+// without a gather.  |H| is at most the read's H section (first
+// occurrences) plus its repeated entries.
+__device__ __forceinline__ bool heavy8(const TileArgs& a, int r) {
+    const int h = a.nsec[2 * (int64_t)r] + a.nhigh[r];
+    return h >= (int)a.mmin[a.tcount[r]];
+}
+
 // Per-block row state of both K = 8 kernels.
 struct Rows8 {
     int rowT[kRows8];            // tuple counts (INT_MAX for rows not taken)
@@ -1552,6 +1563,7 @@ struct Rows8 {
     uint32_t keym[kRows8];       // ... and the rows holding each
     int nkeys, tmin, rep;
     uint32_t rows_ok;
+    int heavy;                   // some row taken is H-heavy
 };
 
 // Warp 0: the row group's rows in [rlo, rhi), their tuple counts and keys.
@@ -1573,7 +1585,8 @@ __device__ __forceinline__ void rows8_setup(const TileArgs& a, Rows8& rs, int rg
         rs.keyv[k] = hr;
         rs.keym[k] = rowsk;
     }
-    if (lane == 0) { rs.tmin = tm; rs.rows_ok = okm; rs.nkeys = __popc(lm); }
+    const bool hv = __any_sync(full, ok && heavy8(a, r));
+    if (lane == 0) { rs.tmin = tm; rs.rows_ok = okm; rs.nkeys = __popc(lm); rs.heavy = hv; }
 }
 
 // The rows with the same H key as column key hc ([same] per row).
@@ -1715,8 +1728,10 @@ __global__ void __launch_bounds__(kTile8HThreads, 1) kmer_tile8h_kernel(TileArgs
             const int c = 32 * q + lane;
             const bool okc = c < a.n;
             const uint32_t same = same8(rs, nkeys, okc ? a.hinfo[c] : 0u);
-            // pairs with [same] belong to the two-phase kernel
-            const uint32_t vmask = okc ? (half_mask(c - r0) & rows_ok & ~same) : 0u;
+            // pairs with [same] belong to the two-phase kernel; the others
+            // can pass only where the row group or the column is H-heavy
+            const bool hv = okc && (rs.heavy || heavy8(a, c));
+            const uint32_t vmask = hv ? (half_mask(c - r0) & rows_ok & ~same) : 0u;
             if (!__any_sync(full, vmask)) continue;
             uint32_t X[B];
             column8<B, true>(a, plane, hkeys, hmask, any_rep, q, c, okc, X);
@@ -1777,8 +1792,11 @@ __global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileA
                 const int c = 32 * q + lane;
                 const bool okc = q < q1 && c >= a.c_lo && c < a.c_hi && c < a.n;
                 same[g] = same8(rs, nkeys, okc ? a.hinfo[c] : 0u);
-                // same_only: the H-only kernel has taken the pairs without [same]
-                vm[g] = okc ? (half_mask(c - r0) & rows_ok & (a.same_only ? same[g] : 0xffffffffu)) : 0u;
+                // same_only: the H-only kernel has taken the pairs without
+                // [same]; those can pass only where the row group or the
+                // column is H-heavy
+                const bool hv = okc && !a.same_only && (rs.heavy || heavy8(a, c));
+                vm[g] = okc ? (half_mask(c - r0) & rows_ok & (same[g] | (hv ? 0xffffffffu : 0u))) : 0u;
 #pragma unroll
                 for (int k = 0; k < B; ++k) XH[g][k] = 0u;
                 if (__any_sync(full, vm[g])) column8<B, true>(a, plane, hkeys, hmask, rep_h, q, c, okc, XH[g]);
@@ -2500,7 +2518,15 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             std::vector<int> items, items_s;
             std::vector<int2> q_s;
             if (split8) {
-                for (int g = 0; g < j.ngroups; ++g)
+                // the H-only kernel's pairs (different H keys) can pass only
+                // where one read is H-heavy (|H| >= mmin[T], heavy8): with no
+                // such read it has nothing to do
+                bool any_heavy = false;
+                for (int i = 0; i < n && !any_heavy; ++i) {
+                    const int h = j.h_nsec[2 * (size_t)i] + j.h_cntmax[(size_t)n + i];
+                    any_heavy = h >= (int)mmin[j.h_t[j.h_perm[i]]];
+                }
+                for (int g = 0; g < j.ngroups && any_heavy; ++g)
                     if (!dense[g]) items.push_back(g);
                 for (int g = 0; g < j.ngroups; ++g) {
                     const int r0 = g * kRows8, r1 = std::min(n, r0 + kRows8);
