@@ -1172,6 +1172,7 @@ struct Stacks {
     uint16_t* q;
     uint8_t* qn;
     uint8_t* qoff;
+    int* next;     // [0]: next column group of the first passes, [1]: next pooled round
 };
 
 // Two phases.  First the warp's column groups [cg0, cg1), a bound pass
@@ -1193,10 +1194,13 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
     const bool bound = a.bound != 0;
     const uint4 gq = guard_quad((uint32_t)a.levels * a.K4, lane);
     uint16_t* s_q = sk.q + warp * (kQDepth * 32);
-    int cg = cg0 + warp;   // this warp's next column group for a first pass
+    // with the bound pass, warps claim column groups and pooled rounds from
+    // the block's counters (sk.next), so that they reach the pool's barrier
+    // together; without it each warp takes every kTileWarps-th group
+    int cg = cg0 + warp - kTileWarps;   // the column group of the current first pass
     int qn = 0;            // column groups on this lane's stack
-    // pool: this warp's next round, the lane's pooled columns, the rounds
-    int pi = warp, pc = 0, pmax = 0;
+    // pool: the lane's pooled columns, the rounds
+    int pi = 0, pc = 0, pmax = 0;
     // entries gathered by live lanes: bound passes, full passes; full-pass
     // columns and rounds
     uint32_t st_bound = 0, st_full = 0, st_cols = 0, st_rounds = 0;
@@ -1218,13 +1222,25 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
     for (;;) {
         bool round;
         if (pool) {
+            int v = 0;
+            if (lane == 0) v = atomicAdd(sk.next + 1, 1);
+            pi = __shfl_sync(full, v, 0);
             if (pi >= pmax) break;
             round = true;
         } else {
             // a full-pass round when enough lanes hold a column or a stack is full
             const unsigned held = __ballot_sync(full, qn > 0);
             round = held != 0u && (__popc(held) >= a.qfire || __any_sync(full, qn == kQDepth));
-            if (!round && cg >= cg1) break;
+            if (!round) {
+                if (bound) {
+                    int v = 0;
+                    if (lane == 0) v = atomicAdd(sk.next, 1);
+                    cg = cg0 + __shfl_sync(full, v, 0);
+                } else {
+                    cg += kTileWarps;
+                }
+                if (cg >= cg1) break;
+            }
         }
         int ccg = 0;
         bool active = true;
@@ -1235,7 +1251,6 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
                 while (w + 1 < kTileWarps && (int)sk.qoff[(w + 1) * 32 + lane] <= pi) ++w;
                 ccg = sk.q[w * (kQDepth * 32) + (pi - (int)sk.qoff[w * 32 + lane]) * 32 + lane];
             }
-            pi += kTileWarps;
         } else if (round) {
             active = qn > 0;
             if (active) {
@@ -1244,7 +1259,6 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
             }
         } else {
             ccg = cg;
-            cg += kTileWarps;
         }
         const int c = ccg * 32 + lane;
         const bool col_ok = active && c >= a.c_lo && c < a.c_hi && c < a.n;
@@ -1350,6 +1364,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
     __shared__ int s_tmax[4];
     __shared__ uint16_t s_q[kTileWarps * kQDepth * 32];
     __shared__ uint8_t s_qn[kTileWarps * 32], s_qoff[kTileWarps * 32];
+    __shared__ int s_next[2];
     const bool queued = a.items != nullptr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int it = 0;; ++it) {
@@ -1399,7 +1414,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
             const unsigned okm = __ballot_sync(0xffffffffu, ok);
             const int tm = (int)__reduce_min_sync(0xffffffffu, (unsigned)tr);
             if (lane == 0) { s_tmin[warp] = tm; s_rows_ok[warp] = okm; }
-            if (warp == 0 && lane == 0) s_any_high = 0;
+            if (warp == 0 && lane == 0) {
+                s_any_high = 0;
+                s_next[0] = 0;
+                s_next[1] = 0;
+            }
             if (a.bound) {
                 // R = mmin[T] - (T - a0), at least 0; rows without a passing
                 // count (mmin = 0xFFFF) are not live
@@ -1456,7 +1475,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
         }
         __syncthreads();
         const RowBound rb{s_rthr, s_rlive, s_tmax};
-        const Stacks sk{s_q, s_qn, s_qoff};
+        const Stacks sk{s_q, s_qn, s_qoff, s_next};
         tile_columns128<B>(a, ej, P, hkeys, hmask, s_any_high != 0, rg, s_rows_ok, s_tmin, s_rowT,
                            rb, sk, max(cg0, 4 * rg), cg1);
         __syncthreads();
@@ -1750,6 +1769,9 @@ __global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileA
     __shared__ uint32_t hmask[kHashSlots];
     __shared__ Rows8 rs;
     __shared__ int s_item[4];
+    // bound of the pairs with [same] after their H sums: bit planes of the
+    // rows' R = mmin[T] - |L| (at least 0) and of their tuple counts
+    __shared__ uint32_t s_rthr[kRPlanes], s_rt[kRPlanes], s_rlive;
     const bool queued = a.items != nullptr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned full = 0xffffffffu;
@@ -1775,7 +1797,24 @@ __global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileA
         const int rg = s_item[0], q0 = s_item[1], q1 = s_item[2];
         const int rlo = queued ? 0 : a.r_lo, rhi = queued ? a.n : min(a.r_hi, a.n);
         const int r0 = rg * kRows8;
-        if (warp == 0) rows8_setup(a, rs, rg, rlo, rhi);
+        if (warp == 0) {
+            rows8_setup(a, rs, rg, rlo, rhi);
+            __syncwarp();
+            // |L| is at most the L section plus the repeated entries
+            const int r = r0 + lane;
+            const bool ok = (rs.rows_ok >> lane) & 1u;
+            const int tr = ok ? a.tcount[r] : 0;
+            const int mm = ok ? (int)a.mmin[tr] : 0xFFFF;
+            const int lb = ok ? a.nsec[2 * (int64_t)r + 1] + a.nhigh[r] : 0;
+            const int R = mm != 0xFFFF ? max(0, mm - lb) : 0;
+#pragma unroll
+            for (int k = 0; k < kRPlanes; ++k) {
+                const unsigned pr = __ballot_sync(full, (R >> k) & 1), pt = __ballot_sync(full, (tr >> k) & 1);
+                if (lane == 0) { s_rthr[k] = pr; s_rt[k] = pt; }
+            }
+            const unsigned lv = __ballot_sync(full, ok && mm != 0xFFFF);
+            if (lane == 0) s_rlive = lv;
+        }
         __syncthreads();
         const uint32_t rows_ok = rs.rows_ok;
         const int nkeys = rs.nkeys;
@@ -1800,6 +1839,27 @@ __global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileA
 #pragma unroll
                 for (int k = 0; k < B; ++k) XH[g][k] = 0u;
                 if (__any_sync(full, vm[g])) column8<B, true>(a, plane, hkeys, hmask, rep_h, q, c, okc, XH[g]);
+                // a pair with [same] has m = mH + mL <= mH + |L_r|: with Tc >=
+                // Tr it can pass only if mH >= R_r; rows longer than the
+                // column keep their pairs
+                const uint32_t sv = same[g] & vm[g];
+                if (sv) {
+                    const uint32_t tc = (uint32_t)(okc ? a.tcount[c] : 0);
+                    uint32_t gt = 0, eq = full, tgt = 0, teq = full;
+#pragma unroll
+                    for (int k = kRPlanes - 1; k >= 0; --k) {
+                        if (k < B) {
+                            const uint32_t rk = s_rthr[k];
+                            gt |= eq & XH[g][k] & ~rk;
+                            eq &= ~(XH[g][k] ^ rk);
+                        }
+                        const uint32_t tk = s_rt[k], cb = ((tc >> k) & 1u) ? full : 0u;
+                        tgt |= teq & tk & ~cb;
+                        teq &= ~(tk ^ cb);
+                    }
+                    const uint32_t alive = sv & (((gt | eq) & s_rlive) | tgt);
+                    vm[g] = (vm[g] & ~same[g]) | alive;
+                }
                 any_same |= (same[g] & vm[g]) != 0u;
             }
             // the L phase only where some pair of the block has [same]
