@@ -264,7 +264,7 @@ int crispy_ctx_trim(crispy_ctx* ctx) {
     for (DevBuf* b : {&k.seq, &k.off, &k.len, &k.t, &k.gstart, &k.gent, &k.ent, &k.cntmax,
                       &k.hinfo, &k.keys, &k.keys_alt, &k.vals, &k.vals_alt, &k.pairs, &k.dists,
                       &k.counter, &k.mmin, &k.smin, &k.work, &k.sort_tmp, &k.tstart, &k.tgent,
-                      &k.tent, &k.bcnt, &k.tgentL, &k.nsec, &k.t0, &k.offp, &k.perm})
+                      &k.tent, &k.bcnt, &k.tgentL, &k.nsec, &k.t0, &k.offp, &k.perm, &k.sq})
         release(ctx, *b);
     release_host(k.h_spill_pairs);
     release_host(k.h_spill_dists);

@@ -69,6 +69,7 @@ struct KmerJob {
     bool spilled = false;
     HostBuf h_spill_pairs, h_spill_dists;
     DevBuf keys, keys_alt, vals, vals_alt, pairs, dists, counter, mmin, smin, work;
+    DevBuf sq;                       // K = 8 same-key pass: queued H sums per block and lane slot
     DevBuf sort_tmp;
 };
 

@@ -510,7 +510,10 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
     __shared__ SchedSmem sm;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
+    // one warp per (group, section): the schedule is a serial chain of warp
+    // collectives, so twice the warps hide twice the latency
+    for (int item = blockIdx.x * kSchedWarps + w; item < 2 * ngroups; item += gridDim.x * kSchedWarps) {
+        const int g = item >> 1, sec = item & 1;
         const int r = g * 32 + lane;
         const bool active = r < n;
         const int rr = active ? r : 0;
@@ -520,14 +523,15 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
         const int E0 = ((int)__reduce_max_sync(full, (unsigned)n0) + 15) / 16 * 16;
         const int E1 = ((int)__reduce_max_sync(full, (unsigned)n1) + 15) / 16 * 16;
         if (lane == 0) {
-            tgent[g] = E0;
-            tgentL[g] = E1;
+            if (sec == 0) tgent[g] = E0;
+            else tgentL[g] = E1;
         }
-        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, E0, ent + gstart[g], 0u,
-                        guard_word, 1u, tent + tstart[g]);
-        __syncwarp();
-        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + n0, E1, ent + gstart[g],
-                        0u, guard_word, 1u, tent + tstart[g] + (int64_t)32 * E0);
+        if (sec == 0)
+            sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, E0, ent + gstart[g], 0u,
+                            guard_word, 1u, tent + tstart[g]);
+        else
+            sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + n0, E1, ent + gstart[g],
+                            0u, guard_word, 1u, tent + tstart[g] + (int64_t)32 * E0);
         __syncwarp();
     }
 }
@@ -612,6 +616,10 @@ struct TileArgs {
     // columns and the rounds
     int split, bound, qfire;
     unsigned long long* gstat;
+    // K = 8 same-key pass with queued L sums (kmer_tile8s_kernel): per
+    // block, per lane slot, sq_cap items of B + 2 words
+    uint32_t* sq;
+    int64_t sq_cap;
     // Cohort (several jobs' reads back to back, each starting at a multiple
     // of 128 positions; 128-row kernel, batched form): per item its job and
     // its end column group; per job (base, n, A, stage_dim) and its
@@ -1575,6 +1583,28 @@ __device__ __forceinline__ bool heavy8(const TileArgs& a, int r) {
     return h >= (int)a.mmin[a.tcount[r]];
 }
 
+// phase8h with a stream length per lane (El steps; lanes past theirs read
+// the guard word) and the warp's largest, Emax.
+template <int B>
+__device__ __forceinline__ void phase8h_lane(const uint32_t* __restrict__ plane, const uint4* ep, int El,
+                                             int Emax, uint32_t* X) {
+    const uint4 guard = make_uint4(0x80008000u, 0x80008000u, 0x80008000u, 0x80008000u);
+    auto ld = [&](int step) { return step < El ? __ldg(ep + (step >> 3) * 32) : guard; };
+    Counter<B> cnt;
+    cnt.clear();
+    uint4 a0 = ld(0), a1 = ld(8);
+    for (int e = 0; e < Emax; e += 32) {
+        const bool two = e + 16 < Emax;
+        const uint4 b0 = two ? ld(e + 16) : guard, b1 = two ? ld(e + 24) : guard;
+        const uint4 n0 = ld(e + 32), n1 = ld(e + 40);
+        const uint32_t ca = gather8h_c16<B>(plane, a0, a1, cnt);
+        if (two) cnt.add_sixteens2(ca, gather8h_c16<B>(plane, b0, b1, cnt));
+        else cnt.add_sixteens1(ca);
+        a0 = n0; a1 = n1;
+    }
+    cnt.planes(X);
+}
+
 // Per-block row state of both K = 8 kernels.
 struct Rows8 {
     int rowT[kRows8];            // tuple counts (INT_MAX for rows not taken)
@@ -1897,6 +1927,178 @@ __global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8_kernel(TileA
 }
 
 // ---------------------------------------------------------------------------
+// Same-key pass with queued L sums (batched form, K = 8).  The two-phase
+// kernel refills its plane twice per round of 64 column groups, and every
+// warp waits at those barriers for the few that still have L work.  This
+// kernel fills the H plane once per row group and takes the H sums of every
+// column group of the row group's same-key range; a lane whose [same] pairs
+// survive the bound (mH >= R_r, or a row longer than the column) stores its
+// H sums, its alive rows and its column group in its own lane slot of the
+// block's queue (global scratch, at most one item per slot and column
+// group).  Then the plane is filled with L once, and rounds take the i-th
+// item of every slot: each lane keeps its lane index, so the L stream's
+// bank schedule still holds, and lanes past their stream read the guard.
+// ---------------------------------------------------------------------------
+template <int B>
+__device__ __forceinline__ void column8L_lane(const TileArgs& a, const uint32_t* plane, const uint32_t* hkeys,
+                                              const uint32_t* hmask, bool any_rep, int q, int c, bool okc,
+                                              uint32_t* X) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint16_t* st = a.tent + a.tstart[q] + 32LL * a.tgent[q];
+    const int El = okc ? a.tgentL[q] : 0;
+    const int Emax = (int)__reduce_max_sync(full, (unsigned)El);
+    phase8h_lane<B>(plane, reinterpret_cast<const uint4*>(st) + lane, El, Emax, X);
+    if (any_rep) {
+        const int nh = okc ? a.nhigh[c] : 0;
+        const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
+        const uint32_t* rp = a.ent + a.gstart[q];
+        for (int j = 0; j < maxh; ++j) {
+            uint32_t w = 0;
+            if (j < nh) {
+                const uint32_t key = __ldg(rp + ent_at(j, lane));
+                if ((key & 0xFFFFu) < 0x8000u) w = hash_find8(hkeys, hmask, key);
+            }
+            Counter<B>::add_at(X, w, 0);
+        }
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(tile8_threads<B>(), 1) kmer_tile8s_kernel(TileArgs a) {
+    constexpr int kThreads = tile8_threads<B>();
+    constexpr int W = B + 2;   // queue item: H sums (B planes), alive rows, column group
+    extern __shared__ __align__(16) uint32_t plane[];
+    __shared__ uint32_t hkeys[kHashSlots];
+    __shared__ uint32_t hmask[kHashSlots];
+    __shared__ Rows8 rs;
+    __shared__ int s_item[3], s_next[2], s_qn[32];
+    __shared__ uint32_t s_rthr[kRPlanes], s_rt[kRPlanes], s_rlive;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned full = 0xffffffffu;
+    uint32_t* qb = a.sq + (int64_t)blockIdx.x * a.sq_cap * W * 32;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned w = atomicAdd(a.queue_head, 1u);
+            const bool ok = (int)w < a.nitems;
+            s_item[0] = ok ? a.items[w] : -1;
+            s_item[1] = ok ? a.item_q[w].x : 0;
+            s_item[2] = ok ? a.item_q[w].y : 0;
+            s_next[0] = 0;
+            s_next[1] = 0;
+        }
+        if (threadIdx.x < 32) s_qn[threadIdx.x] = 0;
+        __syncthreads();
+        const int rg = s_item[0];
+        if (rg < 0) break;
+        const int q0 = max(s_item[1], rg), q1 = s_item[2];
+        const int r0 = rg * kRows8;
+        if (warp == 0) {
+            rows8_setup(a, rs, rg, 0, a.n);
+            __syncwarp();
+            // R = mmin[T] - |L| (at least 0), |L| at most the L section plus
+            // the repeated entries; the rows' tuple counts
+            const int r = r0 + lane;
+            const bool ok = (rs.rows_ok >> lane) & 1u;
+            const int tr = ok ? a.tcount[r] : 0;
+            const int mm = ok ? (int)a.mmin[tr] : 0xFFFF;
+            const int lb = ok ? a.nsec[2 * (int64_t)r + 1] + a.nhigh[r] : 0;
+            const int R = mm != 0xFFFF ? max(0, mm - lb) : 0;
+#pragma unroll
+            for (int k = 0; k < kRPlanes; ++k) {
+                const unsigned pr = __ballot_sync(full, (R >> k) & 1), pt = __ballot_sync(full, (tr >> k) & 1);
+                if (lane == 0) { s_rthr[k] = pr; s_rt[k] = pt; }
+            }
+            const unsigned lv = __ballot_sync(full, ok && mm != 0xFFFF);
+            if (lane == 0) s_rlive = lv;
+        }
+        fill8<true>(a, rs, rg, plane, hkeys, hmask, kThreads);   // begins and ends with a barrier
+        const bool rep_h = rs.rep != 0;
+        const uint32_t rows_ok = rs.rows_ok;
+        const int nkeys = rs.nkeys;
+        // H sums of every column group of the range; survivors of the bound
+        // go on the queue
+        for (;;) {
+            int v = 0;
+            if (lane == 0) v = atomicAdd(&s_next[0], 1);
+            const int q = q0 + __shfl_sync(full, v, 0);
+            if (q >= q1) break;
+            const int c = 32 * q + lane;
+            const bool okc = c < a.n;
+            const uint32_t same = same8(rs, nkeys, okc ? a.hinfo[c] : 0u);
+            const uint32_t vm = okc ? (half_mask(c - r0) & rows_ok & same) : 0u;
+            if (!__any_sync(full, vm)) continue;
+            uint32_t XH[B];
+            column8<B, true>(a, plane, hkeys, hmask, rep_h, q, c, okc, XH);
+            if (vm) {
+                const uint32_t tc = (uint32_t)a.tcount[c];
+                uint32_t gt = 0, eq = full, tgt = 0, teq = full;
+#pragma unroll
+                for (int k = kRPlanes - 1; k >= 0; --k) {
+                    if (k < B) {
+                        const uint32_t rk = s_rthr[k];
+                        gt |= eq & XH[k] & ~rk;
+                        eq &= ~(XH[k] ^ rk);
+                    }
+                    const uint32_t tk = s_rt[k], cb = ((tc >> k) & 1u) ? full : 0u;
+                    tgt |= teq & tk & ~cb;
+                    teq &= ~(tk ^ cb);
+                }
+                const uint32_t alive = vm & (((gt | eq) & s_rlive) | tgt);
+                if (alive) {
+                    const int pos = atomicAdd(&s_qn[lane], 1);
+                    uint32_t* it = qb + (int64_t)pos * W * 32 + lane;
+#pragma unroll
+                    for (int k = 0; k < B; ++k) it[k * 32] = XH[k];
+                    it[B * 32] = alive;
+                    it[(B + 1) * 32] = (uint32_t)q;
+                }
+            }
+        }
+        __syncthreads();
+        const int pmax = (int)__reduce_max_sync(full, (unsigned)s_qn[lane]);
+        if (pmax > 0) {
+            fill8<false>(a, rs, rg, plane, hkeys, hmask, kThreads);
+            const bool rep_l = rs.rep != 0;
+            for (;;) {
+                int v = 0;
+                if (lane == 0) v = atomicAdd(&s_next[1], 1);
+                const int i = __shfl_sync(full, v, 0);
+                if (i >= pmax) break;
+                const bool active = i < s_qn[lane];
+                uint32_t XH[B], alive = 0;
+                int q = 0;
+                if (active) {
+                    const uint32_t* it = qb + (int64_t)i * W * 32 + lane;
+#pragma unroll
+                    for (int k = 0; k < B; ++k) XH[k] = it[k * 32];
+                    alive = it[B * 32];
+                    q = (int)it[(B + 1) * 32];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < B; ++k) XH[k] = 0u;
+                }
+                const int c = 32 * q + lane;
+                const bool okc = active && c < a.n;
+                uint32_t XL[B];
+                column8L_lane<B>(a, plane, hkeys, hmask, rep_l, q, c, okc, XL);
+                // X = XH + (XL & alive), bit-sliced
+                uint32_t X[B];
+                uint32_t carry = 0;
+#pragma unroll
+                for (int k = 0; k < B; ++k) {
+                    const uint32_t y = XL[k] & alive;
+                    X[k] = XH[k] ^ y ^ carry;
+                    carry = (XH[k] & y) | (carry & (XH[k] ^ y));
+                }
+                emit8<B>(a, rs, X, alive, r0, c, okc ? a.tcount[c] : 0);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Exact dense-table kernel: one row read per block with its full count
 // table (two 16-bit counts per word) in shared memory; one column per
 // thread walks its level entries (t, kmer) and counts [cnt_row[kmer] > t].
@@ -2092,6 +2294,16 @@ TileFn tile8_fn_for(int B) {
         case 10: return kmer_tile8_kernel<10>;
         case 11: return kmer_tile8_kernel<11>;
         default: return kmer_tile8_kernel<12>;
+    }
+}
+
+TileFn tile8s_fn_for(int B) {
+    switch (B) {
+        case 8: return kmer_tile8s_kernel<8>;
+        case 9: return kmer_tile8s_kernel<9>;
+        case 10: return kmer_tile8s_kernel<10>;
+        case 11: return kmer_tile8s_kernel<11>;
+        default: return kmer_tile8s_kernel<12>;
     }
 }
 
@@ -2396,7 +2608,7 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
         count_launch(ctx);
         CRISPY_CK(ctx, cudaGetLastError());
     } else if (levels > 0 && j.split) {
-        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        const int sgrid = std::min((2 * j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
         kmer_sched_split_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), nhigh, j.nsec.as<int32_t>(),
             j.bcnt.as<uint16_t>(), n, j.ngroups, (uint32_t)levels * (1u << (2 * k)), j.tgent.as<int32_t>(),
@@ -2480,6 +2692,12 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                         !(split_env && std::strcmp(split_env, "0") == 0);
     TileFn tile_h = split8 ? tile8h_fn_for(B) : nullptr;
     if (split8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8));
+    // the same-key ranges of the split: the kernel that queues its L sums
+    // (CRISPY_KMER_K8_QUEUE=0 selects the two-phase kernel)
+    const char* queue_env = std::getenv("CRISPY_KMER_K8_QUEUE");
+    const bool queue8 = split8 && !(queue_env && std::strcmp(queue_env, "0") == 0);
+    TileFn tile_s = queue8 ? tile8s_fn_for(B) : tile;
+    if (queue8) CRISPY_CK(ctx, cudaFuncSetAttribute(tile_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem8));
     CRISPY_CK(ctx, cudaFuncSetAttribute(kmer_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
 
     // K = 8 jobs hold their reads in the read order built at rebuild: the
@@ -2635,11 +2853,21 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 int per_sm = 1, per_sm_s = 1;
                 const int main_threads = split8 ? kTile8HThreads : tile_threads;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, main_fn, main_threads, main_smem);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, tile, tile_threads, tsmem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, tile_s, tile_threads, tsmem);
                 per_sm = std::max(1, per_sm);
                 per_sm_s = std::max(1, per_sm_s);
                 const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->sm_count, (int64_t)nh);
                 const int grid_s = (int)std::min<int64_t>((int64_t)per_sm_s * ctx->sm_count, (int64_t)ns);
+                if (queue8 && ns) {
+                    // queue scratch: per block and lane slot, one item per
+                    // column group of the widest range
+                    int64_t cap = 1;
+                    for (size_t i = 0; i < ns; ++i)
+                        cap = std::max<int64_t>(cap, q_s[i].y - std::max(q_s[i].x, items_s[i]));
+                    CRISPY_TRY(ensure(ctx, j.sq, (size_t)grid_s * cap * (B + 2) * 32 * 4));
+                    t3.sq = j.sq.as<uint32_t>();
+                    t3.sq_cap = cap;
+                }
                 DenseArgs d2 = da;
                 d2.r_lo = rlo; d2.r_hi = rhi; d2.c_lo = 0; d2.c_hi = n;
                 const std::string key = "kmain," + key_of({(uint64_t)(uintptr_t)j.ent.ptr, (uint64_t)(uintptr_t)j.keys.ptr,
@@ -2652,7 +2880,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)(uintptr_t)j.cntmax.ptr, (uint64_t)(uintptr_t)j.tgentL.ptr, (uint64_t)(uintptr_t)j.nsec.ptr,
                     (uint64_t)n, (uint64_t)K, (uint64_t)B, (uint64_t)cap, (uint64_t)split8,
                     (uint64_t)nh, (uint64_t)ns, (uint64_t)grid, (uint64_t)grid_s, (uint64_t)any_dense, (uint64_t)A,
-                    (uint64_t)rlo, (uint64_t)rhi, (uint64_t)j.split, (uint64_t)t2.bound, (uint64_t)t2.qfire});
+                    (uint64_t)rlo, (uint64_t)rhi, (uint64_t)j.split, (uint64_t)t2.bound, (uint64_t)t2.qfire,
+                    (uint64_t)queue8, (uint64_t)(uintptr_t)t3.sq, (uint64_t)t3.sq_cap});
                 ev_begin(ctx, ctx->ev_kmer, s);
                 CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
@@ -2662,7 +2891,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                         count_launch(ctx);
                     }
                     if (ns) {
-                        tile<<<grid_s, tile_threads, tsmem, s>>>(t3);
+                        tile_s<<<grid_s, tile_threads, tsmem, s>>>(t3);
                         count_launch(ctx);
                     }
                     if (any_dense) {

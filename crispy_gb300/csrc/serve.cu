@@ -117,10 +117,17 @@ size_t run_bytes(const std::vector<Job*>& js, int sms) {
     return base + tag_bytes(maxlen, n, sms);
 }
 
+// K = 8: the same-key pass's queue of H sums, per block (one per SM) and
+// lane slot at most one item of up to 14 words per column group.
+size_t k8_queue_bytes(const Job& j, int sms) {
+    if (j.k != 8) return 0;
+    return (size_t)sms * (size_t)((j.n + 31) / 32 + 1) * 14 * 32 * 4;
+}
+
 void set_estimate(Job& j, int sms) {
     j.maxlen = 0;
     for (int i = 0; i < j.n; ++i) j.maxlen = std::max(j.maxlen, j.len[i]);
-    j.mem_base = estimate_base_bytes(j);
+    j.mem_base = estimate_base_bytes(j) + k8_queue_bytes(j, sms);
     j.mem = j.mem_base + tag_bytes(j.maxlen, j.n, sms);
 }
 

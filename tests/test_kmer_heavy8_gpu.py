@@ -56,3 +56,14 @@ def test_heavy_planted_reads(engine):
     t = cg.default_threshold(len(reads), -1.0, 0)
     counts = [_check(engine, reads, t, mode) for mode in (cg.MODE_BATCHED, cg.MODE_STAGED, cg.MODE_PLAIN)]
     assert counts[0] == counts[1] == counts[2] > 0
+
+
+@pytest.mark.parametrize("queue", ["0", "1"])
+@pytest.mark.parametrize("thr", [0.105, 0.2, 0.6])
+def test_same_key_queue(engine, monkeypatch, queue, thr):
+    # few centroids: large groups of reads with the same H key, so the
+    # same-key ranges span many column groups; both forms of the batched
+    # same-key pass (L sums queued, or the two-phase kernel)
+    monkeypatch.setenv("CRISPY_KMER_K8_QUEUE", queue)
+    reads = synth.make_read_set(synth.ReadSetSpec(2600, 6, 260, "normal", 250, 30, 8, 603))
+    assert _check(engine, reads, thr, cg.MODE_BATCHED) > 0
