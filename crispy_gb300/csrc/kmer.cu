@@ -261,6 +261,142 @@ __global__ void __launch_bounds__(kPrepThreads) kmer_prep_kernel(
 }
 
 // ---------------------------------------------------------------------------
+// Preparation, one warp per read (read sets whose reads hold at most
+// kPrepWarpMaxT tuples).  The same outputs as kmer_prep_kernel -- the set of
+// level entries of each read and of each of its buckets, the bucket and
+// section counts, the largest multiplicity, the high-level count, the K = 8
+// key -- without a block-wide histogram: occurrence ranks come from a
+// 1,024-slot open-addressing table per warp in shared memory (key << 16 |
+// count, one atomic per occurrence), so 48 warps of an SM work on 48 reads
+// at once instead of two blocks on two.  Which occurrence of a K-mer gets
+// which rank, and so the order of entries inside a bucket, is whatever the
+// atomics give; every consumer treats a bucket as a set.
+// ---------------------------------------------------------------------------
+constexpr int kPrepWarpMaxT = 512;
+constexpr int kPrepWarpPer = kPrepWarpMaxT / 32;   // positions per lane
+constexpr int kPrepWarpSlots = 1024;                // table slots per warp (load <= 1/2)
+constexpr int kPrepWarps = 8;                       // warps per block
+constexpr uint32_t kPrepEmpty = 0xFFFFFFFFu;        // key 0xFFFF, count 0xFFFF: never a real slot
+
+// Old count (the occurrence's rank) of K-mer v, after counting it.
+__device__ __forceinline__ uint32_t warp_table_add(uint32_t* tbl, uint32_t v) {
+    uint32_t h = (v * 0x9E3779B1u) >> 22;   // 10 bits: kPrepWarpSlots
+    for (int probe = 0; probe < kPrepWarpSlots; ++probe) {
+        const uint32_t cur = *reinterpret_cast<volatile uint32_t*>(tbl + h);
+        if (cur == kPrepEmpty) {
+            const uint32_t old = atomicCAS(&tbl[h], kPrepEmpty, (v << 16) | 1u);
+            if (old == kPrepEmpty) return 0u;
+            if ((old >> 16) == v) return atomicAdd(&tbl[h], 1u) & 0xFFFFu;
+        } else if ((cur >> 16) == v) {
+            return atomicAdd(&tbl[h], 1u) & 0xFFFFu;
+        }
+        h = (h + 1u) & (kPrepWarpSlots - 1u);
+    }
+    return 0u;   // unreachable: a read has at most kPrepWarpMaxT distinct K-mers
+}
+
+__device__ __forceinline__ uint32_t warp_table_count(const uint32_t* tbl, uint32_t v) {
+    uint32_t h = (v * 0x9E3779B1u) >> 22;
+    for (int probe = 0; probe < kPrepWarpSlots; ++probe) {
+        const uint32_t cur = tbl[h];
+        if (cur == kPrepEmpty) return 0u;
+        if ((cur >> 16) == v) return cur & 0xFFFFu;
+        h = (h + 1u) & (kPrepWarpSlots - 1u);
+    }
+    return 0u;
+}
+
+__global__ void __launch_bounds__(kPrepWarps * 32) kmer_prep_warp_kernel(
+    const uint8_t* __restrict__ seq, const int64_t* __restrict__ off,
+    const int32_t* __restrict__ tcount, int n, int K, int dense_levels,
+    const int64_t* __restrict__ gstart, const int32_t* __restrict__ gent,
+    uint32_t* __restrict__ ent, int32_t* __restrict__ cntmax, int32_t* __restrict__ nhigh,
+    uint32_t* __restrict__ hinfo, uint16_t* __restrict__ bcnt, int32_t* __restrict__ nsec,
+    uint32_t split) {
+    __shared__ __align__(16) uint32_t s_tbl[kPrepWarps][kPrepWarpSlots];
+    __shared__ int s_bc[kPrepWarps][64], s_bs[kPrepWarps][64];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t* tbl = s_tbl[w];
+    int* bc = s_bc[w];
+    int* bs = s_bs[w];
+    const uint32_t K4 = 1u << (2 * K);
+    const int nsections = K == 8 || split ? 2 : 1;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = blockIdx.x * kPrepWarps + w; r < n; r += gridDim.x * kPrepWarps) {
+        uint4* t4 = reinterpret_cast<uint4*>(tbl);
+        for (int i = lane; i < kPrepWarpSlots / 4; i += 32)
+            t4[i] = make_uint4(kPrepEmpty, kPrepEmpty, kPrepEmpty, kPrepEmpty);
+        bc[lane] = 0;
+        bc[lane + 32] = 0;
+        __syncwarp();
+        const int T = tcount[r];
+        const uint8_t* s = seq + off[r];
+        uint32_t* dst = ent + gstart[r >> 5];
+        const int rl = r & 31;
+        const int E = gent[r >> 5];
+        uint32_t val[kPrepWarpPer];
+        int rank[kPrepWarpPer];   // rank in its bucket (dense), -1 high-level, -2 none
+        int mx = 0;
+        uint32_t hm = 0;
+#pragma unroll
+        for (int k = 0; k < kPrepWarpPer; ++k) {
+            const int p = lane + 32 * k;
+            rank[k] = -2;
+            val[k] = 0;
+            if (p < T) {
+                const uint32_t v = kmer_at(s, p, K);
+                const uint32_t t = warp_table_add(tbl, v);
+                val[k] = t * K4 + v;
+                mx = max(mx, (int)t + 1);
+                if (v >= 0x8000u) hm = max(hm, v);
+                rank[k] = (int)t >= dense_levels ? -1 : atomicAdd(&bc[prep_bucket(val[k], K, split)], 1);
+            }
+        }
+        // high-level entries first, in warp order
+        int hpos = 0;
+#pragma unroll
+        for (int k = 0; k < kPrepWarpPer; ++k) {
+            const unsigned m = __ballot_sync(full, rank[k] == -1);
+            if (rank[k] == -1) dst[ent_at(hpos + __popc(m & lt), rl)] = val[k];
+            hpos += __popc(m);
+        }
+        __syncwarp();
+        // then the dense entries by section and bank, banks rotated by the
+        // read's lane in the group (the same order as kmer_prep_kernel)
+        int base = hpos;
+        for (int sec = 0; sec < nsections; ++sec) {
+            const int b = sec * 32 + ((lane + rl) & 31);
+            const int c = bc[b];
+            int x = c;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(full, x, d);
+                if (lane >= d) x += y;
+            }
+            bs[b] = base + x - c;
+            bcnt[(int64_t)r * (32 * nsections) + b] = (uint16_t)c;
+            const int total = __shfl_sync(full, x, 31);
+            if (nsec && lane == 0) nsec[(int64_t)r * 2 + sec] = total;
+            base += total;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < kPrepWarpPer; ++k)
+            if (rank[k] >= 0) dst[ent_at(bs[prep_bucket(val[k], K, split)] + rank[k], rl)] = val[k];
+        for (int p = T + lane; p < E; p += 32) dst[ent_at(p, rl)] = kSentinel;
+        mx = (int)__reduce_max_sync(full, (unsigned)mx);
+        hm = __reduce_max_sync(full, hm);
+        if (lane == 0) {
+            cntmax[r] = mx;
+            nhigh[r] = hpos;
+            hinfo[r] = K == 8 && hm >= 0x8000u ? (hm << 16) | warp_table_count(tbl, hm) : 0u;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // K = 8 read order.  The tile kernel adds a pair's L half only where both
 // reads have the same H key (largest H K-mer and its count, or no H K-mer).
 // Sorting the reads by (H key, tuple count) puts reads of one key next to
@@ -510,10 +646,7 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
     __shared__ SchedSmem sm;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // one warp per (group, section): the schedule is a serial chain of warp
-    // collectives, so twice the warps hide twice the latency
-    for (int item = blockIdx.x * kSchedWarps + w; item < 2 * ngroups; item += gridDim.x * kSchedWarps) {
-        const int g = item >> 1, sec = item & 1;
+    for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
         const int r = g * 32 + lane;
         const bool active = r < n;
         const int rr = active ? r : 0;
@@ -523,15 +656,14 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
         const int E0 = ((int)__reduce_max_sync(full, (unsigned)n0) + 15) / 16 * 16;
         const int E1 = ((int)__reduce_max_sync(full, (unsigned)n1) + 15) / 16 * 16;
         if (lane == 0) {
-            if (sec == 0) tgent[g] = E0;
-            else tgentL[g] = E1;
+            tgent[g] = E0;
+            tgentL[g] = E1;
         }
-        if (sec == 0)
-            sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, E0, ent + gstart[g], 0u,
-                            guard_word, 1u, tent + tstart[g]);
-        else
-            sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + n0, E1, ent + gstart[g],
-                            0u, guard_word, 1u, tent + tstart[g] + (int64_t)32 * E0);
+        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, E0, ent + gstart[g], 0u,
+                        guard_word, 1u, tent + tstart[g]);
+        __syncwarp();
+        sched_stream<8>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + n0, E1, ent + gstart[g],
+                        0u, guard_word, 1u, tent + tstart[g] + (int64_t)32 * E0);
         __syncwarp();
     }
 }
@@ -2540,21 +2672,37 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     const int64_t* loff = k == 8 ? j.offp.as<int64_t>() : j.off.as<int64_t>();
     CRISPY_CK(ctx, cudaMemsetAsync(j.ent.ptr, 0xFF, (size_t)std::max<int64_t>(j.nent, 4) * 4, s));
     const uint32_t K4 = 1u << (2 * k);
-    auto prep = k == 8 ? kmer_prep_kernel<PrepHist12> : kmer_prep_kernel<PrepHist16>;
-    const size_t hsmem = k == 8 ? PrepHist12::bytes(K4) : PrepHist16::bytes(K4);
-    CRISPY_CK(ctx, cudaFuncSetAttribute(prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem));
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep, kPrepThreads, hsmem);
-    const int grid = std::min(n, ctx->sm_count * std::max(1, std::min(per_sm, 8)));
     int32_t* cntmax = j.cntmax.as<int32_t>();
     int32_t* nhigh = cntmax + n;
-    prep<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), loff,
-                                              j.t.as<int32_t>(), n, k, dense_levels_for(k),
-                                              j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
-                                              j.ent.as<uint32_t>(), cntmax, nhigh,
-                                              j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>(),
-                                              k == 8 || j.split ? j.nsec.as<int32_t>() : nullptr,
-                                              (uint32_t)j.split);
+    int32_t* d_nsec = k == 8 || j.split ? j.nsec.as<int32_t>() : nullptr;
+    // one warp per read (a table of occurrence ranks per warp) where the
+    // block kernel's histogram is large: K = 8, reads of up to 512 tuples
+    // (measured 3.9 -> about 1.9 ms on the stress set; at K = 6 the two
+    // kernels tie); CRISPY_KMER_PREP_WARP=1 / 0 forces it on / off
+    const char* pw_env = std::getenv("CRISPY_KMER_PREP_WARP");
+    const bool prep_warp = j.max_t <= kPrepWarpMaxT && (pw_env ? std::strcmp(pw_env, "0") != 0 : k == 8);
+    if (prep_warp) {
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kmer_prep_warp_kernel, kPrepWarps * 32, 0);
+        const int grid = std::min((n + kPrepWarps - 1) / kPrepWarps, ctx->sm_count * std::max(1, per_sm));
+        kmer_prep_warp_kernel<<<grid, kPrepWarps * 32, 0, s>>>(
+            j.seq.as<uint8_t>(), loff, j.t.as<int32_t>(), n, k, dense_levels_for(k), j.gstart.as<int64_t>(),
+            j.gent.as<int32_t>(), j.ent.as<uint32_t>(), cntmax, nhigh, j.hinfo.as<uint32_t>(),
+            j.bcnt.as<uint16_t>(), d_nsec, (uint32_t)j.split);
+    } else {
+        auto prep = k == 8 ? kmer_prep_kernel<PrepHist12> : kmer_prep_kernel<PrepHist16>;
+        const size_t hsmem = k == 8 ? PrepHist12::bytes(K4) : PrepHist16::bytes(K4);
+        CRISPY_CK(ctx, cudaFuncSetAttribute(prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem));
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep, kPrepThreads, hsmem);
+        const int grid = std::min(n, ctx->sm_count * std::max(1, std::min(per_sm, 8)));
+        prep<<<grid, kPrepThreads, hsmem, s>>>(j.seq.as<uint8_t>(), loff,
+                                                  j.t.as<int32_t>(), n, k, dense_levels_for(k),
+                                                  j.gstart.as<int64_t>(), j.gent.as<int32_t>(),
+                                                  j.ent.as<uint32_t>(), cntmax, nhigh,
+                                                  j.hinfo.as<uint32_t>(), j.bcnt.as<uint16_t>(), d_nsec,
+                                                  (uint32_t)j.split);
+    }
     count_launch(ctx);
     CRISPY_CK(ctx, cudaGetLastError());
     const int levels = dense_levels_for(k);
@@ -2608,7 +2756,7 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
         count_launch(ctx);
         CRISPY_CK(ctx, cudaGetLastError());
     } else if (levels > 0 && j.split) {
-        const int sgrid = std::min((2 * j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
         kmer_sched_split_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
             j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), nhigh, j.nsec.as<int32_t>(),
             j.bcnt.as<uint16_t>(), n, j.ngroups, (uint32_t)levels * (1u << (2 * k)), j.tgent.as<int32_t>(),

@@ -70,3 +70,16 @@ def test_split_many_alive_columns(engine):
     reads = synth.make_read_set(synth.ReadSetSpec(2500, 3, 520, "uniform", 300, 500, 6, 504))
     t = cg.default_threshold(len(reads), -1.0, 0)
     assert _check(engine, reads, 6, t, cg.MODE_BATCHED) > 10000
+
+
+@pytest.mark.parametrize("k", [3, 6, 8])
+def test_prep_kernels_agree(engine, monkeypatch, k):
+    # the warp-per-read prep kernel (K = 8 reads of at most 512 tuples, or
+    # CRISPY_KMER_PREP_WARP=1) and the block-per-read kernel
+    # (CRISPY_KMER_PREP_WARP=0) must give the same survivors
+    reads = _reads(700, 510 + k, k=k)
+    t = 0.5 if k < 8 else 0.7
+    monkeypatch.setenv("CRISPY_KMER_PREP_WARP", "0")
+    a = _check(engine, reads, k, t, cg.MODE_BATCHED)
+    monkeypatch.setenv("CRISPY_KMER_PREP_WARP", "1")
+    assert _check(engine, reads, k, t, cg.MODE_BATCHED) == a
