@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
+#include <new>
 #include <functional>
 #include <map>
 #include <string>
@@ -33,6 +35,38 @@ struct HostBuf {
     template <class T> T* as() const { return static_cast<T*>(ptr); }
 };
 
+// Allocator of page-locked host memory for per-read arrays that come back
+// from the device every run (copies into pageable memory go through a
+// staging buffer at a fraction of the link's rate).  Falls back to
+// pageable memory when pinning fails; frees by the kind it got.
+template <class T>
+struct PinnedAlloc {
+    using value_type = T;
+    PinnedAlloc() = default;
+    template <class U> PinnedAlloc(const PinnedAlloc<U>&) {}
+    T* allocate(size_t n) {
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, n * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            p = std::malloc(n * sizeof(T));
+            if (!p) throw std::bad_alloc();
+        }
+        return static_cast<T*>(p);
+    }
+    void deallocate(T* p, size_t) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost) {
+            cudaFreeHost(p);
+        } else {
+            cudaGetLastError();
+            std::free(p);
+        }
+    }
+    template <class U> bool operator==(const PinnedAlloc<U>&) const { return true; }
+    template <class U> bool operator!=(const PinnedAlloc<U>&) const { return false; }
+};
+template <class T> using pinned_vector = std::vector<T, PinnedAlloc<T>>;
+
 // Device-resident k-mer job: the reads of one kmerDist invocation.
 struct KmerJob {
     bool ready = false;
@@ -40,7 +74,7 @@ struct KmerJob {
     int ngroups = 0;            // 32-read groups
     int64_t nent = 0;           // entries in the interleaved level-entry array
     std::vector<int32_t> h_t;   // tuples per read (L - K + 1)
-    std::vector<int32_t> h_cntmax;   // largest k-mer multiplicity per read
+    pinned_vector<int32_t> h_cntmax;   // largest k-mer multiplicity and high-level entries per read
     std::vector<int64_t> h_gstart;   // first entry of each group
     std::vector<int32_t> h_gent;     // entries per lane in each group (multiple of 16)
     std::vector<int64_t> h_tstart;   // tile stream: first entry of each group
@@ -52,14 +86,14 @@ struct KmerJob {
     // sections (a hash of the plane word below split / 256: section 0), 0:
     // one section; the tile kernel bounds each pair after section 0
     int split = 0;
-    std::vector<int32_t> h_nsec;
+    pinned_vector<int32_t> h_nsec;
     // K = 8 read order: per-read arrays above (t, cntmax, hinfo, entries)
     // are by position in it; perm maps position -> read ID, offp holds the
     // offsets by position, t0 the tuple counts by read ID
     DevBuf t0, offp, perm;
-    std::vector<int32_t> h_perm;
+    pinned_vector<int32_t> h_perm;
     // K = 8: H key per position and the run of equal keys holding it
-    std::vector<uint32_t> h_hinfo;
+    pinned_vector<uint32_t> h_hinfo;
     std::vector<int32_t> h_run_lo, h_run_hi;
     bool hkeys_ordered = false;
     // last run's survivors, in stage order: on the device, or (spilled) in
