@@ -1444,6 +1444,8 @@ int crispy_tune_report(char* buf, size_t len) {
             first = false;
         }
     }
+    std::string km = kmer_tune_json();
+    if (!km.empty()) out += out.size() > 1 ? km : km.substr(2);
     out += "]";
     std::strncpy(buf, out.c_str(), len - 1);
     buf[len - 1] = 0;

@@ -241,6 +241,8 @@ struct CohortJob {
     void* user = nullptr;
 };
 int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::vector<int64_t>& counts);
+// The k-mer bound pass's tuned splits as JSON objects, each preceded by ", ".
+std::string kmer_tune_json();
 int gen_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, const std::vector<int64_t>& counts,
                    int band, std::vector<int64_t>& gen_counts);
 

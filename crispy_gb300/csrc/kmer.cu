@@ -46,6 +46,8 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "internal.h"
 
@@ -759,6 +761,7 @@ struct TileArgs {
     // in key bits 44 and up and count per job in job_counter.
     const int* item_job;
     const int* item_cend;
+    const int* item_cstart;   // first column group per item (nullptr: the row group's own)
     const int4* cjob;
     const int* ctbl;
     unsigned long long* job_counter;
@@ -1514,7 +1517,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) kmer_tile128_kernel(TileArgs 
                 s_item[3] = (int)w < a.nitems;
                 if (s_item[3]) {
                     s_item[0] = a.items[w];
-                    s_item[1] = 0;
+                    s_item[1] = a.item_cstart ? a.item_cstart[w] : 0;
                     s_item[2] = a.item_cend ? a.item_cend[w] : (a.n + 31) / 32;
                     s_item[4] = a.item_job ? a.item_job[w] : -1;
                 }
@@ -2479,6 +2482,51 @@ namespace {
 
 // Group layout of the reads in the job's read order (tuple counts t[]):
 // entries per lane and first entry of each 32-read group, uploaded with t.
+// ---- the bound pass's split, tuned per read set --------------------------
+// Section 0's share decides how many columns the bound pass leaves alive,
+// which depends on the reads (99,999 reads of uneven lengths: 112/256 is
+// best; 19,954 reads of N(250, 15): 144/256, and one pass is close).  The
+// split fixes the stream layout, so each candidate costs a rebuild; the
+// batched run times the tile kernel over every kKmerTuneStride-th row group
+// for each candidate once per read set (read count, K and tuple counts) and
+// keeps the fastest for the life of the process.  Any split gives the same
+// survivors, so tuning only picks speed.  CRISPY_KMER_SPLIT fixes the split;
+// CRISPY_AUTOTUNE=0 keeps the default.
+struct KmerTuneEntry {
+    int n, k, split;
+    float ms_best, ms_default;
+    int row_groups;
+};
+std::mutex g_ktune_mu;
+std::map<uint64_t, KmerTuneEntry> g_ktuned;
+constexpr int kKmerTuneMinReads = 8192;
+constexpr int kKmerTuneStride = 8;
+constexpr int kKmerTuneChunk = 256;   // column groups per item of a timing sample
+constexpr int kSplitCandidates[] = {kSplitDefault, 0, 96, 128, 144, 160};
+
+bool kmer_autotune_enabled() {
+    const char* e = std::getenv("CRISPY_AUTOTUNE");
+    return !(e && e[0] == '0');
+}
+
+// CRISPY_KMER_SPLIT, when set (0..255)
+bool kmer_split_env(int* v) {
+    const char* e = std::getenv("CRISPY_KMER_SPLIT");
+    if (!e) return false;
+    if (v) *v = std::max(0, std::min(255, std::atoi(e)));
+    return true;
+}
+
+// FNV-1a over the read count, K and the tuple counts (by read ID)
+uint64_t kmer_fingerprint(const KmerJob& j) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t x) { h = (h ^ x) * 1099511628211ull; };
+    mix((uint64_t)j.n);
+    mix((uint64_t)j.k);
+    for (int r = 0; r < j.n; ++r) mix((uint64_t)(uint32_t)j.h_t[r]);
+    return h;
+}
+
 int kmer_groups(crispy_ctx* ctx, const int32_t* t) {
     KmerJob& j = ctx->kmer;
     const int n = j.n;
@@ -2542,10 +2590,17 @@ int kmer_layout(crispy_ctx* ctx, const int32_t* lengths, int n, int k) {
     j.ngroups = (n + 31) / 32;
     j.split = 0;
     if (tile_rows_for(k) == kRows128) {
-        // CRISPY_KMER_SPLIT: section 0's share of the dense entries in 1/256
-        // (0: one section, no bound pass)
-        j.split = kSplitDefault;
-        if (const char* e = std::getenv("CRISPY_KMER_SPLIT")) j.split = std::max(0, std::min(255, std::atoi(e)));
+        // section 0's share of the dense entries in 1/256 (0: one section,
+        // no bound pass): CRISPY_KMER_SPLIT, else the tuned split of this
+        // read set, else the default
+        if (!kmer_split_env(&j.split)) {
+            j.split = kSplitDefault;
+            if (kmer_autotune_enabled()) {
+                std::lock_guard<std::mutex> g(g_ktune_mu);
+                auto it = g_ktuned.find(kmer_fingerprint(j));
+                if (it != g_ktuned.end()) j.split = it->second.split;
+            }
+        }
     }
     CRISPY_TRY(ensure(ctx, j.off, (size_t)n * 8));
     CRISPY_TRY(ensure(ctx, j.t, (size_t)n * 4));
@@ -2781,7 +2836,11 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     return CRISPY_OK;
 }
 
-int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* npairs) {
+// sample > 0: a timing run of the batched tile kernel over every sample-th
+// row group (no graph, no dense-kernel rows, survivors left unsorted); its
+// duration goes to *sample_ms.
+static int kmer_run_impl(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* npairs, int sample,
+                         float* sample_ms) {
     if (!ctx) return CRISPY_E_INPUT;
     KmerJob& j = ctx->kmer;
     if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_run before kmer_prepare");
@@ -2941,7 +3000,7 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
             // (each with all its columns), longest first.  K = 8 split: the
             // H-only kernel over the 32-row groups, then the two-phase kernel
             // over each row group's same-key column range.
-            std::vector<int> items, items_s;
+            std::vector<int> items, items_s, s_cs, s_ce;
             std::vector<int2> q_s;
             if (split8) {
                 // the H-only kernel's pairs (different H keys) can pass only
@@ -2967,19 +3026,38 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 }
             } else if (fast) {
                 for (int rg = rlo / rows_blk; rg * rows_blk < rhi; ++rg) {
+                    if (sample > 0 && rg % sample != 0) continue;
                     bool any_rows = false;
                     for (int r = rg * rows_blk; r < std::min(n, rg * rows_blk + rows_blk); r += 32)
                         any_rows |= !dense[r >> 5];
-                    if (any_rows) items.push_back(rg);
+                    if (!any_rows) continue;
+                    if (sample > 0) {
+                        // a timing sample: the row group's columns in chunks,
+                        // so that the sample's items keep every SM busy
+                        const int c0 = rg * (rows_blk / 32), c1 = (n + 31) / 32;
+                        for (int c = c0; c < c1; c += kKmerTuneChunk) {
+                            items.push_back(rg);
+                            s_cs.push_back(c);
+                            s_ce.push_back(std::min(c1, c + kKmerTuneChunk));
+                        }
+                    } else {
+                        items.push_back(rg);
+                    }
                 }
             }
             if (!items.empty() || !items_s.empty()) {
-                const size_t nh = items.size(), ns = items_s.size();
-                CRISPY_TRY(ensure(ctx, j.sort_tmp, ns * sizeof(int2) + (nh + ns) * sizeof(int) + 64));
+                const size_t nh = items.size(), ns = items_s.size(), nc = s_cs.size();
+                CRISPY_TRY(ensure(ctx, j.sort_tmp, ns * sizeof(int2) + (nh + ns + 2 * nc) * sizeof(int) + 64));
                 int2* d_q = j.sort_tmp.as<int2>();
                 int* d_items = reinterpret_cast<int*>(d_q + ns);
                 int* d_items_s = d_items + nh;
-                unsigned int* head = reinterpret_cast<unsigned int*>(d_items_s + ns);
+                int* d_cs = d_items_s + ns;
+                int* d_ce = d_cs + nc;
+                unsigned int* head = reinterpret_cast<unsigned int*>(d_ce + nc);
+                if (nc) {
+                    CRISPY_CK(ctx, cudaMemcpyAsync(d_cs, s_cs.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
+                    CRISPY_CK(ctx, cudaMemcpyAsync(d_ce, s_ce.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
+                }
                 if (nh) CRISPY_CK(ctx, cudaMemcpyAsync(d_items, items.data(), nh * sizeof(int), cudaMemcpyHostToDevice, s));
                 if (ns) {
                     CRISPY_CK(ctx, cudaMemcpyAsync(d_items_s, items_s.data(), ns * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -2995,6 +3073,10 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                 // staged form's blocks hold too few to fill the lanes' stacks)
                 t2.bound = j.split != 0;
                 t2.gstat = j.split ? j.counter.as<unsigned long long>() + 1 : nullptr;
+                if (nc) {
+                    t2.item_cstart = d_cs;
+                    t2.item_cend = d_ce;
+                }
                 TileArgs t3 = t2;
                 t3.items = d_items_s; t3.nitems = (int)ns; t3.queue_head = head + 1;
                 t3.item_q = d_q; t3.same_only = 1;
@@ -3030,6 +3112,26 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
                     (uint64_t)nh, (uint64_t)ns, (uint64_t)grid, (uint64_t)grid_s, (uint64_t)any_dense, (uint64_t)A,
                     (uint64_t)rlo, (uint64_t)rhi, (uint64_t)j.split, (uint64_t)t2.bound, (uint64_t)t2.qfire,
                     (uint64_t)queue8, (uint64_t)(uintptr_t)t3.sq, (uint64_t)t3.sq_cap});
+                if (sample > 0) {
+                    cudaEvent_t e0, e1;
+                    CRISPY_CK(ctx, cudaEventCreate(&e0));
+                    CRISPY_CK(ctx, cudaEventCreate(&e1));
+                    CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
+                    CRISPY_CK(ctx, cudaMemsetAsync(head, 0, 8, s));
+                    CRISPY_CK(ctx, cudaEventRecord(e0, s));
+                    if (nh) main_fn<<<grid, main_threads, main_smem, s>>>(t2);
+                    CRISPY_CK(ctx, cudaEventRecord(e1, s));
+                    count_launch(ctx);
+                    CRISPY_CK(ctx, cudaEventSynchronize(e1));
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    CRISPY_CK(ctx, cudaGetLastError());
+                    if (sample_ms) *sample_ms = ms;
+                    *total_out = 0;
+                    return CRISPY_OK;
+                }
                 ev_begin(ctx, ctx->ev_kmer, s);
                 CRISPY_TRY(graph_run(ctx, s, key, [&]() -> int {
                     CRISPY_CK(ctx, cudaMemsetAsync(j.counter.ptr, 0, 64, s));
@@ -3107,6 +3209,10 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     int64_t total = 0;
     j.spilled = false;
     CRISPY_TRY(run_pass(0, n, cap, &total));
+    if (sample > 0) {
+        j.nsurv = 0;
+        return CRISPY_OK;
+    }
     if (total > cap && total <= dev_cap) {
         cap = std::min(dev_cap, total + total / 8 + 1024);
         CRISPY_TRY(run_pass(0, n, cap, &total));
@@ -3172,6 +3278,64 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     ctx->stats.kmer_survivors = j.nsurv;
     if (npairs) *npairs = j.nsurv;
     return CRISPY_OK;
+}
+
+// Stream layout and level entries again, for the job's current split.
+static int kmer_relayout(crispy_ctx* ctx) {
+    KmerJob& j = ctx->kmer;
+    if (j.split) {
+        CRISPY_TRY(ensure(ctx, j.tgentL, (size_t)j.ngroups * 4));
+        CRISPY_TRY(ensure(ctx, j.nsec, (size_t)j.n * 8));
+    }
+    CRISPY_TRY(kmer_groups(ctx, j.h_t.data()));
+    return crispy_kmer_rebuild(ctx);
+}
+
+// The split of this read set: the tuned one, or each candidate timed on the
+// row-group sample (two runs each, the faster counts) and the fastest kept.
+static int kmer_tune_split(crispy_ctx* ctx, float thr) {
+    KmerJob& j = ctx->kmer;
+    const uint64_t fp = kmer_fingerprint(j);
+    int best = -1;
+    {
+        std::lock_guard<std::mutex> g(g_ktune_mu);
+        auto it = g_ktuned.find(fp);
+        if (it != g_ktuned.end()) best = it->second.split;
+    }
+    if (best < 0) {
+        float best_ms = 1e30f, dflt_ms = 0;
+        for (int c : kSplitCandidates) {
+            j.split = c;
+            CRISPY_TRY(kmer_relayout(ctx));
+            float ms = 1e30f;
+            for (int rep = 0; rep < 2; ++rep) {
+                float m = 0;
+                CRISPY_TRY(kmer_run_impl(ctx, thr, CRISPY_MODE_BATCHED, 0, nullptr, kKmerTuneStride, &m));
+                ms = std::min(ms, m);
+            }
+            if (c == kSplitDefault) dflt_ms = ms;
+            if (ms < best_ms) { best_ms = ms; best = c; }
+        }
+        std::lock_guard<std::mutex> g(g_ktune_mu);
+        g_ktuned[fp] = KmerTuneEntry{j.n, j.k, best, best_ms, dflt_ms,
+                                     (int)((j.n + kRows128 * kKmerTuneStride - 1) / (kRows128 * kKmerTuneStride))};
+    }
+    if (j.split != best) {
+        j.split = best;
+        CRISPY_TRY(kmer_relayout(ctx));
+    }
+    return CRISPY_OK;
+}
+
+int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* npairs) {
+    if (!ctx) return CRISPY_E_INPUT;
+    KmerJob& j = ctx->kmer;
+    if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_run before kmer_prepare");
+    cudaSetDevice(ctx->device);
+    if (mode == CRISPY_MODE_BATCHED && tile_rows_for(j.k) == kRows128 && j.n >= kKmerTuneMinReads &&
+        kmer_autotune_enabled() && !kmer_split_env(nullptr))
+        CRISPY_TRY(kmer_tune_split(ctx, thr));
+    return kmer_run_impl(ctx, thr, mode, dists, npairs, 0, nullptr);
 }
 
 int crispy_kmer_fetch(crispy_ctx* ctx, int32_t* pairs, float* dists, int64_t cap, int64_t* count) {
@@ -3244,6 +3408,23 @@ namespace crispy {
 // path the cohort form does not take (K > 6, rows for the dense kernel,
 // more survivors than the device share): the caller then runs the jobs
 // one by one.
+// The bound pass's tuned splits, as JSON objects for crispy_tune_report
+// (each preceded by ", ").
+std::string kmer_tune_json() {
+    std::string out;
+    std::lock_guard<std::mutex> g(g_ktune_mu);
+    for (auto& kv : g_ktuned) {
+        char item[256];
+        snprintf(item, sizeof item,
+                 ", {\"stage\": \"kmer\", \"kernel\": \"kmer_tile128_kernel\", \"reads\": %d, \"k\": %d, "
+                 "\"split\": %d, \"sample_row_groups\": %d, \"ms\": %.4f, \"default_ms\": %.4f}",
+                 kv.second.n, kv.second.k, kv.second.split, kv.second.row_groups, kv.second.ms_best,
+                 kv.second.ms_default);
+        out += item;
+    }
+    return out;
+}
+
 int kmer_run_cohort(crispy_ctx* ctx, const std::vector<CohortJob>& jobs, std::vector<int64_t>& counts) {
     KmerJob& j = ctx->kmer;
     if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer cohort before kmer_prepare");

@@ -83,3 +83,24 @@ def test_prep_kernels_agree(engine, monkeypatch, k):
     a = _check(engine, reads, k, t, cg.MODE_BATCHED)
     monkeypatch.setenv("CRISPY_KMER_PREP_WARP", "1")
     assert _check(engine, reads, k, t, cg.MODE_BATCHED) == a
+
+
+def test_split_autotuned(engine, monkeypatch):
+    # without CRISPY_KMER_SPLIT the batched run of a read set of >= 8,192
+    # reads times each candidate split once and keeps the fastest; a second
+    # run of the same read set reuses it
+    monkeypatch.delenv("CRISPY_KMER_SPLIT", raising=False)
+    monkeypatch.delenv("CRISPY_AUTOTUNE", raising=False)
+    reads = _reads(9000, 520)
+    assert len(reads) >= 8192
+    t = cg.default_threshold(len(reads), -1.0, 0)
+    a = _check(engine, reads, 6, t, cg.MODE_BATCHED)
+
+    def entries():
+        return [e for e in cg.tune_report() if e.get("stage") == "kmer" and e["reads"] == len(reads)]
+
+    e = entries()
+    assert len(e) == 1 and e[0]["split"] in (0, 96, 112, 128, 144, 160)
+    assert _check(engine, reads, 6, t, cg.MODE_BATCHED) == a
+    assert _check(engine, reads, 6, t, cg.MODE_STAGED) == a
+    assert len(entries()) == 1
