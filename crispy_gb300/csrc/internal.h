@@ -163,6 +163,10 @@ struct crispy_ctx {
     crispy::StreamEvents ev_kmer, ev_gen;
     std::map<std::string, crispy::GraphEntry> graphs;   // captured launch sequences
     bool use_graphs = true;
+    // the batched k-mer run may tune its split per read set (off for the
+    // server's contexts: every job is a new read set, and tuning one costs
+    // more than it saves)
+    bool kmer_tune = true;
     size_t mem_cap = 0;      // 0 = unlimited
     size_t mem_in_use = 0;   // bytes held by DevBuf allocations
     // device bytes the current run has asked for (each buffer's largest

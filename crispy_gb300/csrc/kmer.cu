@@ -2489,9 +2489,10 @@ namespace {
 // split fixes the stream layout, so each candidate costs a rebuild; the
 // batched run times the tile kernel over every kKmerTuneStride-th row group
 // for each candidate once per read set (read count, K and tuple counts) and
-// keeps the fastest for the life of the process.  Any split gives the same
-// survivors, so tuning only picks speed.  CRISPY_KMER_SPLIT fixes the split;
-// CRISPY_AUTOTUNE=0 keeps the default.
+// keeps the fastest for the life of the process, from the read set's second
+// batched run on (a one-shot run keeps the default).  Any split gives the
+// same survivors, so tuning only picks speed.  CRISPY_KMER_SPLIT fixes the
+// split; CRISPY_AUTOTUNE=0 keeps the default.
 struct KmerTuneEntry {
     int n, k, split;
     float ms_best, ms_default;
@@ -2499,6 +2500,7 @@ struct KmerTuneEntry {
 };
 std::mutex g_ktune_mu;
 std::map<uint64_t, KmerTuneEntry> g_ktuned;
+std::map<uint64_t, int> g_kseen;   // batched runs per read set not yet tuned
 constexpr int kKmerTuneMinReads = 8192;
 constexpr int kKmerTuneStride = 8;
 constexpr int kKmerTuneChunk = 256;   // column groups per item of a timing sample
@@ -3291,8 +3293,10 @@ static int kmer_relayout(crispy_ctx* ctx) {
     return crispy_kmer_rebuild(ctx);
 }
 
-// The split of this read set: the tuned one, or each candidate timed on the
-// row-group sample (two runs each, the faster counts) and the fastest kept.
+// The split of this read set: the tuned one, or -- from its second batched
+// run in this process on, when tuning can pay for itself -- each candidate
+// timed on the row-group sample (two runs each, the faster counts) and the
+// fastest kept.
 static int kmer_tune_split(crispy_ctx* ctx, float thr) {
     KmerJob& j = ctx->kmer;
     const uint64_t fp = kmer_fingerprint(j);
@@ -3301,6 +3305,7 @@ static int kmer_tune_split(crispy_ctx* ctx, float thr) {
         std::lock_guard<std::mutex> g(g_ktune_mu);
         auto it = g_ktuned.find(fp);
         if (it != g_ktuned.end()) best = it->second.split;
+        else if (g_kseen[fp]++ == 0) return CRISPY_OK;   // first run: the default split
     }
     if (best < 0) {
         float best_ms = 1e30f, dflt_ms = 0;
@@ -3332,8 +3337,8 @@ int crispy_kmer_run(crispy_ctx* ctx, float thr, int mode, int dists, int64_t* np
     KmerJob& j = ctx->kmer;
     if (!j.ready) return fail(ctx, CRISPY_E_STATE, "kmer_run before kmer_prepare");
     cudaSetDevice(ctx->device);
-    if (mode == CRISPY_MODE_BATCHED && tile_rows_for(j.k) == kRows128 && j.n >= kKmerTuneMinReads &&
-        kmer_autotune_enabled() && !kmer_split_env(nullptr))
+    if (mode == CRISPY_MODE_BATCHED && ctx->kmer_tune && tile_rows_for(j.k) == kRows128 &&
+        j.n >= kKmerTuneMinReads && kmer_autotune_enabled() && !kmer_split_env(nullptr))
         CRISPY_TRY(kmer_tune_split(ctx, thr));
     return kmer_run_impl(ctx, thr, mode, dists, npairs, 0, nullptr);
 }

@@ -352,6 +352,7 @@ int crispy_server_create(int device, size_t hbm_budget_bytes, int slots, crispy_
             delete s;
             return rc;
         }
+        c->kmer_tune = false;
         s->ctx.push_back(c);
     }
     for (int i = 0; i < slots; ++i) s->workers.emplace_back(&crispy_server::worker, s, i);

@@ -86,19 +86,21 @@ def test_prep_kernels_agree(engine, monkeypatch, k):
 
 
 def test_split_autotuned(engine, monkeypatch):
-    # without CRISPY_KMER_SPLIT the batched run of a read set of >= 8,192
-    # reads times each candidate split once and keeps the fastest; a second
-    # run of the same read set reuses it
+    # without CRISPY_KMER_SPLIT the second batched run of a read set of >=
+    # 8,192 reads times each candidate split once and keeps the fastest;
+    # later runs of the same read set reuse it
     monkeypatch.delenv("CRISPY_KMER_SPLIT", raising=False)
     monkeypatch.delenv("CRISPY_AUTOTUNE", raising=False)
     reads = _reads(9000, 520)
     assert len(reads) >= 8192
     t = cg.default_threshold(len(reads), -1.0, 0)
-    a = _check(engine, reads, 6, t, cg.MODE_BATCHED)
 
     def entries():
         return [e for e in cg.tune_report() if e.get("stage") == "kmer" and e["reads"] == len(reads)]
 
+    a = _check(engine, reads, 6, t, cg.MODE_BATCHED)
+    assert entries() == []
+    assert _check(engine, reads, 6, t, cg.MODE_BATCHED) == a
     e = entries()
     assert len(e) == 1 and e[0]["split"] in (0, 96, 112, 128, 144, 160)
     assert _check(engine, reads, 6, t, cg.MODE_BATCHED) == a
