@@ -1212,7 +1212,7 @@ int crispy_gen_prepare_from_pre(crispy_ctx* ctx, const crispy_raw* raw) {
     if (n <= 0) return fail(ctx, CRISPY_E_INPUT, "gen_prepare_from_pre: preprocess kept no read");
     if (n > CRISPY_MAX_NUM_READS) return fail(ctx, CRISPY_E_UNSUPPORTED, "numReads %d > %d", n, CRISPY_MAX_NUM_READS);
     g.n = n;
-    g.h_len = len;
+    g.h_len.assign(len.begin(), len.end());
     g.h_woff.resize(n + 1);
     int64_t words = 0;
     g.max_len = 0;

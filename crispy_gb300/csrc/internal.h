@@ -73,12 +73,12 @@ struct KmerJob {
     int n = 0, k = 0, max_len = 0, max_t = 0;
     int ngroups = 0;            // 32-read groups
     int64_t nent = 0;           // entries in the interleaved level-entry array
-    std::vector<int32_t> h_t;   // tuples per read (L - K + 1)
+    pinned_vector<int32_t> h_t;   // tuples per read (L - K + 1)
     pinned_vector<int32_t> h_cntmax;   // largest k-mer multiplicity and high-level entries per read
-    std::vector<int64_t> h_gstart;   // first entry of each group
-    std::vector<int32_t> h_gent;     // entries per lane in each group (multiple of 16)
-    std::vector<int64_t> h_tstart;   // tile stream: first entry of each group
-    std::vector<int32_t> h_tgent;    // tile stream: steps per lane in each group
+    pinned_vector<int64_t> h_gstart;   // first entry of each group
+    pinned_vector<int32_t> h_gent;     // entries per lane in each group (multiple of 16)
+    pinned_vector<int64_t> h_tstart;   // tile stream: first entry of each group
+    pinned_vector<int32_t> h_tgent;    // tile stream: steps per lane in each group
     int64_t ntent = 0;
     DevBuf seq, off, len, t, gstart, gent, ent, cntmax, hinfo, tstart, tgent, tent, bcnt;
     DevBuf tgentL, nsec;             // second-stream steps per group; per-read section counts
@@ -111,8 +111,8 @@ struct KmerJob {
 struct GenJob {
     bool ready = false;
     int n = 0, max_len = 0;
-    std::vector<int32_t> h_len;
-    std::vector<int64_t> h_woff;     // first packed word of each read
+    pinned_vector<int32_t> h_len;
+    pinned_vector<int64_t> h_woff;     // first packed word of each read
     DevBuf seq, off, len, woff, packed;
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
         vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue,
