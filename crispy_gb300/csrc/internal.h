@@ -92,6 +92,7 @@ struct KmerJob {
     // offsets by position, t0 the tuple counts by read ID
     DevBuf t0, offp, perm;
     pinned_vector<int32_t> h_perm;
+    pinned_vector<int32_t> h_tpos;   // tuple counts by position
     // K = 8: H key per position and the run of equal keys holding it
     pinned_vector<uint32_t> h_hinfo;
     std::vector<int32_t> h_run_lo, h_run_hi;

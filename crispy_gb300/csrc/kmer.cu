@@ -1348,137 +1348,137 @@ __device__ void tile_columns128(const TileArgs& a, const EmitJob& ej, const uint
     // columns and rounds
     uint32_t st_bound = 0, st_full = 0, st_cols = 0, st_rounds = 0;
     for (int pool = 0; pool < (bound ? 2 : 1); ++pool) {
-    if (pool) {
-        sk.qn[warp * 32 + lane] = (uint8_t)qn;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            int run = 0;
-            for (int w = 0; w < kTileWarps; ++w) {
-                sk.qoff[w * 32 + threadIdx.x] = (uint8_t)run;
-                run += sk.qn[w * 32 + threadIdx.x];
-            }
-        }
-        __syncthreads();
-        pc = sk.qoff[(kTileWarps - 1) * 32 + lane] + sk.qn[(kTileWarps - 1) * 32 + lane];
-        pmax = (int)__reduce_max_sync(full, (unsigned)pc);
-    }
-    for (;;) {
-        bool round;
         if (pool) {
-            int v = 0;
-            if (lane == 0) v = atomicAdd(sk.next + 1, 1);
-            pi = __shfl_sync(full, v, 0);
-            if (pi >= pmax) break;
-            round = true;
-        } else {
-            // a full-pass round when enough lanes hold a column or a stack is full
-            const unsigned held = __ballot_sync(full, qn > 0);
-            round = held != 0u && (__popc(held) >= a.qfire || __any_sync(full, qn == kQDepth));
-            if (!round) {
-                if (bound) {
-                    int v = 0;
-                    if (lane == 0) v = atomicAdd(sk.next, 1);
-                    cg = cg0 + __shfl_sync(full, v, 0);
-                } else {
-                    cg += kTileWarps;
+            sk.qn[warp * 32 + lane] = (uint8_t)qn;
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                int run = 0;
+                for (int w = 0; w < kTileWarps; ++w) {
+                    sk.qoff[w * 32 + threadIdx.x] = (uint8_t)run;
+                    run += sk.qn[w * 32 + threadIdx.x];
                 }
-                if (cg >= cg1) break;
             }
+            __syncthreads();
+            pc = sk.qoff[(kTileWarps - 1) * 32 + lane] + sk.qn[(kTileWarps - 1) * 32 + lane];
+            pmax = (int)__reduce_max_sync(full, (unsigned)pc);
         }
-        int ccg = 0;
-        bool active = true;
-        if (pool) {
-            active = pi < pc;
-            if (active) {
-                int w = 0;
-                while (w + 1 < kTileWarps && (int)sk.qoff[(w + 1) * 32 + lane] <= pi) ++w;
-                ccg = sk.q[w * (kQDepth * 32) + (pi - (int)sk.qoff[w * 32 + lane]) * 32 + lane];
-            }
-        } else if (round) {
-            active = qn > 0;
-            if (active) {
-                --qn;
-                ccg = s_q[qn * 32 + lane];
-            }
-        } else {
-            ccg = cg;
-        }
-        const int c = ccg * 32 + lane;
-        const bool col_ok = active && c >= a.c_lo && c < a.c_hi && c < a.n;
-        uint32_t vm[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) vm[q] = col_ok ? half_mask(c - r0 - 32 * q) & s_rows_ok[q] : 0u;
-        const bool any_vm = (vm[0] | vm[1] | vm[2] | vm[3]) != 0u;
-        if (!__any_sync(full, any_vm)) continue;
-        // bound pass: section 0 of the group; full pass: every step of the
-        // lane's group (both sections with a split)
-        int El = a.tgent[ccg];
-        if (a.split && (round || !bound)) El += a.tgentL[ccg];
-        const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[ccg]) + lane;
-        Counter<B> cnt[4];
-        if (round) {
-            if (!any_vm) El = 0;
-            const int Emax = (int)__reduce_max_sync(full, (unsigned)El);
-            accumulate128<B, true>(Pb, ep, El, Emax, gq, a.k65536, a.k8 * 2u, cnt);
-        } else {
-            accumulate128<B, false>(Pb, ep, El, El, gq, a.k65536, a.k8 * 2u, cnt);
-        }
-        if (a.gstat && any_vm) {
-            const int2 ns = *reinterpret_cast<const int2*>(a.nsec + 2 * (int64_t)c);
-            if (round) {
-                st_full += (uint32_t)(ns.x + ns.y);
-                ++st_cols;
+        for (;;) {
+            bool round;
+            if (pool) {
+                int v = 0;
+                if (lane == 0) v = atomicAdd(sk.next + 1, 1);
+                pi = __shfl_sync(full, v, 0);
+                if (pi >= pmax) break;
+                round = true;
             } else {
-                st_bound += (uint32_t)ns.x;
-            }
-        }
-        if (round && lane == 0) ++st_rounds;
-        uint32_t X[4][B];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) cnt[q].planes(X[q]);
-        const int tc = col_ok ? a.tcount[c] : 0;
-        if (bound && !round) {
-            bool alive = false;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (!vm[q]) continue;
-                if (tc < rb.tmax[q]) {
-                    alive = true;
-                    continue;
+                // a full-pass round when enough lanes hold a column or a stack is full
+                const unsigned held = __ballot_sync(full, qn > 0);
+                round = held != 0u && (__popc(held) >= a.qfire || __any_sync(full, qn == kQDepth));
+                if (!round) {
+                    if (bound) {
+                        int v = 0;
+                        if (lane == 0) v = atomicAdd(sk.next, 1);
+                        cg = cg0 + __shfl_sync(full, v, 0);
+                    } else {
+                        cg += kTileWarps;
+                    }
+                    if (cg >= cg1) break;
                 }
-                uint32_t gt = 0, eq = full;
-#pragma unroll
-                for (int k = B - 1; k >= 0; --k) {
-                    const uint32_t rk = rb.thr[q * kRPlanes + k];
-                    gt |= eq & X[q][k] & ~rk;
-                    eq &= ~(X[q][k] ^ rk);
+            }
+            int ccg = 0;
+            bool active = true;
+            if (pool) {
+                active = pi < pc;
+                if (active) {
+                    int w = 0;
+                    while (w + 1 < kTileWarps && (int)sk.qoff[(w + 1) * 32 + lane] <= pi) ++w;
+                    ccg = sk.q[w * (kQDepth * 32) + (pi - (int)sk.qoff[w * 32 + lane]) * 32 + lane];
                 }
-                if ((gt | eq) & vm[q] & rb.live[q]) alive = true;
+            } else if (round) {
+                active = qn > 0;
+                if (active) {
+                    --qn;
+                    ccg = s_q[qn * 32 + lane];
+                }
+            } else {
+                ccg = cg;
             }
-            if (alive) {
-                s_q[qn * 32 + lane] = (uint16_t)ccg;
-                ++qn;
+            const int c = ccg * 32 + lane;
+            const bool col_ok = active && c >= a.c_lo && c < a.c_hi && c < a.n;
+            uint32_t vm[4];
+    #pragma unroll
+            for (int q = 0; q < 4; ++q) vm[q] = col_ok ? half_mask(c - r0 - 32 * q) & s_rows_ok[q] : 0u;
+            const bool any_vm = (vm[0] | vm[1] | vm[2] | vm[3]) != 0u;
+            if (!__any_sync(full, any_vm)) continue;
+            // bound pass: section 0 of the group; full pass: every step of the
+            // lane's group (both sections with a split)
+            int El = a.tgent[ccg];
+            if (a.split && (round || !bound)) El += a.tgentL[ccg];
+            const uint4* __restrict__ ep = reinterpret_cast<const uint4*>(a.tent + a.tstart[ccg]) + lane;
+            Counter<B> cnt[4];
+            if (round) {
+                if (!any_vm) El = 0;
+                const int Emax = (int)__reduce_max_sync(full, (unsigned)El);
+                accumulate128<B, true>(Pb, ep, El, Emax, gq, a.k65536, a.k8 * 2u, cnt);
+            } else {
+                accumulate128<B, false>(Pb, ep, El, El, gq, a.k65536, a.k8 * 2u, cnt);
             }
-            continue;
+            if (a.gstat && any_vm) {
+                const int2 ns = *reinterpret_cast<const int2*>(a.nsec + 2 * (int64_t)c);
+                if (round) {
+                    st_full += (uint32_t)(ns.x + ns.y);
+                    ++st_cols;
+                } else {
+                    st_bound += (uint32_t)ns.x;
+                }
+            }
+            if (round && lane == 0) ++st_rounds;
+            uint32_t X[4][B];
+    #pragma unroll
+            for (int q = 0; q < 4; ++q) cnt[q].planes(X[q]);
+            const int tc = col_ok ? a.tcount[c] : 0;
+            if (bound && !round) {
+                bool alive = false;
+    #pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (!vm[q]) continue;
+                    if (tc < rb.tmax[q]) {
+                        alive = true;
+                        continue;
+                    }
+                    uint32_t gt = 0, eq = full;
+    #pragma unroll
+                    for (int k = B - 1; k >= 0; --k) {
+                        const uint32_t rk = rb.thr[q * kRPlanes + k];
+                        gt |= eq & X[q][k] & ~rk;
+                        eq &= ~(X[q][k] ^ rk);
+                    }
+                    if ((gt | eq) & vm[q] & rb.live[q]) alive = true;
+                }
+                if (alive) {
+                    s_q[qn * 32 + lane] = (uint16_t)ccg;
+                    ++qn;
+                }
+                continue;
+            }
+            // rank >= levels: the hash (the entries lead each read's level list)
+            if (any_high) {
+                const int nh = col_ok ? a.nhigh[c] : 0;
+                const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
+                const uint32_t* __restrict__ rp = a.ent + a.gstart[ccg];
+                for (int j = 0; j < maxh; ++j) {
+                    const uint4 w = j < nh ? hash_find4(hkeys, hmask, __ldg(rp + ent_at(j, lane)))
+                                           : make_uint4(0u, 0u, 0u, 0u);
+                    Counter<B>::add_at(X[0], w.x, 0);
+                    Counter<B>::add_at(X[1], w.y, 0);
+                    Counter<B>::add_at(X[2], w.z, 0);
+                    Counter<B>::add_at(X[3], w.w, 0);
+                }
+            }
+    #pragma unroll
+            for (int q = 0; q < 4; ++q)
+                finish_half<B>(a, ej, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
         }
-        // rank >= levels: the hash (the entries lead each read's level list)
-        if (any_high) {
-            const int nh = col_ok ? a.nhigh[c] : 0;
-            const int maxh = (int)__reduce_max_sync(full, (unsigned)nh);
-            const uint32_t* __restrict__ rp = a.ent + a.gstart[ccg];
-            for (int j = 0; j < maxh; ++j) {
-                const uint4 w = j < nh ? hash_find4(hkeys, hmask, __ldg(rp + ent_at(j, lane)))
-                                       : make_uint4(0u, 0u, 0u, 0u);
-                Counter<B>::add_at(X[0], w.x, 0);
-                Counter<B>::add_at(X[1], w.y, 0);
-                Counter<B>::add_at(X[2], w.z, 0);
-                Counter<B>::add_at(X[3], w.w, 0);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            finish_half<B>(a, ej, X[q], vm[q], r0 + 32 * q, s_tmin[q], s_rowT + 32 * q, c, tc);
-    }
     }
     if (a.gstat) {
         const uint32_t b = __reduce_add_sync(full, st_bound), f = __reduce_add_sync(full, st_full);
@@ -2655,13 +2655,13 @@ int kmer_order(crispy_ctx* ctx) {
     j.h_perm.resize(n);
     CRISPY_CK(ctx, cudaMemcpyAsync(j.h_perm.data(), j.perm.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
-    std::vector<int32_t> tp(n);
+    j.h_tpos.resize(n);
     for (int i = 0; i < n; ++i) {
         const int32_t r = j.h_perm[i];
         if (r < 0 || r >= n) return fail(ctx, CRISPY_E_STATE, "read order is not a permutation");
-        tp[i] = j.h_t[r];
+        j.h_tpos[i] = j.h_t[r];
     }
-    return kmer_groups(ctx, tp.data());
+    return kmer_groups(ctx, j.h_tpos.data());
 }
 
 }  // namespace
@@ -3011,7 +3011,7 @@ static int kmer_run_impl(crispy_ctx* ctx, float thr, int mode, int dists, int64_
                 bool any_heavy = false;
                 for (int i = 0; i < n && !any_heavy; ++i) {
                     const int h = j.h_nsec[2 * (size_t)i] + j.h_cntmax[(size_t)n + i];
-                    any_heavy = h >= (int)mmin[j.h_t[j.h_perm[i]]];
+                    any_heavy = h >= (int)mmin[j.h_tpos[i]];
                 }
                 for (int g = 0; g < j.ngroups && any_heavy; ++g)
                     if (!dense[g]) items.push_back(g);
