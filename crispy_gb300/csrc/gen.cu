@@ -1037,13 +1037,16 @@ int gen_finish(crispy_ctx* ctx, cudaStream_t s, const int2* d_pairs, int64_t npa
     CRISPY_TRY(ensure(ctx, g.blocksum, (size_t)ntiles * 4));
     gen_flag_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, s>>>(dist, npairs, thr, g.flags.as<uint8_t>());
     count_launch(ctx);
-    int64_t total = 0;
+    // the per-tile survivor counts give the chunk boundaries and the total:
+    // one read-back
     CRISPY_TRY(compact_flags(ctx, s, g.flags.as<uint8_t>(), npairs, g.surv_idx.as<uint32_t>(),
-                             g.blocksum.as<uint32_t>(), g.scan, &total));
-    std::vector<uint32_t> tile_counts(ntiles);
-    CRISPY_CK(ctx, cudaMemcpyAsync(tile_counts.data(), g.blocksum.ptr, (size_t)ntiles * 4,
-                                   cudaMemcpyDeviceToHost, s));
+                             g.blocksum.as<uint32_t>(), g.scan, nullptr));
+    g.h_tiles.resize(ntiles);
+    uint32_t* tile_counts = g.h_tiles.data();
+    CRISPY_CK(ctx, cudaMemcpyAsync(tile_counts, g.blocksum.ptr, (size_t)ntiles * 4, cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
+    int64_t total = 0;
+    for (int64_t t = 0; t < ntiles; ++t) total += tile_counts[t];
     // chunk boundaries: genCUDA.cu:156-254 -- after each load window, flush
     // when the accumulated survivors reach the window size
     const int64_t tiles_per_window = CRISPY_GEN_WINDOW / kScanTile;

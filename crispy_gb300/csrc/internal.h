@@ -114,6 +114,7 @@ struct GenJob {
     int n = 0, max_len = 0;
     pinned_vector<int32_t> h_len;
     pinned_vector<int64_t> h_woff;     // first packed word of each read
+    pinned_vector<uint32_t> h_tiles;   // survivors per compaction tile (chunk boundaries)
     DevBuf seq, off, len, woff, packed;
     DevBuf pairs, dist, score, ml, al, flags, scan, blocksum, surv_idx, keys, keys_alt,
         vals, vals_alt, out_pairs, out_dists, order, buckets, queue, err, tune_sample, tune_queue,
@@ -261,7 +262,9 @@ int sort_u32_payload(crispy_ctx* ctx, cudaStream_t s, uint32_t* keys, uint32_t* 
                      uint32_t* vals, uint32_t* vals_alt, int64_t n, int key_bits,
                      uint32_t** sorted_keys, uint32_t** sorted_vals, DevBuf& tmp);
 // Stable compaction of indices with flag != 0; per-tile counts returned on
-// the device in tile_counts (tile = kScanTile items).
+// the device in tile_counts (tile = kScanTile items).  With total != nullptr
+// the call waits for the count and returns it; with nullptr it returns at
+// once (the caller reads tile_counts).
 constexpr int kScanTile = 4608;   // divides the 589,824-pair window (128 tiles)
 int compact_flags(crispy_ctx* ctx, cudaStream_t s, const uint8_t* flags, int64_t n,
                   uint32_t* out_idx, uint32_t* tile_counts, DevBuf& tmp, int64_t* total);

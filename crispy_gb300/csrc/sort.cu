@@ -262,7 +262,7 @@ int sort_u32_payload(crispy_ctx* ctx, cudaStream_t s, uint32_t* keys, uint32_t* 
 
 int compact_flags(crispy_ctx* ctx, cudaStream_t s, const uint8_t* flags, int64_t n,
                   uint32_t* out_idx, uint32_t* tile_counts, DevBuf& tmp, int64_t* total) {
-    *total = 0;
+    if (total) *total = 0;
     if (n <= 0) return CRISPY_OK;
     const int nt = (int)((n + kScanTile - 1) / kScanTile);
     CRISPY_TRY(ensure(ctx, tmp, (size_t)(nt + 1) * sizeof(uint32_t)));
@@ -274,6 +274,7 @@ int compact_flags(crispy_ctx* ctx, cudaStream_t s, const uint8_t* flags, int64_t
     cmp_scatter<<<nt, kCmpThreads, 0, s>>>(flags, n, offs, out_idx);
     count_launch(ctx, 3);
     CRISPY_CK(ctx, cudaGetLastError());
+    if (!total) return CRISPY_OK;   // the caller reads tile_counts (and sums them) itself
     uint32_t tot = 0;
     CRISPY_CK(ctx, cudaMemcpyAsync(&tot, offs + nt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     CRISPY_CK(ctx, cudaStreamSynchronize(s));
