@@ -674,13 +674,20 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched_split_kernel(
 // raw list follows its high-level entries, the L section follows the H
 // section.  Each stream indexes a plane of 32-bit words (bank = word mod
 // 32) whose guard words start at 32768: H: K-mer - 0x8000, L: K-mer.
+// The steps of both streams per group are set here from the per-read
+// section counts: H = the largest H section, rounded up to 16 (no spare
+// steps: the H-only kernel is issue-bound, a bank conflict costs it less
+// than a step); L = the largest L section plus kSchedSpare spare steps when
+// it holds 64 entries or more, rounded up to 16.  tstart leaves room for
+// 2 * gent + 32 steps, which bounds the two.
 __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
     const uint32_t* __restrict__ ent, const int64_t* __restrict__ gstart,
-    const int64_t* __restrict__ tstart, const int32_t* __restrict__ tgent,
-    const int32_t* __restrict__ tgentL, const int32_t* __restrict__ nhigh,
+    const int64_t* __restrict__ tstart, int32_t* __restrict__ tgent,
+    int32_t* __restrict__ tgentL, const int32_t* __restrict__ nhigh,
     const int32_t* __restrict__ nsec, const uint16_t* __restrict__ bcnt, int n, int ngroups,
     uint16_t* __restrict__ tent) {
     __shared__ SchedSmem sm;
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int g = blockIdx.x * kSchedWarps + w; g < ngroups; g += gridDim.x * kSchedWarps) {
         const int r = g * 32 + lane;
@@ -688,11 +695,19 @@ __global__ void __launch_bounds__(kSchedWarps * 32) kmer_sched8_kernel(
         const int rr = active ? r : 0;
         const int nh = active ? nhigh[r] : 0;
         const int nH = active ? nsec[(int64_t)rr * 2] : 0;
-        const int EtH = tgent[g];
+        const int nL = active ? nsec[(int64_t)rr * 2 + 1] : 0;
+        const int mh = (int)__reduce_max_sync(full, (unsigned)nH);
+        const int ml = (int)__reduce_max_sync(full, (unsigned)nL);
+        const int EtH = (mh + 15) / 16 * 16;
+        const int EtL = (ml + (ml >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
+        if (lane == 0) {
+            tgent[g] = EtH;
+            tgentL[g] = EtL;
+        }
         sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64, nh, EtH, ent + gstart[g],
                          0x8000u, 32768u, 1u, tent + tstart[g]);
         __syncwarp();
-        sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + nH, tgentL[g],
+        sched_stream<32>(sm, w, lane, active, bcnt + (int64_t)rr * 64 + 32, nh + nH, EtL,
                          ent + gstart[g], 0u, 32768u, 1u, tent + tstart[g] + (int64_t)32 * EtH);
         __syncwarp();
     }
@@ -2764,12 +2779,33 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
     CRISPY_CK(ctx, cudaGetLastError());
     const int levels = dense_levels_for(k);
     if (k == 8) {
-        // stream layouts need the per-read H / L counts: one round trip
+        // the schedule kernel sets both streams' steps per group; the layout
+        // leaves room for them (H <= gent, L <= gent + 32)
+        j.h_tstart.assign(j.ngroups + 1, 0);
+        for (int g = 0; g < j.ngroups; ++g) j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * (2 * j.h_gent[g] + 32);
+        j.ntent = j.h_tstart[j.ngroups];
+        CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
+                                       cudaMemcpyHostToDevice, s));
+        // the per-read H / L counts and H keys come back on a side stream
+        // while the schedule runs
         j.h_nsec.resize(2 * (size_t)n);
-        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_nsec.data(), j.nsec.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
         j.h_hinfo.resize(n);
-        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_hinfo.data(), j.hinfo.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
-        CRISPY_CK(ctx, cudaStreamSynchronize(s));
+        CRISPY_CK(ctx, cudaEventRecord(ctx->fork_ev, s));
+        CRISPY_CK(ctx, cudaStreamWaitEvent(ctx->side[0], ctx->fork_ev, 0));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_nsec.data(), j.nsec.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost,
+                                       ctx->side[0]));
+        CRISPY_CK(ctx, cudaMemcpyAsync(j.h_hinfo.data(), j.hinfo.ptr, (size_t)n * 4, cudaMemcpyDeviceToHost,
+                                       ctx->side[0]));
+        CRISPY_CK(ctx, cudaEventRecord(ctx->join_ev[0], ctx->side[0]));
+        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
+        kmer_sched8_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
+            j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
+            j.tgentL.as<int32_t>(), nhigh, j.nsec.as<int32_t>(), j.bcnt.as<uint16_t>(), n, j.ngroups,
+            j.tent.as<uint16_t>());
+        count_launch(ctx);
+        CRISPY_CK(ctx, cudaGetLastError());
+        CRISPY_CK(ctx, cudaEventSynchronize(ctx->join_ev[0]));
         // runs of equal H keys along the positions; the batched split needs
         // each key in one run (keys ascending, as the read order sorts them)
         j.h_run_lo.resize(n);
@@ -2782,36 +2818,6 @@ int crispy_kmer_rebuild(crispy_ctx* ctx) {
             for (int q = i; q < e; ++q) { j.h_run_lo[q] = i; j.h_run_hi[q] = e; }
             i = e;
         }
-        std::vector<int32_t> tgl(j.ngroups, 0);
-        j.h_tstart.assign(j.ngroups + 1, 0);
-        j.h_tgent.assign(j.ngroups, 0);
-        for (int g = 0; g < j.ngroups; ++g) {
-            int mh = 0, ml = 0;
-            for (int r = g * 32; r < std::min(n, g * 32 + 32); ++r) {
-                mh = std::max(mh, j.h_nsec[2 * (size_t)r]);
-                ml = std::max(ml, j.h_nsec[2 * (size_t)r + 1]);
-            }
-            // no spare steps for H: the H-only kernel is issue-bound, a bank
-            // conflict costs it less than a step
-            j.h_tgent[g] = (mh + 15) / 16 * 16;
-            tgl[g] = (ml + (ml >= 64 ? kSchedSpare : 0) + 15) / 16 * 16;
-            j.h_tstart[g + 1] = j.h_tstart[g] + 32LL * (j.h_tgent[g] + tgl[g]);
-        }
-        j.ntent = j.h_tstart[j.ngroups];
-        CRISPY_TRY(ensure(ctx, j.tent, (size_t)std::max<int64_t>(j.ntent, 8) * 2));
-        CRISPY_CK(ctx, cudaMemcpyAsync(j.tstart.ptr, j.h_tstart.data(), (size_t)(j.ngroups + 1) * 8,
-                                       cudaMemcpyHostToDevice, s));
-        CRISPY_CK(ctx, cudaMemcpyAsync(j.tgent.ptr, j.h_tgent.data(), (size_t)j.ngroups * 4,
-                                       cudaMemcpyHostToDevice, s));
-        CRISPY_CK(ctx, cudaMemcpyAsync(j.tgentL.ptr, tgl.data(), (size_t)j.ngroups * 4,
-                                       cudaMemcpyHostToDevice, s));
-        const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
-        kmer_sched8_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
-            j.ent.as<uint32_t>(), j.gstart.as<int64_t>(), j.tstart.as<int64_t>(), j.tgent.as<int32_t>(),
-            j.tgentL.as<int32_t>(), nhigh, j.nsec.as<int32_t>(), j.bcnt.as<uint16_t>(), n, j.ngroups,
-            j.tent.as<uint16_t>());
-        count_launch(ctx);
-        CRISPY_CK(ctx, cudaGetLastError());
     } else if (levels > 0 && j.split) {
         const int sgrid = std::min((j.ngroups + kSchedWarps - 1) / kSchedWarps, ctx->sm_count * 8);
         kmer_sched_split_kernel<<<sgrid, kSchedWarps * 32, 0, s>>>(
