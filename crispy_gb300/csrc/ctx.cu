@@ -4,8 +4,11 @@
 // checkCudaErrors -> exit(-1) error model (kmerKernel.h:17-26,
 // genKernel.h:17-26): every failure becomes a status code plus a message.
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <new>
+#include <unordered_set>
 
 #include "internal.h"
 
@@ -64,6 +67,34 @@ __global__ void __launch_bounds__(256) lds128_probe_kernel(uint32_t seed, uint32
 }  // namespace
 
 namespace crispy {
+
+static std::mutex g_pageable_mu;
+static std::unordered_set<void*> g_pageable;   // fallback blocks of pinned_or_pageable_alloc
+
+void* pinned_or_pageable_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) == cudaSuccess) return p;
+    cudaGetLastError();
+    p = std::malloc(bytes);
+    if (!p) throw std::bad_alloc();
+    std::lock_guard<std::mutex> g(g_pageable_mu);
+    g_pageable.insert(p);
+    return p;
+}
+
+void pinned_or_pageable_free(void* p) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> g(g_pageable_mu);
+        auto it = g_pageable.find(p);
+        if (it != g_pageable.end()) {
+            g_pageable.erase(it);
+            std::free(p);
+            return;
+        }
+    }
+    if (cudaFreeHost(p) != cudaSuccess) cudaGetLastError();   // CUDA shutting down: the block goes with the process
+}
 
 int fail(crispy_ctx* ctx, int code, const char* fmt, ...) {
     char buf[512];

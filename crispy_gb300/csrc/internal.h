@@ -35,33 +35,20 @@ struct HostBuf {
     template <class T> T* as() const { return static_cast<T*>(ptr); }
 };
 
-// Allocator of page-locked host memory for per-read arrays that come back
-// from the device every run (copies into pageable memory go through a
-// staging buffer at a fraction of the link's rate).  Falls back to
-// pageable memory when pinning fails; frees by the kind it got.
+// Allocator of page-locked host memory for per-read arrays that move
+// between host and device every run (copies from or into pageable memory go
+// through a staging buffer at a fraction of the link's rate).  Falls back to
+// pageable memory when pinning fails; those blocks are recorded, so that a
+// block is always freed by the call that matches its allocation.
+void* pinned_or_pageable_alloc(size_t bytes);
+void pinned_or_pageable_free(void* p);
 template <class T>
 struct PinnedAlloc {
     using value_type = T;
     PinnedAlloc() = default;
     template <class U> PinnedAlloc(const PinnedAlloc<U>&) {}
-    T* allocate(size_t n) {
-        void* p = nullptr;
-        if (cudaHostAlloc(&p, n * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
-            cudaGetLastError();
-            p = std::malloc(n * sizeof(T));
-            if (!p) throw std::bad_alloc();
-        }
-        return static_cast<T*>(p);
-    }
-    void deallocate(T* p, size_t) {
-        cudaPointerAttributes at{};
-        if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost) {
-            cudaFreeHost(p);
-        } else {
-            cudaGetLastError();
-            std::free(p);
-        }
-    }
+    T* allocate(size_t n) { return static_cast<T*>(pinned_or_pageable_alloc(n * sizeof(T))); }
+    void deallocate(T* p, size_t) { pinned_or_pageable_free(p); }
     template <class U> bool operator==(const PinnedAlloc<U>&) const { return true; }
     template <class U> bool operator!=(const PinnedAlloc<U>&) const { return false; }
 };

@@ -3161,7 +3161,7 @@ static int kmer_run_impl(crispy_ctx* ctx, float thr, int mode, int dists, int64_
                 }));
                 ev_end(ctx, ctx->ev_kmer, s);
                 ctx->stats.kmer_launches += 1;
-            } else if (any_dense) {
+            } else if (any_dense && sample == 0) {
                 DenseArgs d2 = da;
                 d2.r_lo = rlo; d2.r_hi = rhi; d2.c_lo = 0; d2.c_hi = n;
                 kmer_dense_kernel<<<std::min(rhi - rlo, 8 * ctx->sm_count), 256, dsmem, s>>>(d2);
