@@ -343,10 +343,13 @@ int crispy_get_stats(const crispy_ctx* ctx, crispy_stats* out);
 /* Enable per-launch event timing (adds events around the hot kernels). */
 int crispy_set_timing(crispy_ctx* ctx, int enable);
 
-/* The autotuner's choices so far, as a JSON array (one object per tuned
- * genDist bin: band, band slots, lanes per pair, slots per lane, pairs per
- * block, sample size, best and untuned times).  Set CRISPY_AUTOTUNE=0 in the
- * environment to disable tuning.  No reference counterpart. */
+/* The autotuner's choices so far, as a JSON array: one object per tuned
+ * genDist bin (stage "gen": band, band slots, lanes per pair, slots per
+ * lane, pairs per block, sample size, best and untuned times) and one per
+ * read set whose k-mer bound-pass split was tuned (stage "kmer": reads, K,
+ * split in 1/256, sampled row groups, best and default times).  Set
+ * CRISPY_AUTOTUNE=0 in the environment to disable tuning.  No reference
+ * counterpart. */
 int crispy_tune_report(char* buf, size_t len);
 
 /* Measured integer-pipe throughput of this GPU in Gop/s (32-bit add/xor
