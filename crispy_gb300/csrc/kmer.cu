@@ -13,24 +13,30 @@
 //     T "level entries" (t-1)*4^K + kmer, one per occurrence, where t is the
 //     occurrence rank of that K-mer in the read.  Then
 //         m(a, b) = #{ entries e of b : e in entries(a) }.
-//   * A block owns 64 row reads and keeps their entry sets in shared memory
-//     as bit planes: 64-bit word P[e] has bit r set iff row read r holds
-//     entry e.  One 64-bit shared load answers one column entry for 64 row
-//     reads.  Levels 1..levels live in dense planes (4^K words each, 128 KB
-//     at K = 6); the rare entries of higher level go to a small
-//     open-addressing hash table in shared memory, so the footprint stays
-//     fixed whatever the reads hold.
+//   * A block owns 128 row reads (64 at K = 7, 32 at K = 8) and keeps their
+//     entry sets in shared memory as bit planes: 128-bit word P[e] has bit r
+//     set iff row read r holds entry e.  One 128-bit shared load answers one
+//     column entry for 128 row reads.  Levels 1..levels live in dense planes
+//     (two levels of 4^K words at K = 6, 128 KB); the rare entries of higher
+//     level go to a small open-addressing hash table in shared memory, so
+//     the footprint stays fixed whatever the reads hold.
 //   * A warp owns 32 column reads (one per lane) and streams their entries
 //     from an interleaved layout (eight consecutive entries of one read in a
 //     uint4, the 32 reads' uint4 of one octet in one 512-byte line), gathers
-//     the plane word of each, and adds its two halves into two sets of 32
+//     the plane word of each, and adds its quarters into four sets of 32
 //     bit-sliced counters with Harley-Seal carry-save trees (LOP3 work
 //     only).  The next 16 entries are in flight while the current 16 are
 //     reduced.  The streamed entries are precomputed 16-bit plane word
-//     indices, ordered per 32-read group so that the 16 lanes of a half-warp
-//     hit 16 different double banks; high-level entries and pads index zero
-//     guard words, so the gather has no branch and the rare high-level
-//     entries get a separate hash pass.
+//     indices, ordered per 32-read group so that the 8 lanes of a
+//     quarter-warp hit 8 different 16-byte banks; high-level entries and
+//     pads index zero guard words, so the gather has no branch and the rare
+//     high-level entries get a separate hash pass.
+//   * Bounds skip work that cannot pass the cut, never changing a count
+//     that can: at K <= 6 the batched form counts a hashed share of each
+//     column's entries first and the rest only where a row may still pass
+//     (m <= m0 + Ta - a0); at K = 8 pairs of reads with different H keys
+//     need a read with |H| >= mmin[T], and same-key pairs whose H sums
+//     already fall short of mmin[Ta] - |L_a| skip their L sums.
 //   * The threshold is an integer test m >= mmin[min(Ta, Tb)], with mmin
 //     tabulated on the host from the reference's float expression (the pass
 //     predicate is monotone in m), first as a bit-sliced compare against a
